@@ -1,0 +1,565 @@
+// Host runtime and C ABI (include/cablegpu.h) of the GB300 cbm() timestep.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/cablegpu.h"
+#include "cbm_step.cuh"
+
+using namespace cg;
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr int kGraphSteps = 8;   // steps per captured CUDA graph
+
+// ---------------------------------------------------------------- field registry
+enum Storage { S_U8, S_F32, S_F64 };
+struct FieldDef {
+  const char* name;
+  int nlayer;
+  int dtype;   // external (host) type
+  int kind;
+  Storage st;  // device storage type
+};
+
+const char* kDiagNames[CG_NDIAG] = {
+  "fe_d", "fh_d", "fev", "fhv", "fhs", "fns", "fnv", "ga_d", "tv_d", "tscrn", "qscrn", "rnet_d", "us", "cduv", "cdtq",
+  "epot", "fes", "fevc", "dgdtg", "fevw", "fpn", "frday_d", "fgpp_d", "fnpp", "fnee", "fra", "frp", "frs", "trad_d",
+  "albedo_vis", "albedo_nir", "transd", "precis", "through", "fwet", "wetfac", "potev", "runoff", "rnof1", "rnof2",
+  "smelt", "ghflux", "sghflux", "drybal", "wetbal", "ebal", "wbal", "qssabs", "rniso", "vlaiw", "tvair", "qvair",
+  "swnet", "lwnet", "wbtot", "gswx_sun", "gswx_shd", "fwsoil", "dryleaf_passes",
+};
+
+std::vector<FieldDef> make_registry() {
+  std::vector<FieldDef> f = {
+    {"iveg", 1, CABLEGPU_I32, CABLEGPU_KIND_PARAM, S_U8},
+    {"isoilm", 1, CABLEGPU_I32, CABLEGPU_KIND_PARAM, S_U8},
+    {"vlai", 1, CABLEGPU_F32, CABLEGPU_KIND_PARAM, S_F32},
+    {"lat", 1, CABLEGPU_F32, CABLEGPU_KIND_PARAM, S_F32},
+    {"lonphase", 1, CABLEGPU_F32, CABLEGPU_KIND_PARAM, S_F32},
+    {"tbase", 1, CABLEGPU_F32, CABLEGPU_KIND_PARAM, S_F32},
+    {"swscale", 1, CABLEGPU_F32, CABLEGPU_KIND_PARAM, S_F32},
+    {"wb", CG_MS, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
+    {"wbice", CG_MS, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
+    {"gammzz1", 1, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
+    {"tgg", CG_MS, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"tggsn", 3, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"ssdn", 3, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"smass", 3, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"sdepth", 3, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"flags", 1, CABLEGPU_I32, CABLEGPU_KIND_STATE, S_U8},
+    {"snowd", 1, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"ssdnn", 1, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"snage", 1, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"pudsto", 1, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"owetfac", 1, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"rtsoil", 1, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"tss", 1, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"wb_lake", 1, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"wbtot1", 1, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"wbtot2", 1, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"cansto", 1, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"cplant", 3, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"csoil", 2, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
+    {"owb", 1, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
+    {"ebal_tot", 1, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
+    {"wbal_tot", 1, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
+    {"out", CG_NOUT, CABLEGPU_F32, CABLEGPU_KIND_OUTPUT, S_F32},
+  };
+  for (int i = 0; i < CG_NDIAG; ++i) f.push_back({kDiagNames[i], 1, CABLEGPU_F32, CABLEGPU_KIND_DIAG, S_F32});
+  f.push_back({"forcing", CG_NFORC, CABLEGPU_F32, CABLEGPU_KIND_FORCING, S_F32});
+  f.push_back({"forcing_in", CG_NFORC, CABLEGPU_F32, CABLEGPU_KIND_FORCING, S_F32});
+  f.push_back({"work_a", CG_NA, CABLEGPU_F32, CABLEGPU_KIND_WORK, S_F32});
+  f.push_back({"work_b", CG_NB, CABLEGPU_F32, CABLEGPU_KIND_WORK, S_F32});
+  return f;
+}
+
+const std::vector<FieldDef>& registry() {
+  static const std::vector<FieldDef> r = make_registry();
+  return r;
+}
+
+size_t storage_bytes(Storage s) { return s == S_U8 ? 1 : (s == S_F32 ? 4 : 8); }
+
+// ---------------------------------------------------------------- kernels
+// One kernel per phase of the timestep (see cbm_step.cuh).
+template <bool kDiag, int kPhase>
+__global__ void __launch_bounds__(kBlock) cbm_phase_kernel(CgDev D, const CgTables* __restrict__ T, StepParams P,
+                                                           const int* __restrict__ clock) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= D.mp) return;
+  StepParams p = P;
+  if (clock) { p.ktau = clock[0]; p.step_index = clock[0] - 1; }
+  if (kPhase == 0) phase_a<kDiag>(D, T, p, t);
+  else if (kPhase == 1) phase_b<kDiag>(D, T, p, t);
+  else phase_c<kDiag>(D, T, p, t);
+}
+
+__global__ void advance_clock_kernel(int* clock) { clock[0] += 1; }
+
+// Cold start: the reference's initial state for a run without restart file.
+__global__ void cold_start_kernel(CgDev D, const CgTables* __restrict__ T, const double* snowd0, const double* tgg0,
+                                  const double* wb0) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= D.mp) return;
+  const int ld = D.ld;
+  const int v = D.iveg[t] - 1, s = D.isoilm[t] - 1;
+  const float swilt = T->soil.swilt[s], sfc = T->soil.sfc[s];
+  const int o = D.tile_id[t];
+  const float wbf = (float)wb0[o], tg = (float)tgg0[o], sn = (float)snowd0[o];
+  for (int k = 0; k < CG_MS; ++k) {
+    D.wb[k * ld + t] = (double)wbf;
+    D.tgg[k * ld + t] = tg;
+    D.wbice[k * ld + t] = (tg < 273.15f) ? (double)wbf * (double)0.8f : 0.0;
+  }
+  const bool snow = sn > 0.0f;
+  for (int k = 0; k < 3; ++k) {
+    D.ssdn[k * ld + t] = snow ? 120.0f : 140.0f;
+    D.tggsn[k * ld + t] = snow ? TFRZ : 273.1f;
+    D.smass[k * ld + t] = 0.f;
+    D.sdepth[k * ld + t] = 0.f;
+  }
+  D.snowd[t] = sn;
+  D.ssdnn[t] = snow ? 120.0f : 140.0f;
+  D.snage[t] = 0.f;
+  D.flags[t] = 2;   // isflag 0, soil_snow first call pending
+  D.gammzz1[t] = 0.0;
+  D.pudsto[t] = 0.f; D.rtsoil[t] = 100.0f; D.tss[t] = tg; D.wb_lake[t] = 0.f; D.wbtot1[t] = 0.f; D.wbtot2[t] = 0.f;
+  D.cansto[t] = 0.f;
+  float ow = fmaxf(0.0f, fminf(1.0f, (wbf - swilt) / (sfc - swilt)));
+  double wbice1 = D.wbice[t];
+  if (wbice1 > 0.) { float r = (float)(wbice1 / (double)wbf); ow = ow * (1.0f - r) * (1.0f - r); }
+  D.owetfac[t] = ow;
+  for (int k = 0; k < 3; ++k) D.cplant[k * ld + t] = T->pft.cplant0[k][v];
+  for (int k = 0; k < 2; ++k) D.csoil[k * ld + t] = T->pft.csoil0[k][v];
+  D.owb[t] = 0.0; D.ebal_tot[t] = 0.0; D.wbal_tot[t] = 0.0;
+}
+
+// Caller-order host arrays <-> device slot order.  dst/src are [nlayer][ld]
+// on the device, stage is [nlayer][mp] in caller order.
+template <typename TD, typename TS>
+__global__ void scatter_in_kernel(TD* dst, const TS* stage, const int* order, int mp, int ld, int nlayer) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= mp) return;
+  const int o = order[s];
+  for (int k = 0; k < nlayer; ++k) dst[(size_t)k * ld + s] = (TD)stage[(size_t)k * mp + o];
+}
+template <typename TD, typename TS>
+__global__ void gather_out_kernel(TD* stage, const TS* src, const int* order, int mp, int ld, int nlayer) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= mp) return;
+  const int o = order[s];
+  for (int k = 0; k < nlayer; ++k) stage[(size_t)k * mp + o] = (TD)src[(size_t)k * ld + s];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- context
+struct cablegpu_ctx {
+  int device = 0;
+  int mp = 0, ld = 0;
+  cudaStream_t stream = nullptr;
+  char* arena = nullptr;
+  size_t arena_bytes = 0;
+  std::vector<void*> field_ptr;    // device pointer per registry entry
+  CgTables* d_tables = nullptr;
+  CgDev dev{};
+  int* d_clock = nullptr;
+  int* d_order = nullptr;          // device slot -> caller tile index
+  char* d_stage = nullptr;         // staging buffer for field copies
+  size_t stage_bytes = 0;
+  int* h_clock = nullptr;          // pinned
+  unsigned int* h_status = nullptr;
+  bool host_forcing = false;
+  CgForcingSpec forc{12345ull, 1, 1800.f};
+  int medlyn = 0, diag = 0, capture_forcing = 0;
+  cudaGraphExec_t graph = nullptr;
+  float graph_dels = -1.f;
+  int graph_diag = -1, graph_medlyn = -1, graph_hostforc = -1, graph_capture = -1;
+  unsigned long long graph_seed = 0;
+  int graph_doy0 = -1;
+  long long launches = 0;
+  std::string err;
+};
+
+namespace {
+
+int fail(cablegpu_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+#define CG_CUDA(c, call)                                                                     \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess) return fail((c), CABLEGPU_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+void bind_device_view(cablegpu_ctx* c) {
+  auto P = [&](const char* n) { return c->field_ptr[cablegpu_field_id(n)]; };
+  CgDev& D = c->dev;
+  D.mp = c->mp; D.ld = c->ld;
+  D.tile_id = c->d_order;
+  D.iveg = (const uint8_t*)P("iveg"); D.isoilm = (const uint8_t*)P("isoilm");
+  D.vlai = (const float*)P("vlai"); D.lat = (const float*)P("lat"); D.lonphase = (const float*)P("lonphase");
+  D.tbase = (const float*)P("tbase"); D.swscale = (const float*)P("swscale");
+  D.wb = (double*)P("wb"); D.wbice = (double*)P("wbice"); D.gammzz1 = (double*)P("gammzz1");
+  D.tgg = (float*)P("tgg"); D.tggsn = (float*)P("tggsn"); D.ssdn = (float*)P("ssdn"); D.smass = (float*)P("smass");
+  D.sdepth = (float*)P("sdepth"); D.flags = (uint8_t*)P("flags"); D.snowd = (float*)P("snowd");
+  D.ssdnn = (float*)P("ssdnn"); D.snage = (float*)P("snage"); D.pudsto = (float*)P("pudsto");
+  D.owetfac = (float*)P("owetfac"); D.rtsoil = (float*)P("rtsoil"); D.tss = (float*)P("tss");
+  D.wb_lake = (float*)P("wb_lake"); D.wbtot1 = (float*)P("wbtot1"); D.wbtot2 = (float*)P("wbtot2");
+  D.cansto = (float*)P("cansto"); D.cplant = (float*)P("cplant"); D.csoil = (float*)P("csoil");
+  D.owb = (double*)P("owb"); D.ebal_tot = (double*)P("ebal_tot"); D.wbal_tot = (double*)P("wbal_tot");
+  D.out = (float*)P("out");
+  D.diag = c->diag ? (float*)P(kDiagNames[0]) : nullptr;
+  D.forcing_in = c->host_forcing ? (const float*)P("forcing_in") : nullptr;
+  D.forcing_out = c->capture_forcing ? (float*)P("forcing") : nullptr;
+  D.work_a = (float*)P("work_a");
+  D.work_b = (float*)P("work_b");
+}
+
+int launch_step(cablegpu_ctx* c, const StepParams& p, const int* clock) {
+  bind_device_view(c);
+  const int grid = (c->mp + kBlock - 1) / kBlock;
+  if (c->diag) {
+    cbm_phase_kernel<true, 0><<<grid, kBlock, 0, c->stream>>>(c->dev, c->d_tables, p, clock);
+    cbm_phase_kernel<true, 1><<<grid, kBlock, 0, c->stream>>>(c->dev, c->d_tables, p, clock);
+    cbm_phase_kernel<true, 2><<<grid, kBlock, 0, c->stream>>>(c->dev, c->d_tables, p, clock);
+  } else {
+    cbm_phase_kernel<false, 0><<<grid, kBlock, 0, c->stream>>>(c->dev, c->d_tables, p, clock);
+    cbm_phase_kernel<false, 1><<<grid, kBlock, 0, c->stream>>>(c->dev, c->d_tables, p, clock);
+    cbm_phase_kernel<false, 2><<<grid, kBlock, 0, c->stream>>>(c->dev, c->d_tables, p, clock);
+  }
+  c->launches += 3;
+  CG_CUDA(c, cudaGetLastError());
+  return CABLEGPU_OK;
+}
+
+StepParams make_params(cablegpu_ctx* c, int ktau, float dels) {
+  StepParams p;
+  p.ktau = ktau;
+  p.dels = dels;
+  p.medlyn = c->medlyn;
+  p.forc = c->forc;
+  p.forc.dels = dels;
+  p.step_index = ktau - 1;
+  return p;
+}
+
+int ensure_graph(cablegpu_ctx* c, float dels) {
+  if (c->graph && c->graph_dels == dels && c->graph_diag == c->diag && c->graph_medlyn == c->medlyn &&
+      c->graph_hostforc == (int)c->host_forcing && c->graph_capture == c->capture_forcing &&
+      c->graph_seed == c->forc.seed && c->graph_doy0 == c->forc.doy0)
+    return CABLEGPU_OK;
+  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+  StepParams p = make_params(c, 0, dels);
+  cudaGraph_t g;
+  CG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  long long before = c->launches;
+  for (int i = 0; i < kGraphSteps; ++i) {
+    int rc = launch_step(c, p, c->d_clock);
+    if (rc) { cudaStreamEndCapture(c->stream, &g); return rc; }
+    advance_clock_kernel<<<1, 1, 0, c->stream>>>(c->d_clock);
+  }
+  c->launches = before;   // captured launches are counted when replayed
+  CG_CUDA(c, cudaStreamEndCapture(c->stream, &g));
+  CG_CUDA(c, cudaGraphInstantiate(&c->graph, g, 0));
+  cudaGraphDestroy(g);
+  c->graph_dels = dels; c->graph_diag = c->diag; c->graph_medlyn = c->medlyn;
+  c->graph_hostforc = (int)c->host_forcing; c->graph_capture = c->capture_forcing;
+  c->graph_seed = c->forc.seed; c->graph_doy0 = c->forc.doy0;
+  return CABLEGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cablegpu_num_fields(void) { return (int)registry().size(); }
+
+int cablegpu_field_info(int id, const char** name, int* nlayer, int* dtype, int* kind) {
+  if (id < 0 || id >= cablegpu_num_fields()) return CABLEGPU_ERR_ARG;
+  const FieldDef& f = registry()[id];
+  if (name) *name = f.name;
+  if (nlayer) *nlayer = f.nlayer;
+  if (dtype) *dtype = f.dtype;
+  if (kind) *kind = f.kind;
+  return CABLEGPU_OK;
+}
+
+int cablegpu_field_id(const char* name) {
+  if (!name) return CABLEGPU_ERR_ARG;
+  const auto& r = registry();
+  for (size_t i = 0; i < r.size(); ++i)
+    if (!std::strcmp(r[i].name, name)) return (int)i;
+  return CABLEGPU_ERR_ARG;
+}
+
+int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out) {
+  if (!tiles || !out || tiles->mp <= 0 || !tiles->iveg || !tiles->isoilm || !tiles->vlai || !tiles->lat)
+    return CABLEGPU_ERR_ARG;
+  for (int i = 0; i < tiles->mp; ++i)
+    if (tiles->iveg[i] < 1 || tiles->iveg[i] > CG_NPFT || tiles->isoilm[i] < 1 || tiles->isoilm[i] > CG_NSOIL)
+      return CABLEGPU_ERR_ARG;
+  auto* c = new cablegpu_ctx();
+  *out = c;
+  c->device = device;
+  c->mp = tiles->mp;
+  c->ld = (tiles->mp + 255) / 256 * 256;
+  CG_CUDA(c, cudaSetDevice(device));
+  CG_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  // one arena, every field 256-byte aligned
+  const auto& r = registry();
+  std::vector<size_t> off(r.size());
+  size_t bytes = 0;
+  for (size_t i = 0; i < r.size(); ++i) {
+    off[i] = bytes;
+    bytes += ((size_t)r[i].nlayer * c->ld * storage_bytes(r[i].st) + 255) / 256 * 256;
+  }
+  c->arena_bytes = bytes;
+  CG_CUDA(c, cudaMalloc(&c->arena, bytes));
+  CG_CUDA(c, cudaMemsetAsync(c->arena, 0, bytes, c->stream));
+  c->field_ptr.resize(r.size());
+  for (size_t i = 0; i < r.size(); ++i) c->field_ptr[i] = c->arena + off[i];
+  // tables
+  CgTables h{};
+  cg_build_tables(&h.pft, &h.soil);
+  CG_CUDA(c, cudaMalloc(&c->d_tables, sizeof(CgTables)));
+  CG_CUDA(c, cudaMemcpyAsync(c->d_tables, &h, sizeof(CgTables), cudaMemcpyHostToDevice, c->stream));
+  // device tile order
+  {
+    std::vector<int> order(c->mp);
+    for (int i = 0; i < c->mp; ++i) order[i] = i;
+    if (tiles->order == 0)
+      std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        if (tiles->iveg[a] != tiles->iveg[b]) return tiles->iveg[a] < tiles->iveg[b];
+        return tiles->isoilm[a] < tiles->isoilm[b];
+      });
+    CG_CUDA(c, cudaMalloc(&c->d_order, sizeof(int) * c->mp));
+    CG_CUDA(c, cudaMemcpy(c->d_order, order.data(), sizeof(int) * c->mp, cudaMemcpyHostToDevice));
+    c->stage_bytes = (size_t)c->mp * 64;
+    CG_CUDA(c, cudaMalloc(&c->d_stage, c->stage_bytes));
+  }
+  CG_CUDA(c, cudaMalloc(&c->d_clock, sizeof(int) * 4));
+  CG_CUDA(c, cudaMallocHost(&c->h_clock, sizeof(int) * 4));
+  CG_CUDA(c, cudaMallocHost(&c->h_status, sizeof(unsigned int)));
+  c->dev.status = nullptr;
+  CG_CUDA(c, cudaMalloc(&c->dev.status, sizeof(unsigned int)));
+  CG_CUDA(c, cudaMemsetAsync(c->dev.status, 0, sizeof(unsigned int), c->stream));
+  // tile description
+  std::vector<float> lon(c->mp, 0.f), tb(c->mp, 288.f), sw(c->mp, 1.f);
+  if (tiles->lonphase) std::memcpy(lon.data(), tiles->lonphase, sizeof(float) * c->mp);
+  if (tiles->tbase) std::memcpy(tb.data(), tiles->tbase, sizeof(float) * c->mp);
+  if (tiles->swscale) std::memcpy(sw.data(), tiles->swscale, sizeof(float) * c->mp);
+  int rc;
+  if ((rc = cablegpu_set_field(c, cablegpu_field_id("iveg"), tiles->iveg))) return rc;
+  if ((rc = cablegpu_set_field(c, cablegpu_field_id("isoilm"), tiles->isoilm))) return rc;
+  if ((rc = cablegpu_set_field(c, cablegpu_field_id("vlai"), tiles->vlai))) return rc;
+  if ((rc = cablegpu_set_field(c, cablegpu_field_id("lat"), tiles->lat))) return rc;
+  if ((rc = cablegpu_set_field(c, cablegpu_field_id("lonphase"), lon.data()))) return rc;
+  if ((rc = cablegpu_set_field(c, cablegpu_field_id("tbase"), tb.data()))) return rc;
+  if ((rc = cablegpu_set_field(c, cablegpu_field_id("swscale"), sw.data()))) return rc;
+  CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CABLEGPU_OK;
+}
+
+int cablegpu_destroy(cablegpu_ctx* c) {
+  if (!c) return CABLEGPU_ERR_ARG;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  cudaFree(c->arena);
+  cudaFree(c->d_tables);
+  cudaFree(c->d_clock);
+  cudaFree(c->d_order);
+  cudaFree(c->d_stage);
+  cudaFree(c->dev.status);
+  cudaFreeHost(c->h_clock);
+  cudaFreeHost(c->h_status);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return CABLEGPU_OK;
+}
+
+int cablegpu_set_field(cablegpu_ctx* c, int id, const void* host) {
+  if (!c || !host || id < 0 || id >= cablegpu_num_fields()) return fail(c, CABLEGPU_ERR_ARG, "set_field: bad argument");
+  const FieldDef& f = registry()[id];
+  const size_t n = (size_t)c->mp;
+  const size_t hes = (f.dtype == CABLEGPU_F64) ? 8 : 4;   // host element size
+  const size_t bytes = n * f.nlayer * hes;
+  if (bytes > c->stage_bytes) return fail(c, CABLEGPU_ERR_ARG, "set_field: field too large");
+  if (f.st == S_U8) {
+    const int* h = (const int*)host;
+    for (size_t i = 0; i < n * f.nlayer; ++i)
+      if (h[i] < 0 || h[i] > 255) return fail(c, CABLEGPU_ERR_ARG, std::string("set_field: value out of range for ") + f.name);
+  }
+  CG_CUDA(c, cudaMemcpyAsync(c->d_stage, host, bytes, cudaMemcpyHostToDevice, c->stream));
+  const int grid = (c->mp + 255) / 256;
+  void* d = c->field_ptr[id];
+  if (f.st == S_U8)
+    scatter_in_kernel<uint8_t, int><<<grid, 256, 0, c->stream>>>((uint8_t*)d, (const int*)c->d_stage, c->d_order, c->mp, c->ld, f.nlayer);
+  else if (f.st == S_F32)
+    scatter_in_kernel<float, float><<<grid, 256, 0, c->stream>>>((float*)d, (const float*)c->d_stage, c->d_order, c->mp, c->ld, f.nlayer);
+  else
+    scatter_in_kernel<double, double><<<grid, 256, 0, c->stream>>>((double*)d, (const double*)c->d_stage, c->d_order, c->mp, c->ld, f.nlayer);
+  CG_CUDA(c, cudaGetLastError());
+  CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CABLEGPU_OK;
+}
+
+int cablegpu_get_field(cablegpu_ctx* c, int id, void* host) {
+  if (!c || !host || id < 0 || id >= cablegpu_num_fields()) return fail(c, CABLEGPU_ERR_ARG, "get_field: bad argument");
+  const FieldDef& f = registry()[id];
+  if (f.kind == CABLEGPU_KIND_DIAG && !c->diag) return fail(c, CABLEGPU_ERR_STATE, "get_field: diagnostics are disabled");
+  const size_t n = (size_t)c->mp;
+  const size_t hes = (f.dtype == CABLEGPU_F64) ? 8 : 4;
+  const size_t bytes = n * f.nlayer * hes;
+  if (bytes > c->stage_bytes) return fail(c, CABLEGPU_ERR_ARG, "get_field: field too large");
+  const int grid = (c->mp + 255) / 256;
+  const void* d = c->field_ptr[id];
+  if (f.st == S_U8)
+    gather_out_kernel<int, uint8_t><<<grid, 256, 0, c->stream>>>((int*)c->d_stage, (const uint8_t*)d, c->d_order, c->mp, c->ld, f.nlayer);
+  else if (f.st == S_F32)
+    gather_out_kernel<float, float><<<grid, 256, 0, c->stream>>>((float*)c->d_stage, (const float*)d, c->d_order, c->mp, c->ld, f.nlayer);
+  else
+    gather_out_kernel<double, double><<<grid, 256, 0, c->stream>>>((double*)c->d_stage, (const double*)d, c->d_order, c->mp, c->ld, f.nlayer);
+  CG_CUDA(c, cudaGetLastError());
+  CG_CUDA(c, cudaMemcpyAsync(host, c->d_stage, bytes, cudaMemcpyDeviceToHost, c->stream));
+  CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CABLEGPU_OK;
+}
+
+int cablegpu_field_device_ptr(cablegpu_ctx* c, int id, void** dptr, int* ld) {
+  if (!c || !dptr || id < 0 || id >= cablegpu_num_fields()) return CABLEGPU_ERR_ARG;
+  *dptr = c->field_ptr[id];
+  if (ld) *ld = c->ld;
+  return CABLEGPU_OK;
+}
+
+int cablegpu_cold_start(cablegpu_ctx* c, const double* snowd0, const double* tgg0, const double* wb0) {
+  if (!c || !snowd0 || !tgg0 || !wb0) return fail(c, CABLEGPU_ERR_ARG, "cold_start: null argument");
+  const size_t n = (size_t)c->mp;
+  double* tmp = nullptr;
+  CG_CUDA(c, cudaMalloc(&tmp, 3 * n * sizeof(double)));
+  CG_CUDA(c, cudaMemcpyAsync(tmp, snowd0, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CG_CUDA(c, cudaMemcpyAsync(tmp + n, tgg0, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CG_CUDA(c, cudaMemcpyAsync(tmp + 2 * n, wb0, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  bind_device_view(c);
+  cold_start_kernel<<<(c->mp + 255) / 256, 256, 0, c->stream>>>(c->dev, c->d_tables, tmp, tmp + n, tmp + 2 * n);
+  CG_CUDA(c, cudaGetLastError());
+  CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  CG_CUDA(c, cudaFree(tmp));
+  return CABLEGPU_OK;
+}
+
+int cablegpu_set_forcing(cablegpu_ctx* c, const float* host_forcing) {
+  if (!c || !host_forcing) return fail(c, CABLEGPU_ERR_ARG, "set_forcing: null argument");
+  c->host_forcing = true;
+  return cablegpu_set_field(c, cablegpu_field_id("forcing_in"), host_forcing);
+}
+
+int cablegpu_set_synthetic_forcing(cablegpu_ctx* c, unsigned long long seed, int doy0) {
+  if (!c || doy0 < 1 || doy0 > 365) return fail(c, CABLEGPU_ERR_ARG, "set_synthetic_forcing: bad argument");
+  c->host_forcing = false;
+  c->forc.seed = seed;
+  c->forc.doy0 = doy0;
+  return CABLEGPU_OK;
+}
+
+int cablegpu_set_options(cablegpu_ctx* c, int medlyn, int diag, int capture_forcing) {
+  if (!c) return CABLEGPU_ERR_ARG;
+  c->medlyn = medlyn ? 1 : 0;
+  c->diag = diag ? 1 : 0;
+  c->capture_forcing = capture_forcing ? 1 : 0;
+  return CABLEGPU_OK;
+}
+
+int cablegpu_step(cablegpu_ctx* c, int ktau, float dels) {
+  if (!c || ktau < 1 || !(dels > 0.f)) return fail(c, CABLEGPU_ERR_ARG, "step: bad argument");
+  return launch_step(c, make_params(c, ktau, dels), nullptr);
+}
+
+int cablegpu_run(cablegpu_ctx* c, int ktau0, int nsteps, float dels) {
+  if (!c || ktau0 < 1 || nsteps < 0 || !(dels > 0.f)) return fail(c, CABLEGPU_ERR_ARG, "run: bad argument");
+  int done = 0;
+  if (nsteps >= kGraphSteps) {
+    int rc = ensure_graph(c, dels);
+    if (rc) return rc;
+    c->h_clock[0] = ktau0;
+    CG_CUDA(c, cudaMemcpyAsync(c->d_clock, c->h_clock, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    while (nsteps - done >= kGraphSteps) {
+      CG_CUDA(c, cudaGraphLaunch(c->graph, c->stream));
+      c->launches += 3 * kGraphSteps;
+      done += kGraphSteps;
+    }
+    // the pinned clock buffer must not be rewritten before the copy ran
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  for (; done < nsteps; ++done) {
+    int rc = launch_step(c, make_params(c, ktau0 + done, dels), nullptr);
+    if (rc) return rc;
+  }
+  return CABLEGPU_OK;
+}
+
+int cablegpu_synchronize(cablegpu_ctx* c) {
+  if (!c) return CABLEGPU_ERR_ARG;
+  CG_CUDA(c, cudaMemcpyAsync(c->h_status, c->dev.status, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+  CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (*c->h_status) {
+    CG_CUDA(c, cudaMemsetAsync(c->dev.status, 0, sizeof(unsigned int), c->stream));
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return fail(c, CABLEGPU_ERR_NONFINITE, "a step produced a non-finite output flux");
+  }
+  return CABLEGPU_OK;
+}
+
+int cablegpu_run_timed(cablegpu_ctx* c, int ktau0, int nsteps, float dels, float* ms_total) {
+  if (!c || !ms_total) return CABLEGPU_ERR_ARG;
+  if (nsteps >= kGraphSteps) { int rc = ensure_graph(c, dels); if (rc) return rc; }
+  cudaEvent_t a, b;
+  CG_CUDA(c, cudaEventCreate(&a));
+  CG_CUDA(c, cudaEventCreate(&b));
+  CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  CG_CUDA(c, cudaEventRecord(a, c->stream));
+  int rc = cablegpu_run(c, ktau0, nsteps, dels);
+  if (rc) return rc;
+  CG_CUDA(c, cudaEventRecord(b, c->stream));
+  CG_CUDA(c, cudaEventSynchronize(b));
+  CG_CUDA(c, cudaEventElapsedTime(ms_total, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return CABLEGPU_OK;
+}
+
+int cablegpu_kernel_timed(cablegpu_ctx* c, int ktau0, int nsteps, float dels, float* ms_per_launch) {
+  if (!c || !ms_per_launch || nsteps <= 0) return CABLEGPU_ERR_ARG;
+  std::vector<cudaEvent_t> ev(2 * nsteps);
+  for (auto& e : ev) CG_CUDA(c, cudaEventCreate(&e));
+  for (int i = 0; i < nsteps; ++i) {
+    CG_CUDA(c, cudaEventRecord(ev[2 * i], c->stream));
+    int rc = launch_step(c, make_params(c, ktau0 + i, dels), nullptr);
+    if (rc) return rc;
+    CG_CUDA(c, cudaEventRecord(ev[2 * i + 1], c->stream));
+  }
+  CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  double tot = 0.0;
+  for (int i = 0; i < nsteps; ++i) {
+    float ms = 0.f;
+    CG_CUDA(c, cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]));
+    tot += ms;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  *ms_per_launch = (float)(tot / nsteps);
+  return CABLEGPU_OK;
+}
+
+long long cablegpu_launch_count(cablegpu_ctx* c) { return c ? c->launches : -1; }
+
+const char* cablegpu_last_error(cablegpu_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+}  // extern "C"

@@ -1,0 +1,233 @@
+// Device-side restatement of CABLE's offline cbm() timestep for one tile
+// (src/offline/cbl_model_driver_offline.F90:38-231) with the offline driver's
+// rescaling and balance checks (src/offline/cable_serial.F90:573-728,
+// src/offline/cable_checks.F90:472-618).  One thread owns one tile for the
+// whole timestep; every call-site below cites the reference routine it
+// restates.
+//
+// Precision policy (GB300: FP64 runs at a small fraction of the FP32 rate):
+//   * FP32 for radiation, canopy energy balance, photosynthesis, snow, soil
+//     fluxes and carbon;
+//   * FP64 storage for soil water / ice (ssnow%wb, ssnow%wbice) and the layer-1
+//     heat capacity, with water increments accumulated in FP64;
+//   * FP64 for the two tridiagonal (Thomas) solves of soil heat and soil
+//     moisture and for the energy / water balance accumulators.
+//
+// Switch set: the reference offline defaults (cable.nml): soil_struc
+// 'default', fwsoil 'standard', ssnow_potev 'HDM', gs_switch 'leuning'
+// (medlyn selectable), litter / or_evap / gw_model / l_rev_corr /
+// call_climate / soil_thermal_fix / redistrb off, diag_soil_resp 'ON',
+// icycle 0.
+#pragma once
+#include <cstdint>
+#include "tables.h"
+#include "forcing.cuh"
+
+namespace cg {
+
+// physical constants (src/params/cable_phys_constants_mod.F90 and friends)
+constexpr float TFRZ = 273.16f, SBOLTZ = 5.67e-8f, EMSOIL = 1.0f, EMLEAF = 1.0f, CAPP = 1004.64f;
+constexpr float HL = 2.5014e6f, HLF = 0.334e6f, DHEAT = 21.5e-6f, GRAV = 9.8086f, RGAS = 8.3143f;
+constexpr float RMAIR = 0.02897f, RMH2O = 0.018016f, CGSNOW = 2090.0f, CSICE = 2.100e3f, CSWAT = 4.218e3f;
+constexpr float DLIQ = 1000.0f, DICE = 921.0f, TETENA = 6.106f, TETENB = 17.27f, TETENC = 237.3f;
+constexpr float VONK = 0.40f, A33 = 1.25f, CSW = 0.50f, CTL = 0.40f, APOL = 0.70f, PRANDT = 0.71f;
+constexpr float CRD = 0.3f, CSD = 0.003f, CCD = 15.0f, CCW_C = 2.0f, USUHM = 0.3f, ZETNEG = -15.0f;
+constexpr float ZETPOS = 1.0f, ZDLIN = 1.0f, UMIN = 0.1f, GAM0 = 28.0e-6f, GAM1 = 0.0509f, GAM2 = 0.0010f;
+constexpr float RGBWC = 1.32f, RGSWC = 1.57f, TREFK = 298.2f, LAI_THRESH = 0.001f, RAD_THRESH = 0.001f;
+constexpr float COSZEN_TOLS = 1.0e-4f, PI_C = 3.1415927f, MAX_GLACIER_SNOWD = 1100.0f, SNOW_CCNSW = 2.0f;
+constexpr float MAX_SSDN = 750.0f, MAX_SCONDS = 2.51f, FROZEN_LIMIT = 0.85f, SNMIN = 1.0f;
+constexpr float GW0 = 0.308f, GW1 = 0.514f, GW2 = 0.178f;
+constexpr int LAKES = 16, ICE_SURF = 17, ICE_SOIL = 9, MAXITER = 20, NITER = 4;
+
+// Number / order of the optional per-tile diagnostics (debug output).
+#define CG_NDIAG 59
+// Headline outputs written every step: fe fh fgpp frday tv rnet ga trad
+#define CG_NOUT 8
+
+// Device view of every per-tile array ([layer][ld] structure of arrays).
+struct CgDev {
+  int mp, ld;
+  // static per tile (device slot order; tile_id = the caller's tile index)
+  const int* tile_id;
+  const uint8_t* iveg;
+  const uint8_t* isoilm;
+  const float* vlai;
+  const float* lat;
+  const float* lonphase;
+  const float* tbase;
+  const float* swscale;
+  // prognostic state
+  double* wb;        // [6]
+  double* wbice;     // [6]
+  double* gammzz1;   // layer-1 heat capacity (J/m2/K)
+  float* tgg;        // [6]
+  float* tggsn;      // [3]
+  float* ssdn;       // [3]
+  float* smass;      // [3]
+  float* sdepth;     // [3]
+  uint8_t* flags;    // bit0 isflag, bit1 soil_snow first call pending
+  float* snowd;
+  float* ssdnn;
+  float* snage;
+  float* pudsto;
+  float* owetfac;
+  float* rtsoil;
+  float* tss;
+  float* wb_lake;
+  float* wbtot1;
+  float* wbtot2;
+  float* cansto;
+  float* cplant;     // [3]
+  float* csoil;      // [2]
+  double* owb;
+  double* ebal_tot;
+  double* wbal_tot;
+  // outputs
+  float* out;              // [CG_NOUT]
+  float* diag;             // [CG_NDIAG] or null
+  float* work_a;           // phase A -> B, C handoff record
+  float* work_b;           // phase B -> C handoff record
+  const float* forcing_in; // [CG_NFORC] host-provided forcing, or null (synthetic)
+  float* forcing_out;      // [CG_NFORC] copy of the forcing used, or null
+  unsigned int* status;    // bit0: non-finite output seen
+};
+
+struct CgTables {
+  CgPftTable pft;
+  CgSoilTable soil;
+};
+
+__device__ __forceinline__ float sqf(float x) { return x * x; }
+__device__ __forceinline__ float pow4(float x) { float y = x * x; return y * y; }
+__device__ __forceinline__ float fsignf(float a, float b) { return signbit(b) ? -fabsf(a) : fabsf(a); }
+
+// cbl_qsat.F90:46-50 (tair in deg C)
+__device__ __forceinline__ float qsatfjh(float tair, float pmb) {
+  return (RMH2O / RMAIR) * (TETENA * expf(TETENB * tair / (TETENC + tair))) / pmb;
+}
+// cbl_friction_vel.F90:112-166
+__device__ __forceinline__ float psim(float zeta) {
+  const float gu = 16.0f, b = 0.667f, xc = 5.0f, d = 0.35f;
+  float z = 0.5f + fsignf(0.5f, zeta);
+  float stable = -zeta - b * (zeta - xc / d) * expf(-d * zeta) - b * xc / d;
+  float x = sqrtf(sqrtf(1.0f + gu * fabsf(zeta)));
+  float unstable = logf((1.0f + x * x) * sqf(1.0f + x) / 8.0f) - 2.0f * atanf(x) + PI_C * 0.5f;
+  return z * stable + (1.0f - z) * unstable;
+}
+// cbl_friction_vel.F90:168-221
+__device__ __forceinline__ float psis(float zeta) {
+  const float gu = 16.0f, b = 0.667f, c = 5.0f, d = 0.35f;
+  float z = 0.5f + fsignf(0.5f, zeta);
+  float stz = fmaxf(0.f, zeta);
+  float w = 1.f + 2.f / 3.f * stz;
+  float stable = -(w * sqrtf(w)) - b * (stz - c / d) * expf(-d * stz) - b * c / d + 1.f;
+  float y = sqrtf(1.0f + gu * fabsf(zeta));
+  float unstable = 2.0f * logf((1.f + y) * 0.5f);
+  return z * stable + (1.0f - z) * unstable;
+}
+
+// Positive root of a*x^2 + b*x + c = 0 as the reference writes it,
+// (-b + sqrt(max(0, b^2 - 4ac))) / (2a), evaluated without cancellation:
+// for b > 0 the algebraically identical 2c / (-b - sqrt(...)) is used.
+__device__ __forceinline__ float qroot(float a, float b, float c) {
+  float disc = sqrtf(fmaxf(0.0f, b * b - 4.0f * c * a));
+  if (b > 0.0f) {
+    float den = -b - disc;
+    return (den != 0.0f) ? (2.0f * c) / den : 0.0f;
+  }
+  return (-b + disc) / (2.0f * a);
+}
+
+// cbl_photosynthesis.F90:52-213 for one leaf (masks applied by the caller)
+__device__ __forceinline__ float photosynthesis_leaf(float csx, float cx1, float cx2, float gswmin, float rdx,
+                                                     float vcmxt3, float vcmxt4, float vx3, float vx4, float gs_coeff,
+                                                     float fwsoil) {
+  const float effc4 = 4000.0f;
+  const float gmf = gswmin * fwsoil / RGSWC;
+  float anrubisco = 0.f, anrubp, ansink = 0.f, ci, coef0, coef1, coef2;
+  coef2 = gmf + gs_coeff * (vcmxt3 - (rdx - vcmxt4));
+  coef1 = (1.0f - csx * gs_coeff) * (vcmxt3 + vcmxt4 - rdx) + gmf * (cx1 - csx) -
+          gs_coeff * (vcmxt3 * cx2 / 2.0f + cx1 * (rdx - vcmxt4));
+  coef0 = -(1.0f - csx * gs_coeff) * (vcmxt3 * cx2 / 2.0f + cx1 * (rdx - vcmxt4)) - gmf * cx1 * csx;
+  if (fabsf(coef2) > 1.0e-9f && fabsf(coef1) < 1.0e-9f) anrubisco = 99999.0f;
+  if (fabsf(coef2) < 1.e-9f && fabsf(coef1) >= 1e-9f) {
+    ci = fmaxf(0.0f, -coef0 / coef1);
+    anrubisco = vcmxt3 * (ci - cx2 / 2.0f) / (ci + cx1) + vcmxt4 - rdx;
+  }
+  if (fabsf(coef2) >= 1.e-9f) {
+    ci = fmaxf(0.0f, qroot(coef2, coef1, coef0));
+    anrubisco = vcmxt3 * (ci - cx2 / 2.0f) / (ci + cx1) + vcmxt4 - rdx;
+  }
+  coef2 = gmf + gs_coeff * (vx3 - (rdx - vx4));
+  coef1 = (1.0f - csx * gs_coeff) * (vx3 + vx4 - rdx) + gmf * (cx2 - csx) - gs_coeff * (vx3 * cx2 / 2.0f + cx2 * (rdx - vx4));
+  coef0 = -(1.0f - csx * gs_coeff) * (vx3 * cx2 / 2.0f + cx2 * (rdx - vx4)) - gmf * cx2 * csx;
+  anrubp = 99999.0f;
+  if (fabsf(coef2) < 1.e-9f && fabsf(coef1) >= 1.e-9f) {
+    ci = fmaxf(0.0f, -coef0 / coef1);
+    anrubp = vx3 * (ci - cx2 / 2.0f) / (ci + cx2) + vx4 - rdx;
+  }
+  if (fabsf(coef2) >= 1.e-9f) {
+    ci = fmaxf(0.0f, qroot(coef2, coef1, coef0));
+    anrubp = vx3 * (ci - cx2 / 2.0f) / (ci + cx2) + vx4 - rdx;
+  }
+  coef2 = gs_coeff;
+  coef1 = gmf + gs_coeff * (rdx - 0.5f * vcmxt3) + effc4 * vcmxt4 - gs_coeff * csx * effc4 * vcmxt4;
+  coef0 = -gmf * csx * effc4 * vcmxt4 + (rdx - 0.5f * vcmxt3) * gmf;
+  if (fabsf(coef2) < 1.0e-9f && fabsf(coef1) < 1.0e-9f) ansink = 99999.0f;
+  if (fabsf(coef2) < 1.e-9f && fabsf(coef1) >= 1.e-9f) ansink = -coef0 / coef1;
+  if (fabsf(coef2) >= 1.e-9f) ansink = qroot(coef2, coef1, coef0);
+  return fminf(fminf(anrubisco, anrubp), ansink);
+}
+
+// cbl_dryLeaf.F90:779-877
+__device__ __forceinline__ float ej3x(float parx, float alpha, float convex, float x) {
+  float s = alpha * parx + x;
+  return fmaxf(0.0f, 0.25f * ((s - sqrtf(s * s - 4.0f * convex * alpha * parx * x)) / (2.0f * convex)));
+}
+__device__ __forceinline__ float ej4x(float parx, float alpha, float convex, float x) {
+  float s = alpha * parx + x;
+  return fmaxf(0.0f, (s - sqrtf(s * s - 4.0f * convex * alpha * parx * x)) / (2.0f * convex));
+}
+__device__ __forceinline__ float xvcmxt4(float x) {
+  return exp2f(0.1f * x - 2.5f) / ((1.0f + expf(0.3f * (13.0f - x))) * (1.0f + expf(0.3f * (x - 36.0f))));
+}
+__device__ __forceinline__ float xvcmxt3(float x) {
+  float num = 1.17461f * expf((73637.0f / (RGAS * TREFK)) * (1.f - TREFK / x));
+  float den = 1.0f + expf((486.0f * x - 149252.0f) / (RGAS * x));
+  return fmaxf(0.0f, num / den);
+}
+__device__ __forceinline__ float xejmxt3(float x) {
+  float num = 1.16715f * expf((50300.0f / (RGAS * TREFK)) * (1.f - TREFK / x));
+  float den = 1.0f + expf((495.0f * x - 152044.0f) / (RGAS * x));
+  return fmaxf(0.0f, num / den);
+}
+
+// FP64 reciprocal seeded from the FP32 one and refined by one Newton step
+// (relative error ~1e-14), so each Thomas row costs a few FP64 FMAs.
+__device__ __forceinline__ double drcp(double d) {
+  double r = (double)(1.0f / (float)d);
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+
+// Tridiagonal solve (cbl_trimb.F90:17-53) in FP64, n <= 9 rows, rhs in place.
+template <int N>
+__device__ __forceinline__ void trimb(const double* a, const double* b, const double* c, double* rhs) {
+  double e[N], g[N];
+  double t = drcp(b[0]);
+  e[0] = c[0] * t;
+  g[0] = rhs[0] * t;
+#pragma unroll
+  for (int k = 1; k < N - 1; ++k) {
+    t = drcp(b[k] - a[k] * e[k - 1]);
+    e[k] = c[k] * t;
+    g[k] = (rhs[k] - a[k] * g[k - 1]) * t;
+  }
+  rhs[N - 1] = (rhs[N - 1] - a[N - 1] * g[N - 2]) * drcp(b[N - 1] - a[N - 1] * e[N - 2]);
+#pragma unroll
+  for (int k = N - 2; k >= 0; --k) rhs[k] = g[k] - e[k] * rhs[k + 1];
+}
+
+}  // namespace cg

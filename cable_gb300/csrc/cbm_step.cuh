@@ -1,0 +1,1476 @@
+// The cbm() timestep as three kernels per step, one thread per tile in each:
+//   phase A  ruff_resist, define_air, masks, init_radiation, albedo,
+//            Surf_wetness_fact, radiation
+//   phase B  define_canopy: 4 Monin-Obukhov iterations of dryLeaf / wetLeaf /
+//            within-canopy / soil evaporation, screen diagnostics, canopy
+//            water budget, soil-coupling derivatives, energy balance
+//   phase C  soil_snow (snow layering, FP64 heat and moisture solves),
+//            snow_aging, carbon, water balance
+// Splitting keeps each kernel's code and register footprint small enough
+// for the instruction cache and for several resident warps per scheduler;
+// the phases hand over per-tile records through HBM (structure of arrays).
+#pragma once
+#include "cbm_physics.cuh"
+
+namespace cg {
+
+struct StepParams {
+  int ktau;          // 1-based step counter of the run (mass_balance init / totals)
+  float dels;        // step length (s)
+  int medlyn;        // gs_switch: 0 leuning, 1 medlyn
+  CgForcingSpec forc;
+  int step_index;    // 0-based counter for the synthetic forcing
+};
+
+__device__ __forceinline__ float ldf(const float* p, int i) { return __ldg(p + i); }
+
+
+// Phase A record (per tile, [CG_NA][ld]): forcing, roughness, air, radiation,
+// interception and the soil liquid water seen by dryLeaf.
+#define CG_NA 52
+// Phase B record (per tile, [CG_NB][ld]): what soil_snow, carbon and the
+// water balance need from define_canopy.
+#define CG_NB 20
+
+template <bool kDiag>
+__device__ __noinline__ void phase_a(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
+  const int ld = D.ld;
+  const float dels = P.dels;
+  // ---------------------------------------------------------------- static
+  const int iveg = D.iveg[t], isoilm = D.isoilm[t];
+  const int v = iveg - 1, so = isoilm - 1;
+  const CgPftTable& V = T->pft;
+  const CgSoilTable& S = T->soil;
+  const float vlai = (iveg >= 14) ? 0.0f : D.vlai[t];   // cable_serial.F90:575
+  const float hc = ldf(V.hc, v), canst1 = ldf(V.canst1, v), dleaf = ldf(V.dleaf, v), extkn = ldf(V.extkn, v);
+  const float xfang = ldf(V.xfang, v);
+  const float refl[2] = {ldf(V.refl1, v), ldf(V.refl2, v)}, taul[2] = {ldf(V.taul1, v), ldf(V.taul2, v)};
+  float froot[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
+  const float ssat = ldf(S.ssat, so), sfc = ldf(S.sfc, so), swilt = ldf(S.swilt, so), css = ldf(S.css, so);
+  const float rhosoil = ldf(S.rhosoil, so);
+  float zse[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) zse[k] = S.zse[k];
+
+  // ---------------------------------------------------------------- state
+  double wb[CG_MS], wbice[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) { wb[k] = D.wb[k * ld + t]; wbice[k] = D.wbice[k * ld + t]; }
+  float tgg[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) tgg[k] = D.tgg[k * ld + t];
+  float tggsn[3], ssdn[3], smass[3], sdepth[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    tggsn[k] = D.tggsn[k * ld + t]; ssdn[k] = D.ssdn[k * ld + t];
+    smass[k] = D.smass[k * ld + t]; sdepth[k] = D.sdepth[k * ld + t];
+  }
+  uint8_t flags = D.flags[t];
+  int isflag = flags & 1;
+  bool first_call = (flags & 2) != 0;
+  double gammzz1 = D.gammzz1[t];
+  float snowd = D.snowd[t], ssdnn = D.ssdnn[t], snage = D.snage[t], pudsto = D.pudsto[t];
+  const float owetfac_in = D.owetfac[t];
+  const float ortsoil = D.rtsoil[t];
+  float wb_lake = D.wb_lake[t], wbtot1 = D.wbtot1[t], wbtot2 = D.wbtot2[t];
+  const float oldcansto = D.cansto[t];
+  const float pudsmx = 0.0f;
+
+  // ---------------------------------------------------------------- forcing
+  float F[CG_NFORC];
+  if (D.forcing_in) {
+#pragma unroll
+    for (int i = 0; i < CG_NFORC; ++i) F[i] = D.forcing_in[i * ld + t];
+  } else {
+    cg_forcing(P.forc, D.lat[t], D.lonphase[t], D.tbase[t], D.swscale[t], (uint32_t)D.tile_id[t],
+               (uint32_t)P.step_index, F);
+  }
+  if (D.forcing_out) {
+#pragma unroll
+    for (int i = 0; i < CG_NFORC; ++i) D.forcing_out[i * ld + t] = F[i];
+  }
+  const float fsd0 = F[CGF_FSD1], fsd1 = F[CGF_FSD2], fld = F[CGF_FLD], precip = F[CGF_PRECIP];
+  const float precip_sn = F[CGF_PRECIP_SN], tk = F[CGF_TK], pmb = F[CGF_PMB], ua = F[CGF_UA], qv = F[CGF_QV];
+  const float ca = F[CGF_CA], coszen = F[CGF_COSZEN], doy = F[CGF_DOY];
+  const float tvrad = tk;
+
+  // wbliq as left by the previous soil_snow call
+  float wbliq0[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) wbliq0[k] = (float)(wb[k] - wbice[k]);
+
+  // lakes top-layer fix (cbl_model_driver_offline.F90:116-121)
+  if (iveg == LAKES && wb[0] < (double)sfc) {
+    wbtot1 = (float)wb[0] * DLIQ * zse[0];
+    wb[0] = sfc;
+    wbtot2 = (float)wb[0] * DLIQ * zse[0];
+  }
+  wb_lake = wb_lake + fmaxf(wbtot2 - wbtot1, 0.f);
+
+  // ---------------------------------------------------------------- ruff_resist
+  // cable_roughness.F90:64-332, roughnessHGT_effLAI_cbl.F90:42-149
+  float hruff, vlaiw, z0soilsn, z0m, disp, zref_uv, zref_tq, zruffs, rt0us, rt1usa, rt1usb, usuh, coexp;
+  {
+    float den_eff = fmaxf(100.0f, ssdnn);
+    hruff = fmaxf(1.0e-6f, hc - (1.2f * snowd / den_eff));
+    vlaiw = vlai * (hruff / fmaxf(0.01f, hc));
+    float z0soil = 0.0009f * fminf(1.0f, vlaiw) + 1.e-4f;
+    z0soilsn = z0soil;
+    if (snowd > 0.01f) z0soilsn = fmaxf(1.e-7f, z0soil - z0soil * fminf(snowd, 10.f) / 10.f);
+    if (snowd > 0.01f && iveg == ICE_SURF) z0soilsn = fmaxf(z0soilsn, 1.e-4f);
+    usuh = fminf(sqrtf(CSD + CRD * (vlaiw * 0.5f)), USUHM);
+    float xx = sqrtf(CCD * fmaxf(vlaiw * 0.5f, 0.0005f));
+    float dh = 1.0f - (1.0f - expf(-xx)) / xx;
+    coexp = usuh / (VONK * CCW_C * (1.0f - dh));
+    if (vlaiw <= LAI_THRESH || hruff < z0soilsn) {
+      z0m = z0soilsn; rt0us = 0.f; disp = 0.f;
+      zref_uv = fmaxf(fmaxf(3.5f + z0m, 40.0f), hruff - disp);
+      zref_tq = zref_uv;
+      zruffs = 0.f; rt1usa = 0.f; rt1usb = 0.f;
+    } else {
+      disp = dh * hruff;
+      z0m = ((1.0f - dh) * expf(logf(CCW_C) - 1.f + 1.f / CCW_C - VONK / usuh)) * hruff;
+      zref_uv = fmaxf(fmaxf(3.5f + z0m, 40.0f), hruff - disp);
+      zref_tq = zref_uv;
+      const float e2 = expf(2.f * CSW * vlaiw);
+      float term2 = expf(2.f * CSW * vlaiw * (1.f - disp / hruff));
+      float term3 = A33 * A33 * CTL * 2.f * CSW * vlaiw;
+      float term5 = fmaxf((2.f / 3.f) * hruff / disp, 1.0f);
+      rt0us = term5 * (ZDLIN * logf(ZDLIN * disp / z0soilsn) + (1.f - ZDLIN)) * (e2 - term2) / term3;
+      zruffs = disp + hruff * A33 * A33 * CTL / VONK / term5;
+      rt1usa = term5 * (term2 - 1.0f) / term3;
+      rt1usb = term5 * (fminf(zref_tq + disp, zruffs) - hruff) / (A33 * A33 * CTL * hruff);
+      rt1usb = fmaxf(rt1usb, 0.0f);
+    }
+  }
+  const float rghlai = vlaiw;
+
+  // define_air (cable_air.F90:51-97) with tvair = tk
+  float rho, cmolar, epsi, visc, psyc, dsatdk;
+  const float rlam = HL;
+  {
+    float tc = tk - TFRZ;
+    float es = TETENA * expf(TETENB * tc / (TETENC + tc));
+    cmolar = pmb * 100.0f / (RGAS * tk);
+    rho = fminf(1.3f, RMAIR * cmolar);
+    epsi = (rlam / CAPP) * (RMH2O / RMAIR) * es * TETENB * TETENC / sqf(TETENC + tc) / pmb;
+    visc = 1e-5f * fmaxf(1.0f, 1.35f + 0.0092f * tc);
+    psyc = pmb * 100.0f * CAPP * RMAIR / rlam / RMH2O;
+    dsatdk = 100.0f * (TETENA * TETENB * TETENC) / sqf(tc + TETENC) * expf(TETENB * tc / (tc + TETENC));
+  }
+  const bool veg_mask = vlaiw > LAI_THRESH;
+  const bool sunlit_veg = veg_mask && (fsd0 + fsd1) > RAD_THRESH;
+
+  // ---------------------------------------------------------------- init_radiation + albedo
+  // cbl_init_radiation.F90:30-392, cbl_spitter.F90, cbl_rhoch.F90,
+  // cbl_albedo.F90:56-386, cbl_snow_albedo.F90:36-161
+  float extkb, extkd, extkbm[2], extkdm[2], fbeam[2], albsoilsn[2], reffdf[2], reffbm[2], cexpkbm[2], cexpkdm[2];
+  float albedo[2];
+  {
+    float xphi1 = 0.f, xphi2 = 0.f;
+    if (veg_mask) {
+      xphi1 = 0.5f - xfang * (0.633f + 0.33f * xfang);
+      xphi2 = 0.877f * (1.0f - 2.0f * xphi1);
+    }
+    const float cos3[3] = {0.96592583f, 0.70710678f, 0.25881905f};   // cos(15, 45, 75 deg)
+    float xk[3];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) xk[b] = veg_mask ? xphi1 / cos3[b] + xphi2 : 0.0f;
+    float c1[2], rhoch[2];
+#pragma unroll
+    for (int b = 0; b < 2; ++b) { c1[b] = sqrtf(1.0f - taul[b] - refl[b]); rhoch[b] = (1.0f - c1[b]) / (1.0f + c1[b]); }
+    extkb = 0.5f; extkd = 0.7f;
+    if (veg_mask)
+      extkd = -logf(GW0 * expf(-xk[0] * vlaiw) + GW1 * expf(-xk[1] * vlaiw) + GW2 * expf(-xk[2] * vlaiw)) / vlaiw;
+    if (veg_mask && coszen > COSZEN_TOLS * 1e-2f) extkb = xphi1 / coszen + xphi2;
+    if (coszen < COSZEN_TOLS * 1e-2f) extkb = 1.0e5f;
+    if (fabsf(extkb - extkd) < 0.001f) extkb = extkd + 0.001f;
+#pragma unroll
+    for (int b = 0; b < 2; ++b) { extkbm[b] = veg_mask ? extkb * c1[b] : 0.0f; extkdm[b] = extkd * c1[b]; }
+    // spitter (cbl_spitter.F90:36-76)
+    {
+      float fsd = fsd0 + fsd1;
+      float tmpr = 0.847f + coszen * (1.04f * coszen - 1.61f);
+      float tmpk = (1.47f - tmpr) / 1.66f;
+      float tmprat = 0.0f;
+      if (coszen > 1.0e-10f && fsd > 10.0f)
+        tmprat = fsd / (1370.0f * (1.0f + 0.033f * cosf(2.0f * PI_C * ((float)(int)doy - 10.0f) / 365.0f)) * coszen);
+      float fb = 0.0f;
+      if (tmprat > 0.22f) fb = 6.4f * sqf(tmprat - 0.22f);
+      if (tmprat > 0.35f) fb = fminf(1.66f * tmprat - 0.4728f, 1.0f);
+      if (tmprat > tmpk) fb = fmaxf(1.0f - tmpr, 0.0f);
+      if (coszen < COSZEN_TOLS * 1e2f) fb = 0.0f;
+      fbeam[0] = fb; fbeam[1] = fb;
+    }
+    // surface_albedosn
+    float soilalb = ldf(S.albsoil_vis, so);
+    if (iveg == LAKES) soilalb = -0.022f * (fminf(275.0f, fmaxf(260.0f, tgg[0])) - 260.0f) + 0.45f;
+    if (snowd > 1.0f && iveg == LAKES) soilalb = 0.85f;
+    float sfact = 0.68f;
+    if (soilalb <= 0.14f) sfact = 0.5f;
+    else if (soilalb <= 0.20f) sfact = 0.62f;
+    albsoilsn[1] = 2.0f * soilalb / (1.0f + sfact);
+    albsoilsn[0] = sfact * albsoilsn[1];
+    float snrat = 0.f, alir = 0.f, alv = 0.f;
+    if (snowd > 1.0f) {
+      float tmp = snowd / fmaxf(ssdnn, 200.0f);
+      snrat = fminf(1.0f, tmp / (tmp + 0.1f));
+      float fage = 1.0f - 1.0f / (1.0f + snage);
+      tmp = fmaxf(0.17365f, coszen);
+      float fzenm = fmaxf(0.0f, (tmp > 0.5f) ? 0.0f : 1.5f / (1.0f + 4.0f * tmp) - 0.5f);
+      tmp = 0.95f * (1.0f - 0.2f * fage);
+      alv = 0.4f * fzenm * (1.0f - tmp) + tmp;
+      tmp = 0.70f * (1.0f - 0.5f * fage);
+      alir = 0.4f * fzenm * (1.0f - tmp) + tmp;
+    }
+    albsoilsn[1] = fminf(0.70f, (1.0f - snrat) * albsoilsn[1] + snrat * alir);
+    albsoilsn[0] = fminf(0.95f, (1.0f - snrat) * albsoilsn[0] + snrat * alv);
+    if (isoilm == ICE_SOIL) { albsoilsn[0] = 0.95f - 0.05f; albsoilsn[1] = 0.70f - 0.05f; }
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      float rhocbm = veg_mask ? 2.0f * extkb / (extkb + extkd) * rhoch[b] : 0.0f;
+      float rhocdf = rhoch[b] * 2.0f * (GW0 * xk[0] / (xk[0] + extkd) + GW1 * xk[1] / (xk[1] + extkd) +
+                                        GW2 * xk[2] / (xk[2] + extkd));
+      cexpkbm[b] = veg_mask ? expf(-fminf(extkbm[b] * vlaiw, 20.0f)) : 0.0f;
+      cexpkdm[b] = expf(-(extkdm[b] * vlaiw));
+      reffdf[b] = albsoilsn[b]; reffbm[b] = albsoilsn[b]; albedo[b] = albsoilsn[b];
+      if (veg_mask) {
+        reffdf[b] = rhocdf + (albsoilsn[b] - rhocdf) * sqf(cexpkdm[b]);
+        reffbm[b] = rhocbm + (albsoilsn[b] - rhocbm) * sqf(cexpkbm[b]);
+        albedo[b] = (1.0f - fbeam[b]) * reffdf[b] + fbeam[b] * reffbm[b];
+      }
+    }
+  }
+
+  // ================================================================ define_canopy
+  // cable_canopy.F90:10-1048
+  float cansto = oldcansto;
+  const float cansat = canst1 * vlaiw;
+  // Surf_wetness_fact (cbl_SurfaceWetness.F90:10-79)
+  float through, fwet, wetfac;
+  {
+    float upper = 4.0f * fminf(dels, 1800.0f) / (60.0f * 1440.0f);
+    float ftemp = fminf(precip - precip_sn, upper);
+    upper = fmaxf(cansat - cansto, 0.0f);
+    float wcint = (ftemp > 0.0f && tk > TFRZ) ? fminf(upper, ftemp) : 0.0f;
+    through = precip_sn + fminf(precip - precip_sn, fmaxf(0.0f, precip - precip_sn - wcint));
+    cansto = cansto + wcint;
+    fwet = fmaxf(0.0f, fminf(0.9f, 0.8f * cansto / fmaxf(cansat, 0.01f)));
+    // initialize_wetfac (cbl_init_wetfac_mod.F90:9-116)
+    float wilting_pt = swilt / 2.0f;
+    float den = fmaxf(0.0830f, sfc - wilting_pt);
+    wetfac = fmaxf(0.0f, fminf(1.0f, ((float)wb[0] - wilting_pt) / den));
+    if (wbice[0] > 0.0) {
+      float ice_ratio = (float)((wbice[0] / wb[0]) * (wbice[0] / wb[0]));
+      float ice_factor = fmaxf(0.5f, 1.0f - fminf(0.2f, ice_ratio));
+      wetfac = wetfac * ice_factor;
+    }
+    if (snowd > 0.1f) wetfac = 0.9f;
+    if (iveg == LAKES) wetfac = (tk >= TFRZ + 5.f) ? 1.0f : 0.7f;
+    wetfac = 0.5f * (wetfac + owetfac_in);
+  }
+  // working variables of the canopy iteration
+  float tvair = tk, qvair = qv, tv = tk;
+  float qstvair = qsatfjh(tvair - TFRZ, pmb);
+  float dva = (qstvair - qvair) * RMAIR / RMH2O * pmb * 100.0f;
+  float dsx = fmaxf(dva, 0.0f);
+  float tlfx = tk, tlfy = tk;
+  float csx[2] = {ca, ca};
+  float gswx[2] = {1e-3f, 1e-3f};
+  float gbhu[2] = {1e-3f, 1e-3f}, gbhf[2] = {1e-3f, 1e-3f};
+  float evapfbl[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) evapfbl[k] = 0.0f;
+  float tss = (float)(1 - isflag) * tgg[0] + (float)isflag * tggsn[0];
+  const float tss4 = pow4(tss);
+  // radiation (cbl_radiation.F90:30-218)
+  float transd, transb, flws, qssabs, fvlai[2], scalex[2], rniso[2], gradis[2], qcan_par[2], swcan;
+  {
+    float cf2n = expf(-extkn * vlaiw);
+    transd = veg_mask ? expf(-extkd * vlaiw) : 1.0f;
+    transb = expf(-fminf(extkb * vlaiw, 30.f));
+    float flpwb = SBOLTZ * pow4(tvrad);
+    float flwv = EMLEAF * flpwb;
+    flws = SBOLTZ * EMSOIL * pow4(tss);
+    float emair = fld / flpwb;
+    float qlw[2] = {0.f, 0.f};
+    gradis[0] = 0.f; gradis[1] = 0.f;
+    if (veg_mask) {
+      gradis[0] = (4.0f * EMLEAF / (CAPP * rho)) * flpwb / tvrad * extkd *
+                  ((1.0f - transb * transd) / (extkb + extkd) + (transd - transb) / (extkb - extkd));
+      gradis[1] = (8.0f * EMLEAF / (CAPP * rho)) * flpwb / tvrad * extkd * (1.0f - transd) / extkd - gradis[0];
+      qlw[0] = (flws - flwv) * extkd * (transd - transb) / (extkb - extkd) +
+               (emair - EMLEAF) * extkd * flpwb * (1.0f - transd * transb) / (extkb + extkd);
+      qlw[1] = (1.0f - transd) * (flws + fld - 2.0f * flwv) - qlw[0];
+    }
+    gradis[0] = fmaxf(1.0e-3f, cmolar * gradis[0]);
+    gradis[1] = fmaxf(1.0e-3f, cmolar * gradis[1]);
+    float qsw[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    if (sunlit_veg) {
+      const float fsdb[2] = {fsd0, fsd1};
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        float cf1 = (1.0f - transb * cexpkdm[b]) / (extkb + extkdm[b]);
+        float cf3 = (1.0f - transb * cexpkbm[b]) / (extkb + extkbm[b]);
+        float direct = fbeam[b] * (1.0f - taul[b] - refl[b]) * extkb *
+                       ((1.f - transb) / extkb - (1.f - transb * transb) / (extkb + extkb));
+        qsw[0][b] = fsdb[b] * ((1.0f - fbeam[b]) * (1.0f - reffdf[b]) * extkdm[b] * cf1 +
+                               fbeam[b] * (1.0f - reffbm[b]) * extkbm[b] * cf3 + direct);
+        qsw[1][b] = fsdb[b] * ((1.0f - fbeam[b]) * (1.0f - reffdf[b]) * extkdm[b] * ((1.0f - cexpkdm[b]) / extkdm[b] - cf1) +
+                               fbeam[b] * (1.f - reffbm[b]) * extkbm[b] * ((1.0f - cexpkbm[b]) / extkbm[b] - cf3) - direct);
+      }
+      qssabs = fsd0 * (fbeam[0] * (1.f - reffbm[0]) * expf(-fminf(extkbm[0] * vlaiw, 20.f)) +
+                       (1.f - fbeam[0]) * (1.f - reffdf[0]) * expf(-fminf(extkdm[0] * vlaiw, 20.f))) +
+               fsd1 * (fbeam[1] * (1.f - reffbm[1]) * cexpkbm[1] + (1.f - fbeam[1]) * (1.f - reffdf[1]) * cexpkdm[1]);
+      scalex[0] = (1.0f - transb * cf2n) / (extkb + extkn);
+      fvlai[0] = (1.0f - transb) / extkb;
+      fvlai[1] = vlaiw - fvlai[0];
+    } else {
+      qssabs = (1.0f - albsoilsn[0]) * fsd0 + (1.0f - albsoilsn[1]) * fsd1;
+      scalex[0] = 0.f; fvlai[0] = 0.f; fvlai[1] = vlaiw;
+    }
+    scalex[1] = (1.0f - cf2n) / extkn - scalex[0];
+    qcan_par[0] = qsw[0][0]; qcan_par[1] = qsw[1][0];
+    rniso[0] = qsw[0][0] + qsw[0][1] + qlw[0];
+    rniso[1] = qsw[1][0] + qsw[1][1] + qlw[1];
+    swcan = qsw[0][0] + qsw[1][0] + qsw[0][1] + qsw[1][1];
+  }
+  const float sum_rad_rniso = rniso[0] + rniso[1];
+  const float sum_rad_gradis = gradis[0] + gradis[1];
+
+  (void)sunlit_veg;
+  {
+    const float rec[CG_NA] = {tk, qv, pmb, ua, fld, ca, precip, precip_sn, vlaiw, hruff, z0soilsn, z0m, disp, zref_uv, zruffs, rt0us, rt1usa, rt1usb, usuh, coexp, rho, cmolar, epsi, visc, psyc, dsatdk, extkb, transd, flws, qssabs, fvlai[0], fvlai[1], scalex[0], scalex[1], rniso[0], rniso[1], gradis[0], gradis[1], qcan_par[0], qcan_par[1], swcan, cansto, through, fwet, wetfac, tss, wbliq0[0], wbliq0[1], wbliq0[2], wbliq0[3], wbliq0[4], wbliq0[5]};
+#pragma unroll
+    for (int i = 0; i < CG_NA; ++i) D.work_a[i * ld + t] = rec[i];
+  }
+  if (iveg == LAKES) D.wb[t] = wb[0];
+  D.wb_lake[t] = wb_lake; D.wbtot1[t] = wbtot1; D.wbtot2[t] = wbtot2;
+  if (kDiag) {
+    D.diag[29 * ld + t] = albedo[0]; D.diag[30 * ld + t] = albedo[1]; D.diag[31 * ld + t] = transd;
+    D.diag[47 * ld + t] = qssabs; D.diag[48 * ld + t] = sum_rad_rniso; D.diag[49 * ld + t] = vlaiw;
+  }
+}
+
+template <bool kDiag>
+__device__ __noinline__ void phase_b(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
+  const int ld = D.ld;
+  const float dels = P.dels;
+  const int iveg = D.iveg[t], isoilm = D.isoilm[t];
+  const int v = iveg - 1, so = isoilm - 1;
+  (void)isoilm;
+  const CgPftTable& V = T->pft;
+  const CgSoilTable& S = T->soil;
+  const float dleaf = ldf(V.dleaf, v);
+  float froot[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
+  const float sfc = ldf(S.sfc, so), swilt = ldf(S.swilt, so);
+  float zse[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) zse[k] = S.zse[k];
+  // phase A record
+  const float* WA = D.work_a;
+  auto A = [&](int i) { return WA[i * ld + t]; };
+  const float tk = A(0), qv = A(1), pmb = A(2), ua = A(3), fld = A(4), ca = A(5);
+  const float vlaiw = A(8), hruff = A(9), z0soilsn = A(10), z0m = A(11), disp = A(12), zref_uv = A(13);
+  const float zref_tq = zref_uv, zruffs = A(14), rt0us = A(15), rt1usa = A(16), rt1usb = A(17), usuh = A(18);
+  const float coexp = A(19), rghlai = vlaiw;
+  const float rho = A(20), cmolar = A(21), epsi = A(22), visc = A(23), psyc = A(24), dsatdk = A(25);
+  const float rlam = HL;
+  const float extkb = A(26), transd = A(27), flws = A(28), qssabs = A(29);
+  const float fvlai[2] = {A(30), A(31)}, scalex[2] = {A(32), A(33)}, rniso[2] = {A(34), A(35)};
+  const float gradis[2] = {A(36), A(37)}, qcan_par[2] = {A(38), A(39)};
+  const float swcan = A(40);
+  float cansto = A(41), through = A(42);
+  const float fwet = A(43);
+  float wetfac = A(44);
+  const float tss = A(45);
+  float wbliq0[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) wbliq0[k] = A(46 + k);
+  const float cansat = ldf(V.canst1, v) * vlaiw;
+  const bool veg_mask = vlaiw > LAI_THRESH;
+  const float sum_rad_rniso = rniso[0] + rniso[1];
+  const float sum_rad_gradis = gradis[0] + gradis[1];
+  const float tss4 = pow4(tss);
+  const float tvrad = tk;
+  // state read by define_canopy
+  const float oldcansto = D.cansto[t], ortsoil = D.rtsoil[t], snowd = D.snowd[t], pudsto = D.pudsto[t];
+  const float tgg[1] = {D.tgg[t]};
+  const double wb[1] = {D.wb[t]}, wbice[1] = {D.wbice[t]};
+  const float pudsmx = 0.0f;
+  // working variables of the canopy iteration (cable_canopy.F90:183-215)
+  float tvair = tk, qvair = qv, tv = tk;
+  float qstvair = qsatfjh(tvair - TFRZ, pmb);
+  float dva = (qstvair - qvair) * RMAIR / RMH2O * pmb * 100.0f;
+  float dsx = fmaxf(dva, 0.0f);
+  float tlfx = tk, tlfy = tk;
+  float csx[2] = {ca, ca};
+  float gswx[2] = {1e-3f, 1e-3f};
+  float gbhu[2] = {1e-3f, 1e-3f}, gbhf[2] = {1e-3f, 1e-3f};
+  float evapfbl[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) evapfbl[k] = 0.0f;
+  // per-PFT photosynthesis parameters (gathered once)
+  const float vcmax = ldf(V.vcmax, v), ejmax = ldf(V.ejmax, v), frac4 = ldf(V.frac4, v);
+  const float conkc0 = ldf(V.conkc0, v), conko0 = ldf(V.conko0, v), ekc = ldf(V.ekc, v), eko = ldf(V.eko, v);
+  const float alpha = ldf(V.alpha, v), convex = ldf(V.convex, v), cfrd = ldf(V.cfrd, v);
+  const float a1gs = ldf(V.a1gs, v), d0gs = ldf(V.d0gs, v), gswmin_p = ldf(V.gswmin, v);
+  const float g0 = ldf(V.g0, v), g1 = ldf(V.g1, v), vbeta = ldf(V.vbeta, v), shelrb = ldf(V.shelrb, v);
+
+  float zetar[NITER] = {0.0f, ZETPOS + 1.f, 0.f, 0.f};
+  float us = 0.f, rt0 = 0.f, rt1 = 0.f, rt1usc = 0.f, rtsoil = ortsoil, cls = 1.f;
+  float fev = 0.f, fhv = 0.f, fnv = 0.f, fns = 0.f, fhs = 0.f, fe = 0.f, fh = 0.f, ga = 0.f, potev = 0.f;
+  float fes = 0.f, fess = 0.f, fesp = 0.f, fevw = 0.f, fhvw = 0.f, fevw_pot = 0.f, fevc = 0.f, epot = 0.f;
+  float ecy = 0.f, hcy = 0.f, rny = 0.f, frday = 0.f, fpn = 0.f, fwsoil = 1.0f, qstss = 0.f;
+  int passes_total = 0;
+  for (int iter = 1; iter <= NITER; ++iter) {
+    const float zi = zetar[iter - 1];
+    // comp_friction_vel (cbl_friction_vel.F90:19-108)
+    {
+      float psim_1 = psim(zi * zref_uv / zref_tq);
+      float rescale = VONK * fmaxf(ua, UMIN);
+      float psim_2 = psim(zi * z0m / zref_tq);
+      us = fminf(fmaxf(1.e-6f, rescale / (logf(zref_uv / z0m) - psim_1 + psim_2)), 10.0f);
+    }
+    // resistances (cable_canopy.F90:276-363)
+    {
+      float xx = 0.5f + fsignf(0.5f, zref_tq + disp - zruffs);
+      float zr = fmaxf(zruffs - disp, z0soilsn);
+      rt1usc = xx * (logf(zref_tq / zr) - psis(zi) + psis(zi * zr / zref_tq)) / VONK;
+      rt0 = fmaxf(5.f, rt0us / us);
+      rt1 = fmaxf(5.f, (rt1usa + rt1usb + rt1usc) / us);
+      rtsoil = veg_mask ? rt0 : rt0 + rt1;
+      rtsoil = fmaxf(5.f, rtsoil);
+      if (rtsoil > 2.f * ortsoil || rtsoil < 0.5f * ortsoil) rtsoil = fmaxf(5.f, 0.5f * (rtsoil + ortsoil));
+    }
+    // boundary-layer conductance (:374-397)
+    if (veg_mask) {
+      float gbvtop = cmolar * APOL * visc / PRANDT / dleaf * sqrtf(us / fmaxf(usuh, 1.e-6f) * dleaf / visc) *
+                     0.89194175f /* prandt**(1/3) */ / shelrb;
+      gbvtop = fmaxf(0.05f, gbvtop);
+      gbhu[0] = gbvtop * (1.0f - expf(-fminf(vlaiw * (0.5f * coexp + extkb), 20.0f))) / (extkb + 0.5f * coexp);
+      gbhu[1] = (2.0f / coexp) * gbvtop * (1.0f - expf(-fminf(0.5f * coexp * vlaiw, 20.0f))) - gbhu[0];
+    }
+    rny = sum_rad_rniso; hcy = 0.f; ecy = rny;
+
+    // ------------------------------------------------ dryLeaf (cbl_dryLeaf.F90:10-666)
+    {
+      if (iter == 1) {   // fwsoil_calc_std (cbl_fwsoil.F90:13-38)
+        float rwater = 0.f;
+#pragma unroll
+        for (int k = 0; k < CG_MS; ++k)
+          rwater += froot[k] * fmaxf(1.0e-9f, fminf(1.0f, (wbliq0[k] - swilt) / (sfc - swilt)));
+        rwater = fmaxf(1.0e-9f, rwater);
+        fwsoil = P.medlyn ? fmaxf(1.0e-4f, fminf(1.0f, rwater)) : fmaxf(1.0e-9f, fminf(1.0f, vbeta * rwater));
+      }
+      float gswmin[2] = {fmaxf(1.e-6f, scalex[0] * gswmin_p), fmaxf(1.e-6f, scalex[1] * gswmin_p)};
+      float gh[2] = {1e-3f, 1e-3f}, ghr[2] = {1e-3f, 1e-3f}, psycst[2] = {psyc, psyc};
+      float rdx[2] = {0.f, 0.f}, anx[2] = {0.f, 0.f}, rdy[2] = {0.f, 0.f}, an_y[2] = {0.f, 0.f};
+      float rnx = sum_rad_rniso, ecx = sum_rad_rniso, hcx = 0.f;
+      float abs_deltlf = 999.0f, deltlf = 0.f;
+      float tlfxx = tlfx;
+      fevc = 0.f;
+#pragma unroll
+      for (int k = 0; k < CG_MS; ++k) evapfbl[k] = 0.f;
+      hcy = 0.f;
+      if (!veg_mask) { rnx = 0.f; ecx = 0.f; ecy = 0.f; abs_deltlf = 0.f; rny = 0.f; }
+      float deltlfy = abs_deltlf;
+      float oldevapfbl[CG_MS];
+      const float sum_gbh = gbhu[0] + gbhf[0] + gbhu[1] + gbhf[1];
+      (void)sum_gbh;
+      for (int k = 1; k <= MAXITER; ++k) {
+        const bool active = veg_mask && abs_deltlf > 0.1f;
+        if (active) {
+          ++passes_total;
+          float gras = fmaxf(1.0e-6f, 1.595E8f * fabsf(tlfx - tvair) * (dleaf * dleaf * dleaf));
+          float gr4 = sqrtf(sqrtf(gras));
+#pragma unroll
+          for (int l = 0; l < 2; ++l) {
+            gbhf[l] = fmaxf(1.e-6f, fvlai[l] * cmolar * 0.5f * DHEAT * gr4 / dleaf);
+            gh[l] = 2.0f * (gbhu[l] + gbhf[l]);
+            ghr[l] = gradis[l] + gh[l];
+          }
+          float vcmxt3[2], vcmxt4[2], vx3[2], vx4[2], gs_coeff[2];
+          float temp = xvcmxt3(tlfx) * vcmax * (1.0f - frac4);
+          vcmxt3[0] = scalex[0] * temp; vcmxt3[1] = scalex[1] * temp;
+          temp = xvcmxt4(tlfx - TFRZ) * vcmax * frac4;
+          vcmxt4[0] = scalex[0] * temp; vcmxt4[1] = scalex[1] * temp;
+          temp = xejmxt3(tlfx) * ejmax * (1.0f - frac4);
+          float ejmxt3[2] = {scalex[0] * temp, scalex[1] * temp};
+          float tdiff = tlfx - TREFK;
+          float arr = (1.0f - TREFK / tlfx) / (RGAS * TREFK);
+          float conkct = conkc0 * expf(ekc * arr);
+          float conkot = conko0 * expf(eko * arr);
+          tlfxx = tlfx;
+          float cx1 = conkct * (1.0f + 0.21f / conkot);
+          float cx2 = 2.0f * GAM0 * (1.0f + GAM1 * tdiff + GAM2 * tdiff * tdiff);
+#pragma unroll
+          for (int l = 0; l < 2; ++l) {
+            float par = qcan_par[l] * 4.6e-6f;
+            vx3[l] = ej3x(par * (1.0f - frac4), alpha, convex, ejmxt3[l]);
+            vx4[l] = ej4x(par * frac4, alpha, convex, vcmxt4[l]);
+            rdx[l] = cfrd * vcmxt3[l] + cfrd * vcmxt4[l];
+          }
+          if (!P.medlyn) {
+            float f = a1gs / (1.0f + dsx / d0gs);
+            gs_coeff[0] = (fwsoil / csx[0]) * f;
+            gs_coeff[1] = (fwsoil / csx[1]) * f;
+          } else {
+            gswmin[0] = g0; gswmin[1] = g0;
+            float vpd = (dsx < 50.0f) ? 0.05f : dsx * 1e-3f;
+            float num = (fwsoil <= 0.05f) ? fwsoil / 0.05f : 1.0f;
+            float t2 = (g1 * fwsoil) * rsqrtf(vpd);
+            gs_coeff[0] = (num + t2) / csx[0];
+            gs_coeff[1] = (num + t2) / csx[1];
+          }
+          // photosynthesis: anx is zeroed and recomputed under the masks
+          anx[0] = 0.f; anx[1] = 0.f;
+          if (fvlai[0] + fvlai[1] > LAI_THRESH) {
+#pragma unroll
+            for (int l = 0; l < 2; ++l)
+              if (fvlai[l] > LAI_THRESH)
+                anx[l] = photosynthesis_leaf(csx[l], cx1, cx2, gswmin[l], rdx[l], vcmxt3[l], vcmxt4[l], vx3[l], vx4[l],
+                                             gs_coeff[l], fwsoil);
+          }
+#pragma unroll
+          for (int l = 0; l < 2; ++l) {
+            if (fvlai[l] > LAI_THRESH) {
+              csx[l] = fmaxf(1.0e-4f, ca - RGBWC * anx[l] / (gbhu[l] + gbhf[l]));
+              gswx[l] = fmaxf(1.e-3f, gswmin[l] * fwsoil + fmaxf(0.0f, RGSWC * gs_coeff[l] * anx[l]));
+              float gw = 1.0f / (1.0f / gswx[l] + 1.0f / (1.075f * (gbhu[l] + gbhf[l])));
+              gw = fmaxf(gw, 0.00001f);
+              psycst[l] = psyc * (ghr[l] / gw);
+            }
+          }
+          const float cpr = CAPP * RMAIR;
+          ecx = (dsatdk * (rniso[0] - cpr * (tvair - tk) * gradis[0]) + cpr * dva * ghr[0]) / (dsatdk + psycst[0]) +
+                (dsatdk * (rniso[1] - cpr * (tvair - tk) * gradis[1]) + cpr * dva * ghr[1]) / (dsatdk + psycst[1]);
+          float local_fevc = (1.0f - fwet) * ecx;
+          if (local_fevc > 0.0f) {
+            // transp_soil_water (cbl_remove_trans.F90:43-93)
+            float diffp = 0.f, se = 0.f;
+#pragma unroll
+            for (int kk = 0; kk < CG_MS; ++kk) {
+              float xx = local_fevc * dels / HL * froot[kk] + diffp;
+              float dk = fmaxf(0.0f, wbliq0[kk] - 1.1f * swilt) * zse[kk] * DLIQ;
+              float xxd = xx - dk;
+              if (xxd > 0.0f) { evapfbl[kk] = dk; diffp = xxd; }
+              else { evapfbl[kk] = xx; diffp = 0.0f; }
+              se += evapfbl[kk];
+            }
+            fevc = se * rlam / dels;
+            ecx = fevc / (1.0f - fwet);
+          }
+          float sgh = gh[0] + gh[1];
+          hcx = (sum_rad_rniso - ecx - cpr * (tvair - tk) * sum_rad_gradis) * sgh / (ghr[0] + ghr[1]);
+          tlfx = tvair + hcx / (cpr * sgh);
+          rnx = sum_rad_rniso - cpr * (tlfx - tk) * sum_rad_gradis;
+          dsx = fmaxf(dva + dsatdk * (tlfx - tvair), 0.0f);
+          deltlf = tlfxx - tlfx;
+          abs_deltlf = fabsf(deltlf);
+        } else {
+          anx[0] = 0.f; anx[1] = 0.f;
+        }
+        // keep the best iterate (:565-582)
+        if (abs_deltlf < fabsf(deltlfy) || k == 1) {
+          if (abs_deltlf < fabsf(deltlfy)) deltlfy = deltlf;
+          rny = rnx; hcy = hcx; ecy = ecx;
+          rdy[0] = rdx[0]; rdy[1] = rdx[1]; an_y[0] = anx[0]; an_y[1] = anx[1];
+#pragma unroll
+          for (int kk = 0; kk < CG_MS; ++kk) oldevapfbl[kk] = evapfbl[kk];
+          tlfy = tlfx;   // damping below is a no-op for k == 1
+        }
+        // damping once k > 5 (:584-590)
+        if (abs_deltlf > 0.1f) {
+          float fac = 0.5f * ((float)max(0, k - 5) / ((float)k - 4.9999f));
+          tlfx = fac * tlfxx + (1.0f - fac) * tlfx;
+        }
+        // a tile that has stopped iterating never changes again: leave now
+        if (!(veg_mask && abs_deltlf > 0.1f)) break;
+      }
+      fevc = (1.0f - fwet) * ecy;
+      if (ecy > 0.0f && fwet < 1.0f && fabsf(ecy - ecx) > 1.0e-6f) {
+        float so2 = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < CG_MS; ++kk) so2 += oldevapfbl[kk];
+        if (!(fabsf(fevc - so2 * rlam / dels) > 1.0e-4f)) {
+#pragma unroll
+          for (int kk = 0; kk < CG_MS; ++kk) evapfbl[kk] = oldevapfbl[kk];
+        }
+      }
+      frday = 12.0f * (rdy[0] + rdy[1]);
+      fpn = fminf(-12.0f * (an_y[0] + an_y[1]), frday);
+    }
+    // ------------------------------------------------ wetLeaf (cbl_wetleaf.F90:9-111)
+    fevw = 0.f; fhvw = 0.f;
+    if (veg_mask) {
+      float sum_gbh = gbhu[0] + gbhf[0] + gbhu[1] + gbhf[1];
+      float ghwet = 2.0f * sum_gbh, gwwet = 1.075f * sum_gbh;
+      float ghrwet = sum_rad_gradis + ghwet;
+      float ccfevw = fminf(cansto * rlam / dels, 2.0f / (1440.0f / (dels / 60.0f)) * rlam);
+      const float cpr = CAPP * RMAIR;
+      float num = dsatdk * (sum_rad_rniso - cpr * (tvair - tk) * sum_rad_gradis) + cpr * dva * ghrwet;
+      float den = dsatdk + psyc * ghrwet / gwwet;
+      fevw = fminf(fwet * num / den, ccfevw);
+      fevw_pot = num / den;
+      fhvw = fwet * (sum_rad_rniso - cpr * (tlfy - tk) * sum_rad_gradis) - fevw;
+    }
+    fev = fevc + fevw;
+    fhv = (1.0f - fwet) * hcy + fhvw;
+    fnv = (1.0f - fwet) * rny + fevw + fhvw;
+    // canopy temperature from the longwave balance (:425-450)
+    if (veg_mask && hruff > z0soilsn) {
+      float lwabv = CAPP * RMAIR * (tlfy - tk) * sum_rad_gradis;
+      float arg = lwabv / (2.0f * (1.0f - transd) * SBOLTZ * EMLEAF) + pow4(tvrad);
+      tv = (arg > 0.0f) ? sqrtf(sqrtf(arg)) : tvrad;
+    } else {
+      tv = tvrad;
+    }
+    fns = qssabs + transd * fld + (1.0f - transd) * EMLEAF * SBOLTZ * pow4(tv) - EMSOIL * SBOLTZ * tss4;
+    // two passes of soil evaporation, separated by the within-canopy update
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+      qstss = qsatfjh(tss - TFRZ, pmb);
+      // Humidity_deficit_method (cbl_pot_evap_snow.F90:79-167)
+      float dq = qstss - (pass == 0 ? qv : qvair);
+      if (snowd > 1.0f || tgg[0] == TFRZ) dq = fmaxf(-0.1e-3f, dq);
+      potev = rho * rlam * dq / rtsoil;
+      // Latent_heat_flux (cbl_latent_heat.F90:15-285)
+      {
+        if (potev < 0.f) wetfac = 1.0f;
+        fess = wetfac * potev;
+        float pwet = fmaxf(0.f, fminf(0.2f, pudsto / fmaxf(1.f, pudsmx)));
+        fess = fess * (1.f - pwet);
+        float frescale = zse[0] * DLIQ * rlam / dels;
+        if (snowd < 0.1f && fess > 0.0f) {
+          float flower = (float)wb[0] - swilt / 2.0f;
+          float fupper = fmaxf(0.f, flower * frescale - evapfbl[0] * rlam / dels);
+          fess = fminf(fess, fupper);
+          fupper = fmaxf((float)(wb[0] - wbice[0] / (double)FROZEN_LIMIT) * frescale, 0.f);
+          fess = fminf(fess, fupper);
+        }
+        cls = 1.f;
+        if (snowd >= 0.1f) { cls = 1.1335f; fess = cls * potev; }
+        if (snowd < 0.1f && potev < 0.f && tss < TFRZ) { cls = 1.1335f; fess = cls * potev; }
+        if (snowd >= 0.1f && potev > 0.f) { cls = 1.1335f; fess = fminf((wetfac * potev) * cls, snowd / dels * rlam * cls); }
+        fesp = fminf(pudsto / dels * rlam, fmaxf(pwet * potev, 0.f));
+        fes = fess + fesp;
+      }
+      fhs = rho * CAPP * (tss - tvair) / rtsoil;
+      if (pass == 0) {
+        // within_canopy (cbl_within_canopy.F90:10-159)
+        float rrbw = (gbhu[0] + gbhf[0] + gbhu[1] + gbhf[1]) / cmolar;
+        float rrsw = (gswx[0] + gswx[1]) / cmolar;
+        float fix_eqn = cls;
+        if (potev > 0.f) fix_eqn = fix_eqn * wetfac;
+        if (veg_mask && hruff > z0soilsn) {
+          float r01 = rt0 * rt1, bs = rrbw * rrsw, g = (1.f + epsi) * rrsw + rrbw;
+          float dmah = (rt0 + rt1) * g + epsi * r01 * bs;
+          float dmbh = (-rlam / CAPP) * r01 * bs;
+          float dmch = g * r01 * (fhv + fhs) / (rho * CAPP);
+          float dmae = (-epsi * CAPP / rlam) * r01 * bs;
+          float dmbe = (rt0 + fix_eqn * rt1) * g + r01 * bs;
+          float dmce = g * r01 * (fev + fes / cls) / (rho * rlam);
+          float det = dmah * dmbe - dmae * dmbh + 1.0e-12f;
+          tvair = tk + (dmbe * dmch - dmbh * dmce) / det;
+          tvair = fminf(fmaxf(tvair, fminf(tss, tk) - 5.0f), fmaxf(tss, tk) + 5.0f);
+          qvair = fmaxf(0.0f, qv + (dmah * dmce - dmae * dmch) / det);
+          qvair = fminf(fmaxf(qvair, fminf(qstss, qv)), fmaxf(qstss, qv));
+          qstvair = qsatfjh(tvair - TFRZ, pmb);
+          dva = (qstvair - qvair) * RMAIR / RMH2O * pmb * 100.f;
+        }
+      }
+    }
+    ga = fns - fhs - fes;
+    fe = fev + fes;
+    fh = fhv + fhs;
+    potev = (potev >= 0.f) ? fmaxf(0.00001f, potev) : fminf(-0.0002f, potev);
+    fevw_pot = (fevw_pot >= 0.f) ? fmaxf(0.000001f, fevw_pot) : fminf(-0.002f, fevw_pot);
+    epot = (fevw_pot + potev / cls) * dels / rlam;
+    // update_zetar (cbl_zetar.F90:13-159)
+    if (iter < NITER) {
+      float z = -(VONK * GRAV * zref_tq * (fh + 0.07f * fe)) / (rho * CAPP * tk * us * us * us);
+      zetar[iter] = fmaxf(ZETNEG, fminf(ZETPOS, z));
+    }
+  }
+
+  // ---------------------------------------------------------------- post-loop (:684-1038)
+  const float z4 = zetar[NITER - 1];
+  const float cduv = us * us / sqf(fmaxf(ua, UMIN));
+  float cdtq = 0.f;
+  if (kDiag)
+    cdtq = cduv * (logf(zref_uv / z0m) - psim(z4 * zref_uv / zref_tq) + psim(z4 * z0m / zref_tq)) /
+           (logf(zref_tq / (0.1f * z0m)) - psis(z4) + psis(z4 * 0.1f * z0m / zref_tq));
+  float tscrn, qscrn;
+  {
+    float tstar = -fh / (rho * CAPP * us);
+    float qstar = -fe / (rho * rlam * us * cls);
+    float zscrn = fmaxf(z0m, 2.0f - disp);
+    float ftemp = (logf(zref_tq / zscrn) - psis(z4) + psis(z4 * zscrn / zref_tq)) / VONK;
+    tscrn = tk - TFRZ - tstar * ftemp;
+    qscrn = qv - qstar * ftemp;
+    const bool scr = veg_mask && hruff > 0.01f;
+    float r_sc = 0.f, rsum = 1.f;
+    if (scr) {
+      float term1 = 0.f, term2 = 0.f, term5 = 0.f;
+      float zscl = fmaxf(z0soilsn, 2.0f);
+      const float e2 = expf(2.f * CSW * rghlai);
+      if (disp > 0.0f) {
+        term1 = expf(2.f * CSW * rghlai * (1.f - zscl / hruff));
+        term2 = expf(2.f * CSW * rghlai * (1.f - disp / hruff));
+        term5 = fmaxf(2.f / 3.f * hruff / disp, 1.f);
+      }
+      float term3 = A33 * A33 * CTL * 2.f * CSW * rghlai;
+      if (zscl < disp) {
+        r_sc = term5 * logf(zscl / z0soilsn) * (e2 - term2) / term3 + term5 * logf(disp / zscl) * (e2 - term1) / term3;
+      } else if (zscl < hruff) {
+        r_sc = rt0us + term5 * (term2 - term1) / term3;
+      } else if (zscl < zruffs) {
+        r_sc = rt0us + rt1usa + term5 * (zscl - hruff) / (A33 * A33 * CTL * hruff);
+      } else {
+        r_sc = rt0us + rt1usa + rt1usb +
+               (logf((zscl - disp) / fmaxf(zruffs - disp, z0soilsn)) - psis((zscl - disp) * z4 / zref_tq) +
+                psis((zruffs - disp) * z4 / zref_tq)) / VONK;
+      }
+      rsum = fminf(1.f, r_sc / fmaxf(1.f, rt0us + rt1usa + rt1usb + rt1usc));
+      tscrn = tss + (tk - tss) * rsum - TFRZ;
+    }
+    float rsts = qsatfjh(tscrn, pmb);
+    float qtgnet = rsts * wetfac - qv;
+    float qsurf = (qtgnet > 0.f) ? rsts * wetfac : 0.1f * rsts * wetfac + 0.9f * qv;
+    if (scr) qscrn = qsurf + (qv - qsurf) * rsum;
+  }
+  // canopy water budget (:881-906)
+  {
+    float dewmm = -(fminf(0.0f, fevw) + fminf(0.0f, fevc)) * dels / rlam;
+    cansto = cansto + dewmm;
+    cansto = fmaxf(cansto - fmaxf(0.0f, fevw) * dels / rlam, 0.0f);
+    float spill = fmaxf(0.0f, cansto - cansat);
+    through = through + spill;
+    cansto = cansto - spill;
+  }
+  const float precis0 = fmaxf(0.f, through);
+  const float delwc = cansto - oldcansto;
+  // soil-coupling derivative (:913-1027, default branch)
+  float dgdtg;
+  {
+    float dfn_dtg = -4.f * EMSOIL * SBOLTZ * tss4 / tss;
+    float dfh_dtg = rho * CAPP / rtsoil;
+    float dfe_ddq = wetfac * rho * rlam * cls / rtsoil;
+    float tc = tss - TFRZ;
+    float ddq_dtg = (RMH2O / RMAIR) / pmb * TETENA * TETENB * TETENC / sqf(TETENC + tc) * expf(TETENB * tc / (TETENC + tc));
+    dgdtg = dfn_dtg - dfh_dtg - dfe_ddq * ddq_dtg;
+  }
+  const float drybal = (ecy + hcy) - sum_rad_rniso + CAPP * RMAIR * (tlfy - tk) * sum_rad_gradis;
+  const float wetbal = fevw + fhvw - sum_rad_rniso * fwet + CAPP * RMAIR * (tlfy - tk) * sum_rad_gradis * fwet;
+  const float swnet = swcan + qssabs;
+  const float lwnet = fld - SBOLTZ * EMLEAF * pow4(tv) * (1.f - transd) - flws * transd;
+  const float owetfac_out = wetfac;   // cbm:192
+  const bool cls_snow = (cls == 1.1335f);
+
+  (void)cls_snow;
+  // energy balance (cable_checks.F90:565-618); fev = fevc + fevw is the same
+  // sum before and after remove_trans moves negative fevc into fevw
+  const float ebal = swnet + fld - SBOLTZ * EMLEAF * pow4(tv) * (1.f - transd) - flws * transd - fev - fes - fh - ga;
+  D.ebal_tot[t] = D.ebal_tot[t] + (double)ebal;
+  D.cansto[t] = cansto;
+  D.rtsoil[t] = rtsoil;
+  D.owetfac[t] = owetfac_out;
+  {
+    const float rec[CG_NB] = {ga, dgdtg, fes, fess, fesp, fevc, fevw, cls, precis0, evapfbl[0], evapfbl[1], evapfbl[2],
+                              evapfbl[3], evapfbl[4], evapfbl[5], delwc, fpn, frday, tv, 0.f};
+#pragma unroll
+    for (int i = 0; i < CG_NB; ++i) D.work_b[i * ld + t] = rec[i];
+  }
+  const float rnet = fns + fnv;
+  const float fgpp = -fpn + frday;
+  const float outv[7] = {fe, fh, fgpp, frday, tv, rnet, ga};
+  bool finite = true;
+#pragma unroll
+  for (int i = 0; i < 7; ++i) { D.out[i * ld + t] = outv[i]; finite = finite && isfinite(outv[i]); }
+  if (!finite) atomicOr(D.status, 1u);
+  if (kDiag) {
+    const int idx[37] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 18, 20, 21, 22, 32, 33, 34, 35,
+                         36, 43, 44, 45, 50, 51, 52, 53, 55, 56, 57, 58};
+    const float val[37] = {fe, fh, fev, fhv, fhs, fns, fnv, ga, tv, tscrn, qscrn, rnet, us, cduv, cdtq, epot, fes,
+                           dgdtg, fpn, frday, fgpp, precis0, through, fwet, owetfac_out, potev, drybal, wetbal, ebal,
+                           tvair, qvair, swnet, lwnet, gswx[0], gswx[1], fwsoil, (float)passes_total};
+#pragma unroll
+    for (int i = 0; i < 37; ++i) D.diag[idx[i] * ld + t] = val[i];
+  }
+}
+
+template <bool kDiag>
+__device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
+  const int ld = D.ld;
+  const float dels = P.dels;
+  const int iveg = D.iveg[t], isoilm = D.isoilm[t];
+  const int v = iveg - 1, so = isoilm - 1;
+  const CgPftTable& V = T->pft;
+  const CgSoilTable& S = T->soil;
+  const float vlai = (iveg >= 14) ? 0.0f : D.vlai[t];
+  float froot[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
+  const float ssat = ldf(S.ssat, so), sfc = ldf(S.sfc, so), swilt = ldf(S.swilt, so), css = ldf(S.css, so);
+  const float rhosoil = ldf(S.rhosoil, so);
+  float zse[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) zse[k] = S.zse[k];
+  // state
+  double wb[CG_MS], wbice[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) { wb[k] = D.wb[k * ld + t]; wbice[k] = D.wbice[k * ld + t]; }
+  float tgg[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) tgg[k] = D.tgg[k * ld + t];
+  float tggsn[3], ssdn[3], smass[3], sdepth[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    tggsn[k] = D.tggsn[k * ld + t]; ssdn[k] = D.ssdn[k * ld + t];
+    smass[k] = D.smass[k * ld + t]; sdepth[k] = D.sdepth[k * ld + t];
+  }
+  const uint8_t flags = D.flags[t];
+  int isflag = flags & 1;
+  bool first_call = (flags & 2) != 0;
+  double gammzz1 = D.gammzz1[t];
+  float snowd = D.snowd[t], ssdnn = D.ssdnn[t], snage = D.snage[t], pudsto = D.pudsto[t];
+  float wb_lake = D.wb_lake[t];
+  const float pudsmx = 0.0f;
+  const float rlam = HL;
+  // phase A and B records
+  const float tk = D.work_a[0 * ld + t], precip = D.work_a[6 * ld + t], precip_sn = D.work_a[7 * ld + t];
+  const float transd = D.work_a[27 * ld + t];
+  auto Bv = [&](int i) { return D.work_b[i * ld + t]; };
+  const float ga = Bv(0), dgdtg = Bv(1), fes = Bv(2), fess = Bv(3), fesp = Bv(4);
+  float fevc = Bv(5), fevw = Bv(6);
+  const float cls = Bv(7), precis0 = Bv(8);
+  float evapfbl[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) evapfbl[k] = Bv(9 + k);
+  const float delwc = Bv(15), fpn = Bv(16), frday = Bv(17), tv = Bv(18);
+  const bool cls_snow = (cls == 1.1335f);
+  float tss;
+  // ================================================================ soil_snow
+  // cbl_soilsnow_main.F90:28-207
+  float precis = precis0;
+  float hcll = fmaxf(0.01f, css * rhosoil);
+  const float t_snwlr = 0.05f;
+  float dtmlt0 = 0.f;
+  const float osnowd = snowd;
+  if (first_call) {
+    gammzz1 = fmax((double)((1.0f - ssat) * css * rhosoil) + (wb[0] - wbice[0]) * (double)(CSWAT * DLIQ) +
+                       wbice[0] * (double)(CSICE * DICE), (double)(css * rhosoil)) * (double)zse[0] +
+              (double)((float)(1 - isflag) * CGSNOW * snowd);
+    first_call = false;
+  }
+  float wblf[CG_MS], wbfice[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) {
+    wblf[k] = fmaxf(0.01f, (float)(wb[k] - wbice[k])) / ssat;
+    wbfice[k] = (float)wbice[k] / ssat;
+  }
+  float sconds[3] = {0.f, 0.f, 0.f};
+  // snowcheck (cbl_snowCheck.F90:9-100)
+  if (snowd <= 0.0f) {
+    isflag = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { ssdn[k] = 120.0f; tggsn[k] = TFRZ; }
+    ssdnn = 120.0f;
+    sdepth[0] = snowd / ssdn[0]; sdepth[1] = 0.f; sdepth[2] = 0.f;
+    smass[0] = snowd; smass[1] = 0.f; smass[2] = 0.f;
+  } else if (snowd < SNMIN * ssdnn) {
+    if (isflag == 1) { ssdn[0] = ssdnn; tgg[0] = tggsn[0]; }
+    isflag = 0;
+    ssdnn = fminf(400.0f, fmaxf(120.0f, ssdn[0]));
+    float tm = fminf(TFRZ, tgg[0]);
+    tggsn[0] = tm; tggsn[1] = tm; tggsn[2] = tm;
+    sdepth[0] = snowd / ssdn[0]; sdepth[1] = 0.f; sdepth[2] = 0.f;
+    smass[0] = snowd; smass[1] = 0.f; smass[2] = 0.f;
+    ssdn[0] = ssdnn; ssdn[1] = ssdnn; ssdn[2] = ssdnn;
+  } else {
+    if (isflag == 0) {
+      float tm = fminf(TFRZ, tgg[0]);
+      tggsn[0] = tm; tggsn[1] = tm; tggsn[2] = tm;
+      ssdn[1] = ssdn[0]; ssdn[2] = ssdn[0];
+      sdepth[0] = t_snwlr;
+      smass[0] = t_snwlr * ssdn[0];
+      smass[1] = (snowd - smass[0]) * 0.4f;
+      smass[2] = (snowd - smass[0]) * 0.6f;
+      sdepth[1] = smass[1] / ssdn[1];
+      sdepth[2] = smass[2] / ssdn[2];
+      ssdnn = (ssdn[0] * smass[0] + ssdn[1] * smass[1] + ssdn[2] * smass[2]) / snowd;
+    }
+    isflag = 1;
+  }
+  // snowdensity (cbl_snowDensity.F90:9-102)
+  if (snowd > 0.1f && isflag == 0) {
+    float tmin1 = fminf(TFRZ, tgg[0]);
+    float s0 = ssdn[0];
+    s0 = fminf(MAX_SSDN, fmaxf(120.0f, s0 + dels * s0 * 3.1e-6f * expf(-0.03f * (273.15f - tmin1) -
+                                                                           ((s0 >= 150.0f) ? 0.046f : 0.0f) * (s0 - 150.0f))));
+    s0 = fminf(MAX_SSDN, s0 + dels * 9.806f * s0 * 0.75f * snowd / (3.0e7f * expf(0.021f * s0 + 0.081f * (273.15f - tmin1))));
+    if (isoilm != 9) s0 = fminf(450.0f, s0);
+    sconds[0] = fmaxf(0.2f, fminf(2.876e-6f * s0 * s0 + 0.074f, MAX_SCONDS));
+    sconds[1] = sconds[0]; sconds[2] = sconds[0];
+    ssdnn = s0;
+    ssdn[0] = s0; ssdn[1] = s0; ssdn[2] = s0;
+  }
+  if (isflag == 1) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      ssdn[k] = ssdn[k] + dels * ssdn[k] * 3.1e-6f *
+                              expf(-0.03f * (273.15f - fminf(TFRZ, tggsn[k])) - ((ssdn[k] >= 150.0f) ? 0.046f : 0.0f) * (ssdn[k] - 150.0f));
+    // overburden compaction; layers 2 and 3 see the updated top-layer density
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float ov = t_snwlr * ssdn[0];
+      if (k >= 1) ov += (k == 1) ? 0.5f * smass[1] : smass[1] + 0.5f * smass[2];
+      ssdn[k] = ssdn[k] + dels * 9.806f * ssdn[k] * ov / (3.0e7f * expf(0.021f * ssdn[k] + 0.081f * (273.15f - fminf(TFRZ, tggsn[k]))));
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) sdepth[k] = smass[k] / ssdn[k];
+    ssdnn = (ssdn[0] * smass[0] + ssdn[1] * smass[1] + ssdn[2] * smass[2]) / snowd;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) sconds[k] = fmaxf(0.2f, fminf(2.876e-6f * ssdn[k] * ssdn[k] + 0.074f, MAX_SCONDS));
+  }
+  // snow_accum (cbl_snowAccum.F90:10-188)
+  float segg;
+  {
+    if (precis > 0.0f && isflag == 0) {
+      snowd = fmaxf(snowd + precip_sn, 0.0f);
+      precis = precis - precip_sn;
+      ssdn[0] = fmaxf(120.0f, ssdn[0] * osnowd / fmaxf(0.01f, snowd) + 120.0f * precip_sn / fmaxf(0.01f, snowd));
+      ssdnn = ssdn[0];
+      if (precis > 0.0f && tgg[0] < TFRZ) {
+        snowd = fmaxf(snowd + precis, 0.0f);
+        float dT = precis * HLF / ((float)gammzz1 + CSWAT * precis);
+        tgg[0] = tgg[0] + dT;
+        dtmlt0 = dtmlt0 + dT;
+        ssdn[0] = fminf(MAX_SSDN, fmaxf(120.0f, ssdn[0] * osnowd / fmaxf(0.01f, snowd) + DLIQ * precis / fmaxf(0.01f, snowd)));
+        if (isoilm != 9) ssdn[0] = fminf(450.0f, ssdn[0]);
+        precis = 0.0f;
+        ssdnn = ssdn[0];
+      }
+    }
+    if (precis > 0.0f && isflag > 0) {
+      snowd = fmaxf(snowd + precip_sn, 0.0f);
+      precis = precis - precip_sn;
+      float osm = smass[0];
+      smass[0] = smass[0] + precip_sn;
+      ssdn[0] = fmaxf(120.0f, ssdn[0] * osm / smass[0] + 120.0f * precip_sn / smass[0]);
+      sdepth[0] = fmaxf(0.02f, smass[0] / ssdn[0]);
+      if (precis > 0.0f) {
+        snowd = fmaxf(snowd + precis, 0.0f);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          float sgamm = ssdn[k] * CGSNOW * sdepth[k];
+          osm = smass[k];
+          float dT = precis * HLF * osm / (sgamm * osnowd);
+          tggsn[k] = tggsn[k] + dT;
+          if (k == 0) dtmlt0 = dtmlt0 + dT;
+          smass[k] = smass[k] + precis * osm / osnowd;
+          ssdn[k] = fmaxf(120.0f, fminf(ssdn[k] * osm / smass[k] + DLIQ * (1.0f - osm / smass[k]), MAX_SSDN));
+          if (isoilm != 9) ssdn[k] = fminf(450.0f, ssdn[k]);
+          sdepth[k] = smass[k] / ssdn[k];
+        }
+        precis = 0.0f;
+      }
+    }
+    segg = fess / HL;
+    if (cls_snow) {
+      float evapsn = dels * fess / (HL + HLF);
+      float xxx = evapsn;
+      if (isflag == 0 && fess > 0.0f) evapsn = fminf(snowd, xxx);
+      if (isflag > 0 && fess > 0.0f) evapsn = fminf(0.9f * smass[0], xxx);
+      snowd = snowd - evapsn;
+      if (isflag > 0) {
+        smass[0] = smass[0] - evapsn;
+        sdepth[0] = fmaxf(0.02f, smass[0] / ssdn[0]);
+      }
+      segg = (HL + HLF) * (xxx - evapsn) / HL / dels;
+    }
+  }
+  // snow_melting (cbl_snowMelt.F90:9-120), first and second call share code
+  auto snow_melting = [&]() -> float {
+    float snowmlt = 0.f;
+    if (snowd > 0.0f && isflag == 0 && tgg[0] >= TFRZ) {
+      float snowflx = (float)((double)(tgg[0] - TFRZ) * gammzz1);
+      snowmlt = fminf(snowflx / HLF, snowd);
+      dtmlt0 = (float)((double)dtmlt0 + (double)(snowmlt * HLF) / gammzz1);
+      snowd = snowd - snowmlt;
+      tgg[0] = (float)((double)tgg[0] - (double)(snowmlt * HLF) / gammzz1);
+    }
+    if (snowd > 0.0f && isflag > 0) {
+      float sm_prev = 0.f;   // smelt1(:,k-1)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        float sgamm = ssdn[k] * CGSNOW * sdepth[k];
+        float snowflx = sm_prev * HLF / dels;
+        tggsn[k] = tggsn[k] + (snowflx * dels + sm_prev * CSWAT * (TFRZ - tggsn[k])) / (sgamm + CSWAT * sm_prev);
+        float osm = smass[k];
+        smass[k] = smass[k] + sm_prev;
+        ssdn[k] = fmaxf(120.0f, fminf(ssdn[k] * osm / smass[k] + DLIQ * (1.0f - osm / smass[k]), MAX_SSDN));
+        if (isoilm != 9) ssdn[k] = fminf(450.0f, ssdn[k]);
+        sdepth[k] = smass[k] / ssdn[k];
+        sgamm = smass[k] * CGSNOW;
+        float sm = 0.f;
+        if (tggsn[k] > TFRZ) {
+          snowflx = (tggsn[k] - TFRZ) * sgamm;
+          sm = fminf(snowflx / HLF, 0.6f * smass[k]);
+          if (k == 0) dtmlt0 = dtmlt0 + sm * HLF / sgamm;
+          smass[k] = smass[k] - sm;
+          tggsn[k] = tggsn[k] - sm * HLF / sgamm;
+          sdepth[k] = smass[k] / ssdn[k];
+        }
+        sm_prev = sm;
+      }
+      // melt of layers 1 and 2 refreezes into the layer below; only the
+      // bottom layer's melt leaves the pack
+      snowmlt = sm_prev;
+      snowd = snowd - snowmlt;
+    }
+    return snowmlt;
+  };
+  float smelt = snow_melting();
+  // snowl_adjust (cbl_snowl_adjust.F90:9-156)
+  if (isflag > 0) {
+    if (sdepth[0] > t_snwlr) {
+      float excd = sdepth[0] - t_snwlr;
+      float excm = excd * ssdn[0];
+      sdepth[0] = sdepth[0] - excd;
+      smass[0] = smass[0] - excm;
+      float osm = smass[1];
+      smass[1] = fmaxf(0.01f, smass[1] + excm);
+      ssdn[1] = fmaxf(120.0f, fminf(MAX_SSDN, ssdn[1] * osm / smass[1] + ssdn[0] * excm / smass[1]));
+      sdepth[1] = smass[1] / ssdn[1];
+      tggsn[1] = tggsn[1] * osm / smass[1] + tggsn[0] * excm / smass[1];
+      smass[2] = fmaxf(0.01f, snowd - smass[0] - smass[1]);
+    } else {
+      float excd = t_snwlr - sdepth[0];
+      float excm = excd * ssdn[1];
+      float osm = smass[0];
+      smass[0] = smass[0] + excm;
+      sdepth[0] = t_snwlr;
+      ssdn[0] = fmaxf(120.0f, fminf(MAX_SSDN, ssdn[0] * osm / smass[0] + ssdn[1] * excm / smass[0]));
+      tggsn[0] = tggsn[0] * osm / smass[0] + tggsn[1] * excm / smass[0];
+      smass[1] = fmaxf(0.01f, smass[1] - excm);
+      sdepth[1] = smass[1] / ssdn[1];
+      smass[2] = fmaxf(0.01f, snowd - smass[0] - smass[1]);
+    }
+    float frac = smass[1] / fmaxf(0.02f, smass[2]);
+    float xfrac = 2.0f / 3.0f / frac;
+    if (xfrac > 1.0f) {
+      float excm = (xfrac - 1.0f) * smass[1];
+      float osm = smass[1];
+      smass[1] = fmaxf(0.01f, smass[1] + excm);
+      tggsn[1] = tggsn[1] * osm / smass[1] + tggsn[2] * excm / smass[1];
+      ssdn[1] = fmaxf(120.0f, fminf(MAX_SSDN, ssdn[1] * osm / smass[1] + ssdn[2] * excm / smass[1]));
+      smass[2] = fmaxf(0.01f, snowd - smass[0] - smass[1]);
+      sdepth[2] = fmaxf(0.02f, smass[2] / ssdn[2]);
+    } else {
+      float excm = (1.f - xfrac) * smass[1];
+      smass[1] = fmaxf(0.01f, smass[1] - excm);
+      sdepth[1] = fmaxf(0.02f, smass[1] / ssdn[1]);
+      float osm = smass[2];
+      smass[2] = fmaxf(0.01f, snowd - smass[0] - smass[1]);
+      tggsn[2] = tggsn[2] * osm / smass[2] + tggsn[1] * excm / smass[2];
+      ssdn[2] = fmaxf(120.0f, fminf(MAX_SSDN, ssdn[2] * osm / smass[2] + ssdn[1] * excm / smass[2]));
+      sdepth[2] = smass[2] / ssdn[2];
+    }
+    isflag = 1;
+    ssdnn = (ssdn[0] * sdepth[0] + ssdn[1] * sdepth[1] + ssdn[2] * sdepth[2]) / (sdepth[0] + sdepth[1] + sdepth[2]);
+  }
+  // stempv (cbl_stempv.F90:13-221) with old_soil_conductivity (cbl_Oldconductivity.F90:7-59)
+  float ghflux, sghflux = 0.f;
+  double gammzz[CG_MS];
+  {
+    const float cnsd = ldf(S.cnsd, so);
+    float ccnsw[CG_MS];
+#pragma unroll
+    for (int k = 0; k < CG_MS; ++k) {
+      if (isoilm == 9) {
+        ccnsw[k] = SNOW_CCNSW;
+      } else {
+        float ew = wblf[k] * ssat;
+        float exp_arg = ew * 4.0943446f /* log 60 */ + wbfice[k] * ssat * 5.5214609f /* log 250 */;
+        float f2 = fmaxf(1.0f, sqrtf(fminf(2.0f, 0.5f * ssat / fminf(ew, 0.5f * ssat))));
+        ccnsw[k] = (exp_arg > 30.f) ? 1.5f * f2 : fminf(cnsd * expf(exp_arg), 1.5f) * f2;
+      }
+    }
+    float coeff[CG_MS + 1];   // coeff(1..ms+1) of the reference, coeff[ms] = 0
+    float coefb;
+    float snowz = 0.f;
+    if (isflag == 0) {
+      snowz = fmaxf(0.f, snowd / ssdnn);
+      ccnsw[0] = (ccnsw[0] - 0.2f) * (zse[0] / (zse[0] + snowz)) + 0.2f;
+      coeff[0] = 0.f;
+    }
+#pragma unroll
+    for (int k = 2; k <= CG_MS; ++k) coeff[k - 1] = 2.0f / (zse[k - 2] / ccnsw[k - 2] + zse[k - 1] / ccnsw[k - 1]);
+    coeff[CG_MS] = 0.f;
+    if (isflag == 0) {
+      coeff[1] = 2.0f / ((zse[0] + snowz) / ccnsw[0] + zse[1] / ccnsw[1]);
+      coefb = coeff[1];
+    }
+    float csn[3];
+    if (isflag != 0) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) sconds[k] = fmaxf(0.2f, fminf(2.876e-6f * ssdn[k] * ssdn[k] + 0.074f, MAX_SCONDS));
+      csn[0] = 2.0f / (sdepth[0] / sconds[0] + sdepth[1] / sconds[1]);
+      csn[1] = 2.0f / (sdepth[1] / sconds[1] + sdepth[2] / sconds[2]);
+      coeff[0] = 2.0f / (sdepth[2] / sconds[2] + zse[0] / ccnsw[0]);
+      coefb = coeff[0];
+    }
+    // heat capacity of the soil layers (FP64 storage of gammzz as in the reference)
+#pragma unroll
+    for (int k = 0; k < CG_MS; ++k) {
+      float g = fmaxf(hcll, (1.0f - ssat) * css * rhosoil + ssat * (wblf[k] * CSWAT * DLIQ + wbfice[k] * CSICE * DICE)) * zse[k];
+      gammzz[k] = (double)g;
+    }
+    if (isflag == 0) gammzz[0] = gammzz[0] + (double)(CGSNOW * snowd);
+    double at[9], bt[9], ct[9], rhs[9];
+    if (isflag == 0) {
+      // soil-only system: snow rows of the reference's 9-row system are
+      // identity rows decoupled from the soil (coeff(1) = 0), so the 6-row
+      // solve gives the same soil temperatures
+#pragma unroll
+      for (int k = 0; k < CG_MS; ++k) {
+        double dtg = (double)dels / gammzz[k];
+        at[k] = -dtg * (double)coeff[k];
+        ct[k] = -dtg * (double)coeff[k + 1];
+        bt[k] = 1.0 - at[k] - ct[k];
+      }
+      bt[0] = bt[0] - (double)dgdtg * (double)dels / gammzz[0];
+      tgg[0] = tgg[0] + (ga - tgg[0] * dgdtg) * dels / (float)gammzz[0];
+#pragma unroll
+      for (int k = 0; k < CG_MS; ++k) rhs[k] = (double)tgg[k];
+      trimb<CG_MS>(at, bt, ct, rhs);
+#pragma unroll
+      for (int k = 0; k < CG_MS; ++k) tgg[k] = (float)rhs[k];
+      ghflux = coefb * (tgg[0] - tgg[1]);
+    } else {
+      const float csnow[4] = {0.f, csn[0], csn[1], coeff[0]};   // coeff(-2..1)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        float sgamm = ssdn[k] * CGSNOW * sdepth[k];
+        double dtg = (double)(dels / sgamm);
+        at[k] = -dtg * (double)csnow[k];
+        ct[k] = -dtg * (double)csnow[k + 1];
+        bt[k] = 1.0 - at[k] - ct[k];
+      }
+#pragma unroll
+      for (int k = 0; k < CG_MS; ++k) {
+        double dtg = (double)dels / gammzz[k];
+        at[3 + k] = -dtg * (double)coeff[k];
+        ct[3 + k] = -dtg * (double)coeff[k + 1];
+        bt[3 + k] = 1.0 - at[3 + k] - ct[3 + k];
+      }
+      float sgamm = ssdn[0] * CGSNOW * sdepth[0];
+      bt[0] = bt[0] - (double)dgdtg * (double)dels / (double)sgamm;
+      tggsn[0] = tggsn[0] + (ga - tggsn[0] * dgdtg) * dels / sgamm;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) rhs[k] = (double)tggsn[k];
+#pragma unroll
+      for (int k = 0; k < CG_MS; ++k) rhs[3 + k] = (double)tgg[k];
+      trimb<9>(at, bt, ct, rhs);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) tggsn[k] = (float)rhs[k];
+#pragma unroll
+      for (int k = 0; k < CG_MS; ++k) tgg[k] = (float)rhs[3 + k];
+      sghflux = csn[0] * (tggsn[0] - tggsn[1]);
+      ghflux = coefb * (tgg[0] - tgg[1]);
+    }
+  }
+  gammzz1 = gammzz[0];
+  tss = (float)(1 - isflag) * tgg[0] + (float)isflag * tggsn[0];
+  smelt = smelt + snow_melting();
+  // remove_trans (cbl_remove_trans.F90:9-40)
+  if (fevc < 0.0f) { fevw = fevw + fevc; fevc = 0.0f; }
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) wb[k] = wb[k] - (double)(evapfbl[k] / (zse[k] * DLIQ));
+  // soilfreeze (cbl_soilfreeze.F90:9-81)
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) {
+    const double zd = (double)(zse[k] * DICE), zl = (double)(zse[k] * DLIQ);
+    if (tgg[k] < TFRZ && (double)FROZEN_LIMIT * wb[k] - wbice[k] > .001) {
+      double sf = fmin((double)FROZEN_LIMIT * wb[k] - wbice[k], ((double)ssat - wb[k]) / (double)(1.0f - DICE / DLIQ));
+      sf = fmin(fmax(0.0, sf) * zd, (double)(TFRZ - tgg[k]) * gammzz[k] / (double)HLF);
+      wbice[k] = fmin(wbice[k] + sf / zd, (double)FROZEN_LIMIT * wb[k]);
+      wb[k] = wb[k] + sf / zd - sf / zl;
+      float g = fmaxf(hcll, (float)((double)((1.0f - ssat) * css * rhosoil) + (wb[k] - wbice[k]) * (double)(CSWAT * DLIQ) +
+                                    wbice[k] * (double)(CSICE * DICE)));
+      gammzz[k] = (double)g * (double)zse[k];
+      if (k == 0 && isflag == 0) gammzz[k] = gammzz[k] + (double)(CGSNOW * snowd);
+      tgg[k] = tgg[k] + (float)sf * HLF / (float)gammzz[k];
+    } else if (tgg[k] > TFRZ && wbice[k] > 0.) {
+      double sm = fmin(wbice[k] * zd, (double)(tgg[k] - TFRZ) * gammzz[k] / (double)HLF);
+      wbice[k] = fmax(0.0, wbice[k] - sm / zd);
+      wb[k] = wb[k] - sm / zd + sm / zl;
+      float g = fmaxf(hcll, (float)((double)((1.0f - ssat) * css * rhosoil) + (wb[k] - wbice[k]) * (double)(CSWAT * DLIQ) +
+                                    wbice[k] * (double)(CSICE * DICE)));
+      gammzz[k] = (double)g * (double)zse[k];
+      if (k == 0 && isflag == 0) gammzz[k] = gammzz[k] + (double)(CGSNOW * snowd);
+      tgg[k] = tgg[k] - (float)sm * HLF / (float)gammzz[k];
+    }
+  }
+  gammzz1 = gammzz[0];
+  // infiltration (cbl_soilsnow_main.F90:139-159)
+  float rnof1, rnof2;
+  float fwtop[3];
+  {
+    float weting = precis + smelt + fmaxf(0.f, pudsto - fesp / HL * dels);
+    float sinfil[3];
+    float rem = weting;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      sinfil[k] = fminf(0.95f * (float)((double)ssat - wb[k]) * zse[k] * DLIQ, rem);
+      rem = rem - sinfil[k];
+    }
+    fwtop[0] = sinfil[0] / dels - segg;
+    fwtop[1] = sinfil[1] / dels;
+    fwtop[2] = sinfil[2] / dels;
+    pudsto = fmaxf(0.f, weting - sinfil[0] - sinfil[1] - sinfil[2]);
+    rnof1 = fmaxf(0.f, pudsto - pudsmx);
+    pudsto = pudsto - rnof1;
+  }
+  // surfbv -> smoisturev (cbl_surfbv.F90:9-146, cbl_smoisturev.F90:11-444, nmeth = -1)
+  {
+    const float hyds = ldf(S.hyds, so), i2bp3 = ldf(S.i2bp3, so), ibp2 = ldf(S.ibp2, so), hsbh = ldf(S.hsbh, so);
+    const float pwb_min = ldf(S.pwb_min, so);
+    float fluxh[CG_MS + 1];
+    fluxh[0] = 0.f; fluxh[CG_MS] = 0.f;
+    float delt_prev = 0.f;
+#pragma unroll
+    for (int k = 1; k <= CG_MS - 1; ++k) {
+      float wbl_k = fmaxf(0.01f, (float)(wb[k - 1] - wbice[k - 1]));
+      float wbl_kp = fmaxf(0.01f, (float)(wb[k] - wbice[k]));
+      float delt = wbl_kp - wbl_k;
+      float wh = fminf(wbl_k, wbl_kp);
+      if (wbice[k - 1] > 0.05 || wbice[k] > 0.01) wh = 0.9f * wbl_k + 0.1f * wbl_kp;
+      float speed_k = hyds * powf(wh / ssat, i2bp3 - 1.f);
+      float rat = delt_prev / (delt + fsignf(1.0e-20f, delt));
+      float phi = fmaxf(fmaxf(0.0f, fminf(1.0f, 2.0f * rat)), fminf(2.0f, rat));
+      speed_k = fminf(speed_k, 0.5f * zse[k - 1] / dels);
+      fluxh[k] = speed_k * (wbl_k + phi * (wh - wbl_k));
+      delt_prev = delt;
+    }
+    if (wb[CG_MS - 1] > (double)sfc) {
+      float wbl_k = fmaxf(0.001f, (float)(wb[CG_MS - 1] - wbice[CG_MS - 1]));
+      float wbl_kp = fmaxf(0.001f, (float)((double)ssat - wbice[CG_MS - 1]));
+      float wh = fminf(wbl_k, wbl_kp);
+      if (wbice[CG_MS - 1] > 0.05) wh = 0.9f * wbl_k + 0.1f * wbl_kp;
+      float speed_k = hyds * powf(wh / ssat, i2bp3 - 1.f);
+      speed_k = 0.5f * speed_k / (1.f - fminf(0.5f, 10.f * (float)wbice[CG_MS - 1]));
+      speed_k = fminf(0.5f * speed_k, 0.5f * zse[CG_MS - 1] / dels);
+      fluxh[CG_MS] = fmaxf(0.0f, speed_k * wbl_k);
+    }
+    float dtt[CG_MS];
+    double wblfd[CG_MS];
+#pragma unroll
+    for (int k = CG_MS; k >= 1; --k) {
+      fluxh[k - 1] = fminf(fluxh[k - 1], (float)((double)ssat - wb[k - 1]) * zse[k - 1] / dels + fluxh[k]);
+      wb[k - 1] = wb[k - 1] + (double)(dels * (fluxh[k - 1] - fluxh[k]) / zse[k - 1]);
+      double ssatcurr = (double)ssat - wbice[k - 1];
+      dtt[k - 1] = (float)((double)dels / ((double)zse[k - 1] * ssatcurr));
+      wblfd[k - 1] = (wb[k - 1] - wbice[k - 1]) / ssatcurr;
+    }
+    rnof2 = dels * fluxh[CG_MS] * DLIQ;
+    double at[CG_MS], bt[CG_MS], ct[CG_MS];
+    at[0] = 0.0; ct[CG_MS - 1] = 0.0;
+#pragma unroll
+    for (int k = 2; k <= CG_MS; ++k) {
+      float wa = (float)wblfd[k - 2], wbv = (float)wblfd[k - 1];
+      float wbh_k = (zse[k - 1] * wa + zse[k - 2] * wbv) / (zse[k - 1] + zse[k - 2]);
+      float fact = powf(wbh_k, ibp2 - 1.f);
+      float icef = fmaxf((float)(wbice[k - 2] / fmax(0.01, wb[k - 2])), (float)(wbice[k - 1] / fmax(0.01, wb[k - 1])));
+      float pwb_wbh = (hsbh * (1.f - fminf(2.f * fminf(0.1f, icef), 0.1f))) * fmaxf(pwb_min, wbh_k * fact);
+      float z3_k = pwb_wbh / ldf(S.zshh, k - 1);
+      at[k - 1] = -(double)dtt[k - 1] * (double)z3_k;
+      ct[k - 2] = -(double)dtt[k - 2] * (double)z3_k;
+    }
+#pragma unroll
+    for (int k = 0; k < CG_MS; ++k) bt[k] = 1.0 - at[k] - ct[k];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) wblfd[k] = wblfd[k] + (double)(dtt[k] * fwtop[k] / DLIQ);
+    trimb<CG_MS>(at, bt, ct, wblfd);
+#pragma unroll
+    for (int k = 0; k < CG_MS; ++k) wb[k] = wblfd[k] * ((double)ssat - wbice[k]) + wbice[k];
+    const double dfactor = (double)(1.0f - DICE / DLIQ);
+#pragma unroll
+    for (int k = 0; k < CG_MS; ++k) {
+      if (wbice[k] > (double)FROZEN_LIMIT * wb[k]) {
+        double sm = (wbice[k] - (double)FROZEN_LIMIT * wb[k]) / (1.0 - (double)FROZEN_LIMIT * dfactor);
+        wbice[k] = wbice[k] - sm;
+        wb[k] = wb[k] - dfactor * sm;
+        tgg[k] = tgg[k] - (float)sm * zse[k] * DICE * HLF / (float)gammzz[k];
+      }
+    }
+  }
+  // surfbv remainder
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) {
+    rnof1 = rnof1 + (float)fmax(wb[k] - (double)ssat, 0.0) * DLIQ * zse[k];
+    wb[k] = fmax((double)(swilt / 4.0f), fmin(wb[k], (double)ssat));
+  }
+  float rnof5 = 0.f;
+  {
+    float smasstot = 0.f;
+    float sm1[3] = {0.f, 0.f, 0.f};
+    if (snowd > MAX_GLACIER_SNOWD) {
+      rnof5 = fminf(0.1f, snowd - MAX_GLACIER_SNOWD);
+      if (isflag == 0) {
+        tgg[0] = tgg[0] - rnof5 * HLF / (float)gammzz1;
+        snowd = snowd - rnof5;
+      } else {
+        smasstot = smass[0] + smass[1] + smass[2];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (snowd > MAX_GLACIER_SNOWD && isflag > 0) {
+        sm1[k] = fminf(rnof5 * smass[k] / smasstot, 0.2f * smass[k]);
+        smass[k] = smass[k] - sm1[k];
+        snowd = snowd - sm1[k];
+      }
+    }
+    if (isflag > 0) rnof5 = sm1[0] + sm1[1] + sm1[2];
+  }
+  if (iveg == LAKES) {
+    float sinfil = fminf(rnof1, wb_lake);
+    rnof1 = fmaxf(0.0f, rnof1 - sinfil);
+    wb_lake = fmaxf(0.0f, wb_lake - sinfil);
+    sinfil = fminf(rnof2, wb_lake);
+    rnof2 = fmaxf(0.0f, rnof2 - sinfil);
+    wb_lake = fmaxf(0.0f, wb_lake - sinfil);
+    float xl = (float)fmax(0.0, (wb[CG_MS - 1] - (double)sfc) * (double)(zse[CG_MS - 1] * DLIQ));
+    sinfil = fminf(xl, wb_lake);
+    wb[CG_MS - 1] = wb[CG_MS - 1] - (double)(sinfil / (zse[CG_MS - 1] * DLIQ));
+    wb_lake = fmaxf(0.0f, wb_lake - sinfil);
+    xl = (float)fmax(0.0, (wb[CG_MS - 1] - (double)(0.5f * (sfc + swilt))) * (double)(zse[CG_MS - 1] * DLIQ));
+    sinfil = fminf(xl, wb_lake);
+    wb[CG_MS - 1] = wb[CG_MS - 1] - (double)(sinfil / (zse[CG_MS - 1] * DLIQ));
+    wb_lake = fmaxf(0.0f, wb_lake - sinfil);
+  }
+  rnof1 = rnof1 / dels + rnof5 / dels;
+  rnof2 = rnof2 / dels;
+  tss = (float)(1 - isflag) * tgg[0] + (float)isflag * tggsn[0];
+  double wbtot = 0.0;
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) wbtot += ((wb[k] - wbice[k]) * (double)DLIQ + wbice[k] * (double)DICE) * (double)zse[k];
+
+  // snow_aging (cbl_snow_aging.F90:11-83)
+  if (snowd > 1.0f) {
+    float dnsnow = fminf(1.0f, 0.1f * fmaxf(0.0f, snowd - osnowd));
+    float tmp = fminf((float)isflag * tggsn[0] + (float)(1 - isflag) * tgg[0], TFRZ);
+    float ar1 = 5000.0f * (1.0f / (TFRZ - 0.01f) - 1.0f / tmp);
+    float ar3;
+    if (isoilm == ICE_SOIL) { ar3 = 0.0000001f; dnsnow = 1.0f; }
+    else ar3 = 0.1f;
+    float dtau = 1.0e-6f * (expf(ar1) + expf(10.0f * ar1) + ar3) * dels;
+    snage = fmaxf(0.0f, (snage + dtau) * (1.0f - dnsnow));
+  }
+  const float trad = sqrtf(sqrtf((1.f - transd) * pow4(tv) + transd * pow4(tss)));
+
+  // carbon, icycle == 0 (cable_carbon.F90:38-360, cbm:214-229)
+  float frp, frpw, frpr, frs;
+  float cplant[3], csoil[2];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) cplant[k] = D.cplant[k * ld + t];
+  csoil[0] = D.csoil[t]; csoil[1] = D.csoil[ld + t];
+  {
+    const float rc0 = V.ratecp[0], rc1 = V.ratecp[1], rc2 = V.ratecp[2];
+    float tot = rc0 * cplant[0] + rc1 * cplant[1] + rc2 * cplant[2];
+    float pc1 = tot - rc0 * cplant[0];
+    float pc1w = pc1 - rc2 * cplant[2];
+    float pc1r = pc1 - rc1 * cplant[1];
+    float tmp1 = fmaxf(3.22f - 0.046f * (tk - TFRZ), 1e-6f);
+    float tmp3 = powf(tmp1, 0.1f * (tk - TFRZ - 20.0f));
+    float c = ldf(V.rp20, v) * tmp3 / 31536000.0f;
+    frp = c * pc1; frpw = c * pc1w; frpr = c * pc1r;
+  }
+  {
+    float den = fmaxf(0.07f, sfc - swilt);
+    float rswc = fmaxf(0.0001f, froot[0] * ((float)wb[1] - swilt)) / den;
+    float tsoil = froot[0] * tgg[1] - TFRZ;
+    float tref = fmaxf(0.f, tgg[CG_MS - 1] - (TFRZ - .05f));
+#pragma unroll
+    for (int k = 1; k < CG_MS; ++k) {
+      rswc += fmaxf(0.0001f, froot[k] * ((float)wb[k] - swilt)) / den;
+      tsoil += froot[k] * tgg[k];
+    }
+    rswc = fminf(1.f, rswc);
+    tsoil = fmaxf(-46.f + 2.f, tsoil);
+    float e0rswc = 52.4f + 285.f * rswc;
+    float ftsoil = fminf(0.0015f, 1.f / (tref + 46.f) - 1.f / (tsoil + 46.f));
+    float sss = fmaxf(-15.f, fminf(1.f, e0rswc * ftsoil));
+    frs = ldf(V.vegcf, v) * (144.0f / 44.0e6f) * fminf(1.f, 1.4f * fmaxf(.3f, .0278f * tsoil + .5f)) * expf(sss) * rswc /
+          (0.16f + rswc);
+  }
+  {
+    float coef_cold = expf(fminf(1.f, -(tv - ldf(V.tvclst, v))));
+    float wbav = 0.f;
+#pragma unroll
+    for (int k = 0; k < CG_MS; ++k) wbav += froot[k] * (float)wb[k];
+    wbav = fmaxf(0.01f, wbav);
+    float campbell = 2.0f - ldf(S.ibp2, so);
+    float esw = fmaxf(1.0f, powf(wbav, campbell) - 1.0f);
+    float eswilt = powf(swilt, campbell) - 1.0f;
+    float relstress = fminf(1.0f, esw / eswilt - 1.0f);
+    float coef_cd = (coef_cold + expf(5.0f * relstress)) * 2.0e-7f;
+    float fcl = expf(-ldf(V.tfcl, v) * vlai);
+    float clitt = (coef_cd + 3.17e-8f) * cplant[0];
+    cplant[0] = cplant[0] - dels * (fpn * fcl + clitt);
+    float fr = fminf(1.f, expf(-ldf(V.rw, v) * 0.9f * 0.0001f * cplant[2] / fmaxf(cplant[1], 0.01f)) / 0.9f);
+    float cfwd = 6.342e-10f * cplant[1];
+    cplant[1] = cplant[1] - dels * (fpn * (1.f - fcl) * (1.f - fr) + frpw + cfwd);
+    float cfrts = 4.53e-9f * cplant[2];
+    cplant[2] = cplant[2] - dels * (fpn * (1.f - fcl) * fr + cfrts + frpr);
+    float cfsf = 1.057e-10f * csoil[0];
+    csoil[0] = csoil[0] + dels * (0.98f * clitt + 0.9f * cfrts + cfwd - cfsf - 0.98f * frs);
+    csoil[1] = csoil[1] + dels * (0.02f * clitt + 0.1f * cfrts + cfsf - 0.02f * frs);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) cplant[k] = fmaxf(0.f, cplant[k]);
+    csoil[0] = fmaxf(0.f, csoil[0]); csoil[1] = fmaxf(0.f, csoil[1]);
+  }
+
+  // driver rescaling (cable_serial.F90:602-605) and balances (cable_checks.F90)
+  const float runoff_mm = (rnof1 + rnof2) * dels;
+  double owb = D.owb[t];
+  if (P.ktau == 1) owb = wbtot;
+  const double delwb = wbtot - owb;
+  const float wbal = (float)((double)(precip - delwc - snowd + osnowd - runoff_mm - (fevw + fevc + fes / cls) * dels / rlam) - delwb);
+  double wbal_tot = D.wbal_tot[t];
+  if (P.ktau == 1) wbal_tot = 0.0;
+  if (P.ktau > 10) wbal_tot += (double)wbal;
+
+  // store
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) { D.wb[k * ld + t] = wb[k]; D.wbice[k * ld + t] = wbice[k]; D.tgg[k * ld + t] = tgg[k]; }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    D.tggsn[k * ld + t] = tggsn[k]; D.ssdn[k * ld + t] = ssdn[k]; D.smass[k * ld + t] = smass[k];
+    D.sdepth[k * ld + t] = sdepth[k]; D.cplant[k * ld + t] = cplant[k];
+  }
+  D.csoil[t] = csoil[0]; D.csoil[ld + t] = csoil[1];
+  D.flags[t] = (uint8_t)(isflag | (first_call ? 2 : 0));
+  D.gammzz1[t] = gammzz1;
+  D.snowd[t] = snowd; D.ssdnn[t] = ssdnn; D.snage[t] = snage; D.pudsto[t] = pudsto;
+  D.tss[t] = tss; D.wb_lake[t] = wb_lake;
+  D.owb[t] = wbtot; D.wbal_tot[t] = wbal_tot;
+  D.out[7 * ld + t] = trad;
+  if (!isfinite(trad)) atomicOr(D.status, 1u);
+  if (kDiag) {
+    const int idx[16] = {17, 19, 23, 24, 25, 26, 27, 28, 37, 38, 39, 40, 41, 42, 46, 54};
+    const float val[16] = {fevc, fevw, -fpn - frp, fpn + frs + frp, frp + frday, frp, frs, trad, runoff_mm,
+                           rnof1 * dels, rnof2 * dels, smelt, ghflux, sghflux, wbal, (float)wbtot};
+#pragma unroll
+    for (int i = 0; i < 16; ++i) D.diag[idx[i] * ld + t] = val[i];
+  }
+}
+
+}  // namespace cg

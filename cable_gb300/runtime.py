@@ -1,0 +1,225 @@
+"""ctypes binding of the C ABI in ``include/cablegpu.h``.
+
+:class:`CableGPU` owns one device context: the per-tile parameters and
+state of ``mp`` tiles resident in GPU memory, advanced by the fused timestep
+kernel.  Field arrays cross the boundary in the reference's Fortran layout,
+``(mp, nlayer)`` column-major, i.e. numpy arrays of shape ``(nlayer, mp)``.
+
+There is no CPU fallback: if the CUDA library cannot be loaded, or no GPU is
+present, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+F32, F64, I32 = 0, 1, 2
+KIND_PARAM, KIND_STATE, KIND_OUTPUT, KIND_DIAG, KIND_FORCING = 0, 1, 2, 3, 4
+NFORCING = 13
+FORCING_FIELDS = ["fsd_vis", "fsd_nir", "fld", "precip", "precip_sn", "tk", "pmb", "ua", "qv", "ca", "coszen", "doy",
+                  "hod"]
+OUTPUT_FIELDS = ["fe", "fh", "fgpp", "frday", "tv", "rnet", "ga", "trad"]
+_NP = {F32: np.float32, F64: np.float64, I32: np.int32}
+
+ERRORS = {-1: "CABLEGPU_ERR_ARG", -2: "CABLEGPU_ERR_CUDA", -3: "CABLEGPU_ERR_NONFINITE", -4: "CABLEGPU_ERR_STATE"}
+
+# Every symbol include/cablegpu.h declares.
+EXPORTS = [
+    "cablegpu_create", "cablegpu_destroy", "cablegpu_cold_start", "cablegpu_num_fields", "cablegpu_field_info",
+    "cablegpu_field_id", "cablegpu_set_field", "cablegpu_get_field", "cablegpu_field_device_ptr",
+    "cablegpu_set_forcing", "cablegpu_set_synthetic_forcing", "cablegpu_set_options", "cablegpu_step",
+    "cablegpu_run", "cablegpu_synchronize", "cablegpu_run_timed", "cablegpu_kernel_timed",
+    "cablegpu_launch_count", "cablegpu_last_error",
+]
+
+_lib = None
+
+
+class CableGPUError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "error"), code, msg))
+        self.code = code
+
+
+class _Tiles(C.Structure):
+    _fields_ = [("mp", C.c_int), ("iveg", C.POINTER(C.c_int)), ("isoilm", C.POINTER(C.c_int)),
+                ("vlai", C.POINTER(C.c_float)), ("lat", C.POINTER(C.c_float)), ("lonphase", C.POINTER(C.c_float)),
+                ("tbase", C.POINTER(C.c_float)), ("swscale", C.POINTER(C.c_float)), ("order", C.c_int)]
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed) the CUDA library and declare its ABI."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise RuntimeError("cable_gb300 CUDA library missing (%s); run cable_gb300.build.build()" % _build.LIB)
+    L = C.CDLL(_build.LIB)
+    vp, ip = C.c_void_p, C.c_int
+    L.cablegpu_create.argtypes = [C.POINTER(_Tiles), ip, C.POINTER(vp)]
+    L.cablegpu_destroy.argtypes = [vp]
+    L.cablegpu_cold_start.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.cablegpu_num_fields.argtypes = []
+    L.cablegpu_field_info.argtypes = [ip, C.POINTER(C.c_char_p), C.POINTER(ip), C.POINTER(ip), C.POINTER(ip)]
+    L.cablegpu_field_id.argtypes = [C.c_char_p]
+    L.cablegpu_set_field.argtypes = [vp, ip, vp]
+    L.cablegpu_get_field.argtypes = [vp, ip, vp]
+    L.cablegpu_field_device_ptr.argtypes = [vp, ip, C.POINTER(vp), C.POINTER(ip)]
+    L.cablegpu_set_forcing.argtypes = [vp, C.POINTER(C.c_float)]
+    L.cablegpu_set_synthetic_forcing.argtypes = [vp, C.c_ulonglong, ip]
+    L.cablegpu_set_options.argtypes = [vp, ip, ip, ip]
+    L.cablegpu_step.argtypes = [vp, ip, C.c_float]
+    L.cablegpu_run.argtypes = [vp, ip, ip, C.c_float]
+    L.cablegpu_synchronize.argtypes = [vp]
+    L.cablegpu_run_timed.argtypes = [vp, ip, ip, C.c_float, C.POINTER(C.c_float)]
+    L.cablegpu_kernel_timed.argtypes = [vp, ip, ip, C.c_float, C.POINTER(C.c_float)]
+    L.cablegpu_launch_count.argtypes = [vp]
+    L.cablegpu_launch_count.restype = C.c_longlong
+    L.cablegpu_last_error.argtypes = [vp]
+    L.cablegpu_last_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def fields():
+    """{name: (id, nlayer, dtype, kind)} of the library's field registry."""
+    L = load()
+    out = {}
+    for i in range(L.cablegpu_num_fields()):
+        n, nl, dt, kd = C.c_char_p(), C.c_int(), C.c_int(), C.c_int()
+        L.cablegpu_field_info(i, C.byref(n), C.byref(nl), C.byref(dt), C.byref(kd))
+        out[n.value.decode()] = (i, nl.value, dt.value, kd.value)
+    return out
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class CableGPU:
+    """One device context holding ``mp`` tiles (see module docstring)."""
+
+    def __init__(self, tiles, device: int = 0, order: int = 0):
+        self.L = load()
+        self.fields = fields()
+        self.mp = int(tiles.mp)
+        self._keep = dict(
+            iveg=np.ascontiguousarray(tiles.iveg, np.int32), isoilm=np.ascontiguousarray(tiles.isoilm, np.int32),
+            vlai=np.ascontiguousarray(tiles.vlai, np.float32), lat=np.ascontiguousarray(tiles.lat, np.float32),
+            lonphase=np.ascontiguousarray(tiles.lonphase, np.float32),
+            tbase=np.ascontiguousarray(tiles.tbase, np.float32),
+            swscale=np.ascontiguousarray(tiles.swscale, np.float32))
+        k = self._keep
+        t = _Tiles(self.mp, _ptr(k["iveg"], C.c_int), _ptr(k["isoilm"], C.c_int), _ptr(k["vlai"], C.c_float),
+                   _ptr(k["lat"], C.c_float), _ptr(k["lonphase"], C.c_float), _ptr(k["tbase"], C.c_float),
+                   _ptr(k["swscale"], C.c_float), int(order))
+        h = C.c_void_p()
+        rc = self.L.cablegpu_create(C.byref(t), device, C.byref(h))
+        self.h = h
+        if rc != 0:
+            msg = self.L.cablegpu_last_error(h).decode() if h.value else "invalid tile description"
+            if h.value:
+                self.L.cablegpu_destroy(h)
+            self.h = C.c_void_p()
+            raise CableGPUError(rc, msg)
+
+    # ------------------------------------------------------------------ util
+    def _check(self, rc):
+        if rc != 0:
+            raise CableGPUError(rc, self.L.cablegpu_last_error(self.h).decode())
+
+    def close(self):
+        if self.h and self.h.value:
+            self.L.cablegpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ------------------------------------------------------------------ setup
+    def cold_start(self, snowd0, tgg0, wb0):
+        a = [np.ascontiguousarray(x, np.float64) for x in (snowd0, tgg0, wb0)]
+        self._check(self.L.cablegpu_cold_start(self.h, *[_ptr(x, C.c_double) for x in a]))
+
+    def set_options(self, medlyn=False, diag=False, capture_forcing=False):
+        self._check(self.L.cablegpu_set_options(self.h, int(medlyn), int(diag), int(capture_forcing)))
+
+    def set_synthetic_forcing(self, seed: int, doy0: int = 1):
+        self._check(self.L.cablegpu_set_synthetic_forcing(self.h, int(seed), int(doy0)))
+
+    def set_forcing(self, forcing):
+        f = np.ascontiguousarray(forcing, np.float32)
+        assert f.shape == (NFORCING, self.mp)
+        self._check(self.L.cablegpu_set_forcing(self.h, _ptr(f, C.c_float)))
+
+    # ------------------------------------------------------------------ fields
+    def get(self, name):
+        fid, nl, dt, _ = self.fields[name]
+        out = np.empty((nl, self.mp), _NP[dt])
+        self._check(self.L.cablegpu_get_field(self.h, fid, out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def set(self, name, value):
+        fid, nl, dt, _ = self.fields[name]
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(value, _NP[dt]), (nl, self.mp)))
+        self._check(self.L.cablegpu_set_field(self.h, fid, a.ctypes.data_as(C.c_void_p)))
+
+    def outputs(self):
+        o = self.get("out")
+        return dict(zip(OUTPUT_FIELDS, o))
+
+    def device_ptr(self, name):
+        p, ld = C.c_void_p(), C.c_int()
+        self._check(self.L.cablegpu_field_device_ptr(self.h, self.fields[name][0], C.byref(p), C.byref(ld)))
+        return p.value, ld.value
+
+    # ------------------------------------------------------------------ time
+    def step(self, ktau: int, dels: float = 1800.0):
+        self._check(self.L.cablegpu_step(self.h, int(ktau), float(dels)))
+
+    def run(self, ktau0: int, nsteps: int, dels: float = 1800.0):
+        self._check(self.L.cablegpu_run(self.h, int(ktau0), int(nsteps), float(dels)))
+
+    def synchronize(self):
+        self._check(self.L.cablegpu_synchronize(self.h))
+
+    def run_timed(self, ktau0, nsteps, dels=1800.0) -> float:
+        ms = C.c_float()
+        self._check(self.L.cablegpu_run_timed(self.h, int(ktau0), int(nsteps), float(dels), C.byref(ms)))
+        return ms.value
+
+    def kernel_timed(self, ktau0, nsteps, dels=1800.0) -> float:
+        ms = C.c_float()
+        self._check(self.L.cablegpu_kernel_timed(self.h, int(ktau0), int(nsteps), float(dels), C.byref(ms)))
+        return ms.value
+
+    def launch_count(self) -> int:
+        return int(self.L.cablegpu_launch_count(self.h))
+
+
+def from_tileset(ts, device: int = 0, seed=None, order: int = 0) -> CableGPU:
+    """Context for a :class:`cable_gb300.workloads.TileSet`, cold-started and
+    driven by the built-in synthetic forcing."""
+    g = CableGPU(ts, device, order)
+    g.cold_start(ts.snowd0, ts.tgg0, ts.wb0)
+    g.set_synthetic_forcing(ts.seed if seed is None else seed, ts.doy0)
+    return g

@@ -1,0 +1,144 @@
+/*
+ * cablegpu.h - C ABI of the GB300 implementation of CABLE's per-timestep
+ * tile physics (the offline cbm() call).
+ *
+ * Replaces, for the offline driver, the reference interface
+ *   SUBROUTINE cbm(ktau, dels, air, bgc, canopy, met, bal, rad, rough, soil,
+ *                  ssnow, sum_flux, veg, climate, xk, c1, rhoch)
+ *   src/offline/cbl_model_driver_offline.F90:38-40
+ * called once per timestep from the serial driver
+ *   src/offline/cable_serial.F90:594-595
+ * and from the MPI worker (src/offline/cable_mpiworker.F90:503).
+ *
+ * Model: the library owns device-resident structure-of-arrays copies of the
+ * per-tile state.  The caller (the Fortran shim in
+ * cable_gb300/fortran/cable_cbm_gpu.F90, or any C/Python host) uploads the
+ * tile parameters and state once, then calls cablegpu_step() once per
+ * timestep (or cablegpu_run() for many steps, replayed as a CUDA graph) and
+ * downloads fields only when it needs them (output steps, restart files).
+ *
+ * Array convention: every per-tile field is a host array of nlayer * mp
+ * elements in Fortran column-major order of the reference's (mp, nlayer)
+ * arrays, i.e. element (tile i, layer k) at [k * mp + i]; the element type
+ * is the field's dtype (CABLEGPU_F32 = REAL, CABLEGPU_F64 = REAL(r_2),
+ * CABLEGPU_I32 = INTEGER).
+ *
+ * Errors: every function returns 0 on success and a negative CABLEGPU_ERR_*
+ * code otherwise; cablegpu_last_error() describes the last failure.  No
+ * entry point traps or aborts.  Calls on one context are not thread-safe and
+ * run in order on the context's CUDA stream.
+ */
+#ifndef CABLEGPU_H
+#define CABLEGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CABLEGPU_OK 0
+#define CABLEGPU_ERR_ARG (-1)        /* bad argument (null, out of range, unknown field) */
+#define CABLEGPU_ERR_CUDA (-2)       /* a CUDA runtime call failed */
+#define CABLEGPU_ERR_NONFINITE (-3)  /* a step produced a non-finite output flux */
+#define CABLEGPU_ERR_STATE (-4)      /* call not valid in the context's current state */
+
+#define CABLEGPU_F32 0
+#define CABLEGPU_F64 1
+#define CABLEGPU_I32 2
+
+#define CABLEGPU_KIND_PARAM 0   /* static per-tile parameter (veg / soil / forcing jitter) */
+#define CABLEGPU_KIND_STATE 1   /* prognostic state carried between steps */
+#define CABLEGPU_KIND_OUTPUT 2  /* written every step */
+#define CABLEGPU_KIND_DIAG 3    /* written every step when diagnostics are enabled */
+#define CABLEGPU_KIND_FORCING 4 /* met forcing of the last step, when capture is enabled */
+#define CABLEGPU_KIND_WORK 5    /* per-tile records handed between the kernels of one step */
+
+#define CABLEGPU_NFORCING 13    /* fsd_vis fsd_nir fld precip precip_sn tk pmb ua qv ca coszen doy hod */
+
+typedef struct cablegpu_ctx cablegpu_ctx;
+
+/* Static description of the tiles (veg%iveg, soil%isoilm, veg%vlai,
+ * rad%latitude).  The three forcing-jitter arrays only drive the built-in
+ * synthetic forcing generator and may be NULL (defaults 0 h, 288 K, 1.0). */
+typedef struct {
+  int mp;
+  const int* iveg;       /* [mp] plant functional type 1..17 */
+  const int* isoilm;     /* [mp] soil type 1..9 */
+  const float* vlai;     /* [mp] leaf area index */
+  const float* lat;      /* [mp] latitude, degrees north */
+  const float* lonphase; /* [mp] local-time offset of the synthetic forcing, hours in [0, 24) */
+  const float* tbase;    /* [mp] base air temperature of the synthetic forcing, K */
+  const float* swscale;  /* [mp] shortwave scale factor of the synthetic forcing */
+  int order;             /* device tile order: 0 = grouped by plant type (default; warps then
+                            follow coherent code paths), 1 = as given.  Field I/O is always in
+                            the caller's order and results do not depend on this choice. */
+} cablegpu_tiles;
+
+/* Creates a context on CUDA device `device` for tiles->mp tiles and uploads
+ * the tile description.  Replaces the per-run set-up the reference driver
+ * does before its time loop (load_parameters, cable_serial.F90:399).  */
+int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out);
+int cablegpu_destroy(cablegpu_ctx* ctx);
+
+/* Cold-start state, as the reference initialises a run without a restart
+ * file (cable_parameters.F90 write_default_params :1188-1262, :1607-1650;
+ * cable_initialise.F90 get_default_inits :72-144; derived_parameters
+ * owetfac :2246-2254): snow water equivalent, soil temperature and soil
+ * moisture per tile (host arrays [mp]; layers start uniform).  */
+int cablegpu_cold_start(cablegpu_ctx* ctx, const double* snowd0, const double* tgg0, const double* wb0);
+
+/* Field registry. */
+int cablegpu_num_fields(void);
+int cablegpu_field_info(int id, const char** name, int* nlayer, int* dtype, int* kind);
+int cablegpu_field_id(const char* name);
+/* Host <-> device copies of one field (host array [nlayer * mp], field dtype).
+ * set: the reference's derived-type components are written by the caller
+ * (e.g. a restart read, cable_initialise.F90 get_restart_data :163-664);
+ * get: the caller reads them back (output / restart write). */
+int cablegpu_set_field(cablegpu_ctx* ctx, int id, const void* host);
+int cablegpu_get_field(cablegpu_ctx* ctx, int id, void* host);
+/* Device pointer and leading dimension (elements between layers) of a field,
+ * for callers that keep their own device-side pipelines. */
+int cablegpu_field_device_ptr(cablegpu_ctx* ctx, int id, void** dptr, int* ld);
+
+/* Met forcing for the next step from host memory, [CABLEGPU_NFORCING][mp]
+ * float (the met_type fields get_met_data fills, cable_input.F90).  Stays in
+ * effect for every later step until replaced or until synthetic forcing is
+ * selected. */
+int cablegpu_set_forcing(cablegpu_ctx* ctx, const float* host_forcing);
+/* Built-in seeded synthetic forcing generated inside the step kernel. */
+int cablegpu_set_synthetic_forcing(cablegpu_ctx* ctx, unsigned long long seed, int doy0);
+
+/* medlyn: 0 = gs_switch 'leuning' (offline cable.nml), 1 = 'medlyn'.
+ * diag: 1 = write the per-tile diagnostics fields every step.
+ * capture_forcing: 1 = keep a copy of each step's forcing (field "forcing"). */
+int cablegpu_set_options(cablegpu_ctx* ctx, int medlyn, int diag, int capture_forcing);
+
+/* One timestep, ktau 1-based (cbm(ktau, dels, ...) followed by the driver's
+ * balance checks).  Asynchronous; errors of the step surface at the next
+ * synchronising call. */
+int cablegpu_step(cablegpu_ctx* ctx, int ktau, float dels);
+/* nsteps timesteps ktau0 .. ktau0+nsteps-1, replayed from a captured CUDA
+ * graph.  Asynchronous. */
+int cablegpu_run(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels);
+/* Waits for all queued work; returns CABLEGPU_ERR_NONFINITE if any step
+ * since the last call produced a non-finite output flux. */
+int cablegpu_synchronize(cablegpu_ctx* ctx);
+
+/* Timing helpers for benchmarks: CUDA events on the context's stream.
+ * run_timed: total milliseconds of cablegpu_run(ktau0, nsteps).
+ * kernel_timed: average milliseconds of one step kernel launch, each launch
+ * bracketed by its own events. */
+int cablegpu_run_timed(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, float* ms_total);
+int cablegpu_kernel_timed(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, float* ms_per_launch);
+/* Number of kernel launches of the timestep issued by this context so far
+ * (three per step). */
+long long cablegpu_launch_count(cablegpu_ctx* ctx);
+
+const char* cablegpu_last_error(cablegpu_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CABLEGPU_H */

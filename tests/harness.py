@@ -1,0 +1,94 @@
+"""Parity harness shared by the GPU tests, __graft_entry__.smoke() and
+bench.py: runs the GPU timestep and the CPU oracle on identical forcing and
+summarises the per-field differences."""
+from __future__ import annotations
+
+import numpy as np
+
+import oracle_lib as O
+
+# GPU diag-field name -> oracle diag name, for the fields compared
+DIAG_MAP = {
+    "fe_d": "fe", "fh_d": "fh", "fev": "fev", "fhv": "fhv", "fhs": "fhs", "fns": "fns", "fnv": "fnv", "ga_d": "ga",
+    "tv_d": "tv", "tscrn": "tscrn", "qscrn": "qscrn", "rnet_d": "rnet", "us": "us", "cduv": "cduv", "cdtq": "cdtq",
+    "fes": "fes", "fevc": "fevc", "fevw": "fevw", "fpn": "fpn", "frday_d": "frday", "fgpp_d": "fgpp",
+    "fnpp": "fnpp", "fnee": "fnee", "frp": "frp", "frs": "frs", "trad_d": "trad", "albedo_vis": "albedo_vis",
+    "albedo_nir": "albedo_nir", "transd": "transd", "precis": "precis", "through": "through", "fwet": "fwet",
+    "wetfac": "wetfac", "potev": "potev", "runoff": "runoff", "ghflux": "ghflux", "sghflux": "sghflux",
+    "drybal": "drybal", "wetbal": "wetbal", "ebal": "ebal", "wbal": "wbal", "qssabs": "qssabs", "rniso": "rniso",
+    "vlaiw": "vlaiw", "tvair": "tvair", "qvair": "qvair", "swnet": "swnet", "lwnet": "lwnet", "wbtot": "wbtot",
+    "gswx_sun": "gswx_sun", "gswx_shd": "gswx_shd", "fwsoil": "fwsoil", "dryleaf_passes": "dryleaf_passes",
+}
+STATE_FIELDS = ["wb", "wbice", "tgg", "tggsn", "ssdn", "smass", "sdepth", "snowd", "ssdnn", "snage", "pudsto",
+                "owetfac", "rtsoil", "tss", "cansto", "cplant", "csoil", "owb", "ebal_tot", "wbal_tot"]
+
+# Tolerances of the spec: fluxes 1e-3 relative with a 1 W/m2 floor,
+# temperatures 0.01 K, soil moisture 1e-5 m3/m3.
+FLUX_FIELDS = {"fe_d", "fh_d", "fev", "fhv", "fhs", "fns", "fnv", "ga_d", "rnet_d", "fes", "fevc", "fevw", "swnet",
+               "lwnet", "qssabs", "rniso"}
+TEMP_FIELDS = {"tv_d", "trad_d", "tgg", "tggsn", "tss", "tvair"}
+MOIST_FIELDS = {"wb", "wbice"}
+
+
+def tolerance(name, ref):
+    ref = np.abs(np.asarray(ref, np.float64))
+    if name in FLUX_FIELDS:
+        return np.maximum(1e-3 * ref, 1.0)
+    if name in TEMP_FIELDS:
+        return np.full(ref.shape, 0.01)
+    if name in MOIST_FIELDS:
+        return np.full(ref.shape, 1e-5)
+    return None
+
+
+def compare(name, gpu, ref):
+    gpu = np.asarray(gpu, np.float64)
+    ref = np.asarray(ref, np.float64)
+    e = gpu - ref
+    out = {"max": float(np.abs(e).max()) if e.size else 0.0, "rms": float(np.sqrt(np.mean(e * e))) if e.size else 0.0}
+    tol = tolerance(name, ref)
+    if tol is not None:
+        within = np.abs(e) <= tol
+        out["frac_within"] = float(within.mean())
+        # RMS against the field's scalar tolerance (fluxes: 1 W/m2 floor)
+        out["tol"] = float(np.min(tol))
+    return out
+
+
+def run_pair(ts, nsteps, ktau0=1, diag=True, host_forcing=False, medlyn=False, precision=0):
+    """Advance the GPU and the oracle ``nsteps`` from a cold start on
+    identical forcing.  Returns (gpu_state, gpu_diag, oracle_state, oracle_diag,
+    forcing [nsteps, 13, mp])."""
+    from cable_gb300 import runtime as R
+    g = R.from_tileset(ts)
+    g.set_options(medlyn=medlyn, diag=diag, capture_forcing=not host_forcing)
+    forc = []
+    if host_forcing:
+        F = O.forcing(ts, ktau0 - 1, nsteps)
+    for n in range(nsteps):
+        if host_forcing:
+            g.set_forcing(F[n])
+        g.step(ktau0 + n, ts.dels)
+        if not host_forcing:
+            forc.append(g.get("forcing"))
+    g.synchronize()
+    if not host_forcing:
+        F = np.stack(forc)
+    gstate = {k: g.get(k) for k in STATE_FIELDS + ["flags"]}
+    gdiag = {k: g.get(k)[0] for k in DIAG_MAP} if diag else {}
+    g.close()
+    st = O.init_state(ts, precision)
+    od = O.run(ts, st, nsteps, ktau0=ktau0, forcing=F, precision=precision, medlyn=medlyn)
+    ostate = O.split_state(st)
+    return gstate, gdiag, ostate, od, F
+
+
+def parity_report(gstate, gdiag, ostate, odiag):
+    rep = {}
+    for k in STATE_FIELDS:
+        og = ostate["gammzz"] if k == "gammzz1" else ostate[k]
+        rep[k] = compare(k, gstate[k], og[: gstate[k].shape[0]])
+    for gk, ok in DIAG_MAP.items():
+        if gk in gdiag:
+            rep[gk] = compare(gk, gdiag[gk], odiag[ok])
+    return rep
