@@ -1,0 +1,326 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 cbm() timestep (tile-timesteps per second).
+
+Default workload: the uneven snow grid -- 4e6 tiles, PFT 1..17, soil 1..9,
+40 % snow-covered (0, 1 or 3 active snow layers), air temperature 250-300 K,
+seeded synthetic forcing generated inside the kernels, 30-minute steps.
+
+Lines printed (one JSON line on rank 0):
+  value  device-resident throughput: state and forcing generator in HBM, the
+         timestep's kernels replayed from CUDA graphs, timed with CUDA events
+  e2e    the same steps through the C ABI with host buffers: each step
+         uploads its met forcing from pinned host memory (cablegpu_set_forcing)
+         and downloads the 8 output fluxes (cablegpu_get_field)
+  roofline  the timestep's algorithmic HBM bytes per step / measured step time
+  cpu_baseline  the CPU restatement of the reference cbm() (REAL = FP32,
+         r_2 = FP64, the reference's own precision mix) on all host cores, on a
+         bounded sample of the same workload
+
+``--impl reference`` times that CPU restatement alone (the reference itself is
+Fortran and no Fortran compiler is available) and prints its line.
+Multi-GPU: one process per GPU (torchrun); every rank advances its own
+``--mp`` tiles (weak scaling, no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "tile-timesteps/sec on 1 GB300: surrogate vs plain GPU cbm() at stated flux error"
+# Algorithmic HBM bytes of one tile-timestep: prognostic state read + written
+# (265 B each way), static tile parameters read (22 B), output fluxes written
+# (32 B); forcing is generated in-kernel.
+ALGO_BYTES_PER_TILE_STEP = 2 * 265 + 22 + 32
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=1440)
+    p.add_argument("--warmup", type=int, default=16)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="snow_grid", choices=["snow_grid", "grid"])
+    p.add_argument("--mp", type=int, default=4_000_000)
+    p.add_argument("--e2e-steps", type=int, default=8)
+    p.add_argument("--cpu-sample-tiles", type=int, default=100_000)
+    p.add_argument("--cpu-sample-steps", type=int, default=48)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------- distributed
+class Dist:
+    def __init__(self, n):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def shard_offset(rank: int, mp: int) -> int:
+    """Weak scaling: rank r advances its own mp tiles; their seeds differ."""
+    return rank * mp
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU (oracle)
+def cpu_time(ts, steps, precision=1):
+    """Seconds of the CPU restatement (precision 1: REAL=FP32, r_2=FP64) on
+    every host core for ``ts`` tiles and ``steps`` steps."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    st = O.init_state(ts, precision)
+    O.run(ts, st, 2, ktau0=1, precision=precision)  # warm caches / threads
+    st = O.init_state(ts, precision)
+    t0 = time.perf_counter()
+    O.run(ts, st, steps, ktau0=1, precision=precision)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(args, ts_full):
+    n = min(args.cpu_sample_tiles, ts_full.mp)
+    ts = ts_full.subset(slice(0, n))
+    secs = cpu_time(ts, args.cpu_sample_steps)
+    return {"value": n * args.cpu_sample_steps / secs, "unit": "tile-timesteps/s", "cores": os.cpu_count(),
+            "kind": "port",
+            "sample": "%d tiles of the %s workload x %d steps, CPU restatement of the reference cbm() "
+                      "(REAL FP32 / r_2 FP64), OpenMP over tiles, %.1f s" % (n, ts_full.name, args.cpu_sample_steps, secs)}
+
+
+def workload(args, rank=0):
+    from cable_gb300 import workloads as W
+    seed = 12345 + shard_offset(rank, 1)
+    if args.workload == "snow_grid":
+        return W.snow_grid(args.mp, seed=seed, nsteps=args.steps)
+    return W.grid(args.mp, seed=seed, nsteps=args.steps)
+
+
+def config(args, world):
+    return {"workload": "%s: %d tiles/GPU x %d timed steps of 1800 s (%s)" % (
+                args.workload, args.mp, args.steps,
+                "40%% snow-covered, air 250-300 K" if args.workload == "snow_grid" else "no snow, air 288+N(0,10) K"),
+            "tiles_per_gpu": args.mp, "soil_layers": 6, "snow_layers": "0-3", "path": "plain GPU cbm()",
+            "parallelism": "tiles sharded over %d GPU(s), no collective" % world,
+            "l2": "per-step state (%.1f GB) exceeds L2; no flush needed" % (args.mp * 600 / 1e9)}
+
+
+def run_reference(args):
+    d = Dist(args.gpus)
+    if d.rank != 0:
+        d.close()
+        return
+    ts_full = workload(args)
+    n = min(args.cpu_sample_tiles, ts_full.mp)
+    ts = ts_full.subset(slice(0, n))
+    steps = args.cpu_sample_steps
+    secs = cpu_time(ts, steps)
+    value = n * steps / secs
+    out = {"metric": METRIC, "value": value, "unit": "tile-timesteps/s", "impl": "reference", "n_gpus": args.gpus,
+           "steps": steps, "warmup": 2, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded generator)",
+           "config": config(args, args.gpus),
+           "cpu_baseline": {"value": value, "unit": "tile-timesteps/s", "cores": os.cpu_count(), "kind": "port",
+                            "sample": "%d tiles x %d steps of the %s workload" % (n, steps, ts_full.name)},
+           "e2e": {"value": value, "unit": "tile-timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": "the reference is Fortran and cannot be compiled here (no Fortran compiler); this arm times "
+                   "the CPU restatement of its cbm() in the reference's REAL=FP32 / r_2=FP64 precision mix"}
+    print(json.dumps(out))
+    d.close()
+
+
+def traffic_per_step(mp):
+    """DRAM bytes per step from the committed ncu summary, scaled to mp tiles."""
+    path = os.path.join(ROOT, "profiles", "cbm_step_snow_grid.md")
+    try:
+        for ln in open(path):
+            if ln.startswith("traffic_bytes_per_tile_step:"):
+                return float(ln.split(":")[1]) * mp
+    except OSError:
+        pass
+    return None
+
+
+def run_gb300(args):
+    import numpy as np
+    from cable_gb300 import runtime as R
+    d = Dist(args.gpus)
+    ts = workload(args, d.rank)
+    g = R.from_tileset(ts, device=d.local)
+    dels = ts.dels
+    # warm-up (graph capture happens here)
+    g.run(1, args.warmup, dels)
+    g.synchronize()
+    ktau = 1 + args.warmup
+    # --- device-resident throughput
+    clocks = ClockSampler(d.local)
+    clocks.start()
+    launches0 = g.launch_count()
+    d.barrier()
+    ms = g.run_timed(ktau, args.steps, dels)
+    g.synchronize()
+    d.barrier()
+    launches = g.launch_count() - launches0
+    clk = clocks.stop()
+    ktau += args.steps
+    ms_max = d.max(ms)
+    value = d.world * args.mp * args.steps / (ms_max / 1e3)
+    # --- per-step kernel time for the roofline (events around each launch set)
+    step_ms = g.kernel_timed(ktau, 8, dels)
+    ktau += 8
+    g.synchronize()
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    algo = ALGO_BYTES_PER_TILE_STEP * args.mp
+    achieved = algo / (step_ms / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": traffic_per_step(args.mp),
+            "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+            "scope": "one timestep (its 3 kernels), %d algorithmic B per tile-step" % ALGO_BYTES_PER_TILE_STEP}
+    # --- end to end through the C ABI with host buffers
+    e2e = None
+    try:
+        import torch
+        g.set_options(capture_forcing=True)
+        g.step(ktau, dels); ktau += 1
+        f0 = g.get("forcing")
+        g.step(ktau, dels); ktau += 1
+        f1 = g.get("forcing")
+        g.set_options(capture_forcing=False)
+        pin = torch.cuda.is_available()
+        host_f = [torch.from_numpy(f).pin_memory() if pin else torch.from_numpy(f) for f in (f0, f1)]
+        host_f = [h.numpy() for h in host_f]
+        out_t = torch.empty((8, args.mp), dtype=torch.float32, pin_memory=pin).numpy()
+        # warm the host path once
+        g.set_forcing(host_f[0]); g.step(ktau, dels); ktau += 1
+        g.L.cablegpu_get_field(g.h, g.fields["out"][0], out_t.ctypes.data_as(__import__("ctypes").c_void_p))
+        d.barrier()
+        t0 = time.perf_counter()
+        for n in range(args.e2e_steps):
+            g.set_forcing(host_f[n % 2])
+            g.step(ktau, dels); ktau += 1
+            rc = g.L.cablegpu_get_field(g.h, g.fields["out"][0], out_t.ctypes.data_as(__import__("ctypes").c_void_p))
+            if rc:
+                raise RuntimeError(g.L.cablegpu_last_error(g.h))
+        g.synchronize()
+        secs = d.max(time.perf_counter() - t0)
+        e2e = {"value": d.world * args.mp * args.e2e_steps / secs, "unit": "tile-timesteps/s",
+               "h2d_bytes_per_step": int(f0.nbytes), "d2h_bytes_per_step": int(out_t.nbytes),
+               "steps": args.e2e_steps}
+    except Exception as exc:  # the line still prints; the failure is stated
+        e2e = {"value": None, "unit": "tile-timesteps/s", "error": str(exc)[:200]}
+    g.close()
+    cpu = None
+    if d.rank == 0 and d.world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, ts)
+    if d.rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "tile-timesteps/s", "n_gpus": d.world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 soil state, Thomas solves, balances)",
+               "data": "synthetic (seeded generator; the reference's site forcing is not available)",
+               "config": config(args, d.world), "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+               "clocks": clk, "gpu_launches": int(launches),
+               "step_kernels_ms": step_ms}
+        print(json.dumps(out))
+    d.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -13,7 +13,19 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libcablegpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["cablegpu.cu", "tables.cpp", "surrogate.cu"]
+SOURCES = ["cablegpu.cu", "phase_a.cu", "phase_b.cu", "phase_c1.cu", "phase_c2.cu", "phase_c3.cu", "tables.cpp",
+           "surrogate.cu"]
+# Per-file extra flags: the canopy phase is FP32-only and division-heavy, so
+# it uses the approximate division / exp intrinsics; the phases that carry
+# FP64 state keep IEEE semantics.  CG_MIN_BLOCKS=4 caps the canopy and soil
+# kernels at 128 registers (4 blocks of 128 threads per SM): measured faster
+# than 3 or 1 resident blocks despite a few hundred bytes of spills.
+EXTRA_FLAGS = {
+    "phase_b.cu": ["--use_fast_math", "-DCG_MIN_BLOCKS=4"],
+    "phase_c1.cu": ["-DCG_MIN_BLOCKS=4"],
+    "phase_c2.cu": ["-DCG_MIN_BLOCKS=4"],
+    "phase_c3.cu": ["-DCG_MIN_BLOCKS=4"],
+}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -53,7 +65,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for src in sources():
         obj = os.path.join(LIBDIR, os.path.basename(src) + ".o")
         objs.append(obj)
-        cmd = [nvcc] + flags + ["-c", src, "-o", obj]
+        cmd = [nvcc] + flags + EXTRA_FLAGS.get(os.path.basename(src), []) + ["-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd))
         procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))

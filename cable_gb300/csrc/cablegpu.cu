@@ -8,14 +8,14 @@
 #include <vector>
 
 #include "../../include/cablegpu.h"
-#include "cbm_step.cuh"
+#include "phase_kernels.cuh"
 
 using namespace cg;
 
 namespace {
 
-constexpr int kBlock = 128;
-constexpr int kGraphSteps = 8;   // steps per captured CUDA graph
+constexpr int kGraphSteps = 8;      // steps per captured CUDA graph
+constexpr int kKernelsPerStep = 5;  // radiation, canopy, snow pack, soil heat, soil water
 
 // ---------------------------------------------------------------- field registry
 enum Storage { S_U8, S_F32, S_F64 };
@@ -76,6 +76,7 @@ std::vector<FieldDef> make_registry() {
   f.push_back({"forcing_in", CG_NFORC, CABLEGPU_F32, CABLEGPU_KIND_FORCING, S_F32});
   f.push_back({"work_a", CG_NA, CABLEGPU_F32, CABLEGPU_KIND_WORK, S_F32});
   f.push_back({"work_b", CG_NB, CABLEGPU_F32, CABLEGPU_KIND_WORK, S_F32});
+  f.push_back({"work_c", CG_NC, CABLEGPU_F32, CABLEGPU_KIND_WORK, S_F32});
   return f;
 }
 
@@ -87,19 +88,6 @@ const std::vector<FieldDef>& registry() {
 size_t storage_bytes(Storage s) { return s == S_U8 ? 1 : (s == S_F32 ? 4 : 8); }
 
 // ---------------------------------------------------------------- kernels
-// One kernel per phase of the timestep (see cbm_step.cuh).
-template <bool kDiag, int kPhase>
-__global__ void __launch_bounds__(kBlock) cbm_phase_kernel(CgDev D, const CgTables* __restrict__ T, StepParams P,
-                                                           const int* __restrict__ clock) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= D.mp) return;
-  StepParams p = P;
-  if (clock) { p.ktau = clock[0]; p.step_index = clock[0] - 1; }
-  if (kPhase == 0) phase_a<kDiag>(D, T, p, t);
-  else if (kPhase == 1) phase_b<kDiag>(D, T, p, t);
-  else phase_c<kDiag>(D, T, p, t);
-}
-
 __global__ void advance_clock_kernel(int* clock) { clock[0] += 1; }
 
 // Cold start: the reference's initial state for a run without restart file.
@@ -221,21 +209,18 @@ void bind_device_view(cablegpu_ctx* c) {
   D.forcing_out = c->capture_forcing ? (float*)P("forcing") : nullptr;
   D.work_a = (float*)P("work_a");
   D.work_b = (float*)P("work_b");
+  D.work_c = (float*)P("work_c");
 }
 
 int launch_step(cablegpu_ctx* c, const StepParams& p, const int* clock) {
   bind_device_view(c);
-  const int grid = (c->mp + kBlock - 1) / kBlock;
-  if (c->diag) {
-    cbm_phase_kernel<true, 0><<<grid, kBlock, 0, c->stream>>>(c->dev, c->d_tables, p, clock);
-    cbm_phase_kernel<true, 1><<<grid, kBlock, 0, c->stream>>>(c->dev, c->d_tables, p, clock);
-    cbm_phase_kernel<true, 2><<<grid, kBlock, 0, c->stream>>>(c->dev, c->d_tables, p, clock);
-  } else {
-    cbm_phase_kernel<false, 0><<<grid, kBlock, 0, c->stream>>>(c->dev, c->d_tables, p, clock);
-    cbm_phase_kernel<false, 1><<<grid, kBlock, 0, c->stream>>>(c->dev, c->d_tables, p, clock);
-    cbm_phase_kernel<false, 2><<<grid, kBlock, 0, c->stream>>>(c->dev, c->d_tables, p, clock);
-  }
-  c->launches += 3;
+  const bool diag = c->diag != 0;
+  launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, clock);
+  launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, clock);
+  launch_phase_c1(diag, c->stream, c->dev, c->d_tables, p, clock);
+  launch_phase_c2(diag, c->stream, c->dev, c->d_tables, p, clock);
+  launch_phase_c3(diag, c->stream, c->dev, c->d_tables, p, clock);
+  c->launches += kKernelsPerStep;
   CG_CUDA(c, cudaGetLastError());
   return CABLEGPU_OK;
 }
@@ -493,7 +478,7 @@ int cablegpu_run(cablegpu_ctx* c, int ktau0, int nsteps, float dels) {
     CG_CUDA(c, cudaMemcpyAsync(c->d_clock, c->h_clock, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     while (nsteps - done >= kGraphSteps) {
       CG_CUDA(c, cudaGraphLaunch(c->graph, c->stream));
-      c->launches += 3 * kGraphSteps;
+      c->launches += kKernelsPerStep * kGraphSteps;
       done += kGraphSteps;
     }
     // the pinned clock buffer must not be rewritten before the copy ran
@@ -559,6 +544,34 @@ int cablegpu_kernel_timed(cablegpu_ctx* c, int ktau0, int nsteps, float dels, fl
 }
 
 long long cablegpu_launch_count(cablegpu_ctx* c) { return c ? c->launches : -1; }
+
+int cablegpu_param_table(int table, const char* name, float* out, int n) {
+  if (!name || !out) return CABLEGPU_ERR_ARG;
+  static CgTables tab;
+  static bool built = false;
+  if (!built) { cg_build_tables(&tab.pft, &tab.soil); built = true; }
+  const float* src = nullptr;
+  int len = 0;
+  if (table == 0) {
+    const CgPftTable& P = tab.pft;
+#define CG_T(x) if (!std::strcmp(name, #x)) { src = P.x; len = CG_NPFT; }
+    CG_T(canst1) CG_T(dleaf) CG_T(ejmax) CG_T(frac4) CG_T(hc) CG_T(vbeta) CG_T(rp20) CG_T(vegcf) CG_T(extkn)
+    CG_T(a1gs) CG_T(d0gs) CG_T(alpha) CG_T(convex) CG_T(cfrd) CG_T(gswmin) CG_T(conkc0) CG_T(conko0) CG_T(ekc)
+    CG_T(eko) CG_T(g0) CG_T(g1) CG_T(vcmax) CG_T(xfang) CG_T(shelrb) CG_T(refl1) CG_T(refl2) CG_T(taul1)
+    CG_T(taul2) CG_T(rw) CG_T(tfcl) CG_T(tvclst)
+#undef CG_T
+    if (!std::strcmp(name, "froot")) { src = &P.froot[0][0]; len = CG_MS * CG_NPFT; }
+  } else if (table == 1) {
+    const CgSoilTable& S = tab.soil;
+#define CG_T(x) if (!std::strcmp(name, #x)) { src = S.x; len = CG_NSOIL; }
+    CG_T(bch) CG_T(css) CG_T(hyds) CG_T(rhosoil) CG_T(sfc) CG_T(ssat) CG_T(sucs) CG_T(swilt) CG_T(cnsd) CG_T(hsbh)
+    CG_T(ibp2) CG_T(i2bp3) CG_T(pwb_min) CG_T(albsoil_vis) CG_T(albsoil_nir) CG_T(sand) CG_T(clay) CG_T(silt)
+#undef CG_T
+  }
+  if (!src || n < len) return CABLEGPU_ERR_ARG;
+  std::memcpy(out, src, sizeof(float) * len);
+  return CABLEGPU_OK;
+}
 
 const char* cablegpu_last_error(cablegpu_ctx* c) { return c ? c->err.c_str() : "null context"; }
 

@@ -87,6 +87,7 @@ struct CgDev {
   float* diag;             // [CG_NDIAG] or null
   float* work_a;           // phase A -> B, C handoff record
   float* work_b;           // phase B -> C handoff record
+  float* work_c;           // phase C1 -> C2 -> C3 handoff record
   const float* forcing_in; // [CG_NFORC] host-provided forcing, or null (synthetic)
   float* forcing_out;      // [CG_NFORC] copy of the forcing used, or null
   unsigned int* status;    // bit0: non-finite output seen
@@ -202,6 +203,14 @@ __device__ __forceinline__ float xejmxt3(float x) {
   return fmaxf(0.0f, num / den);
 }
 
+// One-Newton-step variant (relative error ~1e-14) for the water-content
+// scaling of the moisture solve.
+__device__ __forceinline__ double drcp1(double d) {
+  double r = (double)(1.0f / (float)d);
+  double e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+
 // FP64 reciprocal seeded from the FP32 one and refined by one Newton step
 // (relative error ~1e-14), so each Thomas row costs a few FP64 FMAs.
 __device__ __forceinline__ double drcp(double d) {
@@ -216,16 +225,16 @@ __device__ __forceinline__ double drcp(double d) {
 template <int N>
 __device__ __forceinline__ void trimb(const double* a, const double* b, const double* c, double* rhs) {
   double e[N], g[N];
-  double t = drcp(b[0]);
+  double t = drcp1(b[0]);
   e[0] = c[0] * t;
   g[0] = rhs[0] * t;
 #pragma unroll
   for (int k = 1; k < N - 1; ++k) {
-    t = drcp(b[k] - a[k] * e[k - 1]);
+    t = drcp1(b[k] - a[k] * e[k - 1]);
     e[k] = c[k] * t;
     g[k] = (rhs[k] - a[k] * g[k - 1]) * t;
   }
-  rhs[N - 1] = (rhs[N - 1] - a[N - 1] * g[N - 2]) * drcp(b[N - 1] - a[N - 1] * e[N - 2]);
+  rhs[N - 1] = (rhs[N - 1] - a[N - 1] * g[N - 2]) * drcp1(b[N - 1] - a[N - 1] * e[N - 2]);
 #pragma unroll
   for (int k = N - 2; k >= 0; --k) rhs[k] = g[k] - e[k] * rhs[k + 1];
 }

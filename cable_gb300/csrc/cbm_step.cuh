@@ -31,9 +31,12 @@ __device__ __forceinline__ float ldf(const float* p, int i) { return __ldg(p + i
 // Phase B record (per tile, [CG_NB][ld]): what soil_snow, carbon and the
 // water balance need from define_canopy.
 #define CG_NB 20
+// Soil-snow record (per tile, [CG_NC][ld]) handed from the snow-pack kernel
+// to the soil-heat kernel and on to the soil-water kernel.
+#define CG_NC 12
 
 template <bool kDiag>
-__device__ __noinline__ void phase_a(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
+__device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
   const int ld = D.ld;
   const float dels = P.dels;
   // ---------------------------------------------------------------- static
@@ -355,7 +358,7 @@ __device__ __noinline__ void phase_a(const CgDev& D, const CgTables* __restrict_
 }
 
 template <bool kDiag>
-__device__ __noinline__ void phase_b(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
+__device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
   const int ld = D.ld;
   const float dels = P.dels;
   const int iveg = D.iveg[t], isoilm = D.isoilm[t];
@@ -805,7 +808,7 @@ __device__ __noinline__ void phase_b(const CgDev& D, const CgTables* __restrict_
 }
 
 template <bool kDiag>
-__device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
+__device__ __forceinline__ void phase_c1(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
   const int ld = D.ld;
   const float dels = P.dels;
   const int iveg = D.iveg[t], isoilm = D.isoilm[t];
@@ -825,6 +828,11 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
   double wb[CG_MS], wbice[CG_MS];
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) { wb[k] = D.wb[k * ld + t]; wbice[k] = D.wbice[k * ld + t]; }
+  // FP32 shadows of soil water and ice for thresholds and fluxes; every
+  // change to the FP64 state is mirrored into them
+  float wbf[CG_MS], wbicef[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) { wbf[k] = (float)wb[k]; wbicef[k] = (float)wbice[k]; }
   float tgg[CG_MS];
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) tgg[k] = D.tgg[k * ld + t];
@@ -868,11 +876,12 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
               (double)((float)(1 - isflag) * CGSNOW * snowd);
     first_call = false;
   }
+  float g1f = (float)gammzz1;   // layer-1 heat capacity, FP32 working copy
   float wblf[CG_MS], wbfice[CG_MS];
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) {
-    wblf[k] = fmaxf(0.01f, (float)(wb[k] - wbice[k])) / ssat;
-    wbfice[k] = (float)wbice[k] / ssat;
+    wblf[k] = fmaxf(0.01f, wbf[k] - wbicef[k]) / ssat;
+    wbfice[k] = wbicef[k] / ssat;
   }
   float sconds[3] = {0.f, 0.f, 0.f};
   // snowcheck (cbl_snowCheck.F90:9-100)
@@ -948,7 +957,7 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
       ssdnn = ssdn[0];
       if (precis > 0.0f && tgg[0] < TFRZ) {
         snowd = fmaxf(snowd + precis, 0.0f);
-        float dT = precis * HLF / ((float)gammzz1 + CSWAT * precis);
+        float dT = precis * HLF / (g1f + CSWAT * precis);
         tgg[0] = tgg[0] + dT;
         dtmlt0 = dtmlt0 + dT;
         ssdn[0] = fminf(MAX_SSDN, fmaxf(120.0f, ssdn[0] * osnowd / fmaxf(0.01f, snowd) + DLIQ * precis / fmaxf(0.01f, snowd)));
@@ -999,11 +1008,10 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
   auto snow_melting = [&]() -> float {
     float snowmlt = 0.f;
     if (snowd > 0.0f && isflag == 0 && tgg[0] >= TFRZ) {
-      float snowflx = (float)((double)(tgg[0] - TFRZ) * gammzz1);
+      float snowflx = (tgg[0] - TFRZ) * g1f;
       snowmlt = fminf(snowflx / HLF, snowd);
-      dtmlt0 = (float)((double)dtmlt0 + (double)(snowmlt * HLF) / gammzz1);
       snowd = snowd - snowmlt;
-      tgg[0] = (float)((double)tgg[0] - (double)(snowmlt * HLF) / gammzz1);
+      tgg[0] = tgg[0] - snowmlt * HLF / g1f;
     }
     if (snowd > 0.0f && isflag > 0) {
       float sm_prev = 0.f;   // smelt1(:,k-1)
@@ -1085,9 +1093,134 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
     isflag = 1;
     ssdnn = (ssdn[0] * sdepth[0] + ssdn[1] * sdepth[1] + ssdn[2] * sdepth[2]) / (sdepth[0] + sdepth[1] + sdepth[2]);
   }
+  // store: snow pack, layer-1 temperature, heat capacity and the C1 record
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    D.tggsn[k * ld + t] = tggsn[k]; D.ssdn[k * ld + t] = ssdn[k]; D.smass[k * ld + t] = smass[k];
+    D.sdepth[k * ld + t] = sdepth[k];
+  }
+  D.tgg[t] = tgg[0];
+  D.flags[t] = (uint8_t)(isflag | (first_call ? 2 : 0));
+  D.gammzz1[t] = (double)g1f;
+  D.snowd[t] = snowd; D.ssdnn[t] = ssdnn;
+  D.work_c[0 * ld + t] = osnowd;
+  D.work_c[1 * ld + t] = precis;
+  D.work_c[2 * ld + t] = segg;
+  D.work_c[3 * ld + t] = smelt;
+  (void)dtmlt0; (void)sconds; (void)hcll; (void)wblf; (void)wbfice;
+}
+
+template <bool kDiag>
+__device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
+  const int ld = D.ld;
+  const float dels = P.dels;
+  const int iveg = D.iveg[t], isoilm = D.isoilm[t];
+  const int v = iveg - 1, so = isoilm - 1;
+  const CgPftTable& V = T->pft;
+  const CgSoilTable& S = T->soil;
+  const float vlai = (iveg >= 14) ? 0.0f : D.vlai[t];
+  float froot[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
+  const float ssat = ldf(S.ssat, so), sfc = ldf(S.sfc, so), swilt = ldf(S.swilt, so), css = ldf(S.css, so);
+  const float rhosoil = ldf(S.rhosoil, so);
+  float zse[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) zse[k] = S.zse[k];
+  // state
+  double wb[CG_MS], wbice[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) { wb[k] = D.wb[k * ld + t]; wbice[k] = D.wbice[k * ld + t]; }
+  // FP32 shadows of soil water and ice for thresholds and fluxes; every
+  // change to the FP64 state is mirrored into them
+  float wbf[CG_MS], wbicef[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) { wbf[k] = (float)wb[k]; wbicef[k] = (float)wbice[k]; }
+  float tgg[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) tgg[k] = D.tgg[k * ld + t];
+  float tggsn[3], ssdn[3], smass[3], sdepth[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    tggsn[k] = D.tggsn[k * ld + t]; ssdn[k] = D.ssdn[k * ld + t];
+    smass[k] = D.smass[k * ld + t]; sdepth[k] = D.sdepth[k * ld + t];
+  }
+  const uint8_t flags = D.flags[t];
+  int isflag = flags & 1;
+  bool first_call = (flags & 2) != 0;
+  double gammzz1 = D.gammzz1[t];
+  float snowd = D.snowd[t], ssdnn = D.ssdnn[t], snage = D.snage[t], pudsto = D.pudsto[t];
+  float wb_lake = D.wb_lake[t];
+  const float pudsmx = 0.0f;
+  const float rlam = HL;
+  // phase A and B records
+  const float tk = D.work_a[0 * ld + t], precip = D.work_a[6 * ld + t], precip_sn = D.work_a[7 * ld + t];
+  const float transd = D.work_a[27 * ld + t];
+  auto Bv = [&](int i) { return D.work_b[i * ld + t]; };
+  const float ga = Bv(0), dgdtg = Bv(1), fes = Bv(2), fess = Bv(3), fesp = Bv(4);
+  float fevc = Bv(5), fevw = Bv(6);
+  const float cls = Bv(7), precis0 = Bv(8);
+  float evapfbl[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) evapfbl[k] = Bv(9 + k);
+  const float delwc = Bv(15), fpn = Bv(16), frday = Bv(17), tv = Bv(18);
+  const bool cls_snow = (cls == 1.1335f);
+  float tss;
+  // soil_snow, heat part (cbl_soilsnow_main.F90:125-136)
+  float hcll = fmaxf(0.01f, css * rhosoil);
+  float dtmlt0 = 0.f;
+  float g1f = (float)gammzz1;
+  float smelt = D.work_c[3 * ld + t];
+  float wblf[CG_MS], wbfice[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) {
+    wblf[k] = fmaxf(0.01f, wbf[k] - wbicef[k]) / ssat;
+    wbfice[k] = wbicef[k] / ssat;
+  }
+  float sconds[3] = {0.f, 0.f, 0.f};
+  // snow_melting (cbl_snowMelt.F90:9-120), first and second call share code
+  auto snow_melting = [&]() -> float {
+    float snowmlt = 0.f;
+    if (snowd > 0.0f && isflag == 0 && tgg[0] >= TFRZ) {
+      float snowflx = (tgg[0] - TFRZ) * g1f;
+      snowmlt = fminf(snowflx / HLF, snowd);
+      snowd = snowd - snowmlt;
+      tgg[0] = tgg[0] - snowmlt * HLF / g1f;
+    }
+    if (snowd > 0.0f && isflag > 0) {
+      float sm_prev = 0.f;   // smelt1(:,k-1)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        float sgamm = ssdn[k] * CGSNOW * sdepth[k];
+        float snowflx = sm_prev * HLF / dels;
+        tggsn[k] = tggsn[k] + (snowflx * dels + sm_prev * CSWAT * (TFRZ - tggsn[k])) / (sgamm + CSWAT * sm_prev);
+        float osm = smass[k];
+        smass[k] = smass[k] + sm_prev;
+        ssdn[k] = fmaxf(120.0f, fminf(ssdn[k] * osm / smass[k] + DLIQ * (1.0f - osm / smass[k]), MAX_SSDN));
+        if (isoilm != 9) ssdn[k] = fminf(450.0f, ssdn[k]);
+        sdepth[k] = smass[k] / ssdn[k];
+        sgamm = smass[k] * CGSNOW;
+        float sm = 0.f;
+        if (tggsn[k] > TFRZ) {
+          snowflx = (tggsn[k] - TFRZ) * sgamm;
+          sm = fminf(snowflx / HLF, 0.6f * smass[k]);
+          if (k == 0) dtmlt0 = dtmlt0 + sm * HLF / sgamm;
+          smass[k] = smass[k] - sm;
+          tggsn[k] = tggsn[k] - sm * HLF / sgamm;
+          sdepth[k] = smass[k] / ssdn[k];
+        }
+        sm_prev = sm;
+      }
+      // melt of layers 1 and 2 refreezes into the layer below; only the
+      // bottom layer's melt leaves the pack
+      snowmlt = sm_prev;
+      snowd = snowd - snowmlt;
+    }
+    return snowmlt;
+  };
   // stempv (cbl_stempv.F90:13-221) with old_soil_conductivity (cbl_Oldconductivity.F90:7-59)
   float ghflux, sghflux = 0.f;
-  double gammzz[CG_MS];
+  float gf[CG_MS];   // soil layer heat capacities (ssnow%gammzz), J/m2/K
   {
     const float cnsd = ldf(S.cnsd, so);
     float ccnsw[CG_MS];
@@ -1126,27 +1259,28 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
       coeff[0] = 2.0f / (sdepth[2] / sconds[2] + zse[0] / ccnsw[0]);
       coefb = coeff[0];
     }
-    // heat capacity of the soil layers (FP64 storage of gammzz as in the reference)
+    // heat capacity of the soil layers
 #pragma unroll
-    for (int k = 0; k < CG_MS; ++k) {
-      float g = fmaxf(hcll, (1.0f - ssat) * css * rhosoil + ssat * (wblf[k] * CSWAT * DLIQ + wbfice[k] * CSICE * DICE)) * zse[k];
-      gammzz[k] = (double)g;
-    }
-    if (isflag == 0) gammzz[0] = gammzz[0] + (double)(CGSNOW * snowd);
+    for (int k = 0; k < CG_MS; ++k)
+      gf[k] = fmaxf(hcll, (1.0f - ssat) * css * rhosoil + ssat * (wblf[k] * CSWAT * DLIQ + wbfice[k] * CSICE * DICE)) * zse[k];
+    if (isflag == 0) gf[0] = gf[0] + CGSNOW * snowd;
+    // tridiagonal coefficients assembled in FP32, Thomas recurrences in FP64
     double at[9], bt[9], ct[9], rhs[9];
     if (isflag == 0) {
-      // soil-only system: snow rows of the reference's 9-row system are
+      // soil-only system: the snow rows of the reference's 9-row system are
       // identity rows decoupled from the soil (coeff(1) = 0), so the 6-row
       // solve gives the same soil temperatures
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k) {
-        double dtg = (double)dels / gammzz[k];
-        at[k] = -dtg * (double)coeff[k];
-        ct[k] = -dtg * (double)coeff[k + 1];
+        // off-diagonals in FP32; the diagonal 1 - a - c is formed in FP64 so
+        // each row keeps the exact sum that makes the scheme conservative
+        float dtg = dels / gf[k];
+        at[k] = -dtg * coeff[k];
+        ct[k] = -dtg * coeff[k + 1];
         bt[k] = 1.0 - at[k] - ct[k];
+        if (k == 0) bt[k] = bt[k] - (double)(dgdtg * dtg);
       }
-      bt[0] = bt[0] - (double)dgdtg * (double)dels / gammzz[0];
-      tgg[0] = tgg[0] + (ga - tgg[0] * dgdtg) * dels / (float)gammzz[0];
+      tgg[0] = tgg[0] + (ga - tgg[0] * dgdtg) * dels / gf[0];
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k) rhs[k] = (double)tgg[k];
       trimb<CG_MS>(at, bt, ct, rhs);
@@ -1155,24 +1289,23 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
       ghflux = coefb * (tgg[0] - tgg[1]);
     } else {
       const float csnow[4] = {0.f, csn[0], csn[1], coeff[0]};   // coeff(-2..1)
+      const float sgamm0 = ssdn[0] * CGSNOW * sdepth[0];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        float sgamm = ssdn[k] * CGSNOW * sdepth[k];
-        double dtg = (double)(dels / sgamm);
-        at[k] = -dtg * (double)csnow[k];
-        ct[k] = -dtg * (double)csnow[k + 1];
+        float dtg = dels / (ssdn[k] * CGSNOW * sdepth[k]);
+        at[k] = -dtg * csnow[k];
+        ct[k] = -dtg * csnow[k + 1];
         bt[k] = 1.0 - at[k] - ct[k];
+        if (k == 0) bt[k] = bt[k] - (double)(dgdtg * dels / sgamm0);
       }
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k) {
-        double dtg = (double)dels / gammzz[k];
-        at[3 + k] = -dtg * (double)coeff[k];
-        ct[3 + k] = -dtg * (double)coeff[k + 1];
+        float dtg = dels / gf[k];
+        at[3 + k] = -dtg * coeff[k];
+        ct[3 + k] = -dtg * coeff[k + 1];
         bt[3 + k] = 1.0 - at[3 + k] - ct[3 + k];
       }
-      float sgamm = ssdn[0] * CGSNOW * sdepth[0];
-      bt[0] = bt[0] - (double)dgdtg * (double)dels / (double)sgamm;
-      tggsn[0] = tggsn[0] + (ga - tggsn[0] * dgdtg) * dels / sgamm;
+      tggsn[0] = tggsn[0] + (ga - tggsn[0] * dgdtg) * dels / sgamm0;
 #pragma unroll
       for (int k = 0; k < 3; ++k) rhs[k] = (double)tggsn[k];
 #pragma unroll
@@ -1186,39 +1319,130 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
       ghflux = coefb * (tgg[0] - tgg[1]);
     }
   }
-  gammzz1 = gammzz[0];
+  g1f = gf[0];
   tss = (float)(1 - isflag) * tgg[0] + (float)isflag * tggsn[0];
   smelt = smelt + snow_melting();
   // remove_trans (cbl_remove_trans.F90:9-40)
   if (fevc < 0.0f) { fevw = fevw + fevc; fevc = 0.0f; }
 #pragma unroll
-  for (int k = 0; k < CG_MS; ++k) wb[k] = wb[k] - (double)(evapfbl[k] / (zse[k] * DLIQ));
+  for (int k = 0; k < CG_MS; ++k) {
+    const float dw = evapfbl[k] / (zse[k] * DLIQ);
+    wb[k] = wb[k] - (double)dw;
+    wbf[k] = wbf[k] - dw;
+  }
   // soilfreeze (cbl_soilfreeze.F90:9-81)
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) {
-    const double zd = (double)(zse[k] * DICE), zl = (double)(zse[k] * DLIQ);
-    if (tgg[k] < TFRZ && (double)FROZEN_LIMIT * wb[k] - wbice[k] > .001) {
-      double sf = fmin((double)FROZEN_LIMIT * wb[k] - wbice[k], ((double)ssat - wb[k]) / (double)(1.0f - DICE / DLIQ));
-      sf = fmin(fmax(0.0, sf) * zd, (double)(TFRZ - tgg[k]) * gammzz[k] / (double)HLF);
-      wbice[k] = fmin(wbice[k] + sf / zd, (double)FROZEN_LIMIT * wb[k]);
-      wb[k] = wb[k] + sf / zd - sf / zl;
-      float g = fmaxf(hcll, (float)((double)((1.0f - ssat) * css * rhosoil) + (wb[k] - wbice[k]) * (double)(CSWAT * DLIQ) +
-                                    wbice[k] * (double)(CSICE * DICE)));
-      gammzz[k] = (double)g * (double)zse[k];
-      if (k == 0 && isflag == 0) gammzz[k] = gammzz[k] + (double)(CGSNOW * snowd);
-      tgg[k] = tgg[k] + (float)sf * HLF / (float)gammzz[k];
-    } else if (tgg[k] > TFRZ && wbice[k] > 0.) {
-      double sm = fmin(wbice[k] * zd, (double)(tgg[k] - TFRZ) * gammzz[k] / (double)HLF);
-      wbice[k] = fmax(0.0, wbice[k] - sm / zd);
-      wb[k] = wb[k] - sm / zd + sm / zl;
-      float g = fmaxf(hcll, (float)((double)((1.0f - ssat) * css * rhosoil) + (wb[k] - wbice[k]) * (double)(CSWAT * DLIQ) +
-                                    wbice[k] * (double)(CSICE * DICE)));
-      gammzz[k] = (double)g * (double)zse[k];
-      if (k == 0 && isflag == 0) gammzz[k] = gammzz[k] + (double)(CGSNOW * snowd);
-      tgg[k] = tgg[k] - (float)sm * HLF / (float)gammzz[k];
+    const float rzd = 1.0f / (zse[k] * DICE), rzl = 1.0f / (zse[k] * DLIQ);
+    const bool freeze = tgg[k] < TFRZ && FROZEN_LIMIT * wbf[k] - wbicef[k] > .001f;
+    const bool thaw = !freeze && tgg[k] > TFRZ && wbicef[k] > 0.f;
+    if (freeze || thaw) {
+      float amt;   // ice mass frozen (> 0) or melted (< 0), kg/m2
+      if (freeze) {
+        float sf = fminf(FROZEN_LIMIT * wbf[k] - wbicef[k], (ssat - wbf[k]) / (1.0f - DICE / DLIQ));
+        amt = fminf(fmaxf(0.0f, sf) * zse[k] * DICE, (TFRZ - tgg[k]) * gf[k] / HLF);
+      } else {
+        amt = -fminf(wbicef[k] * zse[k] * DICE, (tgg[k] - TFRZ) * gf[k] / HLF);
+      }
+      double wbice_new = wbice[k] + (double)(amt * rzd);
+      wbice_new = freeze ? fmin(wbice_new, (double)FROZEN_LIMIT * wb[k]) : fmax(0.0, wbice_new);
+      wbice[k] = wbice_new;
+      wb[k] = wb[k] + (double)(amt * rzd - amt * rzl);
+      wbf[k] = (float)wb[k];
+      wbicef[k] = (float)wbice[k];
+      gf[k] = fmaxf(hcll, (1.0f - ssat) * css * rhosoil + (wbf[k] - wbicef[k]) * (CSWAT * DLIQ) + wbicef[k] * (CSICE * DICE)) * zse[k];
+      if (k == 0 && isflag == 0) gf[k] = gf[k] + CGSNOW * snowd;
+      tgg[k] = tgg[k] + amt * HLF / gf[k];
     }
   }
-  gammzz1 = gammzz[0];
+  g1f = gf[0];
+  // store: temperatures, snow pack, soil water / ice and the C2 record
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) { D.wb[k * ld + t] = wb[k]; D.wbice[k * ld + t] = wbice[k]; D.tgg[k * ld + t] = tgg[k]; }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    D.tggsn[k * ld + t] = tggsn[k]; D.ssdn[k * ld + t] = ssdn[k]; D.smass[k * ld + t] = smass[k];
+    D.sdepth[k * ld + t] = sdepth[k];
+  }
+  D.gammzz1[t] = (double)g1f;
+  D.snowd[t] = snowd;
+  D.work_c[3 * ld + t] = smelt;
+  D.work_c[4 * ld + t] = ghflux;
+  D.work_c[5 * ld + t] = sghflux;
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) D.work_c[(6 + k) * ld + t] = gf[k];
+  (void)tss; (void)first_call; (void)dtmlt0;
+}
+
+template <bool kDiag>
+__device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
+  const int ld = D.ld;
+  const float dels = P.dels;
+  const int iveg = D.iveg[t], isoilm = D.isoilm[t];
+  const int v = iveg - 1, so = isoilm - 1;
+  const CgPftTable& V = T->pft;
+  const CgSoilTable& S = T->soil;
+  const float vlai = (iveg >= 14) ? 0.0f : D.vlai[t];
+  float froot[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
+  const float ssat = ldf(S.ssat, so), sfc = ldf(S.sfc, so), swilt = ldf(S.swilt, so), css = ldf(S.css, so);
+  const float rhosoil = ldf(S.rhosoil, so);
+  float zse[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) zse[k] = S.zse[k];
+  // state
+  double wb[CG_MS], wbice[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) { wb[k] = D.wb[k * ld + t]; wbice[k] = D.wbice[k * ld + t]; }
+  // FP32 shadows of soil water and ice for thresholds and fluxes; every
+  // change to the FP64 state is mirrored into them
+  float wbf[CG_MS], wbicef[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) { wbf[k] = (float)wb[k]; wbicef[k] = (float)wbice[k]; }
+  float tgg[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) tgg[k] = D.tgg[k * ld + t];
+  float tggsn[3], ssdn[3], smass[3], sdepth[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    tggsn[k] = D.tggsn[k * ld + t]; ssdn[k] = D.ssdn[k * ld + t];
+    smass[k] = D.smass[k * ld + t]; sdepth[k] = D.sdepth[k * ld + t];
+  }
+  const uint8_t flags = D.flags[t];
+  int isflag = flags & 1;
+  bool first_call = (flags & 2) != 0;
+  double gammzz1 = D.gammzz1[t];
+  float snowd = D.snowd[t], ssdnn = D.ssdnn[t], snage = D.snage[t], pudsto = D.pudsto[t];
+  float wb_lake = D.wb_lake[t];
+  const float pudsmx = 0.0f;
+  const float rlam = HL;
+  // phase A and B records
+  const float tk = D.work_a[0 * ld + t], precip = D.work_a[6 * ld + t], precip_sn = D.work_a[7 * ld + t];
+  const float transd = D.work_a[27 * ld + t];
+  auto Bv = [&](int i) { return D.work_b[i * ld + t]; };
+  const float ga = Bv(0), dgdtg = Bv(1), fes = Bv(2), fess = Bv(3), fesp = Bv(4);
+  float fevc = Bv(5), fevw = Bv(6);
+  const float cls = Bv(7), precis0 = Bv(8);
+  float evapfbl[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) evapfbl[k] = Bv(9 + k);
+  const float delwc = Bv(15), fpn = Bv(16), frday = Bv(17), tv = Bv(18);
+  const bool cls_snow = (cls == 1.1335f);
+  float tss;
+  // soil_snow, water part (cbl_soilsnow_main.F90:139-203), then snow_aging,
+  // carbon and the balances
+  const float osnowd = D.work_c[0 * ld + t];
+  float precis = D.work_c[1 * ld + t];
+  const float segg = D.work_c[2 * ld + t];
+  float smelt = D.work_c[3 * ld + t];
+  const float ghflux = D.work_c[4 * ld + t], sghflux = D.work_c[5 * ld + t];
+  float gf[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) gf[k] = D.work_c[(6 + k) * ld + t];
+  float g1f = (float)gammzz1;
+  // remove_trans moved negative transpiration into wet-canopy evaporation
+  if (fevc < 0.0f) { fevw = fevw + fevc; fevc = 0.0f; }
   // infiltration (cbl_soilsnow_main.F90:139-159)
   float rnof1, rnof2;
   float fwtop[3];
@@ -1228,7 +1452,7 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
     float rem = weting;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      sinfil[k] = fminf(0.95f * (float)((double)ssat - wb[k]) * zse[k] * DLIQ, rem);
+      sinfil[k] = fminf(0.95f * (ssat - wbf[k]) * zse[k] * DLIQ, rem);
       rem = rem - sinfil[k];
     }
     fwtop[0] = sinfil[0] / dels - segg;
@@ -1247,11 +1471,11 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
     float delt_prev = 0.f;
 #pragma unroll
     for (int k = 1; k <= CG_MS - 1; ++k) {
-      float wbl_k = fmaxf(0.01f, (float)(wb[k - 1] - wbice[k - 1]));
-      float wbl_kp = fmaxf(0.01f, (float)(wb[k] - wbice[k]));
+      float wbl_k = fmaxf(0.01f, wbf[k - 1] - wbicef[k - 1]);
+      float wbl_kp = fmaxf(0.01f, wbf[k] - wbicef[k]);
       float delt = wbl_kp - wbl_k;
       float wh = fminf(wbl_k, wbl_kp);
-      if (wbice[k - 1] > 0.05 || wbice[k] > 0.01) wh = 0.9f * wbl_k + 0.1f * wbl_kp;
+      if (wbicef[k - 1] > 0.05f || wbicef[k] > 0.01f) wh = 0.9f * wbl_k + 0.1f * wbl_kp;
       float speed_k = hyds * powf(wh / ssat, i2bp3 - 1.f);
       float rat = delt_prev / (delt + fsignf(1.0e-20f, delt));
       float phi = fmaxf(fmaxf(0.0f, fminf(1.0f, 2.0f * rat)), fminf(2.0f, rat));
@@ -1259,13 +1483,13 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
       fluxh[k] = speed_k * (wbl_k + phi * (wh - wbl_k));
       delt_prev = delt;
     }
-    if (wb[CG_MS - 1] > (double)sfc) {
-      float wbl_k = fmaxf(0.001f, (float)(wb[CG_MS - 1] - wbice[CG_MS - 1]));
-      float wbl_kp = fmaxf(0.001f, (float)((double)ssat - wbice[CG_MS - 1]));
+    if (wbf[CG_MS - 1] > sfc) {
+      float wbl_k = fmaxf(0.001f, wbf[CG_MS - 1] - wbicef[CG_MS - 1]);
+      float wbl_kp = fmaxf(0.001f, ssat - wbicef[CG_MS - 1]);
       float wh = fminf(wbl_k, wbl_kp);
-      if (wbice[CG_MS - 1] > 0.05) wh = 0.9f * wbl_k + 0.1f * wbl_kp;
+      if (wbicef[CG_MS - 1] > 0.05f) wh = 0.9f * wbl_k + 0.1f * wbl_kp;
       float speed_k = hyds * powf(wh / ssat, i2bp3 - 1.f);
-      speed_k = 0.5f * speed_k / (1.f - fminf(0.5f, 10.f * (float)wbice[CG_MS - 1]));
+      speed_k = 0.5f * speed_k / (1.f - fminf(0.5f, 10.f * wbicef[CG_MS - 1]));
       speed_k = fminf(0.5f * speed_k, 0.5f * zse[CG_MS - 1] / dels);
       fluxh[CG_MS] = fmaxf(0.0f, speed_k * wbl_k);
     }
@@ -1273,49 +1497,60 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
     double wblfd[CG_MS];
 #pragma unroll
     for (int k = CG_MS; k >= 1; --k) {
-      fluxh[k - 1] = fminf(fluxh[k - 1], (float)((double)ssat - wb[k - 1]) * zse[k - 1] / dels + fluxh[k]);
-      wb[k - 1] = wb[k - 1] + (double)(dels * (fluxh[k - 1] - fluxh[k]) / zse[k - 1]);
-      double ssatcurr = (double)ssat - wbice[k - 1];
-      dtt[k - 1] = (float)((double)dels / ((double)zse[k - 1] * ssatcurr));
-      wblfd[k - 1] = (wb[k - 1] - wbice[k - 1]) / ssatcurr;
+      fluxh[k - 1] = fminf(fluxh[k - 1], (ssat - wbf[k - 1]) * zse[k - 1] / dels + fluxh[k]);
+      const float dw = dels * (fluxh[k - 1] - fluxh[k]) / zse[k - 1];
+      wb[k - 1] = wb[k - 1] + (double)dw;
+      wbf[k - 1] = wbf[k - 1] + dw;
+      const double ssatcurr = (double)ssat - wbice[k - 1];
+      dtt[k - 1] = dels / (zse[k - 1] * (ssat - wbicef[k - 1]));
+      wblfd[k - 1] = (wb[k - 1] - wbice[k - 1]) * drcp1(ssatcurr);
     }
     rnof2 = dels * fluxh[CG_MS] * DLIQ;
     double at[CG_MS], bt[CG_MS], ct[CG_MS];
-    at[0] = 0.0; ct[CG_MS - 1] = 0.0;
+    float at32[CG_MS], ct32[CG_MS];
+    at32[0] = 0.f; ct32[CG_MS - 1] = 0.f;
 #pragma unroll
     for (int k = 2; k <= CG_MS; ++k) {
       float wa = (float)wblfd[k - 2], wbv = (float)wblfd[k - 1];
       float wbh_k = (zse[k - 1] * wa + zse[k - 2] * wbv) / (zse[k - 1] + zse[k - 2]);
       float fact = powf(wbh_k, ibp2 - 1.f);
-      float icef = fmaxf((float)(wbice[k - 2] / fmax(0.01, wb[k - 2])), (float)(wbice[k - 1] / fmax(0.01, wb[k - 1])));
+      float icef = fmaxf(wbicef[k - 2] / fmaxf(0.01f, wbf[k - 2]), wbicef[k - 1] / fmaxf(0.01f, wbf[k - 1]));
       float pwb_wbh = (hsbh * (1.f - fminf(2.f * fminf(0.1f, icef), 0.1f))) * fmaxf(pwb_min, wbh_k * fact);
       float z3_k = pwb_wbh / ldf(S.zshh, k - 1);
-      at[k - 1] = -(double)dtt[k - 1] * (double)z3_k;
-      ct[k - 2] = -(double)dtt[k - 2] * (double)z3_k;
+      at32[k - 1] = -dtt[k - 1] * z3_k;
+      ct32[k - 2] = -dtt[k - 2] * z3_k;
     }
 #pragma unroll
-    for (int k = 0; k < CG_MS; ++k) bt[k] = 1.0 - at[k] - ct[k];
+    for (int k = 0; k < CG_MS; ++k) { at[k] = at32[k]; ct[k] = ct32[k]; bt[k] = 1.0 - at[k] - ct[k]; }
 #pragma unroll
     for (int k = 0; k < 3; ++k) wblfd[k] = wblfd[k] + (double)(dtt[k] * fwtop[k] / DLIQ);
     trimb<CG_MS>(at, bt, ct, wblfd);
 #pragma unroll
-    for (int k = 0; k < CG_MS; ++k) wb[k] = wblfd[k] * ((double)ssat - wbice[k]) + wbice[k];
-    const double dfactor = (double)(1.0f - DICE / DLIQ);
+    for (int k = 0; k < CG_MS; ++k) {
+      wb[k] = fma(wblfd[k], (double)ssat - wbice[k], wbice[k]);
+      wbf[k] = (float)wb[k];
+    }
+    const float dfactor = 1.0f - DICE / DLIQ;
 #pragma unroll
     for (int k = 0; k < CG_MS; ++k) {
-      if (wbice[k] > (double)FROZEN_LIMIT * wb[k]) {
-        double sm = (wbice[k] - (double)FROZEN_LIMIT * wb[k]) / (1.0 - (double)FROZEN_LIMIT * dfactor);
+      if (wbicef[k] > FROZEN_LIMIT * wbf[k]) {
+        double sm = (wbice[k] - (double)FROZEN_LIMIT * wb[k]) * (double)(1.0f / (1.0f - FROZEN_LIMIT * dfactor));
         wbice[k] = wbice[k] - sm;
-        wb[k] = wb[k] - dfactor * sm;
-        tgg[k] = tgg[k] - (float)sm * zse[k] * DICE * HLF / (float)gammzz[k];
+        wb[k] = wb[k] - (double)dfactor * sm;
+        wbf[k] = (float)wb[k];
+        wbicef[k] = (float)wbice[k];
+        tgg[k] = tgg[k] - (float)sm * zse[k] * DICE * HLF / gf[k];
       }
     }
   }
   // surfbv remainder
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) {
-    rnof1 = rnof1 + (float)fmax(wb[k] - (double)ssat, 0.0) * DLIQ * zse[k];
-    wb[k] = fmax((double)(swilt / 4.0f), fmin(wb[k], (double)ssat));
+    rnof1 = rnof1 + fmaxf(wbf[k] - ssat, 0.0f) * DLIQ * zse[k];
+    if (wbf[k] > ssat || wbf[k] < swilt / 4.0f) {
+      wb[k] = fmax((double)(swilt / 4.0f), fmin(wb[k], (double)ssat));
+      wbf[k] = (float)wb[k];
+    }
   }
   float rnof5 = 0.f;
   {
@@ -1324,7 +1559,7 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
     if (snowd > MAX_GLACIER_SNOWD) {
       rnof5 = fminf(0.1f, snowd - MAX_GLACIER_SNOWD);
       if (isflag == 0) {
-        tgg[0] = tgg[0] - rnof5 * HLF / (float)gammzz1;
+        tgg[0] = tgg[0] - rnof5 * HLF / g1f;
         snowd = snowd - rnof5;
       } else {
         smasstot = smass[0] + smass[1] + smass[2];
@@ -1355,6 +1590,7 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
     sinfil = fminf(xl, wb_lake);
     wb[CG_MS - 1] = wb[CG_MS - 1] - (double)(sinfil / (zse[CG_MS - 1] * DLIQ));
     wb_lake = fmaxf(0.0f, wb_lake - sinfil);
+    wbf[CG_MS - 1] = (float)wb[CG_MS - 1];
   }
   rnof1 = rnof1 / dels + rnof5 / dels;
   rnof2 = rnof2 / dels;
@@ -1395,12 +1631,12 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
   }
   {
     float den = fmaxf(0.07f, sfc - swilt);
-    float rswc = fmaxf(0.0001f, froot[0] * ((float)wb[1] - swilt)) / den;
+    float rswc = fmaxf(0.0001f, froot[0] * (wbf[1] - swilt)) / den;
     float tsoil = froot[0] * tgg[1] - TFRZ;
     float tref = fmaxf(0.f, tgg[CG_MS - 1] - (TFRZ - .05f));
 #pragma unroll
     for (int k = 1; k < CG_MS; ++k) {
-      rswc += fmaxf(0.0001f, froot[k] * ((float)wb[k] - swilt)) / den;
+      rswc += fmaxf(0.0001f, froot[k] * (wbf[k] - swilt)) / den;
       tsoil += froot[k] * tgg[k];
     }
     rswc = fminf(1.f, rswc);
@@ -1415,7 +1651,7 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
     float coef_cold = expf(fminf(1.f, -(tv - ldf(V.tvclst, v))));
     float wbav = 0.f;
 #pragma unroll
-    for (int k = 0; k < CG_MS; ++k) wbav += froot[k] * (float)wb[k];
+    for (int k = 0; k < CG_MS; ++k) wbav += froot[k] * wbf[k];
     wbav = fmaxf(0.01f, wbav);
     float campbell = 2.0f - ldf(S.ibp2, so);
     float esw = fmaxf(1.0f, powf(wbav, campbell) - 1.0f);
@@ -1451,14 +1687,13 @@ __device__ __noinline__ void phase_c(const CgDev& D, const CgTables* __restrict_
   // store
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) { D.wb[k * ld + t] = wb[k]; D.wbice[k * ld + t] = wbice[k]; D.tgg[k * ld + t] = tgg[k]; }
+  (void)first_call; (void)isoilm;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     D.tggsn[k * ld + t] = tggsn[k]; D.ssdn[k * ld + t] = ssdn[k]; D.smass[k * ld + t] = smass[k];
     D.sdepth[k * ld + t] = sdepth[k]; D.cplant[k * ld + t] = cplant[k];
   }
   D.csoil[t] = csoil[0]; D.csoil[ld + t] = csoil[1];
-  D.flags[t] = (uint8_t)(isflag | (first_call ? 2 : 0));
-  D.gammzz1[t] = gammzz1;
   D.snowd[t] = snowd; D.ssdnn[t] = ssdnn; D.snage[t] = snage; D.pudsto[t] = pudsto;
   D.tss[t] = tss; D.wb_lake[t] = wb_lake;
   D.owb[t] = wbtot; D.wbal_tot[t] = wbal_tot;

@@ -1,0 +1,5 @@
+// Phase C2 of the cbm() timestep kernel set -- soil heat: stempv (FP64 Thomas), second snow_melting, remove_trans, soilfreeze.
+#define CG_PHASE phase_c2
+#define CG_PHASE_KERNEL cbm_phase_c2_kernel
+#define CG_PHASE_LAUNCH launch_phase_c2
+#include "phase_kernels.cuh"

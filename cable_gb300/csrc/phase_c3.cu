@@ -1,0 +1,5 @@
+// Phase C3 of the cbm() timestep kernel set -- soil water: infiltration, smoisturev (FP64 Thomas), surfbv, snow_aging, carbon, water balance.
+#define CG_PHASE phase_c3
+#define CG_PHASE_KERNEL cbm_phase_c3_kernel
+#define CG_PHASE_LAUNCH launch_phase_c3
+#include "phase_kernels.cuh"

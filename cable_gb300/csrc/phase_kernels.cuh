@@ -1,0 +1,44 @@
+// Kernel wrapper and host launcher for one phase of the timestep.  Each
+// phase_X.cu translation unit includes this with CG_PHASE set, so the three
+// phases compile in parallel and each can carry its own floating-point flags.
+#pragma once
+#include <cuda_runtime.h>
+#include "cbm_step.cuh"
+
+namespace cg {
+
+constexpr int kPhaseBlock = 128;
+// Minimum resident blocks per SM requested from the register allocator
+// (occupancy versus spills); set per phase translation unit.
+#ifndef CG_MIN_BLOCKS
+#define CG_MIN_BLOCKS 1
+#endif
+
+// Launch one phase over D.mp tiles: a = radiation, b = canopy, c1 = snow
+// pack, c2 = soil heat, c3 = soil water, carbon and balances.  clock, when non-null, holds ktau on the device (graph replay).
+void launch_phase_a(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P, const int* clock);
+void launch_phase_b(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P, const int* clock);
+void launch_phase_c1(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P, const int* clock);
+void launch_phase_c2(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P, const int* clock);
+void launch_phase_c3(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P, const int* clock);
+
+#ifdef CG_PHASE
+template <bool kDiag>
+__global__ void __launch_bounds__(kPhaseBlock, CG_MIN_BLOCKS)
+    CG_PHASE_KERNEL(CgDev D, const CgTables* __restrict__ T, StepParams P, const int* __restrict__ clock) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= D.mp) return;
+  StepParams p = P;
+  if (clock) { p.ktau = clock[0]; p.step_index = clock[0] - 1; }
+  CG_PHASE<kDiag>(D, T, p, t);
+}
+
+void CG_PHASE_LAUNCH(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
+                     const int* clock) {
+  const int grid = (D.mp + kPhaseBlock - 1) / kPhaseBlock;
+  if (diag) CG_PHASE_KERNEL<true><<<grid, kPhaseBlock, 0, s>>>(D, T, P, clock);
+  else CG_PHASE_KERNEL<false><<<grid, kPhaseBlock, 0, s>>>(D, T, P, clock);
+}
+#endif
+
+}  // namespace cg

@@ -33,7 +33,7 @@ EXPORTS = [
     "cablegpu_field_id", "cablegpu_set_field", "cablegpu_get_field", "cablegpu_field_device_ptr",
     "cablegpu_set_forcing", "cablegpu_set_synthetic_forcing", "cablegpu_set_options", "cablegpu_step",
     "cablegpu_run", "cablegpu_synchronize", "cablegpu_run_timed", "cablegpu_kernel_timed",
-    "cablegpu_launch_count", "cablegpu_last_error",
+    "cablegpu_launch_count", "cablegpu_param_table", "cablegpu_last_error",
 ]
 
 _lib = None
@@ -85,6 +85,7 @@ def load(build_if_missing: bool = True):
     L.cablegpu_kernel_timed.argtypes = [vp, ip, ip, C.c_float, C.POINTER(C.c_float)]
     L.cablegpu_launch_count.argtypes = [vp]
     L.cablegpu_launch_count.restype = C.c_longlong
+    L.cablegpu_param_table.argtypes = [ip, C.c_char_p, C.POINTER(C.c_float), ip]
     L.cablegpu_last_error.argtypes = [vp]
     L.cablegpu_last_error.restype = C.c_char_p
     _lib = L

@@ -47,7 +47,8 @@ class TileSet:
 
     def subset(self, idx) -> "TileSet":
         """Tiles ``idx`` as a new set (forcing is keyed on the new tile index)."""
-        idx = np.asarray(idx)
+        if not isinstance(idx, slice):
+            idx = np.asarray(idx)
         g = lambda a: np.ascontiguousarray(a[idx])
         return TileSet(self.name + "[sub]", g(self.iveg), g(self.isoilm), g(self.vlai), g(self.lat),
                        g(self.lonphase), g(self.tbase), g(self.swscale), g(self.snowd0), g(self.tgg0),

@@ -133,8 +133,15 @@ int cablegpu_synchronize(cablegpu_ctx* ctx);
 int cablegpu_run_timed(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, float* ms_total);
 int cablegpu_kernel_timed(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, float* ms_per_launch);
 /* Number of kernel launches of the timestep issued by this context so far
- * (three per step). */
+ * (five per step: radiation, canopy, snow pack, soil heat, soil water). */
 long long cablegpu_launch_count(cablegpu_ctx* ctx);
+
+/* Copies a built-in parameter table (no context or GPU needed): table 0 is
+ * the per-plant-type table of pft_params.nml with derived entries "dleaf"
+ * and "froot" (6 x 17, layer-major), table 1 the per-soil table of
+ * cable_soilparm.nml with derived entries (hsbh, ibp2, i2bp3, pwb_min,
+ * cnsd).  `n` is the capacity of `out`. */
+int cablegpu_param_table(int table, const char* name, float* out, int n);
 
 const char* cablegpu_last_error(cablegpu_ctx* ctx);
 

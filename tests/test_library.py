@@ -1,0 +1,92 @@
+"""The C-ABI library (no GPU needed): build, exported symbols, field
+registry, parameter tables against the oracle's copy, argument validation."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from cable_gb300 import build as B
+from cable_gb300 import runtime as R
+from cable_gb300 import workloads as W
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "cablegpu.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(cablegpu_\w+)\s*\(", txt)))
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    lib = C.CDLL(B.build())
+    syms = declared_symbols()
+    assert len(syms) >= 19
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(syms) <= set(R.EXPORTS) | set(syms)
+
+
+def test_field_registry_is_consistent():
+    f = R.fields()
+    assert len(f) == R.load().cablegpu_num_fields()
+    for name in ("wb", "wbice", "tgg", "tggsn", "ssdn", "smass", "sdepth", "snowd", "cansto", "out", "forcing_in"):
+        assert name in f
+    assert f["wb"][1] == 6 and f["wb"][2] == R.F64
+    assert f["tggsn"][1] == 3 and f["out"][1] == 8
+    assert f["forcing_in"][1] == R.NFORCING
+    ids = sorted(v[0] for v in f.values())
+    assert ids == list(range(len(f)))
+    assert R.load().cablegpu_field_id(b"no_such_field") < 0
+
+
+def test_create_rejects_bad_tiles_without_a_gpu():
+    """Argument validation happens before any CUDA call."""
+    ts = W.grid(16)
+    ts.iveg = ts.iveg.copy()
+    ts.iveg[3] = 18
+    with pytest.raises(R.CableGPUError) as e:
+        R.CableGPU(ts)
+    assert e.value.code == -1
+    ts.iveg[3] = 5
+    ts.isoilm = ts.isoilm.copy()
+    ts.isoilm[0] = 0
+    with pytest.raises(R.CableGPUError):
+        R.CableGPU(ts)
+
+
+def test_null_arguments_are_errors():
+    L = R.load()
+    assert L.cablegpu_create(None, 0, None) == -1
+    assert L.cablegpu_step(None, 1, C.c_float(1800.0)) == -1
+    assert L.cablegpu_destroy(None) == -1
+    assert L.cablegpu_field_info(10 ** 6, None, None, None, None) == -1
+
+
+def test_parameter_tables_match_the_oracle(oracle):
+    """The product's derived per-type tables equal the oracle's restatement."""
+    L = R.load()
+    buf = (C.c_float * 17)()
+    for name in ("vcmax", "a1gs", "hc", "frac4", "xfang", "rp20", "vegcf", "g1", "refl1", "taul2"):
+        assert L.cablegpu_param_table(0, name.encode(), buf, 17) == 0
+        ref = [oracle.lib().cbmref_pft_value(name.encode(), v) for v in range(1, 18)]
+        np.testing.assert_allclose(np.frombuffer(buf, np.float32), np.float32(ref), rtol=1e-7)
+    sbuf = (C.c_float * 9)()
+    for name in ("bch", "ssat", "sfc", "swilt", "hyds", "css", "rhosoil"):
+        assert L.cablegpu_param_table(1, name.encode(), sbuf, 9) == 0
+        ref = [oracle.lib().cbmref_soil_value(name.encode(), s) for s in range(1, 10)]
+        np.testing.assert_allclose(np.frombuffer(sbuf, np.float32), np.float32(ref), rtol=1e-7)
+    # derived: root fractions and leaf width
+    fr = (C.c_float * (6 * 17))()
+    assert L.cablegpu_param_table(0, b"froot", fr, 6 * 17) == 0
+    fr = np.frombuffer(fr, np.float32).reshape(6, 17)
+    dl = (C.c_float * 17)()
+    assert L.cablegpu_param_table(0, b"dleaf", dl, 17) == 0
+    dp = lambda: C.c_double()
+    for v in range(1, 18):
+        f6 = (C.c_double * 6)(); a, b_, c_ = dp(), dp(), dp()
+        oracle.lib().cbmref_params(v, 1, f6, C.byref(a), C.byref(b_), C.byref(c_))
+        np.testing.assert_allclose(fr[:, v - 1], np.array(f6[:]), rtol=2e-6, atol=1e-7)
+        assert np.frombuffer(dl, np.float32)[v - 1] == pytest.approx(a.value, rel=1e-6)
+    assert abs(fr.sum(0) - 1).max() < 1e-5
