@@ -253,6 +253,8 @@ def run_gb300(args):
     # --- per-step kernel time for the roofline (events around each launch set)
     step_ms = g.kernel_timed(ktau, 8, dels)
     ktau += 8
+    phase_ms = g.phase_timed(ktau, 8, dels)
+    ktau += 8
     g.synchronize()
     peaks = {}
     try:
@@ -265,7 +267,9 @@ def run_gb300(args):
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "traffic": traffic_per_step(args.mp),
             "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
-            "scope": "one timestep (its 3 kernels), %d algorithmic B per tile-step" % ALGO_BYTES_PER_TILE_STEP}
+            "scope": "one timestep (its 5 kernels, CUDA events around each step), %d algorithmic B per tile-step"
+                     % ALGO_BYTES_PER_TILE_STEP,
+            "kernels_ms": {k: round(v, 4) for k, v in phase_ms.items()}}
     # --- end to end through the C ABI with host buffers
     e2e = None
     try:

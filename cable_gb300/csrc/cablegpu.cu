@@ -478,7 +478,8 @@ int cablegpu_run(cablegpu_ctx* c, int ktau0, int nsteps, float dels) {
     CG_CUDA(c, cudaMemcpyAsync(c->d_clock, c->h_clock, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     while (nsteps - done >= kGraphSteps) {
       CG_CUDA(c, cudaGraphLaunch(c->graph, c->stream));
-      c->launches += kKernelsPerStep * kGraphSteps;
+      // the five step kernels plus the one-thread clock kernel of each step
+      c->launches += (kKernelsPerStep + 1) * kGraphSteps;
       done += kGraphSteps;
     }
     // the pinned clock buffer must not be rewritten before the copy ran
@@ -540,6 +541,43 @@ int cablegpu_kernel_timed(cablegpu_ctx* c, int ktau0, int nsteps, float dels, fl
   }
   for (auto& e : ev) cudaEventDestroy(e);
   *ms_per_launch = (float)(tot / nsteps);
+  return CABLEGPU_OK;
+}
+
+int cablegpu_phase_timed(cablegpu_ctx* c, int ktau0, int nsteps, float dels, float* ms_per_phase) {
+  if (!c || !ms_per_phase || nsteps <= 0) return CABLEGPU_ERR_ARG;
+  constexpr int K = kKernelsPerStep;
+  std::vector<cudaEvent_t> ev((K + 1) * nsteps);
+  for (auto& e : ev) CG_CUDA(c, cudaEventCreate(&e));
+  bind_device_view(c);
+  const bool diag = c->diag != 0;
+  for (int i = 0; i < nsteps; ++i) {
+    const StepParams p = make_params(c, ktau0 + i, dels);
+    cudaEvent_t* e = &ev[(K + 1) * i];
+    CG_CUDA(c, cudaEventRecord(e[0], c->stream));
+    launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    CG_CUDA(c, cudaEventRecord(e[1], c->stream));
+    launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    CG_CUDA(c, cudaEventRecord(e[2], c->stream));
+    launch_phase_c1(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    CG_CUDA(c, cudaEventRecord(e[3], c->stream));
+    launch_phase_c2(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    CG_CUDA(c, cudaEventRecord(e[4], c->stream));
+    launch_phase_c3(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    CG_CUDA(c, cudaEventRecord(e[5], c->stream));
+    CG_CUDA(c, cudaGetLastError());
+    c->launches += K;
+  }
+  CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < K; ++k) ms_per_phase[k] = 0.f;
+  for (int i = 0; i < nsteps; ++i) {
+    for (int k = 0; k < K; ++k) {
+      float ms = 0.f;
+      CG_CUDA(c, cudaEventElapsedTime(&ms, ev[(K + 1) * i + k], ev[(K + 1) * i + k + 1]));
+      ms_per_phase[k] += ms / nsteps;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
   return CABLEGPU_OK;
 }
 

@@ -203,21 +203,12 @@ __device__ __forceinline__ float xejmxt3(float x) {
   return fmaxf(0.0f, num / den);
 }
 
-// One-Newton-step variant (relative error ~1e-14) for the water-content
-// scaling of the moisture solve.
+// FP64 reciprocal seeded from the FP32 one and refined by one Newton step
+// (relative error ~1e-14), so each Thomas row costs a few FP64 FMAs instead
+// of a full FP64 division.
 __device__ __forceinline__ double drcp1(double d) {
   double r = (double)(1.0f / (float)d);
   double e = fma(-d, r, 1.0);
-  return fma(r, e, r);
-}
-
-// FP64 reciprocal seeded from the FP32 one and refined by one Newton step
-// (relative error ~1e-14), so each Thomas row costs a few FP64 FMAs.
-__device__ __forceinline__ double drcp(double d) {
-  double r = (double)(1.0f / (float)d);
-  double e = fma(-d, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-d, r, 1.0);
   return fma(r, e, r);
 }
 

@@ -33,8 +33,9 @@ EXPORTS = [
     "cablegpu_field_id", "cablegpu_set_field", "cablegpu_get_field", "cablegpu_field_device_ptr",
     "cablegpu_set_forcing", "cablegpu_set_synthetic_forcing", "cablegpu_set_options", "cablegpu_step",
     "cablegpu_run", "cablegpu_synchronize", "cablegpu_run_timed", "cablegpu_kernel_timed",
-    "cablegpu_launch_count", "cablegpu_param_table", "cablegpu_last_error",
+    "cablegpu_launch_count", "cablegpu_param_table", "cablegpu_last_error", "cablegpu_phase_timed",
 ]
+PHASES = ["radiation", "canopy", "snow_pack", "soil_heat", "soil_water"]
 
 _lib = None
 
@@ -83,6 +84,7 @@ def load(build_if_missing: bool = True):
     L.cablegpu_synchronize.argtypes = [vp]
     L.cablegpu_run_timed.argtypes = [vp, ip, ip, C.c_float, C.POINTER(C.c_float)]
     L.cablegpu_kernel_timed.argtypes = [vp, ip, ip, C.c_float, C.POINTER(C.c_float)]
+    L.cablegpu_phase_timed.argtypes = [vp, ip, ip, C.c_float, C.POINTER(C.c_float)]
     L.cablegpu_launch_count.argtypes = [vp]
     L.cablegpu_launch_count.restype = C.c_longlong
     L.cablegpu_param_table.argtypes = [ip, C.c_char_p, C.POINTER(C.c_float), ip]
@@ -212,6 +214,12 @@ class CableGPU:
         ms = C.c_float()
         self._check(self.L.cablegpu_kernel_timed(self.h, int(ktau0), int(nsteps), float(dels), C.byref(ms)))
         return ms.value
+
+    def phase_timed(self, ktau0, nsteps, dels=1800.0) -> dict:
+        """Average milliseconds of each kernel of a step, {phase: ms}."""
+        ms = (C.c_float * len(PHASES))()
+        self._check(self.L.cablegpu_phase_timed(self.h, int(ktau0), int(nsteps), float(dels), ms))
+        return dict(zip(PHASES, [float(x) for x in ms]))
 
     def launch_count(self) -> int:
         return int(self.L.cablegpu_launch_count(self.h))

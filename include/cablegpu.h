@@ -132,8 +132,14 @@ int cablegpu_synchronize(cablegpu_ctx* ctx);
  * bracketed by its own events. */
 int cablegpu_run_timed(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, float* ms_total);
 int cablegpu_kernel_timed(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, float* ms_per_launch);
-/* Number of kernel launches of the timestep issued by this context so far
- * (five per step: radiation, canopy, snow pack, soil heat, soil water). */
+/* phase_timed: average milliseconds of each of the five kernels of a step
+ * (radiation, canopy, snow pack, soil heat, soil water), each bracketed by
+ * its own events; ms_per_phase has 5 elements. */
+int cablegpu_phase_timed(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, float* ms_per_phase);
+/* Number of kernel launches of the timestep issued by this context so far:
+ * five per step (radiation, canopy, snow pack, soil heat, soil water), plus
+ * one single-thread kernel per step that advances the step counter when the
+ * steps run as a replayed CUDA graph (cablegpu_run). */
 long long cablegpu_launch_count(cablegpu_ctx* ctx);
 
 /* Copies a built-in parameter table (no context or GPU needed): table 0 is

@@ -1,0 +1,109 @@
+"""Committed golden fixtures (tests/golden/*.npz, written by
+tests/golden/make_golden.py from the FP64 oracle).
+
+CPU: the oracle still reproduces every fixture, so a change to its physics
+cannot go unnoticed.  GPU: the CUDA timestep, run through the C ABI on the
+fixture's own tiles, matches the fixture within the spec's tolerances
+(fluxes 1e-3 relative with a 1 W/m2 floor, temperatures 0.01 K, soil
+moisture 1e-5 m3/m3)."""
+import os
+
+import numpy as np
+import pytest
+
+import harness as H
+from cable_gb300 import workloads as W
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = ["site5", "grid128", "snow128"]
+# oracle diag name -> GPU diag field
+GPU_DIAG = {"fe": "fe_d", "fh": "fh_d", "fev": "fev", "fes": "fes", "fevc": "fevc", "ga": "ga_d", "tv": "tv_d",
+            "rnet": "rnet_d", "fgpp": "fgpp_d", "frday": "frday_d", "trad": "trad_d", "ebal": "ebal", "wbal": "wbal",
+            "drybal": "drybal", "dryleaf_passes": "dryleaf_passes", "runoff": "runoff", "ghflux": "ghflux"}
+# oracle state name -> GPU field, for the fields with a spec tolerance
+GPU_STATE = {"wb": "wb", "wbice": "wbice", "tgg": "tgg", "tggsn": "tggsn"}
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    t = {k[5:]: z[k] for k in z.files if k.startswith("tile_")}
+    ts = W.TileSet(name, t["iveg"].astype(np.int32), t["isoilm"].astype(np.int32), t["vlai"], t["lat"],
+                   t["lonphase"], t["tbase"], t["swscale"], t["snowd0"], t["tgg0"], t["wb0"],
+                   seed=int(z["seed"]), doy0=int(z["doy0"]), dels=float(z["dels"]), nsteps=int(z["nsteps"]))
+    return ts, z
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_reproduces_fixture(oracle, name):
+    ts, z = load(name)
+    n = int(z["nsteps"])
+    F = oracle.forcing(ts, 0, n)
+    if z["forcing"].shape[0] == n:
+        assert np.array_equal(F, z["forcing"])
+    else:
+        assert np.array_equal(F[-1:], z["forcing"])
+    st = oracle.init_state(ts, 0)
+    names = list(z["diag_names"])
+    if z["diag"].shape[0] == n:
+        for k in range(n):
+            d = oracle.run(ts, st, 1, ktau0=1 + k, forcing=F[k:k + 1], precision=0, nthreads=1)
+            got = np.stack([d[x] for x in names])
+            np.testing.assert_allclose(got, z["diag"][k], rtol=1e-9, atol=1e-9, err_msg="step %d" % k)
+    else:
+        d = oracle.run(ts, st, n, ktau0=1, forcing=F, precision=0, nthreads=1)
+        got = np.stack([d[x] for x in names])
+        np.testing.assert_allclose(got, z["diag"][0], rtol=1e-9, atol=1e-9)
+    s = oracle.split_state(st)
+    for k in z.files:
+        if k.startswith("state_"):
+            np.testing.assert_allclose(s[k[6:]], z[k], rtol=1e-9, atol=1e-9, err_msg=k)
+
+
+def test_fixtures_close_their_balances():
+    """The fixtures themselves satisfy the substitute pins: energy closure
+    per step and leaf energy balance at convergence."""
+    for name in CASES:
+        _, z = load(name)
+        names = list(z["diag_names"])
+        d = z["diag"]
+        assert np.abs(d[:, names.index("ebal")]).max() < 1e-3, name
+        assert np.abs(d[:, names.index("drybal")]).max() < 1e-3, name
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_gpu_matches_fixture(name):
+    from cable_gb300 import runtime as R
+    ts, z = load(name)
+    n = int(z["nsteps"])
+    names = list(z["diag_names"])
+    per_step = z["diag"].shape[0] == n
+    g = R.from_tileset(ts)
+    g.set_options(diag=True, capture_forcing=not per_step)
+    fails = []
+    for k in range(n):
+        if per_step:
+            g.set_forcing(z["forcing"][k])
+        g.step(1 + k, ts.dels)
+        if per_step or k == n - 1:
+            g.synchronize()
+            ref = z["diag"][k if per_step else 0]
+            for j, on in enumerate(names):
+                gn = GPU_DIAG[on]
+                if H.tolerance(gn, ref[j]) is None:
+                    continue
+                rep = H.compare(gn, g.get(gn)[0], ref[j])
+                if rep["frac_within"] < (1.0 if per_step else 0.98):
+                    fails.append((k, gn, rep))
+    if not per_step:
+        fg = g.get("forcing")
+        fc = z["forcing"][0]
+        for i in range(fc.shape[0]):
+            np.testing.assert_allclose(fg[i], fc[i], rtol=2e-5, atol=2e-5 * max(1.0, float(np.abs(fc[i]).max())))
+    for on, gn in GPU_STATE.items():
+        ref = z["state_" + on]
+        rep = H.compare(gn, g.get(gn), ref[: g.get(gn).shape[0]])
+        if rep["frac_within"] < (1.0 if per_step else 0.98):
+            fails.append(("state", gn, rep))
+    g.close()
+    assert not fails, fails[:5]

@@ -90,3 +90,40 @@ def test_parameter_tables_match_the_oracle(oracle):
         np.testing.assert_allclose(fr[:, v - 1], np.array(f6[:]), rtol=2e-6, atol=1e-7)
         assert np.frombuffer(dl, np.float32)[v - 1] == pytest.approx(a.value, rel=1e-6)
     assert abs(fr.sum(0) - 1).max() < 1e-5
+
+
+SHIM = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "cable_gb300", "fortran",
+                    "cable_cbm_gpu.F90")
+
+
+def test_fortran_shim_binds_exported_symbols_and_registry_fields():
+    """No Fortran compiler is available, so the ISO_C_BINDING shim is checked
+    textually: every BIND(C) name is an exported symbol declared in the
+    header, every field it moves is in the registry with the width and type
+    the shim's buffer assumes, and the forcing order matches the ABI's."""
+    src = open(SHIM).read()
+    lib = C.CDLL(B.build())
+    binds = re.findall(r'BIND\(C,\s*name="(\w+)"\)', src)
+    assert len(binds) >= 10
+    declared = set(declared_symbols())
+    for b in binds:
+        assert b in declared and hasattr(lib, b), b
+    f = R.fields()
+    used = set(re.findall(r"CALL (?:put|get)\('(\w+)'", src))
+    assert used, "no field transfers found"
+    missing = used - set(f)
+    assert not missing, missing
+    # buffers the shim uses: r8 (REAL(c_double)) for F64, r4 for F32, flags for I32
+    for name in used:
+        dt = f[name][2]
+        m = re.search(r"CALL (?:put|get)\('%s', C_LOC\((\w+)\)\)" % name, src)
+        buf = m.group(1)
+        want = {R.F64: ("r8",), R.F32: ("r4", "outb"), R.I32: ("flags",)}[dt]
+        assert buf in want, (name, buf, want)
+    order = re.findall(r"forc\(:, (\d+)\) = met%(\w+)(?:\(:, (\d)\))?", src)
+    names = []
+    for idx, comp, band in order:
+        names.append("fsd_" + ("vis" if band == "1" else "nir") if comp == "fsd" else comp)
+    assert names == R.FORCING_FIELDS
+    outs = re.findall(r"(?:canopy|rad)%(\w+) = outb\(:, (\d)\)", src)
+    assert [o[0] for o in sorted(outs, key=lambda x: int(x[1]))] == R.OUTPUT_FIELDS
