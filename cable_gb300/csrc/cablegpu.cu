@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -614,3 +615,81 @@ int cablegpu_param_table(int table, const char* name, float* out, int n) {
 const char* cablegpu_last_error(cablegpu_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- cold start without allocation
+// cablegpu_cold_start stages the three initial-state arrays in a buffer it
+// cudaMallocs and cudaFrees per call.  Some callers cannot allow that: a host
+// model that restarts ensemble members while other streams of the device are
+// busy (cudaFree synchronises the whole device), one that runs with a
+// reserved memory budget or a pool that owns every free byte, and one that
+// re-initialises tiles in a region where allocation calls are forbidden
+// (while another thread is capturing a CUDA graph in global mode).
+// cablegpu_cold_start_noalloc stages the arrays in a fixed device array
+// instead and calls no allocating API (no cudaMalloc/cudaFree, no library
+// that allocates).
+namespace {
+
+constexpr int kNoAllocMaxTiles = CABLEGPU_NOALLOC_MAX_TILES;
+constexpr int kNoAllocMaxDevices = 64;
+
+// 3 x 65536 doubles = 1.5 MiB: snowd0, tgg0, wb0 of up to 65536 tiles.  The
+// host-to-device copies overwrite every element the kernel reads before it
+// runs, so nothing in it has to start at zero.
+static __device__ __align__(256) double g_cold_start_scratch[3 * kNoAllocMaxTiles];
+
+std::mutex g_scratch_mutex;
+double* g_scratch_ptr[kNoAllocMaxDevices] = {};
+
+// Address of the scratch array on the current device, resolved once per
+// device (the first call may load the module's device code, so it belongs
+// before any stream capture).
+cudaError_t scratch_for_device(int device, double** out) {
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_cold_start_scratch);
+    if (e != cudaSuccess) return e;
+    g_scratch_ptr[device] = static_cast<double*>(p);
+  }
+  *out = g_scratch_ptr[device];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" int cablegpu_cold_start_noalloc(cablegpu_ctx* c, const double* snowd0, const double* tgg0,
+                                           const double* wb0) {
+  if (!c || !snowd0 || !tgg0 || !wb0) return fail(c, CABLEGPU_ERR_ARG, "cold_start_noalloc: null argument");
+  if (c->mp > kNoAllocMaxTiles)
+    return fail(c, CABLEGPU_ERR_ARG, "cold_start_noalloc: " + std::to_string(c->mp) + " tiles exceed the " +
+                                         std::to_string(kNoAllocMaxTiles) +
+                                         "-tile limit of its fixed scratch; use cablegpu_cold_start");
+  if (c->device < 0 || c->device >= kNoAllocMaxDevices)
+    return fail(c, CABLEGPU_ERR_ARG, "cold_start_noalloc: device index out of range");
+  int prev = 0;
+  CG_CUDA(c, cudaGetDevice(&prev));
+  CG_CUDA(c, cudaSetDevice(c->device));
+  double* tmp = nullptr;
+  cudaError_t e = scratch_for_device(c->device, &tmp);
+  int rc = CABLEGPU_OK;
+  if (e != cudaSuccess) {
+    rc = fail(c, CABLEGPU_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  } else {
+    const size_t n = (size_t)c->mp;
+    e = cudaMemcpyAsync(tmp, snowd0, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(tmp + n, tgg0, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(tmp + 2 * n, wb0, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+      bind_device_view(c);
+      cold_start_kernel<<<(c->mp + 255) / 256, 256, 0, c->stream>>>(c->dev, c->d_tables, tmp, tmp + n, tmp + 2 * n);
+      e = cudaGetLastError();
+    }
+    // the scratch is shared by every context on the device: it is free again
+    // only once the kernel has consumed it
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = fail(c, CABLEGPU_ERR_CUDA, std::string("cold_start_noalloc: ") + cudaGetErrorString(e));
+  }
+  cudaSetDevice(prev);
+  return rc;
+}

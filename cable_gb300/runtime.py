@@ -34,7 +34,9 @@ EXPORTS = [
     "cablegpu_set_forcing", "cablegpu_set_synthetic_forcing", "cablegpu_set_options", "cablegpu_step",
     "cablegpu_run", "cablegpu_synchronize", "cablegpu_run_timed", "cablegpu_kernel_timed",
     "cablegpu_launch_count", "cablegpu_param_table", "cablegpu_last_error", "cablegpu_phase_timed",
+    "cablegpu_cold_start_noalloc",
 ]
+NOALLOC_MAX_TILES = 65536
 PHASES = ["radiation", "canopy", "snow_pack", "soil_heat", "soil_water"]
 
 _lib = None
@@ -70,6 +72,8 @@ def load(build_if_missing: bool = True):
     L.cablegpu_create.argtypes = [C.POINTER(_Tiles), ip, C.POINTER(vp)]
     L.cablegpu_destroy.argtypes = [vp]
     L.cablegpu_cold_start.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.cablegpu_cold_start_noalloc.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                              C.POINTER(C.c_double)]
     L.cablegpu_num_fields.argtypes = []
     L.cablegpu_field_info.argtypes = [ip, C.POINTER(C.c_char_p), C.POINTER(ip), C.POINTER(ip), C.POINTER(ip)]
     L.cablegpu_field_id.argtypes = [C.c_char_p]
@@ -162,6 +166,12 @@ class CableGPU:
     def cold_start(self, snowd0, tgg0, wb0):
         a = [np.ascontiguousarray(x, np.float64) for x in (snowd0, tgg0, wb0)]
         self._check(self.L.cablegpu_cold_start(self.h, *[_ptr(x, C.c_double) for x in a]))
+
+    def cold_start_noalloc(self, snowd0, tgg0, wb0):
+        """cold_start through the allocation-free entry point (at most
+        NOALLOC_MAX_TILES tiles; calls must not overlap)."""
+        a = [np.ascontiguousarray(x, np.float64) for x in (snowd0, tgg0, wb0)]
+        self._check(self.L.cablegpu_cold_start_noalloc(self.h, *[_ptr(x, C.c_double) for x in a]))
 
     def set_options(self, medlyn=False, diag=False, capture_forcing=False):
         self._check(self.L.cablegpu_set_options(self.h, int(medlyn), int(diag), int(capture_forcing)))

@@ -88,6 +88,22 @@ int cablegpu_destroy(cablegpu_ctx* ctx);
  * moisture per tile (host arrays [mp]; layers start uniform).  */
 int cablegpu_cold_start(cablegpu_ctx* ctx, const double* snowd0, const double* tgg0, const double* wb0);
 
+/* Cold start that allocates nothing (no counterpart in the reference).
+ * Same result as cablegpu_cold_start, but the three input arrays are staged
+ * in a fixed 1.5 MiB device array compiled into the library instead of a
+ * buffer cudaMalloc'd and cudaFree'd per call.  For callers that cannot
+ * allocate or free at that point: a host model restarting tiles while other
+ * streams of the device are busy (cudaFree synchronises the device), one
+ * whose memory pool owns every free byte, or one in a region where another
+ * thread captures a CUDA graph in global mode.  Limits: at most
+ * CABLEGPU_NOALLOC_MAX_TILES tiles (larger contexts get CABLEGPU_ERR_ARG);
+ * the staging array is shared by all contexts on a device, so calls must not
+ * overlap (from any thread); the call returns after its kernel ran.  The
+ * first call on a device resolves the array's address and may load the
+ * library's device code, so make it before any stream capture begins. */
+#define CABLEGPU_NOALLOC_MAX_TILES 65536
+int cablegpu_cold_start_noalloc(cablegpu_ctx* ctx, const double* snowd0, const double* tgg0, const double* wb0);
+
 /* Field registry. */
 int cablegpu_num_fields(void);
 int cablegpu_field_info(int id, const char** name, int* nlayer, int* dtype, int* kind);
