@@ -54,6 +54,9 @@ def parse():
     p.add_argument("--cpu-sample-tiles", type=int, default=100_000)
     p.add_argument("--cpu-sample-steps", type=int, default=48)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-surrogate", action="store_true", help="skip the surrogate arm")
+    p.add_argument("--sur-rows", type=float, default=5e7, help="training rows harvested for the surrogate")
+    p.add_argument("--sur-epochs", type=int, default=20)
     return p.parse_args()
 
 
@@ -184,7 +187,7 @@ def workload(args, rank=0):
 def config(args, world):
     return {"workload": "%s: %d tiles/GPU x %d timed steps of 1800 s (%s)" % (
                 args.workload, args.mp, args.steps,
-                "40%% snow-covered, air 250-300 K" if args.workload == "snow_grid" else "no snow, air 288+N(0,10) K"),
+                "40% snow-covered, air 250-300 K" if args.workload == "snow_grid" else "no snow, air 288+N(0,10) K"),
             "tiles_per_gpu": args.mp, "soil_layers": 6, "snow_layers": "0-3", "path": "plain GPU cbm()",
             "parallelism": "tiles sharded over %d GPU(s), no collective" % world,
             "l2": "per-step state (%.1f GB) exceeds L2; no flush needed" % (args.mp * 600 / 1e9)}
@@ -224,6 +227,80 @@ def traffic_per_step(mp):
     except OSError:
         pass
     return None
+
+
+def surrogate_arm(args, d, ts, plain_value):
+    """The surrogate-accelerated timestep on the same workload: harvest
+    training rows from the plain kernel, train the network on the GPU,
+    time the step with the network in the loop (strict mode: predictions
+    whose closure pass moves the leaf temperature by more than 0.1 K fall
+    back to the plain iteration from its usual start), and measure its
+    error against the plain kernel run side by side from the same state
+    (the plain iteration is the judge; the plain kernel's own agreement with
+    the FP64 oracle is what the GPU tests check)."""
+    import numpy as np
+    from cable_gb300 import runtime as R
+    dels = ts.dels
+    g = R.from_tileset(ts, device=d.local)
+    g.run(1, 8, dels)
+    g.synchronize()
+    veg_steps = 48
+    prob = min(1.0, args.sur_rows / (args.mp * 0.75 * veg_steps))
+    cap = int(args.sur_rows * 1.2) + 4096
+    t0 = time.perf_counter()
+    nrows = g.harvest(9, veg_steps, prob=prob, seed=11, capacity=cap, dels=dels)
+    t_harvest = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    losses = g.surrogate_train(epochs=args.sur_epochs, batch=65536, lr=1e-3, val_frac=0.1, seed=3)
+    t_train = time.perf_counter() - t0
+    params, norm = g.surrogate_weights()
+    # timed: the same number of steps as the plain arm, graph replay
+    g.set_surrogate(1, 0.1)
+    ktau = 9 + veg_steps
+    g.run(ktau, args.warmup, dels)
+    g.synchronize()
+    ktau += args.warmup
+    g.surrogate_stats(reset=True)
+    launches0 = g.launch_count()
+    d.barrier()
+    ms = g.run_timed(ktau, args.steps, dels)
+    g.synchronize()
+    d.barrier()
+    launches = g.launch_count() - launches0
+    ktau += args.steps
+    tried, acc = g.surrogate_stats(reset=True)
+    phase = g.phase_timed(ktau, 8, dels)
+    g.close()
+    value = d.world * args.mp * args.steps / (d.max(ms) / 1e3)
+    # error against the plain kernel from the same state, same forcing
+    nerr = 24
+    pl = R.from_tileset(ts, device=d.local)
+    sg = R.from_tileset(ts, device=d.local)
+    sg.surrogate_weights(params, norm)
+    sg.set_surrogate(1, 0.1)
+    se = {"fe": 0.0, "fh": 0.0, "tv": 0.0}
+    mx = {"fe": 0.0, "fh": 0.0, "tv": 0.0}
+    for k in range(nerr):
+        pl.step(1 + k, dels)
+        sg.step(1 + k, dels)
+        a, b = pl.outputs(), sg.outputs()
+        for f in se:
+            e = b[f].astype(np.float64) - a[f]
+            se[f] += float(np.mean(e * e))
+            mx[f] = max(mx[f], float(np.abs(e).max()))
+    pl.close()
+    sg.close()
+    return {"value": value, "unit": "tile-timesteps/s", "vs_plain": value / plain_value, "mode": "strict, gate 0.1 K",
+            "ms_per_step": d.max(ms) / args.steps, "gpu_launches": int(launches),
+            "kernels_ms": {k: round(v, 4) for k, v in phase.items()},
+            "tried": tried, "closed_in_one_pass": acc, "fallback_frac": (1.0 - acc / tried) if tried else None,
+            "vs_plain_kernel_%d_steps" % nerr: {
+                "le_rmse_wm2": float(np.sqrt(se["fe"] / nerr)), "h_rmse_wm2": float(np.sqrt(se["fh"] / nerr)),
+                "tv_rmse_k": float(np.sqrt(se["tv"] / nerr)), "le_max_wm2": mx["fe"], "tv_max_k": mx["tv"]},
+            "training": {"rows": nrows, "epochs": args.sur_epochs, "batch": 65536, "lr": 1e-3,
+                         "harvest_s": round(t_harvest, 3), "train_s": round(t_train, 3),
+                         "loss_train_val_first": [float(x) for x in losses[0]],
+                         "loss_train_val_last": [float(x) for x in losses[-1]]}}
 
 
 def run_gb300(args):
@@ -303,6 +380,12 @@ def run_gb300(args):
     except Exception as exc:  # the line still prints; the failure is stated
         e2e = {"value": None, "unit": "tile-timesteps/s", "error": str(exc)[:200]}
     g.close()
+    sur = None
+    if not args.no_surrogate:
+        try:
+            sur = surrogate_arm(args, d, ts, value)
+        except Exception as exc:  # the line still prints; the failure is stated
+            sur = {"error": str(exc)[:300]}
     cpu = None
     if d.rank == 0 and d.world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, ts)
@@ -313,7 +396,7 @@ def run_gb300(args):
                "data": "synthetic (seeded generator; the reference's site forcing is not available)",
                "config": config(args, d.world), "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
                "clocks": clk, "gpu_launches": int(launches),
-               "step_kernels_ms": step_ms}
+               "step_kernels_ms": step_ms, "surrogate": sur}
         print(json.dumps(out))
     d.close()
 

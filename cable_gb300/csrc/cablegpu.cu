@@ -10,6 +10,8 @@
 
 #include "../../include/cablegpu.h"
 #include "phase_kernels.cuh"
+#include "surrogate.cuh"
+#include "surrogate_host.h"
 
 using namespace cg;
 
@@ -173,6 +175,24 @@ struct cablegpu_ctx {
   unsigned long long graph_seed = 0;
   int graph_doy0 = -1;
   long long launches = 0;
+  // dryLeaf surrogate: training rows harvested from this context's own
+  // steps, the network trained on them, and the in-loop switch
+  float* d_harvest = nullptr;                // [harvest_cap][16]
+  long long harvest_cap = 0;
+  long long harvest_rows = 0;                // rows filled by the last harvest
+  unsigned long long* d_harvest_n = nullptr;
+  bool harvesting = false;
+  float harvest_prob = 0.f;
+  unsigned long long harvest_seed = 0;
+  SurNet net;
+  bool net_ready = false;
+  int sur_enabled = 0;
+  float sur_gate = 0.1f;
+  unsigned long long* d_sur_stats = nullptr;  // [2]
+  float* d_sur_feat = nullptr;                // [12][ld] network inputs
+  float* d_sur_dt = nullptr;                  // [ld] predicted leaf-temperature change
+  int graph_sur = -1;
+  float graph_gate = -1.f;
   std::string err;
 };
 
@@ -211,13 +231,33 @@ void bind_device_view(cablegpu_ctx* c) {
   D.work_a = (float*)P("work_a");
   D.work_b = (float*)P("work_b");
   D.work_c = (float*)P("work_c");
+  D.harvest = c->harvesting ? c->d_harvest : nullptr;
+  D.harvest_n = c->d_harvest_n;
+  D.harvest_cap = c->harvest_cap;
+  D.harvest_prob = c->harvest_prob;
+  D.harvest_seed = c->harvest_seed;
+  D.sur_feat = c->sur_enabled ? c->d_sur_feat : nullptr;
+  D.sur_dt = c->sur_enabled ? c->d_sur_dt : nullptr;
+  D.sur_gate = c->sur_gate;
+  D.sur_strict = c->sur_enabled == 1 ? 1 : 0;
+  D.sur_stats = c->sur_enabled ? c->d_sur_stats : nullptr;
 }
 
 int launch_step(cablegpu_ctx* c, const StepParams& p, const int* clock) {
   bind_device_view(c);
   const bool diag = c->diag != 0;
-  launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, clock);
-  launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, clock);
+  if (c->sur_enabled) {
+    launch_phase_a_sur(diag, c->stream, c->dev, c->d_tables, p, clock);
+    std::string e;
+    if (sur_infer(c->net, c->d_sur_feat, c->mp, c->ld, c->d_sur_dt, c->dev.status, c->stream, e))
+      return fail(c, CABLEGPU_ERR_CUDA, e);
+    ++c->launches;
+    launch_phase_b_sur(diag, c->stream, c->dev, c->d_tables, p, clock);
+  } else {
+    launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, clock);
+    if (c->harvesting) launch_phase_b_harvest(diag, c->stream, c->dev, c->d_tables, p, clock);
+    else launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, clock);
+  }
   launch_phase_c1(diag, c->stream, c->dev, c->d_tables, p, clock);
   launch_phase_c2(diag, c->stream, c->dev, c->d_tables, p, clock);
   launch_phase_c3(diag, c->stream, c->dev, c->d_tables, p, clock);
@@ -240,7 +280,8 @@ StepParams make_params(cablegpu_ctx* c, int ktau, float dels) {
 int ensure_graph(cablegpu_ctx* c, float dels) {
   if (c->graph && c->graph_dels == dels && c->graph_diag == c->diag && c->graph_medlyn == c->medlyn &&
       c->graph_hostforc == (int)c->host_forcing && c->graph_capture == c->capture_forcing &&
-      c->graph_seed == c->forc.seed && c->graph_doy0 == c->forc.doy0)
+      c->graph_seed == c->forc.seed && c->graph_doy0 == c->forc.doy0 && c->graph_sur == c->sur_enabled &&
+      c->graph_gate == c->sur_gate)
     return CABLEGPU_OK;
   if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   StepParams p = make_params(c, 0, dels);
@@ -259,6 +300,7 @@ int ensure_graph(cablegpu_ctx* c, float dels) {
   c->graph_dels = dels; c->graph_diag = c->diag; c->graph_medlyn = c->medlyn;
   c->graph_hostforc = (int)c->host_forcing; c->graph_capture = c->capture_forcing;
   c->graph_seed = c->forc.seed; c->graph_doy0 = c->forc.doy0;
+  c->graph_sur = c->sur_enabled; c->graph_gate = c->sur_gate;
   return CABLEGPU_OK;
 }
 
@@ -364,6 +406,12 @@ int cablegpu_destroy(cablegpu_ctx* c) {
   cudaFree(c->d_order);
   cudaFree(c->d_stage);
   cudaFree(c->dev.status);
+  if (c->d_harvest) cudaFree(c->d_harvest);
+  if (c->d_harvest_n) cudaFree(c->d_harvest_n);
+  if (c->d_sur_stats) cudaFree(c->d_sur_stats);
+  if (c->d_sur_feat) cudaFree(c->d_sur_feat);
+  if (c->d_sur_dt) cudaFree(c->d_sur_dt);
+  sur_free(c->net);
   cudaFreeHost(c->h_clock);
   cudaFreeHost(c->h_status);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -480,7 +528,7 @@ int cablegpu_run(cablegpu_ctx* c, int ktau0, int nsteps, float dels) {
     while (nsteps - done >= kGraphSteps) {
       CG_CUDA(c, cudaGraphLaunch(c->graph, c->stream));
       // the five step kernels plus the one-thread clock kernel of each step
-      c->launches += (kKernelsPerStep + 1) * kGraphSteps;
+      c->launches += (kKernelsPerStep + 1 + (c->sur_enabled ? 1 : 0)) * kGraphSteps;
       done += kGraphSteps;
     }
     // the pinned clock buffer must not be rewritten before the copy ran
@@ -498,9 +546,13 @@ int cablegpu_synchronize(cablegpu_ctx* c) {
   CG_CUDA(c, cudaMemcpyAsync(c->h_status, c->dev.status, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
   CG_CUDA(c, cudaStreamSynchronize(c->stream));
   if (*c->h_status) {
+    const unsigned int st = *c->h_status;
     CG_CUDA(c, cudaMemsetAsync(c->dev.status, 0, sizeof(unsigned int), c->stream));
     CG_CUDA(c, cudaStreamSynchronize(c->stream));
-    return fail(c, CABLEGPU_ERR_NONFINITE, "a step produced a non-finite output flux");
+    if (st & 1u) return fail(c, CABLEGPU_ERR_NONFINITE, "a step produced a non-finite output flux");
+    return fail(c, CABLEGPU_ERR_CUDA,
+                "surrogate network: a tensor-core pass did not complete in time; the blocks affected used the "
+                "plain dryLeaf iteration");
   }
   return CABLEGPU_OK;
 }
@@ -545,37 +597,152 @@ int cablegpu_kernel_timed(cablegpu_ctx* c, int ktau0, int nsteps, float dels, fl
   return CABLEGPU_OK;
 }
 
+int cablegpu_harvest(cablegpu_ctx* c, int ktau0, int nsteps, float dels, float prob, unsigned long long seed,
+                     long long capacity, long long* nrows) {
+  if (!c || ktau0 < 1 || nsteps < 1 || !(dels > 0.f) || !(prob > 0.f) || prob > 1.f || capacity < 1)
+    return fail(c, CABLEGPU_ERR_ARG, "harvest: bad argument");
+  if (capacity > c->harvest_cap) {
+    if (c->d_harvest) { CG_CUDA(c, cudaFree(c->d_harvest)); c->d_harvest = nullptr; c->harvest_cap = 0; }
+    CG_CUDA(c, cudaMalloc(&c->d_harvest, (size_t)capacity * 16 * sizeof(float)));
+    c->harvest_cap = capacity;
+  }
+  if (!c->d_harvest_n) CG_CUDA(c, cudaMalloc(&c->d_harvest_n, sizeof(unsigned long long)));
+  CG_CUDA(c, cudaMemsetAsync(c->d_harvest_n, 0, sizeof(unsigned long long), c->stream));
+  c->harvesting = true;
+  c->harvest_prob = prob;
+  c->harvest_seed = seed;
+  int rc = CABLEGPU_OK;
+  for (int n = 0; n < nsteps && !rc; ++n) rc = launch_step(c, make_params(c, ktau0 + n, dels), nullptr);
+  c->harvesting = false;
+  if (rc) return rc;
+  unsigned long long h = 0;
+  CG_CUDA(c, cudaMemcpyAsync(&h, c->d_harvest_n, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->harvest_rows = (long long)std::min<unsigned long long>(h, (unsigned long long)c->harvest_cap);
+  if (nrows) *nrows = c->harvest_rows;
+  return CABLEGPU_OK;
+}
+
+int cablegpu_harvest_rows(cablegpu_ctx* c, float* host, long long n) {
+  if (!c || !host || n < 0 || n > c->harvest_rows) return fail(c, CABLEGPU_ERR_ARG, "harvest_rows: bad argument");
+  CG_CUDA(c, cudaMemcpyAsync(host, c->d_harvest, (size_t)n * 16 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CABLEGPU_OK;
+}
+
+static int ensure_net(cablegpu_ctx* c) {
+  if (c->net.params) return CABLEGPU_OK;
+  std::string e;
+  if (sur_alloc(c->net, e)) return fail(c, CABLEGPU_ERR_CUDA, e);
+  CG_CUDA(c, cudaMalloc(&c->d_sur_stats, 2 * sizeof(unsigned long long)));
+  CG_CUDA(c, cudaMemset(c->d_sur_stats, 0, 2 * sizeof(unsigned long long)));
+  CG_CUDA(c, cudaMalloc(&c->d_sur_feat, (size_t)12 * c->ld * sizeof(float)));
+  CG_CUDA(c, cudaMalloc(&c->d_sur_dt, (size_t)c->ld * sizeof(float)));
+  return CABLEGPU_OK;
+}
+
+int cablegpu_surrogate_train(cablegpu_ctx* c, int epochs, int batch, float lr, float val_frac,
+                             unsigned long long seed, float* losses) {
+  if (!c || epochs < 1 || batch < 128 || !(lr > 0.f) || val_frac < 0.f || val_frac >= 1.f)
+    return fail(c, CABLEGPU_ERR_ARG, "surrogate_train: bad argument");
+  const long long nval = (long long)(val_frac * (double)c->harvest_rows);
+  const long long ntrain = c->harvest_rows - nval;
+  if (ntrain < 128) return fail(c, CABLEGPU_ERR_STATE, "surrogate_train: harvest fewer than 128 training rows first");
+  int rc = ensure_net(c);
+  if (rc) return rc;
+  std::string e;
+  rc = sur_fit(c->net, c->d_harvest, ntrain, nval, epochs, batch, lr, seed, true, losses, c->stream, e);
+  if (rc) return fail(c, rc, e);
+  c->net_ready = true;
+  return CABLEGPU_OK;
+}
+
+int cablegpu_surrogate_weights(cablegpu_ctx* c, float* params, float* norm, int set) {
+  if (!c || !params || !norm) return fail(c, CABLEGPU_ERR_ARG, "surrogate_weights: null argument");
+  int rc = ensure_net(c);
+  if (rc) return rc;
+  const size_t pb = cg::sur::NPARAM * sizeof(float), nb = cg::sur::NNORM * sizeof(float);
+  if (set) {
+    CG_CUDA(c, cudaMemcpyAsync(c->net.params, params, pb, cudaMemcpyHostToDevice, c->stream));
+    CG_CUDA(c, cudaMemcpyAsync(c->net.norm, norm, nb, cudaMemcpyHostToDevice, c->stream));
+    std::string e;
+    if (sur_pack(c->net, c->stream, e)) return fail(c, CABLEGPU_ERR_CUDA, e);
+    c->net_ready = true;
+  } else {
+    if (!c->net_ready) return fail(c, CABLEGPU_ERR_STATE, "surrogate_weights: no trained network");
+    CG_CUDA(c, cudaMemcpyAsync(params, c->net.params, pb, cudaMemcpyDeviceToHost, c->stream));
+    CG_CUDA(c, cudaMemcpyAsync(norm, c->net.norm, nb, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CABLEGPU_OK;
+}
+
+int cablegpu_set_surrogate(cablegpu_ctx* c, int mode, float gate_kelvin) {
+  if (!c || mode < 0 || mode > 2 || !(gate_kelvin > 0.f) || gate_kelvin > 0.1f)
+    return fail(c, CABLEGPU_ERR_ARG, "set_surrogate: mode 0..2, gate in (0, 0.1] K");
+  if (mode && !c->net_ready) return fail(c, CABLEGPU_ERR_STATE, "set_surrogate: train or set the network first");
+  c->sur_enabled = mode;
+  c->sur_gate = gate_kelvin;
+  return CABLEGPU_OK;
+}
+
+int cablegpu_surrogate_stats(cablegpu_ctx* c, long long* tried, long long* accepted, int reset) {
+  if (!c || !tried || !accepted) return CABLEGPU_ERR_ARG;
+  *tried = 0;
+  *accepted = 0;
+  if (!c->d_sur_stats) return CABLEGPU_OK;
+  unsigned long long h[2];
+  CG_CUDA(c, cudaMemcpyAsync(h, c->d_sur_stats, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  if (reset) CG_CUDA(c, cudaMemsetAsync(c->d_sur_stats, 0, sizeof(h), c->stream));
+  CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  *tried = (long long)h[0];
+  *accepted = (long long)h[1];
+  return CABLEGPU_OK;
+}
+
 int cablegpu_phase_timed(cablegpu_ctx* c, int ktau0, int nsteps, float dels, float* ms_per_phase) {
   if (!c || !ms_per_phase || nsteps <= 0) return CABLEGPU_ERR_ARG;
-  constexpr int K = kKernelsPerStep;
+  // phases: radiation, canopy, snow pack, soil heat, soil water, surrogate network
+  constexpr int K = kKernelsPerStep + 1;
   std::vector<cudaEvent_t> ev((K + 1) * nsteps);
   for (auto& e : ev) CG_CUDA(c, cudaEventCreate(&e));
   bind_device_view(c);
   const bool diag = c->diag != 0;
+  const bool sur = c->sur_enabled != 0;
   for (int i = 0; i < nsteps; ++i) {
     const StepParams p = make_params(c, ktau0 + i, dels);
     cudaEvent_t* e = &ev[(K + 1) * i];
     CG_CUDA(c, cudaEventRecord(e[0], c->stream));
-    launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    if (sur) launch_phase_a_sur(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    else launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, nullptr);
     CG_CUDA(c, cudaEventRecord(e[1], c->stream));
-    launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    if (sur) {
+      std::string err;
+      if (sur_infer(c->net, c->d_sur_feat, c->mp, c->ld, c->d_sur_dt, c->dev.status, c->stream, err))
+        return fail(c, CABLEGPU_ERR_CUDA, err);
+    }
     CG_CUDA(c, cudaEventRecord(e[2], c->stream));
-    launch_phase_c1(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    if (sur) launch_phase_b_sur(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    else launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, nullptr);
     CG_CUDA(c, cudaEventRecord(e[3], c->stream));
-    launch_phase_c2(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    launch_phase_c1(diag, c->stream, c->dev, c->d_tables, p, nullptr);
     CG_CUDA(c, cudaEventRecord(e[4], c->stream));
-    launch_phase_c3(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    launch_phase_c2(diag, c->stream, c->dev, c->d_tables, p, nullptr);
     CG_CUDA(c, cudaEventRecord(e[5], c->stream));
+    launch_phase_c3(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    CG_CUDA(c, cudaEventRecord(e[6], c->stream));
     CG_CUDA(c, cudaGetLastError());
-    c->launches += K;
+    c->launches += kKernelsPerStep + (sur ? 1 : 0);
   }
   CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  // event intervals: [a][net][b][c1][c2][c3] -> output order a, b, c1, c2, c3, net
+  const int order[K] = {0, 5, 1, 2, 3, 4};
   for (int k = 0; k < K; ++k) ms_per_phase[k] = 0.f;
   for (int i = 0; i < nsteps; ++i) {
     for (int k = 0; k < K; ++k) {
       float ms = 0.f;
       CG_CUDA(c, cudaEventElapsedTime(&ms, ev[(K + 1) * i + k], ev[(K + 1) * i + k + 1]));
-      ms_per_phase[k] += ms / nsteps;
+      ms_per_phase[order[k]] += ms / nsteps;
     }
   }
   for (auto& e : ev) cudaEventDestroy(e);

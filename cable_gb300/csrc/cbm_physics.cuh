@@ -90,7 +90,22 @@ struct CgDev {
   float* work_c;           // phase C1 -> C2 -> C3 handoff record
   const float* forcing_in; // [CG_NFORC] host-provided forcing, or null (synthetic)
   float* forcing_out;      // [CG_NFORC] copy of the forcing used, or null
-  unsigned int* status;    // bit0: non-finite output seen
+  unsigned int* status;    // bit0: non-finite output seen, bit1: surrogate network failed
+  // dryLeaf training-row harvest (null when off): rows of 12 features and 3
+  // targets (sur:: layout), one per sampled (tile, step, MO iteration)
+  float* harvest;
+  unsigned long long* harvest_n;
+  long long harvest_cap;
+  float harvest_prob;
+  unsigned long long harvest_seed;
+  // dryLeaf surrogate (null when off): the radiation kernel writes the
+  // network inputs of each tile, the network kernel the predicted leaf
+  // temperature change of the first Monin-Obukhov iteration
+  float* sur_feat;                 // [12][ld]
+  const float* sur_dt;             // [ld]
+  float sur_gate;                  // K: closure test of the prediction
+  int sur_strict;                  // 1: a prediction that does not close restarts the plain iteration
+  unsigned long long* sur_stats;   // [0] tiles that started from a prediction, [1] closed in one pass
 };
 
 struct CgTables {
@@ -203,31 +218,32 @@ __device__ __forceinline__ float xejmxt3(float x) {
   return fmaxf(0.0f, num / den);
 }
 
-// FP64 reciprocal seeded from the FP32 one and refined by one Newton step
-// (relative error ~1e-14), so each Thomas row costs a few FP64 FMAs instead
-// of a full FP64 division.
-__device__ __forceinline__ double drcp1(double d) {
-  double r = (double)(1.0f / (float)d);
-  double e = fma(-d, r, 1.0);
-  return fma(r, e, r);
-}
-
-// Tridiagonal solve (cbl_trimb.F90:17-53) in FP64, n <= 9 rows, rhs in place.
+// Tridiagonal solve in correction form (the elimination of cbl_trimb.F90:17-53
+// applied to the step's change rather than to the new state).  The soil heat
+// and moisture systems are A x_new = rhs with A = I + M, M the diffusion
+// operator; with x_new = x_old + d the change solves A d = rhs - A x_old,
+// whose right-hand side is the step's source term minus M x_old, formed from
+// differences of the old state (exact in FP32 for temperatures; from FP64
+// differences for soil water).  d is O(the step's change) instead of
+// O(the state), so FP32 elimination leaves an error of ~1e-7 of the change,
+// far below the FP32 rounding of the stored temperatures, and d = 0 exactly
+// when the state is at equilibrium: no drift from rounding.  A is
+// diagonally dominant (an M-matrix), so elimination without pivoting is
+// stable.  r holds the right-hand side on entry and d on exit.
 template <int N>
-__device__ __forceinline__ void trimb(const double* a, const double* b, const double* c, double* rhs) {
-  double e[N], g[N];
-  double t = drcp1(b[0]);
+__device__ __forceinline__ void trid_correction(const float* a, const float* b, const float* c, float* r) {
+  float e[N];
+  float t = 1.0f / b[0];
   e[0] = c[0] * t;
-  g[0] = rhs[0] * t;
+  r[0] = r[0] * t;
 #pragma unroll
-  for (int k = 1; k < N - 1; ++k) {
-    t = drcp1(b[k] - a[k] * e[k - 1]);
+  for (int k = 1; k < N; ++k) {
+    t = 1.0f / (b[k] - a[k] * e[k - 1]);
     e[k] = c[k] * t;
-    g[k] = (rhs[k] - a[k] * g[k - 1]) * t;
+    r[k] = (r[k] - a[k] * r[k - 1]) * t;
   }
-  rhs[N - 1] = (rhs[N - 1] - a[N - 1] * g[N - 2]) * drcp1(b[N - 1] - a[N - 1] * e[N - 2]);
 #pragma unroll
-  for (int k = N - 2; k >= 0; --k) rhs[k] = g[k] - e[k] * rhs[k + 1];
+  for (int k = N - 2; k >= 0; --k) r[k] = r[k] - e[k] * r[k + 1];
 }
 
 }  // namespace cg

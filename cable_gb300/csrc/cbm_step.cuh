@@ -35,7 +35,8 @@ __device__ __forceinline__ float ldf(const float* p, int i) { return __ldg(p + i
 // to the soil-heat kernel and on to the soil-water kernel.
 #define CG_NC 12
 
-template <bool kDiag>
+// kSurFeat: also write the dryLeaf surrogate network's inputs (D.sur_feat).
+template <bool kDiag, bool kSurFeat = false>
 __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
   const int ld = D.ld;
   const float dels = P.dels;
@@ -72,14 +73,10 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
   }
   uint8_t flags = D.flags[t];
   int isflag = flags & 1;
-  bool first_call = (flags & 2) != 0;
-  double gammzz1 = D.gammzz1[t];
-  float snowd = D.snowd[t], ssdnn = D.ssdnn[t], snage = D.snage[t], pudsto = D.pudsto[t];
+  float snowd = D.snowd[t], ssdnn = D.ssdnn[t], snage = D.snage[t];
   const float owetfac_in = D.owetfac[t];
-  const float ortsoil = D.rtsoil[t];
   float wb_lake = D.wb_lake[t], wbtot1 = D.wbtot1[t], wbtot2 = D.wbtot2[t];
   const float oldcansto = D.cansto[t];
-  const float pudsmx = 0.0f;
 
   // ---------------------------------------------------------------- forcing
   float F[CG_NFORC];
@@ -148,7 +145,6 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
       rt1usb = fmaxf(rt1usb, 0.0f);
     }
   }
-  const float rghlai = vlaiw;
 
   // define_air (cable_air.F90:51-97) with tvair = tk
   float rho, cmolar, epsi, visc, psyc, dsatdk;
@@ -275,14 +271,10 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
     wetfac = 0.5f * (wetfac + owetfac_in);
   }
   // working variables of the canopy iteration
-  float tvair = tk, qvair = qv, tv = tk;
+  float tvair = tk, qvair = qv;
   float qstvair = qsatfjh(tvair - TFRZ, pmb);
   float dva = (qstvair - qvair) * RMAIR / RMH2O * pmb * 100.0f;
   float dsx = fmaxf(dva, 0.0f);
-  float tlfx = tk, tlfy = tk;
-  float csx[2] = {ca, ca};
-  float gswx[2] = {1e-3f, 1e-3f};
-  float gbhu[2] = {1e-3f, 1e-3f}, gbhf[2] = {1e-3f, 1e-3f};
   float evapfbl[CG_MS];
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) evapfbl[k] = 0.0f;
@@ -341,13 +333,31 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
     swcan = qsw[0][0] + qsw[1][0] + qsw[0][1] + qsw[1][1];
   }
   const float sum_rad_rniso = rniso[0] + rniso[1];
-  const float sum_rad_gradis = gradis[0] + gradis[1];
 
   (void)sunlit_veg;
   {
     const float rec[CG_NA] = {tk, qv, pmb, ua, fld, ca, precip, precip_sn, vlaiw, hruff, z0soilsn, z0m, disp, zref_uv, zruffs, rt0us, rt1usa, rt1usb, usuh, coexp, rho, cmolar, epsi, visc, psyc, dsatdk, extkb, transd, flws, qssabs, fvlai[0], fvlai[1], scalex[0], scalex[1], rniso[0], rniso[1], gradis[0], gradis[1], qcan_par[0], qcan_par[1], swcan, cansto, through, fwet, wetfac, tss, wbliq0[0], wbliq0[1], wbliq0[2], wbliq0[3], wbliq0[4], wbliq0[5]};
 #pragma unroll
     for (int i = 0; i < CG_NA; ++i) D.work_a[i * ld + t] = rec[i];
+  }
+  if (kSurFeat) {
+    // inputs of the dryLeaf surrogate network at the start of the first
+    // Monin-Obukhov iteration (canopy kernel state there: leaf and canopy air
+    // at tk, neutral stability, fwsoil_calc_std of cbl_fwsoil.F90:13-38)
+    float rwater = 0.f;
+#pragma unroll
+    for (int k = 0; k < CG_MS; ++k)
+      rwater += froot[k] * fmaxf(1.0e-9f, fminf(1.0f, (wbliq0[k] - swilt) / (sfc - swilt)));
+    rwater = fmaxf(1.0e-9f, rwater);
+    const float fwsoil = P.medlyn ? fmaxf(1.0e-4f, fminf(1.0f, rwater))
+                                  : fmaxf(1.0e-9f, fminf(1.0f, ldf(V.vbeta, v) * rwater));
+    const float us1 = fminf(fmaxf(1.e-6f, VONK * fmaxf(ua, UMIN) / logf(zref_uv / z0m)), 10.0f);
+    const float sc = scalex[0] + scalex[1];
+    const float f[12] = {qcan_par[0], qcan_par[1], tk, dsx, ca, ldf(V.vcmax, v) * sc,
+                         ldf(V.ejmax, v) * (1.0f - ldf(V.frac4, v)) * sc, P.medlyn ? ldf(V.g1, v) : ldf(V.a1gs, v),
+                         fwsoil, vlaiw, us1, tk};
+#pragma unroll
+    for (int i = 0; i < 12; ++i) D.sur_feat[i * ld + t] = f[i];
   }
   if (iveg == LAKES) D.wb[t] = wb[0];
   D.wb_lake[t] = wb_lake; D.wbtot1[t] = wbtot1; D.wbtot2[t] = wbtot2;
@@ -357,7 +367,12 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
   }
 }
 
-template <bool kDiag>
+// kHarvest: sampled tiles append a training row for the surrogate network
+// (features at the start of the first Monin-Obukhov iteration's dryLeaf and
+// its converged result) to D.harvest.  kSur: the first
+// iteration's dryLeaf starts from the network's leaf temperature (the
+// surrogate; see the comment at its use).
+template <bool kDiag, bool kHarvest = false, bool kSur = false>
 __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
   const int ld = D.ld;
   const float dels = P.dels;
@@ -430,6 +445,9 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
   float fes = 0.f, fess = 0.f, fesp = 0.f, fevw = 0.f, fhvw = 0.f, fevw_pot = 0.f, fevc = 0.f, epot = 0.f;
   float ecy = 0.f, hcy = 0.f, rny = 0.f, frday = 0.f, fpn = 0.f, fwsoil = 1.0f, qstss = 0.f;
   int passes_total = 0;
+  // surrogate and harvest bookkeeping
+  unsigned int sur_tried = 0, sur_accepted = 0;
+  const bool harvesting = kHarvest && D.harvest != nullptr;
   for (int iter = 1; iter <= NITER; ++iter) {
     const float zi = zetar[iter - 1];
     // comp_friction_vel (cbl_friction_vel.F90:19-108)
@@ -470,6 +488,27 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
         rwater = fmaxf(1.0e-9f, rwater);
         fwsoil = P.medlyn ? fmaxf(1.0e-4f, fminf(1.0f, rwater)) : fmaxf(1.0e-9f, fminf(1.0f, vbeta * rwater));
       }
+      // surrogate inputs: the state the first iteration starts from
+      const float tlf_entry = tlfx;
+      bool sampled = false;
+      if (harvesting && iter == 1 && veg_mask) {
+        uint32_t c[4] = {(uint32_t)D.tile_id[t], (uint32_t)P.step_index, 0xD1EAF001u, 0u};
+        cg_philox(c, D.harvest_seed);
+        sampled = cg_u01(c[0]) < D.harvest_prob;
+      }
+      float feat[12];
+      if (sampled) {
+        const float sc = scalex[0] + scalex[1];
+        feat[0] = qcan_par[0]; feat[1] = qcan_par[1]; feat[2] = tlfx; feat[3] = dsx; feat[4] = ca;
+        feat[5] = vcmax * sc; feat[6] = ejmax * (1.0f - frac4) * sc; feat[7] = P.medlyn ? g1 : a1gs;
+        feat[8] = fwsoil; feat[9] = vlaiw; feat[10] = us; feat[11] = tvair;
+      }
+      bool sur_try = false;
+      float tlf_sur = tlfx;
+      if (kSur && iter == 1 && veg_mask) {
+        const float dt = D.sur_dt[t];
+        if (isfinite(dt)) { sur_try = true; tlf_sur = tlf_entry + dt; }
+      }
       float gswmin[2] = {fmaxf(1.e-6f, scalex[0] * gswmin_p), fmaxf(1.e-6f, scalex[1] * gswmin_p)};
       float gh[2] = {1e-3f, 1e-3f}, ghr[2] = {1e-3f, 1e-3f}, psycst[2] = {psyc, psyc};
       float rdx[2] = {0.f, 0.f}, anx[2] = {0.f, 0.f}, rdy[2] = {0.f, 0.f}, an_y[2] = {0.f, 0.f};
@@ -483,10 +522,26 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
       if (!veg_mask) { rnx = 0.f; ecx = 0.f; ecy = 0.f; abs_deltlf = 0.f; rny = 0.f; }
       float deltlfy = abs_deltlf;
       float oldevapfbl[CG_MS];
-      const float sum_gbh = gbhu[0] + gbhf[0] + gbhu[1] + gbhf[1];
-      (void)sum_gbh;
+      // With the surrogate the first iteration starts from the network's
+      // leaf temperature.  The first pass is the closure test of the
+      // prediction: when the leaf energy balance evaluated there moves the
+      // leaf temperature by at most D.sur_gate the tile is done in one pass.
+      // Otherwise, in strict mode the tile restarts the plain iteration from
+      // its usual start (bitwise the plain result); in warm mode the plain
+      // iteration continues from the prediction to the gate as its
+      // convergence test (cbl_dryLeaf.F90 uses 0.1 K).
+      float conv = 0.1f;
+      // entry state, for the strict mode's restart of the plain iteration
+      const float dsx_entry = dsx, csx_entry[2] = {csx[0], csx[1]}, gswx_entry[2] = {gswx[0], gswx[1]};
+      const float gbhf_entry[2] = {gbhf[0], gbhf[1]};
+      if (sur_try) {
+        ++sur_tried;
+        tlfx = tlf_sur;
+        dsx = fmaxf(dva + dsatdk * (tlfx - tvair), 0.0f);
+        conv = D.sur_gate;
+      }
       for (int k = 1; k <= MAXITER; ++k) {
-        const bool active = veg_mask && abs_deltlf > 0.1f;
+        const bool active = veg_mask && abs_deltlf > conv;
         if (active) {
           ++passes_total;
           float gras = fmaxf(1.0e-6f, 1.595E8f * fabsf(tlfx - tvair) * (dleaf * dleaf * dleaf));
@@ -588,12 +643,35 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
           tlfy = tlfx;   // damping below is a no-op for k == 1
         }
         // damping once k > 5 (:584-590)
-        if (abs_deltlf > 0.1f) {
+        if (abs_deltlf > conv) {
           float fac = 0.5f * ((float)max(0, k - 5) / ((float)k - 4.9999f));
           tlfx = fac * tlfxx + (1.0f - fac) * tlfx;
         }
+        if (kSur && sur_try && k == 1) {
+          if (abs_deltlf <= conv) {
+            ++sur_accepted;
+          } else if (D.sur_strict) {
+            // strict: the prediction did not close, so the tile runs the
+            // plain iteration from its usual start, exactly as without the
+            // surrogate
+            tlfx = tlf_entry; dsx = dsx_entry;
+            csx[0] = csx_entry[0]; csx[1] = csx_entry[1];
+            gswx[0] = gswx_entry[0]; gswx[1] = gswx_entry[1];
+            gbhf[0] = gbhf_entry[0]; gbhf[1] = gbhf_entry[1];
+            rnx = sum_rad_rniso; ecx = sum_rad_rniso; hcx = 0.f;
+            abs_deltlf = 999.0f; deltlf = 0.f; deltlfy = abs_deltlf;
+            fevc = 0.f; hcy = 0.f;
+#pragma unroll
+            for (int kk = 0; kk < CG_MS; ++kk) evapfbl[kk] = 0.f;
+            rdx[0] = rdx[1] = anx[0] = anx[1] = rdy[0] = rdy[1] = an_y[0] = an_y[1] = 0.f;
+            conv = 0.1f;
+            sur_try = false;
+            k = 0;
+            continue;
+          }
+        }
         // a tile that has stopped iterating never changes again: leave now
-        if (!(veg_mask && abs_deltlf > 0.1f)) break;
+        if (!(veg_mask && abs_deltlf > conv)) break;
       }
       fevc = (1.0f - fwet) * ecy;
       if (ecy > 0.0f && fwet < 1.0f && fabsf(ecy - ecx) > 1.0e-6f) {
@@ -607,6 +685,18 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
       }
       frday = 12.0f * (rdy[0] + rdy[1]);
       fpn = fminf(-12.0f * (an_y[0] + an_y[1]), frday);
+      // training row: features at entry, converged stomatal conductance,
+      // net assimilation and leaf temperature change
+      if (sampled) {
+        const unsigned long long slot = atomicAdd(D.harvest_n, 1ull);
+        if (slot < (unsigned long long)D.harvest_cap) {
+          float4* r = reinterpret_cast<float4*>(D.harvest + slot * 16);
+          r[0] = make_float4(feat[0], feat[1], feat[2], feat[3]);
+          r[1] = make_float4(feat[4], feat[5], feat[6], feat[7]);
+          r[2] = make_float4(feat[8], feat[9], feat[10], feat[11]);
+          r[3] = make_float4(gswx[0] + gswx[1], an_y[0] + an_y[1], tlfy - tlf_entry, 0.f);
+        }
+      }
     }
     // ------------------------------------------------ wetLeaf (cbl_wetleaf.F90:9-111)
     fevw = 0.f; fhvw = 0.f;
@@ -779,6 +869,15 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
   // energy balance (cable_checks.F90:565-618); fev = fevc + fevw is the same
   // sum before and after remove_trans moves negative fevc into fevw
   const float ebal = swnet + fld - SBOLTZ * EMLEAF * pow4(tv) * (1.f - transd) - flws * transd - fev - fes - fh - ga;
+  if (kSur && D.sur_stats) {
+    // warp totals, one atomic per warp
+    const unsigned int a = __reduce_add_sync(__activemask(), sur_tried);
+    const unsigned int b = __reduce_add_sync(__activemask(), sur_accepted);
+    if ((threadIdx.x & 31) == (__ffs(__activemask()) - 1)) {
+      if (a) atomicAdd(&D.sur_stats[0], (unsigned long long)a);
+      if (b) atomicAdd(&D.sur_stats[1], (unsigned long long)b);
+    }
+  }
   D.ebal_tot[t] = D.ebal_tot[t] + (double)ebal;
   D.cansto[t] = cansto;
   D.rtsoil[t] = rtsoil;
@@ -815,7 +914,6 @@ __device__ __forceinline__ void phase_c1(const CgDev& D, const CgTables* __restr
   const int v = iveg - 1, so = isoilm - 1;
   const CgPftTable& V = T->pft;
   const CgSoilTable& S = T->soil;
-  const float vlai = (iveg >= 14) ? 0.0f : D.vlai[t];
   float froot[CG_MS];
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
@@ -846,13 +944,9 @@ __device__ __forceinline__ void phase_c1(const CgDev& D, const CgTables* __restr
   int isflag = flags & 1;
   bool first_call = (flags & 2) != 0;
   double gammzz1 = D.gammzz1[t];
-  float snowd = D.snowd[t], ssdnn = D.ssdnn[t], snage = D.snage[t], pudsto = D.pudsto[t];
-  float wb_lake = D.wb_lake[t];
-  const float pudsmx = 0.0f;
-  const float rlam = HL;
+  float snowd = D.snowd[t], ssdnn = D.ssdnn[t];
   // phase A and B records
-  const float tk = D.work_a[0 * ld + t], precip = D.work_a[6 * ld + t], precip_sn = D.work_a[7 * ld + t];
-  const float transd = D.work_a[27 * ld + t];
+  const float precip_sn = D.work_a[7 * ld + t];
   auto Bv = [&](int i) { return D.work_b[i * ld + t]; };
   const float ga = Bv(0), dgdtg = Bv(1), fes = Bv(2), fess = Bv(3), fesp = Bv(4);
   float fevc = Bv(5), fevw = Bv(6);
@@ -862,7 +956,6 @@ __device__ __forceinline__ void phase_c1(const CgDev& D, const CgTables* __restr
   for (int k = 0; k < CG_MS; ++k) evapfbl[k] = Bv(9 + k);
   const float delwc = Bv(15), fpn = Bv(16), frday = Bv(17), tv = Bv(18);
   const bool cls_snow = (cls == 1.1335f);
-  float tss;
   // ================================================================ soil_snow
   // cbl_soilsnow_main.F90:28-207
   float precis = precis0;
@@ -1118,7 +1211,6 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
   const int v = iveg - 1, so = isoilm - 1;
   const CgPftTable& V = T->pft;
   const CgSoilTable& S = T->soil;
-  const float vlai = (iveg >= 14) ? 0.0f : D.vlai[t];
   float froot[CG_MS];
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
@@ -1149,13 +1241,8 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
   int isflag = flags & 1;
   bool first_call = (flags & 2) != 0;
   double gammzz1 = D.gammzz1[t];
-  float snowd = D.snowd[t], ssdnn = D.ssdnn[t], snage = D.snage[t], pudsto = D.pudsto[t];
-  float wb_lake = D.wb_lake[t];
-  const float pudsmx = 0.0f;
-  const float rlam = HL;
+  float snowd = D.snowd[t], ssdnn = D.ssdnn[t];
   // phase A and B records
-  const float tk = D.work_a[0 * ld + t], precip = D.work_a[6 * ld + t], precip_sn = D.work_a[7 * ld + t];
-  const float transd = D.work_a[27 * ld + t];
   auto Bv = [&](int i) { return D.work_b[i * ld + t]; };
   const float ga = Bv(0), dgdtg = Bv(1), fes = Bv(2), fess = Bv(3), fesp = Bv(4);
   float fevc = Bv(5), fevw = Bv(6);
@@ -1164,7 +1251,6 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) evapfbl[k] = Bv(9 + k);
   const float delwc = Bv(15), fpn = Bv(16), frday = Bv(17), tv = Bv(18);
-  const bool cls_snow = (cls == 1.1335f);
   float tss;
   // soil_snow, heat part (cbl_soilsnow_main.F90:125-136)
   float hcll = fmaxf(0.01f, css * rhosoil);
@@ -1264,57 +1350,71 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
     for (int k = 0; k < CG_MS; ++k)
       gf[k] = fmaxf(hcll, (1.0f - ssat) * css * rhosoil + ssat * (wblf[k] * CSWAT * DLIQ + wbfice[k] * CSICE * DICE)) * zse[k];
     if (isflag == 0) gf[0] = gf[0] + CGSNOW * snowd;
-    // tridiagonal coefficients assembled in FP32, Thomas recurrences in FP64
-    double at[9], bt[9], ct[9], rhs[9];
+    // Implicit heat conduction (cbl_stempv.F90:98-217) solved for the
+    // temperature change of the step (trid_correction).  Row k of the
+    // reference's system is a_k T_{k-1} + b_k T_k + c_k T_{k+1} = rhs_k with
+    // b_k = 1 - a_k - c_k, minus dgdtg * dtg on the surface row, and rhs the
+    // old temperatures after the explicit surface update
+    // T_1 + (ga - T_1 dgdtg) dtg (:129-131, :201-204).  Subtracting A T_old
+    // leaves ga * dtg on the surface row and -a_k (T_{k-1} - T_k)
+    // - c_k (T_{k+1} - T_k) everywhere: the surface-coupling terms in dgdtg
+    // cancel exactly.
     if (isflag == 0) {
       // soil-only system: the snow rows of the reference's 9-row system are
       // identity rows decoupled from the soil (coeff(1) = 0), so the 6-row
       // solve gives the same soil temperatures
+      float a[CG_MS], b[CG_MS], c[CG_MS], r[CG_MS];
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k) {
-        // off-diagonals in FP32; the diagonal 1 - a - c is formed in FP64 so
-        // each row keeps the exact sum that makes the scheme conservative
-        float dtg = dels / gf[k];
-        at[k] = -dtg * coeff[k];
-        ct[k] = -dtg * coeff[k + 1];
-        bt[k] = 1.0 - at[k] - ct[k];
-        if (k == 0) bt[k] = bt[k] - (double)(dgdtg * dtg);
+        const float dtg = dels / gf[k];
+        a[k] = -dtg * coeff[k];
+        c[k] = -dtg * coeff[k + 1];
+        b[k] = 1.0f - a[k] - c[k];
+        const float up = (k > 0) ? tgg[k - 1] - tgg[k] : 0.f;
+        const float dn = (k < CG_MS - 1) ? tgg[k + 1] - tgg[k] : 0.f;
+        r[k] = -(a[k] * up + c[k] * dn);
+        if (k == 0) {
+          b[0] = b[0] - dgdtg * dtg;
+          r[0] = r[0] + ga * dtg;
+        }
       }
-      tgg[0] = tgg[0] + (ga - tgg[0] * dgdtg) * dels / gf[0];
+      trid_correction<CG_MS>(a, b, c, r);
 #pragma unroll
-      for (int k = 0; k < CG_MS; ++k) rhs[k] = (double)tgg[k];
-      trimb<CG_MS>(at, bt, ct, rhs);
-#pragma unroll
-      for (int k = 0; k < CG_MS; ++k) tgg[k] = (float)rhs[k];
+      for (int k = 0; k < CG_MS; ++k) tgg[k] = tgg[k] + r[k];
       ghflux = coefb * (tgg[0] - tgg[1]);
     } else {
+      // rows 0-2 snow layers, 3-8 soil layers
       const float csnow[4] = {0.f, csn[0], csn[1], coeff[0]};   // coeff(-2..1)
-      const float sgamm0 = ssdn[0] * CGSNOW * sdepth[0];
+      float x[9], a[9], b[9], c[9], r[9];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        float dtg = dels / (ssdn[k] * CGSNOW * sdepth[k]);
-        at[k] = -dtg * csnow[k];
-        ct[k] = -dtg * csnow[k + 1];
-        bt[k] = 1.0 - at[k] - ct[k];
-        if (k == 0) bt[k] = bt[k] - (double)(dgdtg * dels / sgamm0);
+        x[k] = tggsn[k];
+        const float dtg = dels / (ssdn[k] * CGSNOW * sdepth[k]);
+        a[k] = -dtg * csnow[k];
+        c[k] = -dtg * csnow[k + 1];
       }
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k) {
-        float dtg = dels / gf[k];
-        at[3 + k] = -dtg * coeff[k];
-        ct[3 + k] = -dtg * coeff[k + 1];
-        bt[3 + k] = 1.0 - at[3 + k] - ct[3 + k];
+        x[3 + k] = tgg[k];
+        const float dtg = dels / gf[k];
+        a[3 + k] = -dtg * coeff[k];
+        c[3 + k] = -dtg * coeff[k + 1];
       }
-      tggsn[0] = tggsn[0] + (ga - tggsn[0] * dgdtg) * dels / sgamm0;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) rhs[k] = (double)tggsn[k];
+      for (int k = 0; k < 9; ++k) {
+        b[k] = 1.0f - a[k] - c[k];
+        const float up = (k > 0) ? x[k - 1] - x[k] : 0.f;
+        const float dn = (k < 8) ? x[k + 1] - x[k] : 0.f;
+        r[k] = -(a[k] * up + c[k] * dn);
+      }
+      const float dtg0 = dels / (ssdn[0] * CGSNOW * sdepth[0]);
+      b[0] = b[0] - dgdtg * dtg0;
+      r[0] = r[0] + ga * dtg0;
+      trid_correction<9>(a, b, c, r);
 #pragma unroll
-      for (int k = 0; k < CG_MS; ++k) rhs[3 + k] = (double)tgg[k];
-      trimb<9>(at, bt, ct, rhs);
+      for (int k = 0; k < 3; ++k) tggsn[k] = x[k] + r[k];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) tggsn[k] = (float)rhs[k];
-#pragma unroll
-      for (int k = 0; k < CG_MS; ++k) tgg[k] = (float)rhs[3 + k];
+      for (int k = 0; k < CG_MS; ++k) tgg[k] = x[3 + k] + r[3 + k];
       sghflux = csn[0] * (tggsn[0] - tggsn[1]);
       ghflux = coefb * (tgg[0] - tgg[1]);
     }
@@ -1418,7 +1518,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   const float pudsmx = 0.0f;
   const float rlam = HL;
   // phase A and B records
-  const float tk = D.work_a[0 * ld + t], precip = D.work_a[6 * ld + t], precip_sn = D.work_a[7 * ld + t];
+  const float tk = D.work_a[0 * ld + t], precip = D.work_a[6 * ld + t];
   const float transd = D.work_a[27 * ld + t];
   auto Bv = [&](int i) { return D.work_b[i * ld + t]; };
   const float ga = Bv(0), dgdtg = Bv(1), fes = Bv(2), fess = Bv(3), fesp = Bv(4);
@@ -1428,7 +1528,6 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) evapfbl[k] = Bv(9 + k);
   const float delwc = Bv(15), fpn = Bv(16), frday = Bv(17), tv = Bv(18);
-  const bool cls_snow = (cls == 1.1335f);
   float tss;
   // soil_snow, water part (cbl_soilsnow_main.F90:139-203), then snow_aging,
   // carbon and the balances
@@ -1493,41 +1592,63 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
       speed_k = fminf(0.5f * speed_k, 0.5f * zse[CG_MS - 1] / dels);
       fluxh[CG_MS] = fmaxf(0.0f, speed_k * wbl_k);
     }
-    float dtt[CG_MS];
-    double wblfd[CG_MS];
+    // drainage step (cbl_smoisturev.F90, nmeth = -1 explicit part)
 #pragma unroll
     for (int k = CG_MS; k >= 1; --k) {
       fluxh[k - 1] = fminf(fluxh[k - 1], (ssat - wbf[k - 1]) * zse[k - 1] / dels + fluxh[k]);
       const float dw = dels * (fluxh[k - 1] - fluxh[k]) / zse[k - 1];
       wb[k - 1] = wb[k - 1] + (double)dw;
       wbf[k - 1] = wbf[k - 1] + dw;
-      const double ssatcurr = (double)ssat - wbice[k - 1];
-      dtt[k - 1] = dels / (zse[k - 1] * (ssat - wbicef[k - 1]));
-      wblfd[k - 1] = (wb[k - 1] - wbice[k - 1]) * drcp1(ssatcurr);
     }
     rnof2 = dels * fluxh[CG_MS] * DLIQ;
-    double at[CG_MS], bt[CG_MS], ct[CG_MS];
-    float at32[CG_MS], ct32[CG_MS];
-    at32[0] = 0.f; ct32[CG_MS - 1] = 0.f;
+    // Implicit diffusion of the liquid fraction x = (wb - wbice) /
+    // (ssat - wbice) (cbl_smoisturev.F90, trimb on wblfsp), solved for the
+    // change of x (trid_correction): the right-hand side is the top layers'
+    // infiltration source minus M x_old, with the differences of x between
+    // layers formed from FP64 differences of the state, so they are exact
+    // to FP32 rounding and zero for a uniform column.
+    double liq[CG_MS];
+    float sat[CG_MS], x[CG_MS], dtt[CG_MS];
+#pragma unroll
+    for (int k = 0; k < CG_MS; ++k) {
+      liq[k] = wb[k] - wbice[k];
+      sat[k] = ssat - wbicef[k];
+      x[k] = (float)liq[k] / sat[k];
+      dtt[k] = dels / (zse[k] * sat[k]);
+    }
+    // dx[k] = x_{k-1} - x_k = (liq_{k-1} - liq_k) / sat_{k-1}
+    //         + x_k (wbice_{k-1} - wbice_k) / sat_{k-1}
+    float dx[CG_MS + 1];
+    dx[0] = 0.f; dx[CG_MS] = 0.f;
+#pragma unroll
+    for (int k = 1; k < CG_MS; ++k) {
+      const float dl = (float)(liq[k - 1] - liq[k]);
+      const float di = (float)(wbice[k - 1] - wbice[k]);
+      dx[k] = (dl + x[k] * di) / sat[k - 1];
+    }
+    float a[CG_MS], b[CG_MS], c[CG_MS], r[CG_MS];
+    a[0] = 0.f; c[CG_MS - 1] = 0.f;
 #pragma unroll
     for (int k = 2; k <= CG_MS; ++k) {
-      float wa = (float)wblfd[k - 2], wbv = (float)wblfd[k - 1];
-      float wbh_k = (zse[k - 1] * wa + zse[k - 2] * wbv) / (zse[k - 1] + zse[k - 2]);
+      float wbh_k = (zse[k - 1] * x[k - 2] + zse[k - 2] * x[k - 1]) / (zse[k - 1] + zse[k - 2]);
       float fact = powf(wbh_k, ibp2 - 1.f);
       float icef = fmaxf(wbicef[k - 2] / fmaxf(0.01f, wbf[k - 2]), wbicef[k - 1] / fmaxf(0.01f, wbf[k - 1]));
       float pwb_wbh = (hsbh * (1.f - fminf(2.f * fminf(0.1f, icef), 0.1f))) * fmaxf(pwb_min, wbh_k * fact);
       float z3_k = pwb_wbh / ldf(S.zshh, k - 1);
-      at32[k - 1] = -dtt[k - 1] * z3_k;
-      ct32[k - 2] = -dtt[k - 2] * z3_k;
+      a[k - 1] = -dtt[k - 1] * z3_k;
+      c[k - 2] = -dtt[k - 2] * z3_k;
     }
 #pragma unroll
-    for (int k = 0; k < CG_MS; ++k) { at[k] = at32[k]; ct[k] = ct32[k]; bt[k] = 1.0 - at[k] - ct[k]; }
-#pragma unroll
-    for (int k = 0; k < 3; ++k) wblfd[k] = wblfd[k] + (double)(dtt[k] * fwtop[k] / DLIQ);
-    trimb<CG_MS>(at, bt, ct, wblfd);
+    for (int k = 0; k < CG_MS; ++k) {
+      b[k] = 1.0f - a[k] - c[k];
+      r[k] = -a[k] * dx[k] + c[k] * dx[k + 1];
+      if (k < 3) r[k] = r[k] + dtt[k] * fwtop[k] / DLIQ;
+    }
+    trid_correction<CG_MS>(a, b, c, r);
+    // wb_new = wbice + (x_old + d) (ssat - wbice) = wb + d (ssat - wbice)
 #pragma unroll
     for (int k = 0; k < CG_MS; ++k) {
-      wb[k] = fma(wblfd[k], (double)ssat - wbice[k], wbice[k]);
+      wb[k] = wb[k] + (double)(r[k] * sat[k]);
       wbf[k] = (float)wb[k];
     }
     const float dfactor = 1.0f - DICE / DLIQ;

@@ -34,10 +34,12 @@ EXPORTS = [
     "cablegpu_set_forcing", "cablegpu_set_synthetic_forcing", "cablegpu_set_options", "cablegpu_step",
     "cablegpu_run", "cablegpu_synchronize", "cablegpu_run_timed", "cablegpu_kernel_timed",
     "cablegpu_launch_count", "cablegpu_param_table", "cablegpu_last_error", "cablegpu_phase_timed",
-    "cablegpu_cold_start_noalloc",
+    "cablegpu_cold_start_noalloc", "cablegpu_harvest", "cablegpu_harvest_rows", "cablegpu_surrogate_train",
+    "cablegpu_surrogate_weights", "cablegpu_set_surrogate", "cablegpu_surrogate_stats", "cablegpu_mlp_sizes",
+    "cablegpu_mlp_forward", "cablegpu_mlp_grad", "cablegpu_mlp_fit", "cablegpu_mlp_last_error",
 ]
 NOALLOC_MAX_TILES = 65536
-PHASES = ["radiation", "canopy", "snow_pack", "soil_heat", "soil_water"]
+PHASES = ["radiation", "canopy", "snow_pack", "soil_heat", "soil_water", "surrogate_net"]
 
 _lib = None
 
@@ -74,6 +76,20 @@ def load(build_if_missing: bool = True):
     L.cablegpu_cold_start.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.cablegpu_cold_start_noalloc.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                               C.POINTER(C.c_double)]
+    fp = C.POINTER(C.c_float)
+    L.cablegpu_mlp_sizes.argtypes = [C.POINTER(ip), C.POINTER(ip), C.POINTER(ip)]
+    L.cablegpu_mlp_forward.argtypes = [fp, fp, fp, C.c_longlong, fp]
+    L.cablegpu_mlp_grad.argtypes = [fp, fp, fp, C.c_longlong, fp, fp]
+    L.cablegpu_mlp_fit.argtypes = [fp, C.c_longlong, C.c_longlong, ip, ip, C.c_float, C.c_ulonglong, fp, fp, fp]
+    L.cablegpu_harvest.argtypes = [vp, ip, ip, C.c_float, C.c_float, C.c_ulonglong, C.c_longlong,
+                                   C.POINTER(C.c_longlong)]
+    L.cablegpu_harvest_rows.argtypes = [vp, fp, C.c_longlong]
+    L.cablegpu_surrogate_train.argtypes = [vp, ip, ip, C.c_float, C.c_float, C.c_ulonglong, fp]
+    L.cablegpu_surrogate_weights.argtypes = [vp, fp, fp, ip]
+    L.cablegpu_set_surrogate.argtypes = [vp, ip, C.c_float]
+    L.cablegpu_surrogate_stats.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), ip]
+    L.cablegpu_mlp_last_error.argtypes = []
+    L.cablegpu_mlp_last_error.restype = C.c_char_p
     L.cablegpu_num_fields.argtypes = []
     L.cablegpu_field_info.argtypes = [ip, C.POINTER(C.c_char_p), C.POINTER(ip), C.POINTER(ip), C.POINTER(ip)]
     L.cablegpu_field_id.argtypes = [C.c_char_p]
@@ -111,6 +127,71 @@ def fields():
 
 def _ptr(a, t):
     return a.ctypes.data_as(C.POINTER(t))
+
+
+# ---------------------------------------------------------------- surrogate network
+MLP_NPARAM, MLP_NNORM, MLP_ROW = 5187, 30, 16
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, np.float32)
+    if shape is not None:
+        assert a.shape == shape, (a.shape, shape)
+    return a
+
+
+def _mlp_check(rc):
+    if rc != 0:
+        raise CableGPUError(rc, load().cablegpu_mlp_last_error().decode())
+
+
+def mlp_forward(params, norm, rows):
+    """Raw network outputs [n][3] for training-format rows [n][16]."""
+    L = load()
+    rows = _f32(rows)
+    n = rows.shape[0]
+    y = np.empty((n, 3), np.float32)
+    _mlp_check(L.cablegpu_mlp_forward(_ptr(_f32(params, (MLP_NPARAM,)), C.c_float),
+                                      _ptr(_f32(norm, (MLP_NNORM,)), C.c_float), _ptr(rows, C.c_float), n,
+                                      _ptr(y, C.c_float)))
+    return y
+
+
+def mlp_grad(params, norm, rows):
+    """(mean squared normalised error, its gradient w.r.t. the parameters)."""
+    L = load()
+    rows = _f32(rows)
+    g = np.empty(MLP_NPARAM, np.float32)
+    loss = C.c_float()
+    _mlp_check(L.cablegpu_mlp_grad(_ptr(_f32(params, (MLP_NPARAM,)), C.c_float),
+                                   _ptr(_f32(norm, (MLP_NNORM,)), C.c_float), _ptr(rows, C.c_float),
+                                   rows.shape[0], _ptr(g, C.c_float), C.byref(loss)))
+    return float(loss.value), g
+
+
+def mlp_fit(rows, nval, epochs=20, batch=65536, lr=1e-3, seed=1):
+    """Trains a fresh network on rows[:-nval] (validation rows[-nval:]);
+    returns (params, norm, losses [epochs][2] = train, validation MSE)."""
+    L = load()
+    rows = _f32(rows)
+    ntrain = rows.shape[0] - nval
+    p = np.empty(MLP_NPARAM, np.float32)
+    nrm = np.empty(MLP_NNORM, np.float32)
+    losses = np.empty((epochs, 2), np.float32)
+    _mlp_check(L.cablegpu_mlp_fit(_ptr(rows, C.c_float), ntrain, nval, epochs, batch, lr, seed,
+                                  _ptr(p, C.c_float), _ptr(nrm, C.c_float), _ptr(losses, C.c_float)))
+    return p, nrm, losses
+
+
+def mlp_unpack(params):
+    """{W1, b1, W2, b2, W3, b3} views of a parameter vector."""
+    p = np.asarray(params)
+    return {"W1": p[0:768].reshape(64, 12), "b1": p[768:832], "W2": p[832:4928].reshape(64, 64),
+            "b2": p[4928:4992], "W3": p[4992:5184].reshape(3, 64), "b3": p[5184:5187]}
+
+
+def mlp_pack(d):
+    return np.concatenate([np.ravel(d[k]) for k in ("W1", "b1", "W2", "b2", "W3", "b3")]).astype(np.float32)
 
 
 class CableGPU:
@@ -230,6 +311,49 @@ class CableGPU:
         ms = (C.c_float * len(PHASES))()
         self._check(self.L.cablegpu_phase_timed(self.h, int(ktau0), int(nsteps), float(dels), ms))
         return dict(zip(PHASES, [float(x) for x in ms]))
+
+    # ---------------------------------------------------------- surrogate
+    def harvest(self, ktau0, nsteps, prob, seed=7, capacity=None, dels=1800.0) -> int:
+        """Runs nsteps plain steps that record dryLeaf training rows; returns
+        the number of rows filled."""
+        if capacity is None:
+            capacity = max(1024, int(self.mp * nsteps * 4 * prob * 1.3) + 1024)
+        n = C.c_longlong()
+        self._check(self.L.cablegpu_harvest(self.h, int(ktau0), int(nsteps), float(dels), float(prob), int(seed),
+                                            int(capacity), C.byref(n)))
+        return int(n.value)
+
+    def harvest_rows(self, n):
+        out = np.empty((int(n), MLP_ROW), np.float32)
+        self._check(self.L.cablegpu_harvest_rows(self.h, _ptr(out, C.c_float), int(n)))
+        return out
+
+    def surrogate_train(self, epochs=20, batch=65536, lr=1e-3, val_frac=0.1, seed=1):
+        losses = np.zeros((epochs, 2), np.float32)
+        self._check(self.L.cablegpu_surrogate_train(self.h, int(epochs), int(batch), float(lr), float(val_frac),
+                                                    int(seed), _ptr(losses, C.c_float)))
+        return losses
+
+    def surrogate_weights(self, params=None, norm=None):
+        """Returns (params, norm); sets them first when given."""
+        if params is not None:
+            p, n = _f32(params, (MLP_NPARAM,)), _f32(norm, (MLP_NNORM,))
+            self._check(self.L.cablegpu_surrogate_weights(self.h, _ptr(p, C.c_float), _ptr(n, C.c_float), 1))
+            return p, n
+        p = np.empty(MLP_NPARAM, np.float32)
+        n = np.empty(MLP_NNORM, np.float32)
+        self._check(self.L.cablegpu_surrogate_weights(self.h, _ptr(p, C.c_float), _ptr(n, C.c_float), 0))
+        return p, n
+
+    def set_surrogate(self, mode=1, gate=0.1):
+        """mode 0 off, 1 strict (unclosed predictions restart the plain
+        iteration), 2 warm (the iteration continues from the prediction)."""
+        self._check(self.L.cablegpu_set_surrogate(self.h, int(mode), float(gate)))
+
+    def surrogate_stats(self, reset=False):
+        tried, acc = C.c_longlong(), C.c_longlong()
+        self._check(self.L.cablegpu_surrogate_stats(self.h, C.byref(tried), C.byref(acc), int(reset)))
+        return int(tried.value), int(acc.value)
 
     def launch_count(self) -> int:
         return int(self.L.cablegpu_launch_count(self.h))

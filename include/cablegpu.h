@@ -148,9 +148,10 @@ int cablegpu_synchronize(cablegpu_ctx* ctx);
  * bracketed by its own events. */
 int cablegpu_run_timed(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, float* ms_total);
 int cablegpu_kernel_timed(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, float* ms_per_launch);
-/* phase_timed: average milliseconds of each of the five kernels of a step
- * (radiation, canopy, snow pack, soil heat, soil water), each bracketed by
- * its own events; ms_per_phase has 5 elements. */
+/* phase_timed: average milliseconds of each kernel of a step (radiation,
+ * canopy, snow pack, soil heat, soil water, and the surrogate network, 0
+ * when it is off), each bracketed by its own events; ms_per_phase has 6
+ * elements. */
 int cablegpu_phase_timed(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, float* ms_per_phase);
 /* Number of kernel launches of the timestep issued by this context so far:
  * five per step (radiation, canopy, snow pack, soil heat, soil water), plus
@@ -164,6 +165,70 @@ long long cablegpu_launch_count(cablegpu_ctx* ctx);
  * cable_soilparm.nml with derived entries (hsbh, ibp2, i2bp3, pwb_min,
  * cnsd).  `n` is the capacity of `out`. */
 int cablegpu_param_table(int table, const char* name, float* out, int n);
+
+/* ---------------------------------------------------------------- dryLeaf surrogate
+ * No counterpart in the reference: a small network (12 inputs -> 64 -> 64 ->
+ * 3, SiLU, BF16 tensor-core kernels with FP32 accumulation) that predicts
+ * the converged result of the dryLeaf leaf energy-balance / photosynthesis /
+ * stomatal-conductance iteration (cbl_dryLeaf.F90:10-666) from the state
+ * the iteration starts from.  With the surrogate enabled, each Monin-Obukhov
+ * iteration of each vegetated tile runs one dryLeaf pass from the predicted
+ * leaf temperature; the tile accepts it when that pass moves the leaf
+ * temperature by at most `gate` K (the leaf energy-balance residual of the
+ * prediction; the plain iteration itself stops at 0.1 K) and otherwise runs
+ * the plain iteration from its usual start, so every accepted tile meets the
+ * plain iteration's own convergence test.
+ *
+ * Inputs (training-row columns 0-11): sunlit and shaded absorbed PAR (W/m2),
+ * leaf temperature at entry (K), leaf-surface vapour pressure deficit (Pa),
+ * air CO2 (mol/mol), canopy vcmax and C3 jmax (mol/m2/s, scaled by the
+ * sunlit+shaded leaf scaling), stomatal slope (a1gs, or g1 under medlyn),
+ * soil-moisture stress factor, LAI, friction velocity (m/s), within-canopy
+ * air temperature (K).  Targets (columns 12-14): stomatal conductance to
+ * water (mol/m2/s), net assimilation (mol/m2/s), leaf temperature change
+ * over the iteration (K).  Column 15 is unused. */
+
+/* Runs nsteps plain steps that also append one training row for each
+ * sampled (vegetated tile, Monin-Obukhov iteration), sampled with
+ * probability `prob` from a counter-based hash of (tile, step, iteration,
+ * seed), into a device buffer of `capacity` rows.  *nrows: rows filled. */
+int cablegpu_harvest(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, float prob, unsigned long long seed,
+                     long long capacity, long long* nrows);
+/* Copies the first n harvested rows ([n][16] float) to the host. */
+int cablegpu_harvest_rows(cablegpu_ctx* ctx, float* host, long long n);
+/* Trains a fresh network on the harvested rows with the library's own
+ * tensor-core forward/backward kernels and Adam: the last val_frac of the
+ * rows are held out; epochs of batches of `batch` rows, one random
+ * permutation per epoch.  losses: [epochs][2] mean squared normalised
+ * error (train, validation), may be NULL. */
+int cablegpu_surrogate_train(cablegpu_ctx* ctx, int epochs, int batch, float lr, float val_frac,
+                             unsigned long long seed, float* losses);
+/* Get (set = 0) or set (set = 1) the network: params [5187] (W1 [64][12],
+ * b1 [64], W2 [64][64], b2 [64], W3 [3][64], b3 [3]) and norm [30] (input
+ * mean [12], input 1/sd [12], output mean [3], output sd [3]). */
+int cablegpu_surrogate_weights(cablegpu_ctx* ctx, float* params, float* norm, int set);
+/* mode 0: surrogate off.  1 (strict): a tile whose prediction does not
+ * close within `gate` K restarts the plain iteration from its usual start
+ * (its result is bitwise the plain kernel's).  2 (warm): the plain
+ * iteration continues from the prediction with `gate` as its convergence
+ * test.  gate in (0, 0.1] K.  Each step then runs one more kernel (the
+ * network over all tiles, on the tensor cores). */
+int cablegpu_set_surrogate(cablegpu_ctx* ctx, int mode, float gate_kelvin);
+/* Tiles x Monin-Obukhov iterations that tried the surrogate and that
+ * accepted it since the last reset; reset = 1 zeroes the counters. */
+int cablegpu_surrogate_stats(cablegpu_ctx* ctx, long long* tried, long long* accepted, int reset);
+
+/* Context-free network kernels on host arrays (rows in the training-row
+ * layout above): forward pass (y [n][3], raw units), loss and gradient of
+ * the mean squared normalised error (grad [5187]), and training of a fresh
+ * network on rows [0, ntrain) validated on [ntrain, ntrain + nval). */
+int cablegpu_mlp_sizes(int* nparam, int* nnorm, int* row);
+int cablegpu_mlp_forward(const float* params, const float* norm, const float* rows, long long n, float* y);
+int cablegpu_mlp_grad(const float* params, const float* norm, const float* rows, long long n, float* grad,
+                      float* loss);
+int cablegpu_mlp_fit(const float* rows, long long ntrain, long long nval, int epochs, int batch, float lr,
+                     unsigned long long seed, float* params_out, float* norm_out, float* losses);
+const char* cablegpu_mlp_last_error(void);
 
 const char* cablegpu_last_error(cablegpu_ctx* ctx);
 

@@ -49,11 +49,20 @@ def make_case(name):
     F = O.forcing(ts, 0, nsteps)
     st = O.init_state(ts, 0)
     steps = []
+    mix = None
     if per_step:
+        # the same run in the reference's own precision mix (REAL = FP32,
+        # r_2 = FP64): its distance from the FP64 run is the reference's
+        # precision noise, the floor any FP32 implementation is held to
+        st32 = O.init_state(ts, 1)
+        steps32 = []
         for n in range(nsteps):
             d = O.run(ts, st, 1, ktau0=1 + n, forcing=F[n:n + 1], precision=0, nthreads=1)
             steps.append(np.stack([d[k] for k in DIAG]))
+            d = O.run(ts, st32, 1, ktau0=1 + n, forcing=F[n:n + 1], precision=1, nthreads=1)
+            steps32.append(np.stack([d[k] for k in DIAG]))
         diag = np.stack(steps)                      # [nsteps, ndiag, mp]
+        mix = np.stack(steps32)
     else:
         d = O.run(ts, st, nsteps, ktau0=1, forcing=F, precision=0, nthreads=1)
         diag = np.stack([d[k] for k in DIAG])[None]  # [1, ndiag, mp]
@@ -64,6 +73,8 @@ def make_case(name):
     out = {"diag": diag, "diag_names": np.array(DIAG), "forcing": F if per_step else F[-1:],
            "nsteps": np.int32(nsteps),
            "dels": np.float32(ts.dels), "seed": np.uint64(ts.seed), "doy0": np.int32(ts.doy0)}
+    if mix is not None:
+        out["diag_precision_mix"] = mix
     for k in STATE:
         out["state_" + k] = s[k]
     for k in TILE:

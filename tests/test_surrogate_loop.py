@@ -1,0 +1,105 @@
+"""The dryLeaf surrogate end to end on the GPU: harvest training rows from
+the plain kernel, train the network with the library's own tensor-core
+kernels, run the timestep with the network in the loop, and compare with
+the method without it (the plain iteration's usual start, which a network
+predicting no change reproduces) and with the FP64 oracle (latent heat RMSE
+at most 2 W/m2, canopy temperature RMSE at most 0.05 K)."""
+import numpy as np
+import pytest
+
+import harness as H
+from cable_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def trained():
+    from cable_gb300 import runtime as R
+    ts = W.snow_grid(20000, seed=31, nsteps=96)
+    g = R.from_tileset(ts)
+    n = g.harvest(1, 96, prob=0.2, seed=5)
+    rows = g.harvest_rows(n)
+    losses = g.surrogate_train(epochs=12, batch=8192, lr=2e-3, val_frac=0.1, seed=2)
+    params, norm = g.surrogate_weights()
+    g.close()
+    return rows, losses, params, norm
+
+
+def test_harvest_rows_are_physical(trained):
+    rows, _, _, _ = trained
+    assert rows.shape[0] > 150_000
+    assert np.all(np.isfinite(rows[:, :15]))
+    assert rows[:, 0].min() > -10 and rows[:, 1].min() > -10               # absorbed PAR (W/m2; the
+    # reference's shaded-leaf PAR can come out slightly negative at low sun)
+    assert np.all((rows[:, 2] > 200) & (rows[:, 2] < 350))                 # leaf temperature at entry
+    assert np.all(rows[:, 8] > 0) and np.all(rows[:, 8] <= 1)              # soil moisture stress
+    assert np.all(rows[:, 12] >= 1e-3 - 1e-6)                              # gs floor of dryLeaf
+    assert np.abs(rows[:, 14]).max() < 30                                  # leaf temperature change
+
+
+def test_training_reduces_validation_error(trained):
+    _, losses, _, _ = trained
+    assert np.all(np.isfinite(losses))
+    assert losses[-1, 1] < 0.5 * losses[0, 1] or losses[-1, 1] < 0.1, losses
+    assert losses[-1, 1] < 0.5, losses
+
+
+def _run(ts, params, norm, mode, nsteps):
+    from cable_gb300 import runtime as R
+    g = R.from_tileset(ts)
+    g.set_options(diag=True, capture_forcing=True)
+    if mode:
+        g.surrogate_weights(params, norm)
+        g.set_surrogate(mode, 0.1)
+        g.surrogate_stats(reset=True)
+    F, passes = [], 0.0
+    for k in range(nsteps):
+        g.step(1 + k)
+        F.append(g.get("forcing"))
+        passes += float(g.get("dryleaf_passes")[0].sum())
+    g.synchronize()
+    state = {k: g.get(k) for k in H.STATE_FIELDS}
+    diag = {k: g.get(k)[0] for k in H.DIAG_MAP}
+    stats = g.surrogate_stats() if mode else (0, 0)
+    g.close()
+    return state, diag, np.stack(F), passes, stats
+
+
+def _zero_net(norm):
+    """A network that predicts no leaf-temperature change: the iteration
+    then starts where it starts without the surrogate."""
+    from cable_gb300 import runtime as R
+    z = np.zeros(R.MLP_NPARAM, np.float32)
+    n = norm.copy()
+    n[24:27] = 0.0
+    return z, n
+
+
+def test_network_gains_over_the_plain_start(trained):
+    _, _, params, norm = trained
+    ts = W.snow_grid(8000, seed=77, nsteps=24)          # other tiles and forcing than the training run
+    _, _, _, p_net, (tried, acc) = _run(ts, params, norm, 1, 24)
+    zp, zn = _zero_net(norm)
+    _, _, _, p_zero, (tried0, acc0) = _run(ts, zp, zn, 1, 24)
+    _, _, _, p_warm, _ = _run(ts, params, norm, 2, 24)
+    _, _, _, p_plain, _ = _run(ts, params, norm, 0, 24)
+    assert tried == tried0 > 0
+    # one-pass closures of the first Monin-Obukhov iteration's dryLeaf
+    assert acc > 2 * acc0, (acc, acc0, tried)
+    # warm start: fewer dryLeaf passes than the plain iteration
+    assert p_warm < p_plain, (p_warm, p_plain)
+    # strict mode costs at most one extra pass per rejected prediction
+    assert p_net <= p_plain + (tried - acc) + 1e-6
+
+
+def test_strict_surrogate_error_against_fp64(oracle, trained):
+    _, _, params, norm = trained
+    ts = W.snow_grid(8000, seed=78, nsteps=48)
+    s_sur, d_sur, F, _, (tried, acc) = _run(ts, params, norm, 1, 48)
+    st = oracle.init_state(ts, 0)
+    od = oracle.run(ts, st, 48, forcing=F, precision=0)
+    e_le = np.sqrt(np.mean((d_sur["fe_d"] - od["fe"]) ** 2))
+    e_tv = np.sqrt(np.mean((d_sur["tv_d"] - od["tv"]) ** 2))
+    assert e_le <= 2.0, e_le
+    assert e_tv <= 0.05, e_tv
