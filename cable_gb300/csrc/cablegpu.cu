@@ -189,7 +189,6 @@ struct cablegpu_ctx {
   int sur_enabled = 0;
   float sur_gate = 0.1f;
   unsigned long long* d_sur_stats = nullptr;  // [2]
-  float* d_sur_feat = nullptr;                // [12][ld] network inputs
   float* d_sur_dt = nullptr;                  // [ld] predicted leaf-temperature change
   int graph_sur = -1;
   float graph_gate = -1.f;
@@ -236,27 +235,34 @@ void bind_device_view(cablegpu_ctx* c) {
   D.harvest_cap = c->harvest_cap;
   D.harvest_prob = c->harvest_prob;
   D.harvest_seed = c->harvest_seed;
-  D.sur_feat = c->sur_enabled ? c->d_sur_feat : nullptr;
   D.sur_dt = c->sur_enabled ? c->d_sur_dt : nullptr;
   D.sur_gate = c->sur_gate;
   D.sur_strict = c->sur_enabled == 1 ? 1 : 0;
   D.sur_stats = c->sur_enabled ? c->d_sur_stats : nullptr;
 }
 
+// the surrogate network over all tiles, reading the radiation kernel's record
+int launch_sur_net(cablegpu_ctx* c) {
+  std::string e;
+  if (sur_infer(c->net, c->dev.work_a, c->dev.iveg, c->dev.isoilm, c->d_tables, c->medlyn, c->mp, c->ld, c->d_sur_dt,
+                c->dev.status, c->stream, e))
+    return fail(c, CABLEGPU_ERR_CUDA, e);
+  return CABLEGPU_OK;
+}
+
 int launch_step(cablegpu_ctx* c, const StepParams& p, const int* clock) {
   bind_device_view(c);
   const bool diag = c->diag != 0;
+  launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, clock);
   if (c->sur_enabled) {
-    launch_phase_a_sur(diag, c->stream, c->dev, c->d_tables, p, clock);
-    std::string e;
-    if (sur_infer(c->net, c->d_sur_feat, c->mp, c->ld, c->d_sur_dt, c->dev.status, c->stream, e))
-      return fail(c, CABLEGPU_ERR_CUDA, e);
+    int rc = launch_sur_net(c);
+    if (rc) return rc;
     ++c->launches;
     launch_phase_b_sur(diag, c->stream, c->dev, c->d_tables, p, clock);
+  } else if (c->harvesting) {
+    launch_phase_b_harvest(diag, c->stream, c->dev, c->d_tables, p, clock);
   } else {
-    launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, clock);
-    if (c->harvesting) launch_phase_b_harvest(diag, c->stream, c->dev, c->d_tables, p, clock);
-    else launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, clock);
+    launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, clock);
   }
   launch_phase_c1(diag, c->stream, c->dev, c->d_tables, p, clock);
   launch_phase_c2(diag, c->stream, c->dev, c->d_tables, p, clock);
@@ -409,7 +415,6 @@ int cablegpu_destroy(cablegpu_ctx* c) {
   if (c->d_harvest) cudaFree(c->d_harvest);
   if (c->d_harvest_n) cudaFree(c->d_harvest_n);
   if (c->d_sur_stats) cudaFree(c->d_sur_stats);
-  if (c->d_sur_feat) cudaFree(c->d_sur_feat);
   if (c->d_sur_dt) cudaFree(c->d_sur_dt);
   sur_free(c->net);
   cudaFreeHost(c->h_clock);
@@ -636,7 +641,6 @@ static int ensure_net(cablegpu_ctx* c) {
   if (sur_alloc(c->net, e)) return fail(c, CABLEGPU_ERR_CUDA, e);
   CG_CUDA(c, cudaMalloc(&c->d_sur_stats, 2 * sizeof(unsigned long long)));
   CG_CUDA(c, cudaMemset(c->d_sur_stats, 0, 2 * sizeof(unsigned long long)));
-  CG_CUDA(c, cudaMalloc(&c->d_sur_feat, (size_t)12 * c->ld * sizeof(float)));
   CG_CUDA(c, cudaMalloc(&c->d_sur_dt, (size_t)c->ld * sizeof(float)));
   return CABLEGPU_OK;
 }
@@ -713,13 +717,11 @@ int cablegpu_phase_timed(cablegpu_ctx* c, int ktau0, int nsteps, float dels, flo
     const StepParams p = make_params(c, ktau0 + i, dels);
     cudaEvent_t* e = &ev[(K + 1) * i];
     CG_CUDA(c, cudaEventRecord(e[0], c->stream));
-    if (sur) launch_phase_a_sur(diag, c->stream, c->dev, c->d_tables, p, nullptr);
-    else launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, nullptr);
     CG_CUDA(c, cudaEventRecord(e[1], c->stream));
     if (sur) {
-      std::string err;
-      if (sur_infer(c->net, c->d_sur_feat, c->mp, c->ld, c->d_sur_dt, c->dev.status, c->stream, err))
-        return fail(c, CABLEGPU_ERR_CUDA, err);
+      int rc = launch_sur_net(c);
+      if (rc) return rc;
     }
     CG_CUDA(c, cudaEventRecord(e[2], c->stream));
     if (sur) launch_phase_b_sur(diag, c->stream, c->dev, c->d_tables, p, nullptr);

@@ -98,10 +98,8 @@ struct CgDev {
   long long harvest_cap;
   float harvest_prob;
   unsigned long long harvest_seed;
-  // dryLeaf surrogate (null when off): the radiation kernel writes the
-  // network inputs of each tile, the network kernel the predicted leaf
+  // dryLeaf surrogate (null when off): the network kernel's predicted leaf
   // temperature change of the first Monin-Obukhov iteration
-  float* sur_feat;                 // [12][ld]
   const float* sur_dt;             // [ld]
   float sur_gate;                  // K: closure test of the prediction
   int sur_strict;                  // 1: a prediction that does not close restarts the plain iteration

@@ -35,8 +35,7 @@ __device__ __forceinline__ float ldf(const float* p, int i) { return __ldg(p + i
 // to the soil-heat kernel and on to the soil-water kernel.
 #define CG_NC 12
 
-// kSurFeat: also write the dryLeaf surrogate network's inputs (D.sur_feat).
-template <bool kDiag, bool kSurFeat = false>
+template <bool kDiag>
 __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
   const int ld = D.ld;
   const float dels = P.dels;
@@ -339,25 +338,6 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
     const float rec[CG_NA] = {tk, qv, pmb, ua, fld, ca, precip, precip_sn, vlaiw, hruff, z0soilsn, z0m, disp, zref_uv, zruffs, rt0us, rt1usa, rt1usb, usuh, coexp, rho, cmolar, epsi, visc, psyc, dsatdk, extkb, transd, flws, qssabs, fvlai[0], fvlai[1], scalex[0], scalex[1], rniso[0], rniso[1], gradis[0], gradis[1], qcan_par[0], qcan_par[1], swcan, cansto, through, fwet, wetfac, tss, wbliq0[0], wbliq0[1], wbliq0[2], wbliq0[3], wbliq0[4], wbliq0[5]};
 #pragma unroll
     for (int i = 0; i < CG_NA; ++i) D.work_a[i * ld + t] = rec[i];
-  }
-  if (kSurFeat) {
-    // inputs of the dryLeaf surrogate network at the start of the first
-    // Monin-Obukhov iteration (canopy kernel state there: leaf and canopy air
-    // at tk, neutral stability, fwsoil_calc_std of cbl_fwsoil.F90:13-38)
-    float rwater = 0.f;
-#pragma unroll
-    for (int k = 0; k < CG_MS; ++k)
-      rwater += froot[k] * fmaxf(1.0e-9f, fminf(1.0f, (wbliq0[k] - swilt) / (sfc - swilt)));
-    rwater = fmaxf(1.0e-9f, rwater);
-    const float fwsoil = P.medlyn ? fmaxf(1.0e-4f, fminf(1.0f, rwater))
-                                  : fmaxf(1.0e-9f, fminf(1.0f, ldf(V.vbeta, v) * rwater));
-    const float us1 = fminf(fmaxf(1.e-6f, VONK * fmaxf(ua, UMIN) / logf(zref_uv / z0m)), 10.0f);
-    const float sc = scalex[0] + scalex[1];
-    const float f[12] = {qcan_par[0], qcan_par[1], tk, dsx, ca, ldf(V.vcmax, v) * sc,
-                         ldf(V.ejmax, v) * (1.0f - ldf(V.frac4, v)) * sc, P.medlyn ? ldf(V.g1, v) : ldf(V.a1gs, v),
-                         fwsoil, vlaiw, us1, tk};
-#pragma unroll
-    for (int i = 0; i < 12; ++i) D.sur_feat[i * ld + t] = f[i];
   }
   if (iveg == LAKES) D.wb[t] = wb[0];
   D.wb_lake[t] = wb_lake; D.wbtot1[t] = wbtot1; D.wbtot2[t] = wbtot2;
@@ -1592,13 +1572,15 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
       speed_k = fminf(0.5f * speed_k, 0.5f * zse[CG_MS - 1] / dels);
       fluxh[CG_MS] = fmaxf(0.0f, speed_k * wbl_k);
     }
-    // drainage step (cbl_smoisturev.F90, nmeth = -1 explicit part)
+    // drainage step (cbl_smoisturev.F90, nmeth = -1 explicit part); its
+    // FP32 increments join the diffusion increments below in one FP64
+    // update of the state
+    float dwd[CG_MS];
 #pragma unroll
     for (int k = CG_MS; k >= 1; --k) {
       fluxh[k - 1] = fminf(fluxh[k - 1], (ssat - wbf[k - 1]) * zse[k - 1] / dels + fluxh[k]);
-      const float dw = dels * (fluxh[k - 1] - fluxh[k]) / zse[k - 1];
-      wb[k - 1] = wb[k - 1] + (double)dw;
-      wbf[k - 1] = wbf[k - 1] + dw;
+      dwd[k - 1] = dels * (fluxh[k - 1] - fluxh[k]) / zse[k - 1];
+      wbf[k - 1] = wbf[k - 1] + dwd[k - 1];
     }
     rnof2 = dels * fluxh[CG_MS] * DLIQ;
     // Implicit diffusion of the liquid fraction x = (wb - wbice) /
@@ -1607,23 +1589,22 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     // infiltration source minus M x_old, with the differences of x between
     // layers formed from FP64 differences of the state, so they are exact
     // to FP32 rounding and zero for a uniform column.
-    double liq[CG_MS];
     float sat[CG_MS], x[CG_MS], dtt[CG_MS];
 #pragma unroll
     for (int k = 0; k < CG_MS; ++k) {
-      liq[k] = wb[k] - wbice[k];
       sat[k] = ssat - wbicef[k];
-      x[k] = (float)liq[k] / sat[k];
+      x[k] = (wbf[k] - wbicef[k]) / sat[k];   // conductivity weighting only
       dtt[k] = dels / (zse[k] * sat[k]);
     }
     // dx[k] = x_{k-1} - x_k = (liq_{k-1} - liq_k) / sat_{k-1}
-    //         + x_k (wbice_{k-1} - wbice_k) / sat_{k-1}
+    //         + x_k (wbice_{k-1} - wbice_k) / sat_{k-1},
+    // liq_{k-1} - liq_k = (wb_{k-1} - wb_k) + (dw_{k-1} - dw_k) - di
     float dx[CG_MS + 1];
     dx[0] = 0.f; dx[CG_MS] = 0.f;
 #pragma unroll
     for (int k = 1; k < CG_MS; ++k) {
-      const float dl = (float)(liq[k - 1] - liq[k]);
-      const float di = (float)(wbice[k - 1] - wbice[k]);
+      const float di = (wbicef[k - 1] != 0.f || wbicef[k] != 0.f) ? (float)(wbice[k - 1] - wbice[k]) : 0.f;
+      const float dl = (float)(wb[k - 1] - wb[k]) + (dwd[k - 1] - dwd[k]) - di;
       dx[k] = (dl + x[k] * di) / sat[k - 1];
     }
     float a[CG_MS], b[CG_MS], c[CG_MS], r[CG_MS];
@@ -1645,11 +1626,12 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
       if (k < 3) r[k] = r[k] + dtt[k] * fwtop[k] / DLIQ;
     }
     trid_correction<CG_MS>(a, b, c, r);
-    // wb_new = wbice + (x_old + d) (ssat - wbice) = wb + d (ssat - wbice)
+    // wb_new = wbice + (x_old + d) (ssat - wbice) = wb + dw + d (ssat - wbice)
 #pragma unroll
     for (int k = 0; k < CG_MS; ++k) {
-      wb[k] = wb[k] + (double)(r[k] * sat[k]);
-      wbf[k] = (float)wb[k];
+      const float inc = r[k] * sat[k];
+      wb[k] = wb[k] + (double)(dwd[k] + inc);
+      wbf[k] = wbf[k] + inc;
     }
     const float dfactor = 1.0f - DICE / DLIQ;
 #pragma unroll
@@ -1716,9 +1698,15 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   rnof1 = rnof1 / dels + rnof5 / dels;
   rnof2 = rnof2 / dels;
   tss = (float)(1 - isflag) * tgg[0] + (float)isflag * tggsn[0];
+  // column water (mm): sum of zse (DLIQ (wb - wbice) + DICE wbice)
+  constexpr double ZL[CG_MS] = {(double)0.022f * DLIQ, (double)0.058f * DLIQ, (double)0.154f * DLIQ,
+                                (double)0.409f * DLIQ, (double)1.085f * DLIQ, (double)2.872f * DLIQ};
+  constexpr double ZI[CG_MS] = {(double)0.022f * (DICE - DLIQ), (double)0.058f * (DICE - DLIQ),
+                                (double)0.154f * (DICE - DLIQ), (double)0.409f * (DICE - DLIQ),
+                                (double)1.085f * (DICE - DLIQ), (double)2.872f * (DICE - DLIQ)};
   double wbtot = 0.0;
 #pragma unroll
-  for (int k = 0; k < CG_MS; ++k) wbtot += ((wb[k] - wbice[k]) * (double)DLIQ + wbice[k] * (double)DICE) * (double)zse[k];
+  for (int k = 0; k < CG_MS; ++k) wbtot = fma(wbice[k], ZI[k], fma(wb[k], ZL[k], wbtot));
 
   // snow_aging (cbl_snow_aging.F90:11-83)
   if (snowd > 1.0f) {

@@ -18,9 +18,6 @@ constexpr int kPhaseBlock = 128;
 // pack, c2 = soil heat, c3 = soil water, carbon and balances.  clock, when non-null, holds ktau on the device (graph replay).
 void launch_phase_a(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P, const int* clock);
 void launch_phase_b(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P, const int* clock);
-// radiation that also writes the surrogate network's inputs (D.sur_feat)
-void launch_phase_a_sur(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
-                        const int* clock);
 // canopy whose first dryLeaf iteration starts from the surrogate (D.sur_dt)
 void launch_phase_b_sur(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
                         const int* clock);

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/cablegpu.h"
+#include "cbm_physics.cuh"
 #include "surrogate.cuh"
 #include "surrogate_host.h"
 
@@ -412,11 +413,18 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_kernel(FwdArgs a) {
 
 // ------------------------------------------------------------------ in-step inference
 // Predicted leaf-temperature change of the first Monin-Obukhov iteration of
-// every tile, from the inputs the radiation kernel wrote ([12][ld], one
-// array per input so each load is coalesced).  Persistent: each CTA walks
-// 128-tile chunks.
+// every tile.  The inputs are formed here from the radiation kernel's
+// hand-off record (work_a, one array per word so each load is coalesced) and
+// the plant-type tables, exactly as the canopy kernel sees them when that
+// iteration starts: leaf and canopy air at tk, neutral stability
+// (cbl_friction_vel.F90 with psim(0) = 0), fwsoil_calc_std
+// (cbl_fwsoil.F90:13-38).  Persistent: each CTA walks 128-tile chunks.
 struct InferArgs {
-  const float* feat;   // [12][ld]
+  const float* work_a;   // [CG_NA][ld]
+  const uint8_t* iveg;
+  const uint8_t* isoilm;
+  const CgTables* tables;
+  int medlyn;
   int mp, ld;
   const uint8_t* packed;
   const float* params;
@@ -451,8 +459,33 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_soa_kernel(InferArgs a) {
     const int t = c * 128 + s;
     const bool valid = t < a.mp;
     float xn[NIN], y[NOUT];
+    if (valid) {
+      auto A = [&](int i) { return __ldg(a.work_a + (size_t)i * a.ld + t); };
+      const int v = a.iveg[t] - 1;
+      const CgPftTable& V = a.tables->pft;
+      const float tk = A(0), qv = A(1), pmb = A(2), ua = A(3), ca = A(5), vlaiw = A(8), z0m = A(11);
+      const float zref_uv = A(13), sc = A(32) + A(33);
+      const float dva = (qsatfjh(tk - TFRZ, pmb) - qv) * RMAIR / RMH2O * pmb * 100.0f;
+      // fwsoil from the soil liquid water the radiation kernel recorded
+      const CgSoilTable& S = a.tables->soil;
+      const int so = a.isoilm[t] - 1;
+      const float swilt = S.swilt[so], sfc = S.sfc[so];
+      float rwater = 0.f;
 #pragma unroll
-    for (int f = 0; f < NIN; ++f) xn[f] = valid ? (a.feat[(size_t)f * a.ld + t] - nrm[f]) * nrm[12 + f] : 0.f;
+      for (int k = 0; k < CG_MS; ++k)
+        rwater += V.froot[k][v] * fmaxf(1.0e-9f, fminf(1.0f, (A(46 + k) - swilt) / (sfc - swilt)));
+      rwater = fmaxf(1.0e-9f, rwater);
+      const float fwsoil = a.medlyn ? fmaxf(1.0e-4f, fminf(1.0f, rwater)) : fmaxf(1.0e-9f, fminf(1.0f, V.vbeta[v] * rwater));
+      const float us1 = fminf(fmaxf(1.e-6f, VONK * fmaxf(ua, UMIN) / logf(zref_uv / z0m)), 10.0f);
+      const float f[NIN] = {A(38), A(39), tk, fmaxf(dva, 0.0f), ca, V.vcmax[v] * sc,
+                            V.ejmax[v] * (1.0f - V.frac4[v]) * sc, a.medlyn ? V.g1[v] : V.a1gs[v],
+                            fwsoil, vlaiw, us1, tk};
+#pragma unroll
+      for (int q = 0; q < NIN; ++q) xn[q] = (f[q] - nrm[q]) * nrm[12 + q];
+    } else {
+#pragma unroll
+      for (int q = 0; q < NIN; ++q) xn[q] = 0.f;
+    }
     ok = forward128(smem, taddr, phase, xn, y);
     if (!ok) break;
     if (valid) a.dt[t] = y[2] * nrm[29] + nrm[26];
@@ -608,10 +641,10 @@ void sur_free(SurNet& n) {
   n = SurNet();
 }
 
-int sur_infer(const SurNet& n, const float* feat, int mp, int ld, float* dt, unsigned int* status, cudaStream_t st,
-              std::string& err) {
+int sur_infer(const SurNet& n, const float* work_a, const uint8_t* iveg, const uint8_t* isoilm, const CgTables* tables,
+              int medlyn, int mp, int ld, float* dt, unsigned int* status, cudaStream_t st, std::string& err) {
   InferArgs a;
-  a.feat = feat; a.mp = mp; a.ld = ld; a.packed = n.packed; a.params = n.params; a.norm = n.norm; a.dt = dt;
+  a.work_a = work_a; a.iveg = iveg; a.isoilm = isoilm; a.tables = tables; a.medlyn = medlyn; a.mp = mp; a.ld = ld; a.packed = n.packed; a.params = n.params; a.norm = n.norm; a.dt = dt;
   a.status = status;
   const int chunks = (mp + 127) / 128;
   const int grid = std::max(1, std::min(chunks, 8 * n.nblk));

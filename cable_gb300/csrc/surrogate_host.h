@@ -25,10 +25,13 @@ struct SurNet {
 int sur_alloc(SurNet& n, std::string& err);
 void sur_free(SurNet& n);
 int sur_pack(SurNet& n, cudaStream_t st, std::string& err);
-// Predicted first-iteration leaf-temperature change dt [mp] of every tile
-// from the inputs feat [12][ld] (stream-ordered, one kernel launch).
-int sur_infer(const SurNet& n, const float* feat, int mp, int ld, float* dt, unsigned int* status, cudaStream_t st,
-              std::string& err);
+// Predicted first-iteration leaf-temperature change dt [mp] of every tile,
+// its inputs formed from the radiation kernel's hand-off record work_a
+// ([CG_NA][ld]) and the tile tables (stream-ordered, one kernel launch).
+namespace cg { struct CgTables; }
+int sur_infer(const SurNet& n, const float* work_a, const uint8_t* iveg, const uint8_t* isoilm,
+              const cg::CgTables* tables, int medlyn, int mp, int ld, float* dt, unsigned int* status,
+              cudaStream_t st, std::string& err);
 // Trains on rows [0, ntrain) of d_rows, validating on [ntrain, ntrain+nval);
 // losses: [epochs][2] (train, validation mean squared normalised error).
 int sur_fit(SurNet& n, const float* d_rows, long long ntrain, long long nval, int epochs, int batch, float lr,
