@@ -261,7 +261,10 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
     float den = fmaxf(0.0830f, sfc - wilting_pt);
     wetfac = fmaxf(0.0f, fminf(1.0f, ((float)wb[0] - wilting_pt) / den));
     if (wbice[0] > 0.0) {
-      float ice_ratio = (float)((wbice[0] / wb[0]) * (wbice[0] / wb[0]));
+      // (wbice / wb)^2 in FP32: the quotient of the FP32-rounded values is
+      // within a few ulp of the reference's r_2 quotient rounded to REAL
+      const float q = (float)wbice[0] / (float)wb[0];
+      float ice_ratio = q * q;
       float ice_factor = fmaxf(0.5f, 1.0f - fminf(0.2f, ice_ratio));
       wetfac = wetfac * ice_factor;
     }
@@ -1298,7 +1301,7 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
         float ew = wblf[k] * ssat;
         float exp_arg = ew * 4.0943446f /* log 60 */ + wbfice[k] * ssat * 5.5214609f /* log 250 */;
         float f2 = fmaxf(1.0f, sqrtf(fminf(2.0f, 0.5f * ssat / fminf(ew, 0.5f * ssat))));
-        ccnsw[k] = (exp_arg > 30.f) ? 1.5f * f2 : fminf(cnsd * expf(exp_arg), 1.5f) * f2;
+        ccnsw[k] = (exp_arg > 30.f) ? 1.5f * f2 : fminf(cnsd * __expf(exp_arg), 1.5f) * f2;
       }
     }
     float coeff[CG_MS + 1];   // coeff(1..ms+1) of the reference, coeff[ms] = 0
@@ -1555,7 +1558,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
       float delt = wbl_kp - wbl_k;
       float wh = fminf(wbl_k, wbl_kp);
       if (wbicef[k - 1] > 0.05f || wbicef[k] > 0.01f) wh = 0.9f * wbl_k + 0.1f * wbl_kp;
-      float speed_k = hyds * powf(wh / ssat, i2bp3 - 1.f);
+      float speed_k = hyds * __powf(wh / ssat, i2bp3 - 1.f);
       float rat = delt_prev / (delt + fsignf(1.0e-20f, delt));
       float phi = fmaxf(fmaxf(0.0f, fminf(1.0f, 2.0f * rat)), fminf(2.0f, rat));
       speed_k = fminf(speed_k, 0.5f * zse[k - 1] / dels);
@@ -1567,7 +1570,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
       float wbl_kp = fmaxf(0.001f, ssat - wbicef[CG_MS - 1]);
       float wh = fminf(wbl_k, wbl_kp);
       if (wbicef[CG_MS - 1] > 0.05f) wh = 0.9f * wbl_k + 0.1f * wbl_kp;
-      float speed_k = hyds * powf(wh / ssat, i2bp3 - 1.f);
+      float speed_k = hyds * __powf(wh / ssat, i2bp3 - 1.f);
       speed_k = 0.5f * speed_k / (1.f - fminf(0.5f, 10.f * wbicef[CG_MS - 1]));
       speed_k = fminf(0.5f * speed_k, 0.5f * zse[CG_MS - 1] / dels);
       fluxh[CG_MS] = fmaxf(0.0f, speed_k * wbl_k);
@@ -1612,7 +1615,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
 #pragma unroll
     for (int k = 2; k <= CG_MS; ++k) {
       float wbh_k = (zse[k - 1] * x[k - 2] + zse[k - 2] * x[k - 1]) / (zse[k - 1] + zse[k - 2]);
-      float fact = powf(wbh_k, ibp2 - 1.f);
+      float fact = __powf(wbh_k, ibp2 - 1.f);
       float icef = fmaxf(wbicef[k - 2] / fmaxf(0.01f, wbf[k - 2]), wbicef[k - 1] / fmaxf(0.01f, wbf[k - 1]));
       float pwb_wbh = (hsbh * (1.f - fminf(2.f * fminf(0.1f, icef), 0.1f))) * fmaxf(pwb_min, wbh_k * fact);
       float z3_k = pwb_wbh / ldf(S.zshh, k - 1);
@@ -1716,7 +1719,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     float ar3;
     if (isoilm == ICE_SOIL) { ar3 = 0.0000001f; dnsnow = 1.0f; }
     else ar3 = 0.1f;
-    float dtau = 1.0e-6f * (expf(ar1) + expf(10.0f * ar1) + ar3) * dels;
+    float dtau = 1.0e-6f * (__expf(ar1) + __expf(10.0f * ar1) + ar3) * dels;
     snage = fmaxf(0.0f, (snage + dtau) * (1.0f - dnsnow));
   }
   const float trad = sqrtf(sqrtf((1.f - transd) * pow4(tv) + transd * pow4(tss)));
@@ -1734,7 +1737,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     float pc1w = pc1 - rc2 * cplant[2];
     float pc1r = pc1 - rc1 * cplant[1];
     float tmp1 = fmaxf(3.22f - 0.046f * (tk - TFRZ), 1e-6f);
-    float tmp3 = powf(tmp1, 0.1f * (tk - TFRZ - 20.0f));
+    float tmp3 = __powf(tmp1, 0.1f * (tk - TFRZ - 20.0f));
     float c = ldf(V.rp20, v) * tmp3 / 31536000.0f;
     frp = c * pc1; frpw = c * pc1w; frpr = c * pc1r;
   }
@@ -1753,24 +1756,24 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     float e0rswc = 52.4f + 285.f * rswc;
     float ftsoil = fminf(0.0015f, 1.f / (tref + 46.f) - 1.f / (tsoil + 46.f));
     float sss = fmaxf(-15.f, fminf(1.f, e0rswc * ftsoil));
-    frs = ldf(V.vegcf, v) * (144.0f / 44.0e6f) * fminf(1.f, 1.4f * fmaxf(.3f, .0278f * tsoil + .5f)) * expf(sss) * rswc /
+    frs = ldf(V.vegcf, v) * (144.0f / 44.0e6f) * fminf(1.f, 1.4f * fmaxf(.3f, .0278f * tsoil + .5f)) * __expf(sss) * rswc /
           (0.16f + rswc);
   }
   {
-    float coef_cold = expf(fminf(1.f, -(tv - ldf(V.tvclst, v))));
+    float coef_cold = __expf(fminf(1.f, -(tv - ldf(V.tvclst, v))));
     float wbav = 0.f;
 #pragma unroll
     for (int k = 0; k < CG_MS; ++k) wbav += froot[k] * wbf[k];
     wbav = fmaxf(0.01f, wbav);
     float campbell = 2.0f - ldf(S.ibp2, so);
-    float esw = fmaxf(1.0f, powf(wbav, campbell) - 1.0f);
-    float eswilt = powf(swilt, campbell) - 1.0f;
+    float esw = fmaxf(1.0f, __powf(wbav, campbell) - 1.0f);
+    float eswilt = __powf(swilt, campbell) - 1.0f;
     float relstress = fminf(1.0f, esw / eswilt - 1.0f);
-    float coef_cd = (coef_cold + expf(5.0f * relstress)) * 2.0e-7f;
-    float fcl = expf(-ldf(V.tfcl, v) * vlai);
+    float coef_cd = (coef_cold + __expf(5.0f * relstress)) * 2.0e-7f;
+    float fcl = __expf(-ldf(V.tfcl, v) * vlai);
     float clitt = (coef_cd + 3.17e-8f) * cplant[0];
     cplant[0] = cplant[0] - dels * (fpn * fcl + clitt);
-    float fr = fminf(1.f, expf(-ldf(V.rw, v) * 0.9f * 0.0001f * cplant[2] / fmaxf(cplant[1], 0.01f)) / 0.9f);
+    float fr = fminf(1.f, __expf(-ldf(V.rw, v) * 0.9f * 0.0001f * cplant[2] / fmaxf(cplant[1], 0.01f)) / 0.9f);
     float cfwd = 6.342e-10f * cplant[1];
     cplant[1] = cplant[1] - dels * (fpn * (1.f - fcl) * (1.f - fr) + frpw + cfwd);
     float cfrts = 4.53e-9f * cplant[2];
