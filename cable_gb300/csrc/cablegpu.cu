@@ -192,6 +192,11 @@ struct cablegpu_ctx {
   float* d_sur_dt = nullptr;                  // [ld] predicted leaf-temperature change
   int graph_sur = -1;
   float graph_gate = -1.f;
+  // threads per block of the five step kernels (radiation, canopy, snow
+  // pack, soil heat, soil water) and the tile order the context was built with
+  int block[5] = {128, 128, 128, 128, 128};
+  int graph_block[5] = {0, 0, 0, 0, 0};
+  int order = 0;
   std::string err;
 };
 
@@ -253,20 +258,21 @@ int launch_sur_net(cablegpu_ctx* c) {
 int launch_step(cablegpu_ctx* c, const StepParams& p, const int* clock) {
   bind_device_view(c);
   const bool diag = c->diag != 0;
-  launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, clock);
+  const int* bk = c->block;
+  launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, clock, bk[0]);
   if (c->sur_enabled) {
     int rc = launch_sur_net(c);
     if (rc) return rc;
     ++c->launches;
-    launch_phase_b_sur(diag, c->stream, c->dev, c->d_tables, p, clock);
+    launch_phase_b_sur(diag, c->stream, c->dev, c->d_tables, p, clock, bk[1]);
   } else if (c->harvesting) {
-    launch_phase_b_harvest(diag, c->stream, c->dev, c->d_tables, p, clock);
+    launch_phase_b_harvest(diag, c->stream, c->dev, c->d_tables, p, clock, bk[1]);
   } else {
-    launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, clock);
+    launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, clock, bk[1]);
   }
-  launch_phase_c1(diag, c->stream, c->dev, c->d_tables, p, clock);
-  launch_phase_c2(diag, c->stream, c->dev, c->d_tables, p, clock);
-  launch_phase_c3(diag, c->stream, c->dev, c->d_tables, p, clock);
+  launch_phase_c1(diag, c->stream, c->dev, c->d_tables, p, clock, bk[2]);
+  launch_phase_c2(diag, c->stream, c->dev, c->d_tables, p, clock, bk[3]);
+  launch_phase_c3(diag, c->stream, c->dev, c->d_tables, p, clock, bk[4]);
   c->launches += kKernelsPerStep;
   CG_CUDA(c, cudaGetLastError());
   return CABLEGPU_OK;
@@ -287,7 +293,7 @@ int ensure_graph(cablegpu_ctx* c, float dels) {
   if (c->graph && c->graph_dels == dels && c->graph_diag == c->diag && c->graph_medlyn == c->medlyn &&
       c->graph_hostforc == (int)c->host_forcing && c->graph_capture == c->capture_forcing &&
       c->graph_seed == c->forc.seed && c->graph_doy0 == c->forc.doy0 && c->graph_sur == c->sur_enabled &&
-      c->graph_gate == c->sur_gate)
+      c->graph_gate == c->sur_gate && std::equal(c->block, c->block + 5, c->graph_block))
     return CABLEGPU_OK;
   if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   StepParams p = make_params(c, 0, dels);
@@ -307,6 +313,7 @@ int ensure_graph(cablegpu_ctx* c, float dels) {
   c->graph_hostforc = (int)c->host_forcing; c->graph_capture = c->capture_forcing;
   c->graph_seed = c->forc.seed; c->graph_doy0 = c->forc.doy0;
   c->graph_sur = c->sur_enabled; c->graph_gate = c->sur_gate;
+  std::copy(c->block, c->block + 5, c->graph_block);
   return CABLEGPU_OK;
 }
 
@@ -335,14 +342,29 @@ int cablegpu_field_id(const char* name) {
 }
 
 int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out) {
-  if (!tiles || !out || tiles->mp <= 0 || !tiles->iveg || !tiles->isoilm || !tiles->vlai || !tiles->lat)
+  if (!tiles || !out || tiles->mp <= 0 || !tiles->iveg || !tiles->isoilm || !tiles->vlai || !tiles->lat ||
+      tiles->order < -1 || tiles->order > 2)
     return CABLEGPU_ERR_ARG;
   for (int i = 0; i < tiles->mp; ++i)
     if (tiles->iveg[i] < 1 || tiles->iveg[i] > CG_NPFT || tiles->isoilm[i] < 1 || tiles->isoilm[i] > CG_NSOIL)
       return CABLEGPU_ERR_ARG;
+  if (tiles->order == -1) {
+    // autotuned: tile order and block sizes measured on a sample of these tiles
+    int best_order = 0, blocks[5];
+    float ms = 0.f;
+    int rc = cablegpu_autotune(tiles, device, std::min(tiles->mp, 4 << 20), 8, &best_order, blocks, &ms);
+    if (rc) return rc;
+    cablegpu_tiles t = *tiles;
+    t.order = best_order;
+    rc = cablegpu_create(&t, device, out);
+    if (rc) return rc;
+    std::copy(blocks, blocks + 5, (*out)->block);
+    return CABLEGPU_OK;
+  }
   auto* c = new cablegpu_ctx();
   *out = c;
   c->device = device;
+  c->order = tiles->order;
   c->mp = tiles->mp;
   c->ld = (tiles->mp + 255) / 256 * 256;
   CG_CUDA(c, cudaSetDevice(device));
@@ -369,11 +391,27 @@ int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out)
   {
     std::vector<int> order(c->mp);
     for (int i = 0; i < c->mp; ++i) order[i] = i;
-    if (tiles->order == 0)
-      std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        if (tiles->iveg[a] != tiles->iveg[b]) return tiles->iveg[a] < tiles->iveg[b];
-        return tiles->isoilm[a] < tiles->isoilm[b];
-      });
+    if (tiles->order == 0 || tiles->order == 2) {
+      // sort key, most significant first: plant type, soil type (order 0);
+      // plant type, local solar hour, 5-degree latitude band, LAI (order 2),
+      // so a warp's tiles share radiation and hence iteration counts
+      std::vector<std::pair<unsigned long long, int>> key(c->mp);
+      for (int i = 0; i < c->mp; ++i) {
+        unsigned long long k = (unsigned long long)(tiles->iveg[i] & 0xff) << 56;
+        if (tiles->order == 0) {
+          k |= (unsigned long long)(tiles->isoilm[i] & 0xff) << 48;
+        } else {
+          const float ph = tiles->lonphase ? tiles->lonphase[i] : 0.f;
+          const int hr = std::min(23, std::max(0, (int)ph));
+          const int band = std::min(63, std::max(0, (int)((tiles->lat[i] + 90.f) / 5.f)));
+          const int lai = std::min(255, std::max(0, (int)(tiles->vlai[i] * 32.f)));
+          k |= (unsigned long long)hr << 48 | (unsigned long long)band << 40 | (unsigned long long)lai << 32;
+        }
+        key[i] = {k, i};
+      }
+      std::sort(key.begin(), key.end());
+      for (int i = 0; i < c->mp; ++i) order[i] = key[i].second;
+    }
     CG_CUDA(c, cudaMalloc(&c->d_order, sizeof(int) * c->mp));
     CG_CUDA(c, cudaMemcpy(c->d_order, order.data(), sizeof(int) * c->mp, cudaMemcpyHostToDevice));
     c->stage_bytes = (size_t)c->mp * 64;
@@ -717,21 +755,21 @@ int cablegpu_phase_timed(cablegpu_ctx* c, int ktau0, int nsteps, float dels, flo
     const StepParams p = make_params(c, ktau0 + i, dels);
     cudaEvent_t* e = &ev[(K + 1) * i];
     CG_CUDA(c, cudaEventRecord(e[0], c->stream));
-    launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, nullptr, c->block[0]);
     CG_CUDA(c, cudaEventRecord(e[1], c->stream));
     if (sur) {
       int rc = launch_sur_net(c);
       if (rc) return rc;
     }
     CG_CUDA(c, cudaEventRecord(e[2], c->stream));
-    if (sur) launch_phase_b_sur(diag, c->stream, c->dev, c->d_tables, p, nullptr);
-    else launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    if (sur) launch_phase_b_sur(diag, c->stream, c->dev, c->d_tables, p, nullptr, c->block[1]);
+    else launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, nullptr, c->block[1]);
     CG_CUDA(c, cudaEventRecord(e[3], c->stream));
-    launch_phase_c1(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    launch_phase_c1(diag, c->stream, c->dev, c->d_tables, p, nullptr, c->block[2]);
     CG_CUDA(c, cudaEventRecord(e[4], c->stream));
-    launch_phase_c2(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    launch_phase_c2(diag, c->stream, c->dev, c->d_tables, p, nullptr, c->block[3]);
     CG_CUDA(c, cudaEventRecord(e[5], c->stream));
-    launch_phase_c3(diag, c->stream, c->dev, c->d_tables, p, nullptr);
+    launch_phase_c3(diag, c->stream, c->dev, c->d_tables, p, nullptr, c->block[4]);
     CG_CUDA(c, cudaEventRecord(e[6], c->stream));
     CG_CUDA(c, cudaGetLastError());
     c->launches += kKernelsPerStep + (sur ? 1 : 0);
@@ -748,6 +786,71 @@ int cablegpu_phase_timed(cablegpu_ctx* c, int ktau0, int nsteps, float dels, flo
     }
   }
   for (auto& e : ev) cudaEventDestroy(e);
+  return CABLEGPU_OK;
+}
+
+int cablegpu_set_blocks(cablegpu_ctx* c, const int* block5) {
+  if (!c || !block5) return CABLEGPU_ERR_ARG;
+  for (int k = 0; k < 5; ++k)
+    if (block5[k] < 32 || block5[k] > 256 || block5[k] % 32) return fail(c, CABLEGPU_ERR_ARG, "set_blocks: 32..256, multiple of 32");
+  std::copy(block5, block5 + 5, c->block);
+  return CABLEGPU_OK;
+}
+
+int cablegpu_get_config(cablegpu_ctx* c, int* order, int* block5) {
+  if (!c) return CABLEGPU_ERR_ARG;
+  if (order) *order = c->order;
+  if (block5) std::copy(c->block, c->block + 5, block5);
+  return CABLEGPU_OK;
+}
+
+int cablegpu_autotune(const cablegpu_tiles* tiles, int device, int sample_tiles, int nsteps, int* order_out,
+                      int* block5_out, float* ms_out) {
+  if (!tiles || tiles->mp <= 0 || sample_tiles < 1024 || nsteps < 1 || !order_out || !block5_out)
+    return CABLEGPU_ERR_ARG;
+  // an evenly strided sample of the tiles, cold-started without snow at
+  // 285 K and 0.25 soil moisture, driven by the synthetic forcing
+  const int n = std::min(sample_tiles, tiles->mp);
+  std::vector<int> iveg(n), isoil(n);
+  std::vector<float> vlai(n), lat(n), ph(n), tb(n), sw(n);
+  for (int i = 0; i < n; ++i) {
+    const int j = (int)((long long)i * tiles->mp / n);
+    iveg[i] = tiles->iveg[j]; isoil[i] = tiles->isoilm[j]; vlai[i] = tiles->vlai[j]; lat[i] = tiles->lat[j];
+    ph[i] = tiles->lonphase ? tiles->lonphase[j] : 0.f;
+    tb[i] = tiles->tbase ? tiles->tbase[j] : 288.f;
+    sw[i] = tiles->swscale ? tiles->swscale[j] : 1.f;
+  }
+  std::vector<double> sn(n, 0.0), tg(n, 285.0), wb(n, 0.25);
+  const int cand_block[3] = {64, 128, 256};
+  float best = 1e30f;
+  for (int order = 0; order <= 2; ++order) {
+    cablegpu_tiles t = {n, iveg.data(), isoil.data(), vlai.data(), lat.data(), ph.data(), tb.data(), sw.data(), order};
+    cablegpu_ctx* c = nullptr;
+    int rc = cablegpu_create(&t, device, &c);
+    if (!rc) rc = cablegpu_cold_start(c, sn.data(), tg.data(), wb.data());
+    if (!rc) rc = cablegpu_set_synthetic_forcing(c, 1234567ull, 1);
+    if (!rc) rc = cablegpu_run(c, 1, 4, 1800.f);
+    float per[5] = {1e30f, 1e30f, 1e30f, 1e30f, 1e30f};
+    int pick[5] = {128, 128, 128, 128, 128};
+    for (int b = 0; b < 3 && !rc; ++b) {
+      int bb[5];
+      std::fill(bb, bb + 5, cand_block[b]);
+      rc = cablegpu_set_blocks(c, bb);
+      float ms[6];
+      if (!rc) rc = cablegpu_phase_timed(c, 5 + b * nsteps, nsteps, 1800.f, ms);
+      for (int k = 0; k < 5 && !rc; ++k)
+        if (ms[k] < per[k]) { per[k] = ms[k]; pick[k] = cand_block[b]; }
+    }
+    if (c) cablegpu_destroy(c);
+    if (rc) return rc;
+    const float tot = per[0] + per[1] + per[2] + per[3] + per[4];
+    if (tot < best) {
+      best = tot;
+      *order_out = order;
+      std::copy(pick, pick + 5, block5_out);
+    }
+  }
+  if (ms_out) *ms_out = best;
   return CABLEGPU_OK;
 }
 

@@ -8,7 +8,7 @@ namespace cg {
 
 // The canopy kernel that also records dryLeaf training rows.
 template <bool kDiag>
-__global__ void __launch_bounds__(kPhaseBlock, CG_MIN_BLOCKS)
+__global__ void __maxnreg__(CG_MAXNREG)
     cbm_phase_b_harvest_kernel(CgDev D, const CgTables* __restrict__ T, StepParams P, const int* __restrict__ clock) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= D.mp) return;
@@ -18,16 +18,16 @@ __global__ void __launch_bounds__(kPhaseBlock, CG_MIN_BLOCKS)
 }
 
 void launch_phase_b_harvest(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
-                            const int* clock) {
-  const int grid = (D.mp + kPhaseBlock - 1) / kPhaseBlock;
-  if (diag) cbm_phase_b_harvest_kernel<true><<<grid, kPhaseBlock, 0, s>>>(D, T, P, clock);
-  else cbm_phase_b_harvest_kernel<false><<<grid, kPhaseBlock, 0, s>>>(D, T, P, clock);
+                            const int* clock, int block) {
+  const int grid = (D.mp + block - 1) / block;
+  if (diag) cbm_phase_b_harvest_kernel<true><<<grid, block, 0, s>>>(D, T, P, clock);
+  else cbm_phase_b_harvest_kernel<false><<<grid, block, 0, s>>>(D, T, P, clock);
 }
 
 // The canopy kernel whose first dryLeaf iteration starts from the
 // surrogate network's prediction (D.sur_dt).
 template <bool kDiag>
-__global__ void __launch_bounds__(kPhaseBlock, CG_MIN_BLOCKS)
+__global__ void __maxnreg__(CG_MAXNREG)
     cbm_phase_b_sur_kernel(CgDev D, const CgTables* __restrict__ T, StepParams P, const int* __restrict__ clock) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= D.mp) return;
@@ -37,10 +37,10 @@ __global__ void __launch_bounds__(kPhaseBlock, CG_MIN_BLOCKS)
 }
 
 void launch_phase_b_sur(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
-                        const int* clock) {
-  const int grid = (D.mp + kPhaseBlock - 1) / kPhaseBlock;
-  if (diag) cbm_phase_b_sur_kernel<true><<<grid, kPhaseBlock, 0, s>>>(D, T, P, clock);
-  else cbm_phase_b_sur_kernel<false><<<grid, kPhaseBlock, 0, s>>>(D, T, P, clock);
+                        const int* clock, int block) {
+  const int grid = (D.mp + block - 1) / block;
+  if (diag) cbm_phase_b_sur_kernel<true><<<grid, block, 0, s>>>(D, T, P, clock);
+  else cbm_phase_b_sur_kernel<false><<<grid, block, 0, s>>>(D, T, P, clock);
 }
 
 }  // namespace cg

@@ -7,30 +7,35 @@
 
 namespace cg {
 
-constexpr int kPhaseBlock = 128;
-// Minimum resident blocks per SM requested from the register allocator
-// (occupancy versus spills); set per phase translation unit.
-#ifndef CG_MIN_BLOCKS
-#define CG_MIN_BLOCKS 1
+constexpr int kPhaseBlock = 128;   // default threads per block; launches take any multiple of 32 up to 256
+// Registers per thread (occupancy versus spills), set per phase translation
+// unit; independent of the block size chosen at launch.
+#ifndef CG_MAXNREG
+#define CG_MAXNREG 128
 #endif
 
 // Launch one phase over D.mp tiles: a = radiation, b = canopy, c1 = snow
 // pack, c2 = soil heat, c3 = soil water, carbon and balances.  clock, when non-null, holds ktau on the device (graph replay).
-void launch_phase_a(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P, const int* clock);
-void launch_phase_b(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P, const int* clock);
+void launch_phase_a(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
+                    const int* clock, int block = kPhaseBlock);
+void launch_phase_b(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
+                    const int* clock, int block = kPhaseBlock);
 // canopy whose first dryLeaf iteration starts from the surrogate (D.sur_dt)
 void launch_phase_b_sur(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
-                        const int* clock);
+                    const int* clock, int block = kPhaseBlock);
 // canopy that also appends dryLeaf training rows to D.harvest
 void launch_phase_b_harvest(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
-                            const int* clock);
-void launch_phase_c1(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P, const int* clock);
-void launch_phase_c2(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P, const int* clock);
-void launch_phase_c3(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P, const int* clock);
+                    const int* clock, int block = kPhaseBlock);
+void launch_phase_c1(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
+                    const int* clock, int block = kPhaseBlock);
+void launch_phase_c2(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
+                    const int* clock, int block = kPhaseBlock);
+void launch_phase_c3(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
+                    const int* clock, int block = kPhaseBlock);
 
 #ifdef CG_PHASE
 template <bool kDiag>
-__global__ void __launch_bounds__(kPhaseBlock, CG_MIN_BLOCKS)
+__global__ void __maxnreg__(CG_MAXNREG)
     CG_PHASE_KERNEL(CgDev D, const CgTables* __restrict__ T, StepParams P, const int* __restrict__ clock) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= D.mp) return;
@@ -40,10 +45,10 @@ __global__ void __launch_bounds__(kPhaseBlock, CG_MIN_BLOCKS)
 }
 
 void CG_PHASE_LAUNCH(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
-                     const int* clock) {
-  const int grid = (D.mp + kPhaseBlock - 1) / kPhaseBlock;
-  if (diag) CG_PHASE_KERNEL<true><<<grid, kPhaseBlock, 0, s>>>(D, T, P, clock);
-  else CG_PHASE_KERNEL<false><<<grid, kPhaseBlock, 0, s>>>(D, T, P, clock);
+                     const int* clock, int block) {
+  const int grid = (D.mp + block - 1) / block;
+  if (diag) CG_PHASE_KERNEL<true><<<grid, block, 0, s>>>(D, T, P, clock);
+  else CG_PHASE_KERNEL<false><<<grid, block, 0, s>>>(D, T, P, clock);
 }
 #endif
 

@@ -37,6 +37,7 @@ EXPORTS = [
     "cablegpu_cold_start_noalloc", "cablegpu_harvest", "cablegpu_harvest_rows", "cablegpu_surrogate_train",
     "cablegpu_surrogate_weights", "cablegpu_set_surrogate", "cablegpu_surrogate_stats", "cablegpu_mlp_sizes",
     "cablegpu_mlp_forward", "cablegpu_mlp_grad", "cablegpu_mlp_fit", "cablegpu_mlp_last_error",
+    "cablegpu_set_blocks", "cablegpu_get_config", "cablegpu_autotune",
 ]
 NOALLOC_MAX_TILES = 65536
 PHASES = ["radiation", "canopy", "snow_pack", "soil_heat", "soil_water", "surrogate_net"]
@@ -105,6 +106,9 @@ def load(build_if_missing: bool = True):
     L.cablegpu_run_timed.argtypes = [vp, ip, ip, C.c_float, C.POINTER(C.c_float)]
     L.cablegpu_kernel_timed.argtypes = [vp, ip, ip, C.c_float, C.POINTER(C.c_float)]
     L.cablegpu_phase_timed.argtypes = [vp, ip, ip, C.c_float, C.POINTER(C.c_float)]
+    L.cablegpu_set_blocks.argtypes = [vp, C.POINTER(ip)]
+    L.cablegpu_get_config.argtypes = [vp, C.POINTER(ip), C.POINTER(ip)]
+    L.cablegpu_autotune.argtypes = [C.POINTER(_Tiles), ip, ip, ip, C.POINTER(ip), C.POINTER(ip), C.POINTER(C.c_float)]
     L.cablegpu_launch_count.argtypes = [vp]
     L.cablegpu_launch_count.restype = C.c_longlong
     L.cablegpu_param_table.argtypes = [ip, C.c_char_p, C.POINTER(C.c_float), ip]
@@ -198,6 +202,8 @@ class CableGPU:
     """One device context holding ``mp`` tiles (see module docstring)."""
 
     def __init__(self, tiles, device: int = 0, order: int = 0):
+        """order: 0 grouped by plant and soil type, 1 as given, 2 grouped by
+        plant type, local solar hour, latitude band and LAI, -1 autotuned."""
         self.L = load()
         self.fields = fields()
         self.mp = int(tiles.mp)
@@ -207,10 +213,7 @@ class CableGPU:
             lonphase=np.ascontiguousarray(tiles.lonphase, np.float32),
             tbase=np.ascontiguousarray(tiles.tbase, np.float32),
             swscale=np.ascontiguousarray(tiles.swscale, np.float32))
-        k = self._keep
-        t = _Tiles(self.mp, _ptr(k["iveg"], C.c_int), _ptr(k["isoilm"], C.c_int), _ptr(k["vlai"], C.c_float),
-                   _ptr(k["lat"], C.c_float), _ptr(k["lonphase"], C.c_float), _ptr(k["tbase"], C.c_float),
-                   _ptr(k["swscale"], C.c_float), int(order))
+        t = self._tiles_struct(order)
         h = C.c_void_p()
         rc = self.L.cablegpu_create(C.byref(t), device, C.byref(h))
         self.h = h
@@ -220,6 +223,12 @@ class CableGPU:
                 self.L.cablegpu_destroy(h)
             self.h = C.c_void_p()
             raise CableGPUError(rc, msg)
+
+    def _tiles_struct(self, order):
+        k = self._keep
+        return _Tiles(self.mp, _ptr(k["iveg"], C.c_int), _ptr(k["isoilm"], C.c_int), _ptr(k["vlai"], C.c_float),
+                      _ptr(k["lat"], C.c_float), _ptr(k["lonphase"], C.c_float), _ptr(k["tbase"], C.c_float),
+                      _ptr(k["swscale"], C.c_float), int(order))
 
     # ------------------------------------------------------------------ util
     def _check(self, rc):
@@ -355,8 +364,38 @@ class CableGPU:
         self._check(self.L.cablegpu_surrogate_stats(self.h, C.byref(tried), C.byref(acc), int(reset)))
         return int(tried.value), int(acc.value)
 
+    def set_blocks(self, blocks):
+        b = (C.c_int * 5)(*[int(x) for x in blocks])
+        self._check(self.L.cablegpu_set_blocks(self.h, b))
+
+    def config(self):
+        """(tile order, [block size of the five step kernels])"""
+        o = C.c_int()
+        b = (C.c_int * 5)()
+        self._check(self.L.cablegpu_get_config(self.h, C.byref(o), b))
+        return int(o.value), list(b)
+
     def launch_count(self) -> int:
         return int(self.L.cablegpu_launch_count(self.h))
+
+
+def autotune(ts, device: int = 0, sample_tiles: int = 262144, nsteps: int = 8):
+    """(best tile order, [block sizes], sample ms/step) for a TileSet."""
+    g = object.__new__(CableGPU)
+    g.L = load()
+    g.mp = int(ts.mp)
+    g._keep = dict(
+        iveg=np.ascontiguousarray(ts.iveg, np.int32), isoilm=np.ascontiguousarray(ts.isoilm, np.int32),
+        vlai=np.ascontiguousarray(ts.vlai, np.float32), lat=np.ascontiguousarray(ts.lat, np.float32),
+        lonphase=np.ascontiguousarray(ts.lonphase, np.float32), tbase=np.ascontiguousarray(ts.tbase, np.float32),
+        swscale=np.ascontiguousarray(ts.swscale, np.float32))
+    t = g._tiles_struct(0)
+    o, ms = C.c_int(), C.c_float()
+    b = (C.c_int * 5)()
+    rc = g.L.cablegpu_autotune(C.byref(t), device, int(sample_tiles), int(nsteps), C.byref(o), b, C.byref(ms))
+    if rc != 0:
+        raise CableGPUError(rc, "autotune failed")
+    return int(o.value), list(b), float(ms.value)
 
 
 def from_tileset(ts, device: int = 0, seed=None, order: int = 0) -> CableGPU:

@@ -70,9 +70,12 @@ typedef struct {
   const float* lonphase; /* [mp] local-time offset of the synthetic forcing, hours in [0, 24) */
   const float* tbase;    /* [mp] base air temperature of the synthetic forcing, K */
   const float* swscale;  /* [mp] shortwave scale factor of the synthetic forcing */
-  int order;             /* device tile order: 0 = grouped by plant type (default; warps then
-                            follow coherent code paths), 1 = as given.  Field I/O is always in
-                            the caller's order and results do not depend on this choice. */
+  int order;             /* device tile order: 0 = grouped by plant and soil type (default; warps
+                            then follow coherent code paths), 1 = as given, 2 = grouped by plant
+                            type, local solar hour, latitude band and LAI (warps then share
+                            iteration counts), -1 = chosen by cablegpu_autotune_order on a sample
+                            of these tiles.  Field I/O is always in the caller's order and
+                            results do not depend on this choice. */
 } cablegpu_tiles;
 
 /* Creates a context on CUDA device `device` for tiles->mp tiles and uploads
@@ -158,6 +161,22 @@ int cablegpu_phase_timed(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, f
  * one single-thread kernel per step that advances the step counter when the
  * steps run as a replayed CUDA graph (cablegpu_run). */
 long long cablegpu_launch_count(cablegpu_ctx* ctx);
+
+/* Launch configuration.  set_blocks: threads per block of the five step
+ * kernels (radiation, canopy, snow pack, soil heat, soil water), each a
+ * multiple of 32 in [32, 256]; results do not depend on them.  get_config:
+ * the tile order the context was built with and the current block sizes. */
+int cablegpu_set_blocks(cablegpu_ctx* ctx, const int* block5);
+int cablegpu_get_config(cablegpu_ctx* ctx, int* order, int* block5);
+/* Autotuner: times tile orders 0, 1, 2 and block sizes 64, 128, 256 of each
+ * step kernel on an evenly strided sample of `sample_tiles` of the tiles
+ * (synthetic forcing, nsteps timed steps per candidate) and returns the
+ * fastest order, the fastest block size of each kernel and the step time
+ * (ms) they give on the sample.  cablegpu_create with tiles->order == -1
+ * runs it on up to 4,194,304 of the tiles and builds the context with its
+ * choice. */
+int cablegpu_autotune(const cablegpu_tiles* tiles, int device, int sample_tiles, int nsteps, int* order_out,
+                      int* block5_out, float* ms_out);
 
 /* Copies a built-in parameter table (no context or GPU needed): table 0 is
  * the per-plant-type table of pft_params.nml with derived entries "dleaf"

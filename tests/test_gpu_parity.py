@@ -184,3 +184,32 @@ def test_medlyn_switch_matches_oracle(runtime):
     rep = H.parity_report(gs, gd, os_, od)
     for k in ("fe_d", "fh_d", "tv_d", "tgg", "wb"):
         assert rep[k]["frac_within"] > 0.995, (k, rep[k])
+
+
+def test_autotuned_order_and_block_sizes_leave_results_unchanged(runtime):
+    """Tile order and block sizes (chosen by the autotuner, or set by hand)
+    change only the speed: every field is bitwise the same."""
+    R = runtime
+    ts = W.snow_grid(20000, nsteps=6)
+    fields = ("wb", "wbice", "tgg", "tggsn", "out", "snowd", "cplant", "rtsoil")
+    runs = []
+    for order, blocks in ((0, None), (-1, None), (2, [64, 256, 32, 96, 128]), (1, [256, 64, 128, 32, 256])):
+        g = R.from_tileset(ts, order=order)
+        o, b = g.config()
+        assert o in (0, 1, 2) and all(x % 32 == 0 and 32 <= x <= 256 for x in b)
+        if blocks:
+            g.set_blocks(blocks)
+            assert g.config()[1] == blocks
+        g.run(1, 6)
+        g.synchronize()
+        runs.append({k: g.get(k) for k in fields})
+        g.close()
+    for r in runs[1:]:
+        for k in fields:
+            assert np.array_equal(runs[0][k], r[k]), k
+    with pytest.raises(R.CableGPUError):
+        g = R.from_tileset(ts)
+        try:
+            g.set_blocks([100, 128, 128, 128, 128])
+        finally:
+            g.close()
