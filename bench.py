@@ -50,7 +50,7 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="snow_grid", choices=["snow_grid", "grid"])
     p.add_argument("--mp", type=int, default=4_000_000)
-    p.add_argument("--e2e-steps", type=int, default=8)
+    p.add_argument("--e2e-steps", type=int, default=64)
     p.add_argument("--cpu-sample-tiles", type=int, default=100_000)
     p.add_argument("--cpu-sample-steps", type=int, default=48)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -353,36 +353,43 @@ def run_gb300(args):
             "scope": "one timestep (its 5 kernels, CUDA events around each step), %d algorithmic B per tile-step"
                      % ALGO_BYTES_PER_TILE_STEP,
             "kernels_ms": {k: round(v, 4) for k, v in phase_ms.items()}}
-    # --- end to end through the C ABI with host buffers
+    # --- end to end through the C ABI with host buffers.  Host arrays are in
+    # the caller's tile order, so this context uses tile order 3 (the
+    # climate-coherent order within 2^18-tile chunks of the caller's order),
+    # which keeps the reordering of each step's forcing and outputs L2-local.
     e2e = None
     try:
         import torch
+        g.close()
+        g = R.from_tileset(ts, device=d.local, order=3)
+        g.set_blocks(blocks)
         g.set_options(capture_forcing=True)
-        g.step(ktau, dels); ktau += 1
+        g.step(1, dels)
         f0 = g.get("forcing")
-        g.step(ktau, dels); ktau += 1
+        g.step(2, dels)
         f1 = g.get("forcing")
         g.set_options(capture_forcing=False)
+        ktau = 3
         pin = torch.cuda.is_available()
         host_f = [torch.from_numpy(f).pin_memory() if pin else torch.from_numpy(f) for f in (f0, f1)]
-        host_f = [h.numpy() for h in host_f]
-        out_t = torch.empty((8, args.mp), dtype=torch.float32, pin_memory=pin).numpy()
-        # warm the host path once
-        g.set_forcing(host_f[0]); g.step(ktau, dels); ktau += 1
-        g.L.cablegpu_get_field(g.h, g.fields["out"][0], out_t.ctypes.data_as(__import__("ctypes").c_void_p))
+        host_f = [np.ascontiguousarray(h.numpy()) for h in host_f]
+        outs = [torch.empty((8, args.mp), dtype=torch.float32, pin_memory=pin).numpy() for _ in range(2)]
+        # warm the pipelined host path (staging buffers, copy streams)
+        for n in range(2):
+            g.step_host(ktau, host_f[n], outs[n], dels); ktau += 1
+        g.synchronize()
         d.barrier()
         t0 = time.perf_counter()
         for n in range(args.e2e_steps):
-            g.set_forcing(host_f[n % 2])
-            g.step(ktau, dels); ktau += 1
-            rc = g.L.cablegpu_get_field(g.h, g.fields["out"][0], out_t.ctypes.data_as(__import__("ctypes").c_void_p))
-            if rc:
-                raise RuntimeError(g.L.cablegpu_last_error(g.h))
+            # every step uploads its forcing from pinned host memory and
+            # downloads its 8 output fluxes; copies overlap neighbouring steps
+            g.step_host(ktau, host_f[n % 2], outs[n % 2], dels); ktau += 1
         g.synchronize()
         secs = d.max(time.perf_counter() - t0)
         e2e = {"value": d.world * args.mp * args.e2e_steps / secs, "unit": "tile-timesteps/s",
-               "h2d_bytes_per_step": int(f0.nbytes), "d2h_bytes_per_step": int(out_t.nbytes),
-               "steps": args.e2e_steps}
+               "h2d_bytes_per_step": int(f0.nbytes), "d2h_bytes_per_step": int(outs[0].nbytes),
+               "steps": args.e2e_steps, "tile_order": 3,
+               "path": "cablegpu_step_host: pinned host buffers, one copy stream per direction"}
     except Exception as exc:  # the line still prints; the failure is stated
         e2e = {"value": None, "unit": "tile-timesteps/s", "error": str(exc)[:200]}
     g.close()

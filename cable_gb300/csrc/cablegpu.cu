@@ -197,6 +197,16 @@ struct cablegpu_ctx {
   int block[5] = {128, 128, 128, 128, 128};
   int graph_block[5] = {0, 0, 0, 0, 0};
   int order = 0;
+  // pipelined host I/O (cablegpu_step_host): one copy stream per direction
+  // (an upload must not queue behind the previous step's download) and two
+  // slots of device staging for the forcing in and the outputs out
+  cudaStream_t cstream = nullptr, dstream = nullptr;
+  float* d_fin[2] = {nullptr, nullptr};    // [CG_NFORC][mp] caller order
+  float* d_fout[2] = {nullptr, nullptr};   // [CG_NOUT][mp] caller order
+  cudaEvent_t ev_h2d[2] = {}, ev_used[2] = {}, ev_step[2] = {}, ev_d2h[2] = {};
+  bool io_ready = false;
+  const float* io_forcing = nullptr;          // staging slot the current step_host step reads
+  long long io_count = 0;
   std::string err;
 };
 
@@ -231,6 +241,11 @@ void bind_device_view(cablegpu_ctx* c) {
   D.out = (float*)P("out");
   D.diag = c->diag ? (float*)P(kDiagNames[0]) : nullptr;
   D.forcing_in = c->host_forcing ? (const float*)P("forcing_in") : nullptr;
+  D.forcing_caller_order = 0;
+  if (c->io_forcing) {
+    D.forcing_in = c->io_forcing;
+    D.forcing_caller_order = 1;
+  }
   D.forcing_out = c->capture_forcing ? (float*)P("forcing") : nullptr;
   D.work_a = (float*)P("work_a");
   D.work_b = (float*)P("work_b");
@@ -343,7 +358,7 @@ int cablegpu_field_id(const char* name) {
 
 int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out) {
   if (!tiles || !out || tiles->mp <= 0 || !tiles->iveg || !tiles->isoilm || !tiles->vlai || !tiles->lat ||
-      tiles->order < -1 || tiles->order > 2)
+      tiles->order < -1 || tiles->order > 3)
     return CABLEGPU_ERR_ARG;
   for (int i = 0; i < tiles->mp; ++i)
     if (tiles->iveg[i] < 1 || tiles->iveg[i] > CG_NPFT || tiles->isoilm[i] < 1 || tiles->isoilm[i] > CG_NSOIL)
@@ -391,13 +406,17 @@ int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out)
   {
     std::vector<int> order(c->mp);
     for (int i = 0; i < c->mp; ++i) order[i] = i;
-    if (tiles->order == 0 || tiles->order == 2) {
+    if (tiles->order == 0 || tiles->order == 2 || tiles->order == 3) {
       // sort key, most significant first: plant type, soil type (order 0);
       // plant type, local solar hour, 5-degree latitude band, LAI (order 2),
-      // so a warp's tiles share radiation and hence iteration counts
+      // so a warp's tiles share radiation and hence iteration counts; order 3
+      // is order 2 applied within consecutive chunks of 2^18 caller tiles,
+      // so host-order forcing and outputs of a chunk stay L2-resident while
+      // they are gathered into device order (cablegpu_step_host)
       std::vector<std::pair<unsigned long long, int>> key(c->mp);
       for (int i = 0; i < c->mp; ++i) {
         unsigned long long k = (unsigned long long)(tiles->iveg[i] & 0xff) << 56;
+        if (tiles->order == 3) k = (unsigned long long)(i >> 18) << 51 | (unsigned long long)(tiles->iveg[i] & 0xff) << 43;
         if (tiles->order == 0) {
           k |= (unsigned long long)(tiles->isoilm[i] & 0xff) << 48;
         } else {
@@ -405,7 +424,10 @@ int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out)
           const int hr = std::min(23, std::max(0, (int)ph));
           const int band = std::min(63, std::max(0, (int)((tiles->lat[i] + 90.f) / 5.f)));
           const int lai = std::min(255, std::max(0, (int)(tiles->vlai[i] * 32.f)));
-          k |= (unsigned long long)hr << 48 | (unsigned long long)band << 40 | (unsigned long long)lai << 32;
+          if (tiles->order == 2)
+            k |= (unsigned long long)hr << 48 | (unsigned long long)band << 40 | (unsigned long long)lai << 32;
+          else
+            k |= (unsigned long long)hr << 38 | (unsigned long long)band << 32 | (unsigned long long)lai << 24;
         }
         key[i] = {k, i};
       }
@@ -453,6 +475,18 @@ int cablegpu_destroy(cablegpu_ctx* c) {
   if (c->d_harvest) cudaFree(c->d_harvest);
   if (c->d_harvest_n) cudaFree(c->d_harvest_n);
   if (c->d_sur_stats) cudaFree(c->d_sur_stats);
+  if (c->io_ready) {
+    cudaStreamSynchronize(c->cstream);
+    cudaStreamSynchronize(c->dstream);
+    for (int i = 0; i < 2; ++i) {
+      cudaFree(c->d_fin[i]);
+      cudaFree(c->d_fout[i]);
+      cudaEventDestroy(c->ev_h2d[i]); cudaEventDestroy(c->ev_used[i]);
+      cudaEventDestroy(c->ev_step[i]); cudaEventDestroy(c->ev_d2h[i]);
+    }
+    cudaStreamDestroy(c->cstream);
+    cudaStreamDestroy(c->dstream);
+  }
   if (c->d_sur_dt) cudaFree(c->d_sur_dt);
   sur_free(c->net);
   cudaFreeHost(c->h_clock);
@@ -584,8 +618,57 @@ int cablegpu_run(cablegpu_ctx* c, int ktau0, int nsteps, float dels) {
   return CABLEGPU_OK;
 }
 
+int cablegpu_step_host(cablegpu_ctx* c, int ktau, float dels, const float* host_forcing, float* host_out) {
+  if (!c || ktau < 1 || !(dels > 0.f) || !host_forcing || !host_out)
+    return fail(c, CABLEGPU_ERR_ARG, "step_host: bad argument");
+  if (!c->io_ready) {
+    CG_CUDA(c, cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking));
+    CG_CUDA(c, cudaStreamCreateWithFlags(&c->dstream, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+      CG_CUDA(c, cudaMalloc(&c->d_fin[i], sizeof(float) * CG_NFORC * c->mp));
+      CG_CUDA(c, cudaMalloc(&c->d_fout[i], sizeof(float) * CG_NOUT * c->mp));
+      for (cudaEvent_t* e : {&c->ev_h2d[i], &c->ev_used[i], &c->ev_step[i], &c->ev_d2h[i]})
+        CG_CUDA(c, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+      // slot free from the start
+      CG_CUDA(c, cudaEventRecord(c->ev_used[i], c->stream));
+      CG_CUDA(c, cudaEventRecord(c->ev_d2h[i], c->dstream));
+    }
+    c->io_ready = true;
+  }
+  const int slot = (int)(c->io_count & 1);
+  const size_t fb = sizeof(float) * CG_NFORC * c->mp, ob = sizeof(float) * CG_NOUT * c->mp;
+  const int grid = (c->mp + 255) / 256;
+  // upload this step's forcing once the step two back has consumed the slot
+  CG_CUDA(c, cudaStreamWaitEvent(c->cstream, c->ev_used[slot], 0));
+  CG_CUDA(c, cudaMemcpyAsync(c->d_fin[slot], host_forcing, fb, cudaMemcpyHostToDevice, c->cstream));
+  CG_CUDA(c, cudaEventRecord(c->ev_h2d[slot], c->cstream));
+  // the step (the radiation kernel reads the forcing from the staging slot
+  // in caller order), then the outputs back into caller order once the
+  // slot's previous download is done
+  CG_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_h2d[slot], 0));
+  c->io_forcing = c->d_fin[slot];
+  int rc = launch_step(c, make_params(c, ktau, dels), nullptr);
+  c->io_forcing = nullptr;
+  if (rc) return rc;
+  CG_CUDA(c, cudaEventRecord(c->ev_used[slot], c->stream));
+  CG_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_d2h[slot], 0));
+  gather_out_kernel<float, float><<<grid, 256, 0, c->stream>>>(c->d_fout[slot], (const float*)c->field_ptr[cablegpu_field_id("out")],
+                                                               c->d_order, c->mp, c->ld, CG_NOUT);
+  CG_CUDA(c, cudaGetLastError());
+  CG_CUDA(c, cudaEventRecord(c->ev_step[slot], c->stream));
+  CG_CUDA(c, cudaStreamWaitEvent(c->dstream, c->ev_step[slot], 0));
+  CG_CUDA(c, cudaMemcpyAsync(host_out, c->d_fout[slot], ob, cudaMemcpyDeviceToHost, c->dstream));
+  CG_CUDA(c, cudaEventRecord(c->ev_d2h[slot], c->dstream));
+  ++c->io_count;
+  return CABLEGPU_OK;
+}
+
 int cablegpu_synchronize(cablegpu_ctx* c) {
   if (!c) return CABLEGPU_ERR_ARG;
+  if (c->io_ready) {
+    CG_CUDA(c, cudaStreamSynchronize(c->cstream));
+    CG_CUDA(c, cudaStreamSynchronize(c->dstream));
+  }
   CG_CUDA(c, cudaMemcpyAsync(c->h_status, c->dev.status, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
   CG_CUDA(c, cudaStreamSynchronize(c->stream));
   if (*c->h_status) {
@@ -823,7 +906,7 @@ int cablegpu_autotune(const cablegpu_tiles* tiles, int device, int sample_tiles,
   std::vector<double> sn(n, 0.0), tg(n, 285.0), wb(n, 0.25);
   const int cand_block[3] = {64, 128, 256};
   float best = 1e30f;
-  for (int order = 0; order <= 2; ++order) {
+  for (int order = 0; order <= 3; ++order) {
     cablegpu_tiles t = {n, iveg.data(), isoil.data(), vlai.data(), lat.data(), ph.data(), tb.data(), sw.data(), order};
     cablegpu_ctx* c = nullptr;
     int rc = cablegpu_create(&t, device, &c);

@@ -89,6 +89,7 @@ struct CgDev {
   float* work_b;           // phase B -> C handoff record
   float* work_c;           // phase C1 -> C2 -> C3 handoff record
   const float* forcing_in; // [CG_NFORC] host-provided forcing, or null (synthetic)
+  int forcing_caller_order; // 1: forcing_in is [CG_NFORC][mp] in the caller's tile order
   float* forcing_out;      // [CG_NFORC] copy of the forcing used, or null
   unsigned int* status;    // bit0: non-finite output seen, bit1: surrogate network failed
   // dryLeaf training-row harvest (null when off): rows of 12 features and 3

@@ -80,8 +80,12 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
   // ---------------------------------------------------------------- forcing
   float F[CG_NFORC];
   if (D.forcing_in) {
+    // device tile order, or the caller's order straight from the host-I/O
+    // staging buffer (one gather instead of a reordering pass)
+    const size_t base = D.forcing_caller_order ? (size_t)D.tile_id[t] : (size_t)t;
+    const size_t stride = D.forcing_caller_order ? (size_t)D.mp : (size_t)ld;
 #pragma unroll
-    for (int i = 0; i < CG_NFORC; ++i) F[i] = D.forcing_in[i * ld + t];
+    for (int i = 0; i < CG_NFORC; ++i) F[i] = D.forcing_in[i * stride + base];
   } else {
     cg_forcing(P.forc, D.lat[t], D.lonphase[t], D.tbase[t], D.swscale[t], (uint32_t)D.tile_id[t],
                (uint32_t)P.step_index, F);

@@ -37,7 +37,7 @@ EXPORTS = [
     "cablegpu_cold_start_noalloc", "cablegpu_harvest", "cablegpu_harvest_rows", "cablegpu_surrogate_train",
     "cablegpu_surrogate_weights", "cablegpu_set_surrogate", "cablegpu_surrogate_stats", "cablegpu_mlp_sizes",
     "cablegpu_mlp_forward", "cablegpu_mlp_grad", "cablegpu_mlp_fit", "cablegpu_mlp_last_error",
-    "cablegpu_set_blocks", "cablegpu_get_config", "cablegpu_autotune",
+    "cablegpu_set_blocks", "cablegpu_get_config", "cablegpu_autotune", "cablegpu_step_host",
 ]
 NOALLOC_MAX_TILES = 65536
 PHASES = ["radiation", "canopy", "snow_pack", "soil_heat", "soil_water", "surrogate_net"]
@@ -106,6 +106,7 @@ def load(build_if_missing: bool = True):
     L.cablegpu_run_timed.argtypes = [vp, ip, ip, C.c_float, C.POINTER(C.c_float)]
     L.cablegpu_kernel_timed.argtypes = [vp, ip, ip, C.c_float, C.POINTER(C.c_float)]
     L.cablegpu_phase_timed.argtypes = [vp, ip, ip, C.c_float, C.POINTER(C.c_float)]
+    L.cablegpu_step_host.argtypes = [vp, ip, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.cablegpu_set_blocks.argtypes = [vp, C.POINTER(ip)]
     L.cablegpu_get_config.argtypes = [vp, C.POINTER(ip), C.POINTER(ip)]
     L.cablegpu_autotune.argtypes = [C.POINTER(_Tiles), ip, ip, ip, C.POINTER(ip), C.POINTER(ip), C.POINTER(C.c_float)]
@@ -301,6 +302,14 @@ class CableGPU:
 
     def run(self, ktau0: int, nsteps: int, dels: float = 1800.0):
         self._check(self.L.cablegpu_run(self.h, int(ktau0), int(nsteps), float(dels)))
+
+    def step_host(self, ktau, forcing, out, dels: float = 1800.0):
+        """Pipelined step with host I/O: forcing [13][mp] float32 in, out
+        [8][mp] float32 filled asynchronously (valid after synchronize())."""
+        assert forcing.dtype == np.float32 and forcing.flags["C_CONTIGUOUS"] and forcing.shape == (NFORCING, self.mp)
+        assert out.dtype == np.float32 and out.flags["C_CONTIGUOUS"] and out.shape == (8, self.mp)
+        self._check(self.L.cablegpu_step_host(self.h, int(ktau), float(dels), _ptr(forcing, C.c_float),
+                                              _ptr(out, C.c_float)))
 
     def synchronize(self):
         self._check(self.L.cablegpu_synchronize(self.h))

@@ -73,8 +73,9 @@ typedef struct {
   int order;             /* device tile order: 0 = grouped by plant and soil type (default; warps
                             then follow coherent code paths), 1 = as given, 2 = grouped by plant
                             type, local solar hour, latitude band and LAI (warps then share
-                            iteration counts), -1 = chosen by cablegpu_autotune_order on a sample
-                            of these tiles.  Field I/O is always in the caller's order and
+                            iteration counts), 3 = order 2 within consecutive chunks of 2^18
+                            tiles (keeps host-order I/O of cablegpu_step_host L2-local), -1 =
+                            chosen by the autotuner (cablegpu_autotune) on these tiles.  Field I/O is always in the caller's order and
                             results do not depend on this choice. */
 } cablegpu_tiles;
 
@@ -141,6 +142,16 @@ int cablegpu_step(cablegpu_ctx* ctx, int ktau, float dels);
 /* nsteps timesteps ktau0 .. ktau0+nsteps-1, replayed from a captured CUDA
  * graph.  Asynchronous. */
 int cablegpu_run(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels);
+/* One timestep with host-memory I/O, pipelined: uploads host_forcing
+ * ([CABLEGPU_NFORCING][mp] float, as for cablegpu_set_forcing) on a copy
+ * stream, runs the step, and downloads the 8 output fluxes (field "out",
+ * [8][mp] float) into host_out.  Asynchronous: copies of one step overlap the
+ * kernels of its neighbours (two staging slots), so host_forcing must stay
+ * unchanged and host_out unread until cablegpu_synchronize; pinned host
+ * memory makes the copies asynchronous.  The forcing applies to this step
+ * only.  Replaces the per-step get_met_data -> cbm -> write_output sequence
+ * of the offline driver (cable_serial.F90:594-640). */
+int cablegpu_step_host(cablegpu_ctx* ctx, int ktau, float dels, const float* host_forcing, float* host_out);
 /* Waits for all queued work; returns CABLEGPU_ERR_NONFINITE if any step
  * since the last call produced a non-finite output flux. */
 int cablegpu_synchronize(cablegpu_ctx* ctx);
@@ -168,7 +179,7 @@ long long cablegpu_launch_count(cablegpu_ctx* ctx);
  * the tile order the context was built with and the current block sizes. */
 int cablegpu_set_blocks(cablegpu_ctx* ctx, const int* block5);
 int cablegpu_get_config(cablegpu_ctx* ctx, int* order, int* block5);
-/* Autotuner: times tile orders 0, 1, 2 and block sizes 64, 128, 256 of each
+/* Autotuner: times tile orders 0-3 and block sizes 64, 128, 256 of each
  * step kernel on an evenly strided sample of `sample_tiles` of the tiles
  * (synthetic forcing, nsteps timed steps per candidate) and returns the
  * fastest order, the fastest block size of each kernel and the step time

@@ -193,10 +193,10 @@ def test_autotuned_order_and_block_sizes_leave_results_unchanged(runtime):
     ts = W.snow_grid(20000, nsteps=6)
     fields = ("wb", "wbice", "tgg", "tggsn", "out", "snowd", "cplant", "rtsoil")
     runs = []
-    for order, blocks in ((0, None), (-1, None), (2, [64, 256, 32, 96, 128]), (1, [256, 64, 128, 32, 256])):
+    for order, blocks in ((0, None), (-1, None), (2, [64, 256, 32, 96, 128]), (1, [256, 64, 128, 32, 256]), (3, None)):
         g = R.from_tileset(ts, order=order)
         o, b = g.config()
-        assert o in (0, 1, 2) and all(x % 32 == 0 and 32 <= x <= 256 for x in b)
+        assert o in (0, 1, 2, 3) and all(x % 32 == 0 and 32 <= x <= 256 for x in b)
         if blocks:
             g.set_blocks(blocks)
             assert g.config()[1] == blocks
@@ -213,3 +213,34 @@ def test_autotuned_order_and_block_sizes_leave_results_unchanged(runtime):
             g.set_blocks([100, 128, 128, 128, 128])
         finally:
             g.close()
+
+
+def test_pipelined_host_io_step_equals_set_forcing_step_get(runtime):
+    """cablegpu_step_host (copies overlapped with neighbouring steps) gives
+    bitwise the outputs and state of set_forcing + step + get_field."""
+    R = runtime
+    ts = W.snow_grid(30000, nsteps=5)
+    g = R.from_tileset(ts)
+    g.set_options(capture_forcing=True)
+    F = []
+    for n in range(5):
+        g.step(1 + n)
+        F.append(g.get("forcing"))
+    g.close()
+    a = R.from_tileset(ts)
+    outs_a = []
+    for n in range(5):
+        a.set_forcing(F[n])
+        a.step(1 + n)
+        outs_a.append(a.get("out"))
+    b = R.from_tileset(ts, order=2)
+    outs_b = [np.empty((8, ts.mp), np.float32) for _ in range(5)]
+    for n in range(5):
+        b.step_host(1 + n, np.ascontiguousarray(F[n]), outs_b[n])
+    b.synchronize()
+    for n in range(5):
+        assert np.array_equal(outs_a[n], outs_b[n]), n
+    for k in ("wb", "tgg", "snowd", "cansto"):
+        assert np.array_equal(a.get(k), b.get(k)), k
+    a.close()
+    b.close()
