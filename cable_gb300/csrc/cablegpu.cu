@@ -21,7 +21,7 @@ constexpr int kGraphSteps = 8;      // steps per captured CUDA graph
 constexpr int kKernelsPerStep = 5;  // radiation, canopy, snow pack, soil heat, soil water
 
 // ---------------------------------------------------------------- field registry
-enum Storage { S_U8, S_F32, S_F64 };
+enum Storage { S_U8, S_F32, S_F64, S_DF };   // S_DF: double-FP32 pairs (hi rows, then lo rows)
 struct FieldDef {
   const char* name;
   int nlayer;
@@ -47,8 +47,8 @@ std::vector<FieldDef> make_registry() {
     {"lonphase", 1, CABLEGPU_F32, CABLEGPU_KIND_PARAM, S_F32},
     {"tbase", 1, CABLEGPU_F32, CABLEGPU_KIND_PARAM, S_F32},
     {"swscale", 1, CABLEGPU_F32, CABLEGPU_KIND_PARAM, S_F32},
-    {"wb", CG_MS, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
-    {"wbice", CG_MS, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
+    {"wb", CG_MS, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_DF},
+    {"wbice", CG_MS, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_DF},
     {"gammzz1", 1, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
     {"tgg", CG_MS, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
     {"tggsn", 3, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
@@ -88,7 +88,7 @@ const std::vector<FieldDef>& registry() {
   return r;
 }
 
-size_t storage_bytes(Storage s) { return s == S_U8 ? 1 : (s == S_F32 ? 4 : 8); }
+size_t storage_bytes(Storage s) { return s == S_U8 ? 1 : (s == S_F32 ? 4 : 8); }   // S_DF: 2 x 4 bytes
 
 // ---------------------------------------------------------------- kernels
 __global__ void advance_clock_kernel(int* clock) { clock[0] += 1; }
@@ -103,10 +103,11 @@ __global__ void cold_start_kernel(CgDev D, const CgTables* __restrict__ T, const
   const float swilt = T->soil.swilt[s], sfc = T->soil.sfc[s];
   const int o = D.tile_id[t];
   const float wbf = (float)wb0[o], tg = (float)tgg0[o], sn = (float)snowd0[o];
+  const df32 ice0 = (tg < 273.15f) ? df_from_double((double)wbf * (double)0.8f) : df32{0.f, 0.f};
   for (int k = 0; k < CG_MS; ++k) {
-    D.wb[k * ld + t] = (double)wbf;
+    df_store(D.wb, CG_MS, ld, k, t, df32{wbf, 0.f});
     D.tgg[k * ld + t] = tg;
-    D.wbice[k * ld + t] = (tg < 273.15f) ? (double)wbf * (double)0.8f : 0.0;
+    df_store(D.wbice, CG_MS, ld, k, t, ice0);
   }
   const bool snow = sn > 0.0f;
   for (int k = 0; k < 3; ++k) {
@@ -123,7 +124,7 @@ __global__ void cold_start_kernel(CgDev D, const CgTables* __restrict__ T, const
   D.pudsto[t] = 0.f; D.rtsoil[t] = 100.0f; D.tss[t] = tg; D.wb_lake[t] = 0.f; D.wbtot1[t] = 0.f; D.wbtot2[t] = 0.f;
   D.cansto[t] = 0.f;
   float ow = fmaxf(0.0f, fminf(1.0f, (wbf - swilt) / (sfc - swilt)));
-  double wbice1 = D.wbice[t];
+  const double wbice1 = df_to_double(ice0);
   if (wbice1 > 0.) { float r = (float)(wbice1 / (double)wbf); ow = ow * (1.0f - r) * (1.0f - r); }
   D.owetfac[t] = ow;
   for (int k = 0; k < 3; ++k) D.cplant[k * ld + t] = T->pft.cplant0[k][v];
@@ -146,6 +147,19 @@ __global__ void gather_out_kernel(TD* stage, const TS* src, const int* order, in
   if (s >= mp) return;
   const int o = order[s];
   for (int k = 0; k < nlayer; ++k) stage[(size_t)k * mp + o] = (TD)src[(size_t)k * ld + s];
+}
+// double-FP32 fields: host FP64 <-> device (hi, lo) rows
+__global__ void scatter_in_df_kernel(float* dst, const double* stage, const int* order, int mp, int ld, int nlayer) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= mp) return;
+  const int o = order[s];
+  for (int k = 0; k < nlayer; ++k) df_store(dst, nlayer, ld, k, s, df_from_double(stage[(size_t)k * mp + o]));
+}
+__global__ void gather_out_df_kernel(double* stage, const float* src, const int* order, int mp, int ld, int nlayer) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= mp) return;
+  const int o = order[s];
+  for (int k = 0; k < nlayer; ++k) stage[(size_t)k * mp + o] = df_to_double(df_load(src, nlayer, ld, k, s));
 }
 
 }  // namespace
@@ -230,7 +244,7 @@ void bind_device_view(cablegpu_ctx* c) {
   D.iveg = (const uint8_t*)P("iveg"); D.isoilm = (const uint8_t*)P("isoilm");
   D.vlai = (const float*)P("vlai"); D.lat = (const float*)P("lat"); D.lonphase = (const float*)P("lonphase");
   D.tbase = (const float*)P("tbase"); D.swscale = (const float*)P("swscale");
-  D.wb = (double*)P("wb"); D.wbice = (double*)P("wbice"); D.gammzz1 = (double*)P("gammzz1");
+  D.wb = (float*)P("wb"); D.wbice = (float*)P("wbice"); D.gammzz1 = (double*)P("gammzz1");
   D.tgg = (float*)P("tgg"); D.tggsn = (float*)P("tggsn"); D.ssdn = (float*)P("ssdn"); D.smass = (float*)P("smass");
   D.sdepth = (float*)P("sdepth"); D.flags = (uint8_t*)P("flags"); D.snowd = (float*)P("snowd");
   D.ssdnn = (float*)P("ssdnn"); D.snage = (float*)P("snage"); D.pudsto = (float*)P("pudsto");
@@ -515,6 +529,8 @@ int cablegpu_set_field(cablegpu_ctx* c, int id, const void* host) {
     scatter_in_kernel<uint8_t, int><<<grid, 256, 0, c->stream>>>((uint8_t*)d, (const int*)c->d_stage, c->d_order, c->mp, c->ld, f.nlayer);
   else if (f.st == S_F32)
     scatter_in_kernel<float, float><<<grid, 256, 0, c->stream>>>((float*)d, (const float*)c->d_stage, c->d_order, c->mp, c->ld, f.nlayer);
+  else if (f.st == S_DF)
+    scatter_in_df_kernel<<<grid, 256, 0, c->stream>>>((float*)d, (const double*)c->d_stage, c->d_order, c->mp, c->ld, f.nlayer);
   else
     scatter_in_kernel<double, double><<<grid, 256, 0, c->stream>>>((double*)d, (const double*)c->d_stage, c->d_order, c->mp, c->ld, f.nlayer);
   CG_CUDA(c, cudaGetLastError());
@@ -536,6 +552,8 @@ int cablegpu_get_field(cablegpu_ctx* c, int id, void* host) {
     gather_out_kernel<int, uint8_t><<<grid, 256, 0, c->stream>>>((int*)c->d_stage, (const uint8_t*)d, c->d_order, c->mp, c->ld, f.nlayer);
   else if (f.st == S_F32)
     gather_out_kernel<float, float><<<grid, 256, 0, c->stream>>>((float*)c->d_stage, (const float*)d, c->d_order, c->mp, c->ld, f.nlayer);
+  else if (f.st == S_DF)
+    gather_out_df_kernel<<<grid, 256, 0, c->stream>>>((double*)c->d_stage, (const float*)d, c->d_order, c->mp, c->ld, f.nlayer);
   else
     gather_out_kernel<double, double><<<grid, 256, 0, c->stream>>>((double*)c->d_stage, (const double*)d, c->d_order, c->mp, c->ld, f.nlayer);
   CG_CUDA(c, cudaGetLastError());

@@ -57,8 +57,8 @@ struct CgDev {
   const float* tbase;
   const float* swscale;
   // prognostic state
-  double* wb;        // [6]
-  double* wbice;     // [6]
+  float* wb;         // [6] as double-FP32 pairs: hi layers 0..5, lo layers 6..11
+  float* wbice;      // [6] likewise
   double* gammzz1;   // layer-1 heat capacity (J/m2/K)
   float* tgg;        // [6]
   float* tggsn;      // [3]
@@ -113,6 +113,56 @@ struct CgTables {
 };
 
 __device__ __forceinline__ float sqf(float x) { return x * x; }
+
+// ---------------------------------------------------------------- double-FP32 state
+// Soil water and ice (REAL(r_2) in the reference) are carried as unevaluated
+// sums hi + lo of two FP32 numbers with |lo| <= ulp(hi) / 2: a 48-bit
+// significand (relative precision ~4e-15), updated with error-free FP32
+// transformations (Knuth's two-sum, Dekker's fast two-sum and FMA-based
+// products), so the soil kernels keep FP64-class state without issuing FP64
+// instructions, which GB300 executes at a small fraction of the FP32 rate.
+// Field layout: [2 * n][ld] floats, hi of layer k at row k, lo at row n + k.
+struct df32 {
+  float hi, lo;
+};
+__device__ __forceinline__ df32 df_load(const float* p, int n, int ld, int k, int t) {
+  return {p[k * ld + t], p[(n + k) * ld + t]};
+}
+__device__ __forceinline__ void df_store(float* p, int n, int ld, int k, int t, df32 v) {
+  p[k * ld + t] = v.hi;
+  p[(n + k) * ld + t] = v.lo;
+}
+__device__ __forceinline__ df32 df_norm(float s, float e) {   // fast two-sum, |s| >= |e|
+  const float hi = s + e;
+  return {hi, e - (hi - s)};
+}
+// a + b for an FP32 b
+__device__ __forceinline__ df32 df_add(df32 a, float b) {
+  const float s = a.hi + b;
+  const float bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (b - bb);
+  return df_norm(s, e + a.lo);
+}
+__device__ __forceinline__ df32 df_add(df32 a, df32 b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (b.hi - bb);
+  return df_norm(s, e + (a.lo + b.lo));
+}
+// a * c for an FP32 c
+__device__ __forceinline__ df32 df_mul(df32 a, float c) {
+  const float p = a.hi * c;
+  const float e = fmaf(a.hi, c, -p);
+  return df_norm(p, fmaf(a.lo, c, e));
+}
+// a - b rounded to FP32
+__device__ __forceinline__ float df_sub(df32 a, df32 b) { return (a.hi - b.hi) + (a.lo - b.lo); }
+__device__ __forceinline__ bool df_lt(df32 a, df32 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ double df_to_double(df32 a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ df32 df_from_double(double d) {
+  const float hi = (float)d;
+  return {hi, (float)(d - (double)hi)};
+}
 __device__ __forceinline__ float pow4(float x) { float y = x * x; return y * y; }
 __device__ __forceinline__ float fsignf(float a, float b) { return signbit(b) ? -fabsf(a) : fabsf(a); }
 

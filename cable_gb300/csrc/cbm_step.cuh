@@ -58,9 +58,9 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
   for (int k = 0; k < CG_MS; ++k) zse[k] = S.zse[k];
 
   // ---------------------------------------------------------------- state
-  double wb[CG_MS], wbice[CG_MS];
+  df32 wb[CG_MS], wbice[CG_MS];
 #pragma unroll
-  for (int k = 0; k < CG_MS; ++k) { wb[k] = D.wb[k * ld + t]; wbice[k] = D.wbice[k * ld + t]; }
+  for (int k = 0; k < CG_MS; ++k) { wb[k] = df_load(D.wb, CG_MS, ld, k, t); wbice[k] = df_load(D.wbice, CG_MS, ld, k, t); }
   float tgg[CG_MS];
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) tgg[k] = D.tgg[k * ld + t];
@@ -102,13 +102,13 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
   // wbliq as left by the previous soil_snow call
   float wbliq0[CG_MS];
 #pragma unroll
-  for (int k = 0; k < CG_MS; ++k) wbliq0[k] = (float)(wb[k] - wbice[k]);
+  for (int k = 0; k < CG_MS; ++k) wbliq0[k] = df_sub(wb[k], wbice[k]);
 
   // lakes top-layer fix (cbl_model_driver_offline.F90:116-121)
-  if (iveg == LAKES && wb[0] < (double)sfc) {
-    wbtot1 = (float)wb[0] * DLIQ * zse[0];
-    wb[0] = sfc;
-    wbtot2 = (float)wb[0] * DLIQ * zse[0];
+  if (iveg == LAKES && df_lt(wb[0], df32{sfc, 0.f})) {
+    wbtot1 = wb[0].hi * DLIQ * zse[0];
+    wb[0] = df32{sfc, 0.f};
+    wbtot2 = wb[0].hi * DLIQ * zse[0];
   }
   wb_lake = wb_lake + fmaxf(wbtot2 - wbtot1, 0.f);
 
@@ -263,11 +263,11 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
     // initialize_wetfac (cbl_init_wetfac_mod.F90:9-116)
     float wilting_pt = swilt / 2.0f;
     float den = fmaxf(0.0830f, sfc - wilting_pt);
-    wetfac = fmaxf(0.0f, fminf(1.0f, ((float)wb[0] - wilting_pt) / den));
-    if (wbice[0] > 0.0) {
+    wetfac = fmaxf(0.0f, fminf(1.0f, (wb[0].hi - wilting_pt) / den));
+    if (wbice[0].hi > 0.0f) {
       // (wbice / wb)^2 in FP32: the quotient of the FP32-rounded values is
       // within a few ulp of the reference's r_2 quotient rounded to REAL
-      const float q = (float)wbice[0] / (float)wb[0];
+      const float q = wbice[0].hi / wb[0].hi;
       float ice_ratio = q * q;
       float ice_factor = fmaxf(0.5f, 1.0f - fminf(0.2f, ice_ratio));
       wetfac = wetfac * ice_factor;
@@ -346,7 +346,7 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
 #pragma unroll
     for (int i = 0; i < CG_NA; ++i) D.work_a[i * ld + t] = rec[i];
   }
-  if (iveg == LAKES) D.wb[t] = wb[0];
+  if (iveg == LAKES) df_store(D.wb, CG_MS, ld, 0, t, wb[0]);
   D.wb_lake[t] = wb_lake; D.wbtot1[t] = wbtot1; D.wbtot2[t] = wbtot2;
   if (kDiag) {
     D.diag[29 * ld + t] = albedo[0]; D.diag[30 * ld + t] = albedo[1]; D.diag[31 * ld + t] = transd;
@@ -405,7 +405,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
   // state read by define_canopy
   const float oldcansto = D.cansto[t], ortsoil = D.rtsoil[t], snowd = D.snowd[t], pudsto = D.pudsto[t];
   const float tgg[1] = {D.tgg[t]};
-  const double wb[1] = {D.wb[t]}, wbice[1] = {D.wbice[t]};
+  const df32 wb[1] = {df_load(D.wb, CG_MS, ld, 0, t)}, wbice[1] = {df_load(D.wbice, CG_MS, ld, 0, t)};
   const float pudsmx = 0.0f;
   // working variables of the canopy iteration (cable_canopy.F90:183-215)
   float tvair = tk, qvair = qv, tv = tk;
@@ -727,10 +727,10 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
         fess = fess * (1.f - pwet);
         float frescale = zse[0] * DLIQ * rlam / dels;
         if (snowd < 0.1f && fess > 0.0f) {
-          float flower = (float)wb[0] - swilt / 2.0f;
+          float flower = wb[0].hi - swilt / 2.0f;
           float fupper = fmaxf(0.f, flower * frescale - evapfbl[0] * rlam / dels);
           fess = fminf(fess, fupper);
-          fupper = fmaxf((float)(wb[0] - wbice[0] / (double)FROZEN_LIMIT) * frescale, 0.f);
+          fupper = fmaxf(((wb[0].hi - wbice[0].hi / FROZEN_LIMIT) + (wb[0].lo - wbice[0].lo / FROZEN_LIMIT)) * frescale, 0.f);
           fess = fminf(fess, fupper);
         }
         cls = 1.f;
@@ -910,14 +910,14 @@ __device__ __forceinline__ void phase_c1(const CgDev& D, const CgTables* __restr
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) zse[k] = S.zse[k];
   // state
-  double wb[CG_MS], wbice[CG_MS];
+  df32 wb[CG_MS], wbice[CG_MS];
 #pragma unroll
-  for (int k = 0; k < CG_MS; ++k) { wb[k] = D.wb[k * ld + t]; wbice[k] = D.wbice[k * ld + t]; }
+  for (int k = 0; k < CG_MS; ++k) { wb[k] = df_load(D.wb, CG_MS, ld, k, t); wbice[k] = df_load(D.wbice, CG_MS, ld, k, t); }
   // FP32 shadows of soil water and ice for thresholds and fluxes; every
-  // change to the FP64 state is mirrored into them
+  // change to the state is mirrored into them
   float wbf[CG_MS], wbicef[CG_MS];
 #pragma unroll
-  for (int k = 0; k < CG_MS; ++k) { wbf[k] = (float)wb[k]; wbicef[k] = (float)wbice[k]; }
+  for (int k = 0; k < CG_MS; ++k) { wbf[k] = wb[k].hi; wbicef[k] = wbice[k].hi; }
   float tgg[CG_MS];
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) tgg[k] = D.tgg[k * ld + t];
@@ -951,8 +951,9 @@ __device__ __forceinline__ void phase_c1(const CgDev& D, const CgTables* __restr
   float dtmlt0 = 0.f;
   const float osnowd = snowd;
   if (first_call) {
-    gammzz1 = fmax((double)((1.0f - ssat) * css * rhosoil) + (wb[0] - wbice[0]) * (double)(CSWAT * DLIQ) +
-                       wbice[0] * (double)(CSICE * DICE), (double)(css * rhosoil)) * (double)zse[0] +
+    const double wb0 = df_to_double(wb[0]), wbice0 = df_to_double(wbice[0]);
+    gammzz1 = fmax((double)((1.0f - ssat) * css * rhosoil) + (wb0 - wbice0) * (double)(CSWAT * DLIQ) +
+                       wbice0 * (double)(CSICE * DICE), (double)(css * rhosoil)) * (double)zse[0] +
               (double)((float)(1 - isflag) * CGSNOW * snowd);
     first_call = false;
   }
@@ -1207,14 +1208,14 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) zse[k] = S.zse[k];
   // state
-  double wb[CG_MS], wbice[CG_MS];
+  df32 wb[CG_MS], wbice[CG_MS];
 #pragma unroll
-  for (int k = 0; k < CG_MS; ++k) { wb[k] = D.wb[k * ld + t]; wbice[k] = D.wbice[k * ld + t]; }
+  for (int k = 0; k < CG_MS; ++k) { wb[k] = df_load(D.wb, CG_MS, ld, k, t); wbice[k] = df_load(D.wbice, CG_MS, ld, k, t); }
   // FP32 shadows of soil water and ice for thresholds and fluxes; every
-  // change to the FP64 state is mirrored into them
+  // change to the state is mirrored into them
   float wbf[CG_MS], wbicef[CG_MS];
 #pragma unroll
-  for (int k = 0; k < CG_MS; ++k) { wbf[k] = (float)wb[k]; wbicef[k] = (float)wbice[k]; }
+  for (int k = 0; k < CG_MS; ++k) { wbf[k] = wb[k].hi; wbicef[k] = wbice[k].hi; }
   float tgg[CG_MS];
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) tgg[k] = D.tgg[k * ld + t];
@@ -1414,8 +1415,8 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) {
     const float dw = evapfbl[k] / (zse[k] * DLIQ);
-    wb[k] = wb[k] - (double)dw;
-    wbf[k] = wbf[k] - dw;
+    wb[k] = df_add(wb[k], -dw);
+    wbf[k] = wb[k].hi;
   }
   // soilfreeze (cbl_soilfreeze.F90:9-81)
 #pragma unroll
@@ -1431,12 +1432,17 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
       } else {
         amt = -fminf(wbicef[k] * zse[k] * DICE, (tgg[k] - TFRZ) * gf[k] / HLF);
       }
-      double wbice_new = wbice[k] + (double)(amt * rzd);
-      wbice_new = freeze ? fmin(wbice_new, (double)FROZEN_LIMIT * wb[k]) : fmax(0.0, wbice_new);
+      df32 wbice_new = df_add(wbice[k], amt * rzd);
+      if (freeze) {
+        const df32 cap = df_mul(wb[k], FROZEN_LIMIT);
+        if (df_lt(cap, wbice_new)) wbice_new = cap;
+      } else if (wbice_new.hi < 0.f) {
+        wbice_new = df32{0.f, 0.f};
+      }
       wbice[k] = wbice_new;
-      wb[k] = wb[k] + (double)(amt * rzd - amt * rzl);
-      wbf[k] = (float)wb[k];
-      wbicef[k] = (float)wbice[k];
+      wb[k] = df_add(wb[k], amt * rzd - amt * rzl);
+      wbf[k] = wb[k].hi;
+      wbicef[k] = wbice[k].hi;
       gf[k] = fmaxf(hcll, (1.0f - ssat) * css * rhosoil + (wbf[k] - wbicef[k]) * (CSWAT * DLIQ) + wbicef[k] * (CSICE * DICE)) * zse[k];
       if (k == 0 && isflag == 0) gf[k] = gf[k] + CGSNOW * snowd;
       tgg[k] = tgg[k] + amt * HLF / gf[k];
@@ -1445,7 +1451,11 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
   g1f = gf[0];
   // store: temperatures, snow pack, soil water / ice and the C2 record
 #pragma unroll
-  for (int k = 0; k < CG_MS; ++k) { D.wb[k * ld + t] = wb[k]; D.wbice[k * ld + t] = wbice[k]; D.tgg[k * ld + t] = tgg[k]; }
+  for (int k = 0; k < CG_MS; ++k) {
+    df_store(D.wb, CG_MS, ld, k, t, wb[k]);
+    df_store(D.wbice, CG_MS, ld, k, t, wbice[k]);
+    D.tgg[k * ld + t] = tgg[k];
+  }
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     D.tggsn[k * ld + t] = tggsn[k]; D.ssdn[k * ld + t] = ssdn[k]; D.smass[k * ld + t] = smass[k];
@@ -1479,14 +1489,14 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) zse[k] = S.zse[k];
   // state
-  double wb[CG_MS], wbice[CG_MS];
+  df32 wb[CG_MS], wbice[CG_MS];
 #pragma unroll
-  for (int k = 0; k < CG_MS; ++k) { wb[k] = D.wb[k * ld + t]; wbice[k] = D.wbice[k * ld + t]; }
+  for (int k = 0; k < CG_MS; ++k) { wb[k] = df_load(D.wb, CG_MS, ld, k, t); wbice[k] = df_load(D.wbice, CG_MS, ld, k, t); }
   // FP32 shadows of soil water and ice for thresholds and fluxes; every
-  // change to the FP64 state is mirrored into them
+  // change to the state is mirrored into them
   float wbf[CG_MS], wbicef[CG_MS];
 #pragma unroll
-  for (int k = 0; k < CG_MS; ++k) { wbf[k] = (float)wb[k]; wbicef[k] = (float)wbice[k]; }
+  for (int k = 0; k < CG_MS; ++k) { wbf[k] = wb[k].hi; wbicef[k] = wbice[k].hi; }
   float tgg[CG_MS];
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) tgg[k] = D.tgg[k * ld + t];
@@ -1610,8 +1620,8 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     dx[0] = 0.f; dx[CG_MS] = 0.f;
 #pragma unroll
     for (int k = 1; k < CG_MS; ++k) {
-      const float di = (wbicef[k - 1] != 0.f || wbicef[k] != 0.f) ? (float)(wbice[k - 1] - wbice[k]) : 0.f;
-      const float dl = (float)(wb[k - 1] - wb[k]) + (dwd[k - 1] - dwd[k]) - di;
+      const float di = (wbicef[k - 1] != 0.f || wbicef[k] != 0.f) ? df_sub(wbice[k - 1], wbice[k]) : 0.f;
+      const float dl = df_sub(wb[k - 1], wb[k]) + (dwd[k - 1] - dwd[k]) - di;
       dx[k] = (dl + x[k] * di) / sat[k - 1];
     }
     float a[CG_MS], b[CG_MS], c[CG_MS], r[CG_MS];
@@ -1636,20 +1646,19 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     // wb_new = wbice + (x_old + d) (ssat - wbice) = wb + dw + d (ssat - wbice)
 #pragma unroll
     for (int k = 0; k < CG_MS; ++k) {
-      const float inc = r[k] * sat[k];
-      wb[k] = wb[k] + (double)(dwd[k] + inc);
-      wbf[k] = wbf[k] + inc;
+      wb[k] = df_add(wb[k], dwd[k] + r[k] * sat[k]);
+      wbf[k] = wb[k].hi;
     }
     const float dfactor = 1.0f - DICE / DLIQ;
 #pragma unroll
     for (int k = 0; k < CG_MS; ++k) {
       if (wbicef[k] > FROZEN_LIMIT * wbf[k]) {
-        double sm = (wbice[k] - (double)FROZEN_LIMIT * wb[k]) * (double)(1.0f / (1.0f - FROZEN_LIMIT * dfactor));
-        wbice[k] = wbice[k] - sm;
-        wb[k] = wb[k] - (double)dfactor * sm;
-        wbf[k] = (float)wb[k];
-        wbicef[k] = (float)wbice[k];
-        tgg[k] = tgg[k] - (float)sm * zse[k] * DICE * HLF / gf[k];
+        const float sm = df_sub(wbice[k], df_mul(wb[k], FROZEN_LIMIT)) * (1.0f / (1.0f - FROZEN_LIMIT * dfactor));
+        wbice[k] = df_add(wbice[k], -sm);
+        wb[k] = df_add(wb[k], -dfactor * sm);
+        wbf[k] = wb[k].hi;
+        wbicef[k] = wbice[k].hi;
+        tgg[k] = tgg[k] - sm * zse[k] * DICE * HLF / gf[k];
       }
     }
   }
@@ -1657,9 +1666,12 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) {
     rnof1 = rnof1 + fmaxf(wbf[k] - ssat, 0.0f) * DLIQ * zse[k];
-    if (wbf[k] > ssat || wbf[k] < swilt / 4.0f) {
-      wb[k] = fmax((double)(swilt / 4.0f), fmin(wb[k], (double)ssat));
-      wbf[k] = (float)wb[k];
+    if (wbf[k] > ssat) {
+      wb[k] = df32{ssat, 0.f};
+      wbf[k] = ssat;
+    } else if (wbf[k] < swilt / 4.0f) {
+      wb[k] = df32{swilt / 4.0f, 0.f};
+      wbf[k] = swilt / 4.0f;
     }
   }
   float rnof5 = 0.f;
@@ -1692,15 +1704,15 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     sinfil = fminf(rnof2, wb_lake);
     rnof2 = fmaxf(0.0f, rnof2 - sinfil);
     wb_lake = fmaxf(0.0f, wb_lake - sinfil);
-    float xl = (float)fmax(0.0, (wb[CG_MS - 1] - (double)sfc) * (double)(zse[CG_MS - 1] * DLIQ));
+    float xl = fmaxf(0.0f, df_sub(wb[CG_MS - 1], df32{sfc, 0.f}) * (zse[CG_MS - 1] * DLIQ));
     sinfil = fminf(xl, wb_lake);
-    wb[CG_MS - 1] = wb[CG_MS - 1] - (double)(sinfil / (zse[CG_MS - 1] * DLIQ));
+    wb[CG_MS - 1] = df_add(wb[CG_MS - 1], -(sinfil / (zse[CG_MS - 1] * DLIQ)));
     wb_lake = fmaxf(0.0f, wb_lake - sinfil);
-    xl = (float)fmax(0.0, (wb[CG_MS - 1] - (double)(0.5f * (sfc + swilt))) * (double)(zse[CG_MS - 1] * DLIQ));
+    xl = fmaxf(0.0f, df_sub(wb[CG_MS - 1], df32{0.5f * (sfc + swilt), 0.f}) * (zse[CG_MS - 1] * DLIQ));
     sinfil = fminf(xl, wb_lake);
-    wb[CG_MS - 1] = wb[CG_MS - 1] - (double)(sinfil / (zse[CG_MS - 1] * DLIQ));
+    wb[CG_MS - 1] = df_add(wb[CG_MS - 1], -(sinfil / (zse[CG_MS - 1] * DLIQ)));
     wb_lake = fmaxf(0.0f, wb_lake - sinfil);
-    wbf[CG_MS - 1] = (float)wb[CG_MS - 1];
+    wbf[CG_MS - 1] = wb[CG_MS - 1].hi;
   }
   rnof1 = rnof1 / dels + rnof5 / dels;
   rnof2 = rnof2 / dels;
@@ -1711,9 +1723,13 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   constexpr double ZI[CG_MS] = {(double)0.022f * (DICE - DLIQ), (double)0.058f * (DICE - DLIQ),
                                 (double)0.154f * (DICE - DLIQ), (double)0.409f * (DICE - DLIQ),
                                 (double)1.085f * (DICE - DLIQ), (double)2.872f * (DICE - DLIQ)};
-  double wbtot = 0.0;
+  // summed in double-FP32 (weights rounded to FP32 once; the same every
+  // step, so the step-to-step change the water balance uses is unaffected)
+  df32 wsum{0.f, 0.f};
 #pragma unroll
-  for (int k = 0; k < CG_MS; ++k) wbtot = fma(wbice[k], ZI[k], fma(wb[k], ZL[k], wbtot));
+  for (int k = 0; k < CG_MS; ++k)
+    wsum = df_add(df_add(wsum, df_mul(wb[k], (float)ZL[k])), df_mul(wbice[k], (float)ZI[k]));
+  const double wbtot = df_to_double(wsum);
 
   // snow_aging (cbl_snow_aging.F90:11-83)
   if (snowd > 1.0f) {
@@ -1802,7 +1818,11 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
 
   // store
 #pragma unroll
-  for (int k = 0; k < CG_MS; ++k) { D.wb[k * ld + t] = wb[k]; D.wbice[k * ld + t] = wbice[k]; D.tgg[k * ld + t] = tgg[k]; }
+  for (int k = 0; k < CG_MS; ++k) {
+    df_store(D.wb, CG_MS, ld, k, t, wb[k]);
+    df_store(D.wbice, CG_MS, ld, k, t, wbice[k]);
+    D.tgg[k * ld + t] = tgg[k];
+  }
   (void)first_call; (void)isoilm;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
