@@ -55,6 +55,9 @@ def parse():
     p.add_argument("--cpu-sample-steps", type=int, default=48)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-surrogate", action="store_true", help="skip the surrogate arm")
+    p.add_argument("--order", type=int, default=-1, help="tile order; -1 = autotuned (default)")
+    p.add_argument("--blocks", default=None, help="threads per block of the five step kernels, e.g. 64,64,64,64,256 "
+                                                  "(with --order; default: autotuned)")
     p.add_argument("--sur-rows", type=float, default=5e7, help="training rows harvested for the surrogate")
     p.add_argument("--sur-epochs", type=int, default=20)
     return p.parse_args()
@@ -312,7 +315,9 @@ def run_gb300(args):
     d = Dist(args.gpus)
     ts = workload(args, d.rank)
     t0 = time.perf_counter()
-    g = R.from_tileset(ts, device=d.local, order=-1)   # tile order and block sizes autotuned
+    g = R.from_tileset(ts, device=d.local, order=args.order)   # -1: tile order and block sizes autotuned
+    if args.blocks:
+        g.set_blocks([int(x) for x in args.blocks.split(",")])
     t_create = time.perf_counter() - t0
     order, blocks = g.config()
     dels = ts.dels
