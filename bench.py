@@ -410,7 +410,7 @@ def run_gb300(args):
     if d.rank == 0:
         out = {"metric": METRIC, "value": value, "unit": "tile-timesteps/s", "n_gpus": d.world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-               "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 soil state, Thomas solves, balances)",
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32 (double-f32 soil water state, f64 balance accumulators)",
                "data": "synthetic (seeded generator; the reference's site forcing is not available)",
                "config": dict(config(args, d.world), autotuned={"tile_order": order, "blocks": blocks,
                                                                  "create_and_tune_s": round(t_create, 2)}),

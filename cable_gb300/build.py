@@ -18,12 +18,12 @@ SOURCES = ["cablegpu.cu", "phase_a.cu", "phase_b.cu", "phase_c1.cu", "phase_c2.c
 # Per-file extra flags: the canopy phase is FP32-only and division-heavy, so
 # it uses the approximate division / exp intrinsics; the phases that carry
 # FP64 state keep IEEE semantics.  CG_MAXNREG caps registers per thread,
-# chosen per kernel from measured step times at 4M tiles (radiation and soil
-# heat 80, canopy 96, snow pack and soil water 128: 6, 5 and 4 blocks of 128
-# threads per SM), trading a few hundred bytes of spills for occupancy; the
+# chosen per kernel from measured step times at 4M tiles (radiation 64, soil
+# heat 80, canopy 96, snow pack and soil water 128), trading a few hundred
+# bytes of spills for occupancy; the
 # block size itself is a launch-time choice (autotuned).
 EXTRA_FLAGS = {
-    "phase_a.cu": ["-DCG_MAXNREG=80"],
+    "phase_a.cu": ["-DCG_MAXNREG=64"],
     "phase_b.cu": ["--use_fast_math", "-DCG_MAXNREG=96"],
     "phase_c1.cu": ["-DCG_MAXNREG=128"],
     "phase_c2.cu": ["-DCG_MAXNREG=80"],

@@ -220,6 +220,7 @@ struct cablegpu_ctx {
   cudaEvent_t ev_h2d[2] = {}, ev_used[2] = {}, ev_step[2] = {}, ev_d2h[2] = {};
   bool io_ready = false;
   const float* io_forcing = nullptr;          // staging slot the current step_host step reads
+  float* io_out = nullptr;                    // staging slot it writes its outputs to (caller order)
   long long io_count = 0;
   std::string err;
 };
@@ -260,6 +261,7 @@ void bind_device_view(cablegpu_ctx* c) {
     D.forcing_in = c->io_forcing;
     D.forcing_caller_order = 1;
   }
+  D.out_caller = c->io_out;
   D.forcing_out = c->capture_forcing ? (float*)P("forcing") : nullptr;
   D.work_a = (float*)P("work_a");
   D.work_b = (float*)P("work_b");
@@ -655,24 +657,22 @@ int cablegpu_step_host(cablegpu_ctx* c, int ktau, float dels, const float* host_
   }
   const int slot = (int)(c->io_count & 1);
   const size_t fb = sizeof(float) * CG_NFORC * c->mp, ob = sizeof(float) * CG_NOUT * c->mp;
-  const int grid = (c->mp + 255) / 256;
   // upload this step's forcing once the step two back has consumed the slot
   CG_CUDA(c, cudaStreamWaitEvent(c->cstream, c->ev_used[slot], 0));
   CG_CUDA(c, cudaMemcpyAsync(c->d_fin[slot], host_forcing, fb, cudaMemcpyHostToDevice, c->cstream));
   CG_CUDA(c, cudaEventRecord(c->ev_h2d[slot], c->cstream));
-  // the step (the radiation kernel reads the forcing from the staging slot
-  // in caller order), then the outputs back into caller order once the
-  // slot's previous download is done
+  // the step: the radiation kernel reads the forcing from the staging slot
+  // and the canopy and soil-water kernels write the outputs to the output
+  // slot, both in caller order, once the slot's previous download is done
   CG_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_h2d[slot], 0));
+  CG_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_d2h[slot], 0));
   c->io_forcing = c->d_fin[slot];
+  c->io_out = c->d_fout[slot];
   int rc = launch_step(c, make_params(c, ktau, dels), nullptr);
   c->io_forcing = nullptr;
+  c->io_out = nullptr;
   if (rc) return rc;
   CG_CUDA(c, cudaEventRecord(c->ev_used[slot], c->stream));
-  CG_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_d2h[slot], 0));
-  gather_out_kernel<float, float><<<grid, 256, 0, c->stream>>>(c->d_fout[slot], (const float*)c->field_ptr[cablegpu_field_id("out")],
-                                                               c->d_order, c->mp, c->ld, CG_NOUT);
-  CG_CUDA(c, cudaGetLastError());
   CG_CUDA(c, cudaEventRecord(c->ev_step[slot], c->stream));
   CG_CUDA(c, cudaStreamWaitEvent(c->dstream, c->ev_step[slot], 0));
   CG_CUDA(c, cudaMemcpyAsync(host_out, c->d_fout[slot], ob, cudaMemcpyDeviceToHost, c->dstream));

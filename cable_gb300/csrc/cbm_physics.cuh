@@ -84,6 +84,7 @@ struct CgDev {
   double* wbal_tot;
   // outputs
   float* out;              // [CG_NOUT]
+  float* out_caller;       // [CG_NOUT][mp] copy of out in the caller's tile order (host-I/O steps), or null
   float* diag;             // [CG_NDIAG] or null
   float* work_a;           // phase A -> B, C handoff record
   float* work_b;           // phase B -> C handoff record

@@ -881,6 +881,11 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
   bool finite = true;
 #pragma unroll
   for (int i = 0; i < 7; ++i) { D.out[i * ld + t] = outv[i]; finite = finite && isfinite(outv[i]); }
+  if (D.out_caller) {
+    const size_t o = (size_t)D.tile_id[t];
+#pragma unroll
+    for (int i = 0; i < 7; ++i) D.out_caller[(size_t)i * D.mp + o] = outv[i];
+  }
   if (!finite) atomicOr(D.status, 1u);
   if (kDiag) {
     const int idx[37] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 18, 20, 21, 22, 32, 33, 34, 35,
@@ -1834,6 +1839,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   D.tss[t] = tss; D.wb_lake[t] = wb_lake;
   D.owb[t] = wbtot; D.wbal_tot[t] = wbal_tot;
   D.out[7 * ld + t] = trad;
+  if (D.out_caller) D.out_caller[(size_t)7 * D.mp + D.tile_id[t]] = trad;
   if (!isfinite(trad)) atomicOr(D.status, 1u);
   if (kDiag) {
     const int idx[16] = {17, 19, 23, 24, 25, 26, 27, 28, 37, 38, 39, 40, 41, 42, 46, 54};

@@ -455,30 +455,47 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_soa_kernel(InferArgs a) {
   uint32_t phase = 0;
   bool ok = true;
   const int nchunks = (a.mp + 127) / 128;
+  // the record words the inputs need, loaded one chunk ahead so the loads
+  // of chunk c + gridDim.x are in flight while chunk c's tensor-core passes
+  // run
+  constexpr int NW = 19;
+  constexpr int words[NW] = {0, 1, 2, 3, 5, 8, 11, 13, 32, 33, 38, 39, 46, 47, 48, 49, 50, 51, 0};
+  auto fetch = [&](int c, float* w, int& iv, int& so) {
+    const int t = c * 128 + s;
+    if (c < nchunks && t < a.mp) {
+#pragma unroll
+      for (int q = 0; q < NW - 1; ++q) w[q] = __ldg(a.work_a + (size_t)words[q] * a.ld + t);
+      iv = a.iveg[t] - 1;
+      so = a.isoilm[t] - 1;
+    } else {
+      iv = -1;
+      so = -1;
+    }
+  };
+  float w[NW];
+  int iv, so;
+  fetch(blockIdx.x, w, iv, so);
   for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const int t = c * 128 + s;
-    const bool valid = t < a.mp;
+    const bool valid = iv >= 0;
     float xn[NIN], y[NOUT];
     if (valid) {
-      auto A = [&](int i) { return __ldg(a.work_a + (size_t)i * a.ld + t); };
-      const int v = a.iveg[t] - 1;
       const CgPftTable& V = a.tables->pft;
-      const float tk = A(0), qv = A(1), pmb = A(2), ua = A(3), ca = A(5), vlaiw = A(8), z0m = A(11);
-      const float zref_uv = A(13), sc = A(32) + A(33);
+      const CgSoilTable& S = a.tables->soil;
+      const float tk = w[0], qv = w[1], pmb = w[2], ua = w[3], ca = w[4], vlaiw = w[5], z0m = w[6];
+      const float zref_uv = w[7], sc = w[8] + w[9];
       const float dva = (qsatfjh(tk - TFRZ, pmb) - qv) * RMAIR / RMH2O * pmb * 100.0f;
       // fwsoil from the soil liquid water the radiation kernel recorded
-      const CgSoilTable& S = a.tables->soil;
-      const int so = a.isoilm[t] - 1;
       const float swilt = S.swilt[so], sfc = S.sfc[so];
       float rwater = 0.f;
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k)
-        rwater += V.froot[k][v] * fmaxf(1.0e-9f, fminf(1.0f, (A(46 + k) - swilt) / (sfc - swilt)));
+        rwater += V.froot[k][iv] * fmaxf(1.0e-9f, fminf(1.0f, (w[12 + k] - swilt) / (sfc - swilt)));
       rwater = fmaxf(1.0e-9f, rwater);
-      const float fwsoil = a.medlyn ? fmaxf(1.0e-4f, fminf(1.0f, rwater)) : fmaxf(1.0e-9f, fminf(1.0f, V.vbeta[v] * rwater));
+      const float fwsoil = a.medlyn ? fmaxf(1.0e-4f, fminf(1.0f, rwater)) : fmaxf(1.0e-9f, fminf(1.0f, V.vbeta[iv] * rwater));
       const float us1 = fminf(fmaxf(1.e-6f, VONK * fmaxf(ua, UMIN) / logf(zref_uv / z0m)), 10.0f);
-      const float f[NIN] = {A(38), A(39), tk, fmaxf(dva, 0.0f), ca, V.vcmax[v] * sc,
-                            V.ejmax[v] * (1.0f - V.frac4[v]) * sc, a.medlyn ? V.g1[v] : V.a1gs[v],
+      const float f[NIN] = {w[10], w[11], tk, fmaxf(dva, 0.0f), ca, V.vcmax[iv] * sc,
+                            V.ejmax[iv] * (1.0f - V.frac4[iv]) * sc, a.medlyn ? V.g1[iv] : V.a1gs[iv],
                             fwsoil, vlaiw, us1, tk};
 #pragma unroll
       for (int q = 0; q < NIN; ++q) xn[q] = (f[q] - nrm[q]) * nrm[12 + q];
@@ -486,6 +503,7 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_soa_kernel(InferArgs a) {
 #pragma unroll
       for (int q = 0; q < NIN; ++q) xn[q] = 0.f;
     }
+    fetch(c + gridDim.x, w, iv, so);
     ok = forward128(smem, taddr, phase, xn, y);
     if (!ok) break;
     if (valid) a.dt[t] = y[2] * nrm[29] + nrm[26];
