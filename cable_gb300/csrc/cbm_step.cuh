@@ -1196,6 +1196,55 @@ __device__ __forceinline__ void phase_c1(const CgDev& D, const CgTables* __restr
   (void)dtmlt0; (void)sconds; (void)hcll; (void)wblf; (void)wbfice;
 }
 
+// snow pack state that snow_melting updates
+struct CgSnowPack {
+  float tggsn[3], ssdn[3], smass[3], sdepth[3];
+  float snowd, tgg0, dtmlt0;
+};
+
+// snow_melting (cbl_snowMelt.F90:9-120): melt of the snow lumped with soil
+// layer 1 (isflag 0) or of the 3-layer pack, returning the melt that leaves
+// the pack.  g1f: layer-1 heat capacity (J/m2/K).
+static __device__ __noinline__ float cg_snow_melting(CgSnowPack& p, int isflag, int isoilm, float g1f, float dels) {
+  float snowmlt = 0.f;
+  if (p.snowd > 0.0f && isflag == 0 && p.tgg0 >= TFRZ) {
+    float snowflx = (p.tgg0 - TFRZ) * g1f;
+    snowmlt = fminf(snowflx / HLF, p.snowd);
+    p.snowd = p.snowd - snowmlt;
+    p.tgg0 = p.tgg0 - snowmlt * HLF / g1f;
+  }
+  if (p.snowd > 0.0f && isflag > 0) {
+    float sm_prev = 0.f;   // smelt1(:,k-1)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float sgamm = p.ssdn[k] * CGSNOW * p.sdepth[k];
+      float snowflx = sm_prev * HLF / dels;
+      p.tggsn[k] = p.tggsn[k] + (snowflx * dels + sm_prev * CSWAT * (TFRZ - p.tggsn[k])) / (sgamm + CSWAT * sm_prev);
+      float osm = p.smass[k];
+      p.smass[k] = p.smass[k] + sm_prev;
+      p.ssdn[k] = fmaxf(120.0f, fminf(p.ssdn[k] * osm / p.smass[k] + DLIQ * (1.0f - osm / p.smass[k]), MAX_SSDN));
+      if (isoilm != 9) p.ssdn[k] = fminf(450.0f, p.ssdn[k]);
+      p.sdepth[k] = p.smass[k] / p.ssdn[k];
+      sgamm = p.smass[k] * CGSNOW;
+      float sm = 0.f;
+      if (p.tggsn[k] > TFRZ) {
+        snowflx = (p.tggsn[k] - TFRZ) * sgamm;
+        sm = fminf(snowflx / HLF, 0.6f * p.smass[k]);
+        if (k == 0) p.dtmlt0 = p.dtmlt0 + sm * HLF / sgamm;
+        p.smass[k] = p.smass[k] - sm;
+        p.tggsn[k] = p.tggsn[k] - sm * HLF / sgamm;
+        p.sdepth[k] = p.smass[k] / p.ssdn[k];
+      }
+      sm_prev = sm;
+    }
+    // melt of layers 1 and 2 refreezes into the layer below; only the
+    // bottom layer's melt leaves the pack
+    snowmlt = sm_prev;
+    p.snowd = p.snowd - snowmlt;
+  }
+  return snowmlt;
+}
+
 template <bool kDiag>
 __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
   const int ld = D.ld;
@@ -1257,45 +1306,20 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
     wbfice[k] = wbicef[k] / ssat;
   }
   float sconds[3] = {0.f, 0.f, 0.f};
-  // snow_melting (cbl_snowMelt.F90:9-120), first and second call share code
-  auto snow_melting = [&]() -> float {
-    float snowmlt = 0.f;
-    if (snowd > 0.0f && isflag == 0 && tgg[0] >= TFRZ) {
-      float snowflx = (tgg[0] - TFRZ) * g1f;
-      snowmlt = fminf(snowflx / HLF, snowd);
-      snowd = snowd - snowmlt;
-      tgg[0] = tgg[0] - snowmlt * HLF / g1f;
-    }
-    if (snowd > 0.0f && isflag > 0) {
-      float sm_prev = 0.f;   // smelt1(:,k-1)
+  // snow_melting (cbl_snowMelt.F90:9-120): called twice, kept out of line
+  // (one copy of its code keeps the kernel's instruction working set small)
+  CgSnowPack sp;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        float sgamm = ssdn[k] * CGSNOW * sdepth[k];
-        float snowflx = sm_prev * HLF / dels;
-        tggsn[k] = tggsn[k] + (snowflx * dels + sm_prev * CSWAT * (TFRZ - tggsn[k])) / (sgamm + CSWAT * sm_prev);
-        float osm = smass[k];
-        smass[k] = smass[k] + sm_prev;
-        ssdn[k] = fmaxf(120.0f, fminf(ssdn[k] * osm / smass[k] + DLIQ * (1.0f - osm / smass[k]), MAX_SSDN));
-        if (isoilm != 9) ssdn[k] = fminf(450.0f, ssdn[k]);
-        sdepth[k] = smass[k] / ssdn[k];
-        sgamm = smass[k] * CGSNOW;
-        float sm = 0.f;
-        if (tggsn[k] > TFRZ) {
-          snowflx = (tggsn[k] - TFRZ) * sgamm;
-          sm = fminf(snowflx / HLF, 0.6f * smass[k]);
-          if (k == 0) dtmlt0 = dtmlt0 + sm * HLF / sgamm;
-          smass[k] = smass[k] - sm;
-          tggsn[k] = tggsn[k] - sm * HLF / sgamm;
-          sdepth[k] = smass[k] / ssdn[k];
-        }
-        sm_prev = sm;
-      }
-      // melt of layers 1 and 2 refreezes into the layer below; only the
-      // bottom layer's melt leaves the pack
-      snowmlt = sm_prev;
-      snowd = snowd - snowmlt;
-    }
-    return snowmlt;
+  for (int k = 0; k < 3; ++k) { sp.tggsn[k] = tggsn[k]; sp.ssdn[k] = ssdn[k]; sp.smass[k] = smass[k]; sp.sdepth[k] = sdepth[k]; }
+  auto snow_melting = [&]() -> float {
+    sp.snowd = snowd; sp.tgg0 = tgg[0]; sp.dtmlt0 = dtmlt0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { sp.tggsn[k] = tggsn[k]; sp.ssdn[k] = ssdn[k]; sp.smass[k] = smass[k]; sp.sdepth[k] = sdepth[k]; }
+    const float m = cg_snow_melting(sp, isflag, isoilm, g1f, dels);
+    snowd = sp.snowd; tgg[0] = sp.tgg0; dtmlt0 = sp.dtmlt0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { tggsn[k] = sp.tggsn[k]; ssdn[k] = sp.ssdn[k]; smass[k] = sp.smass[k]; sdepth[k] = sp.sdepth[k]; }
+    return m;
   };
   // stempv (cbl_stempv.F90:13-221) with old_soil_conductivity (cbl_Oldconductivity.F90:7-59)
   float ghflux, sghflux = 0.f;
