@@ -1654,6 +1654,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
       dx[k] = (dl + x[k] * di) / sat[k - 1];
     }
     float a[CG_MS], b[CG_MS], c[CG_MS], r[CG_MS];
+    float z3[CG_MS];   // z3[k]: conductance of the interface between layers k-1 and k
     a[0] = 0.f; c[CG_MS - 1] = 0.f;
 #pragma unroll
     for (int k = 2; k <= CG_MS; ++k) {
@@ -1661,9 +1662,9 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
       float fact = __powf(wbh_k, ibp2 - 1.f);
       float icef = fmaxf(wbicef[k - 2] / fmaxf(0.01f, wbf[k - 2]), wbicef[k - 1] / fmaxf(0.01f, wbf[k - 1]));
       float pwb_wbh = (hsbh * (1.f - fminf(2.f * fminf(0.1f, icef), 0.1f))) * fmaxf(pwb_min, wbh_k * fact);
-      float z3_k = pwb_wbh / ldf(S.zshh, k - 1);
-      a[k - 1] = -dtt[k - 1] * z3_k;
-      c[k - 2] = -dtt[k - 2] * z3_k;
+      z3[k - 1] = pwb_wbh / ldf(S.zshh, k - 1);
+      a[k - 1] = -dtt[k - 1] * z3[k - 1];
+      c[k - 2] = -dtt[k - 2] * z3[k - 1];
     }
 #pragma unroll
     for (int k = 0; k < CG_MS; ++k) {
@@ -1672,10 +1673,25 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
       if (k < 3) r[k] = r[k] + dtt[k] * fwtop[k] / DLIQ;
     }
     trid_correction<CG_MS>(a, b, c, r);
-    // wb_new = wbice + (x_old + d) (ssat - wbice) = wb + dw + d (ssat - wbice)
+    // Row k of the solve reads d_k = dtt_k (G_k - G_{k+1} + src_k) with the
+    // interface flux G_k = z3_k (dx_k + d_{k-1} - d_k), and dtt_k sat_k =
+    // dels / zse_k.  The state is updated in that flux form: each interface
+    // carries one FP32 amount (explicit drainage plus implicit diffusion, m
+    // of water per step) that leaves one layer and enters the next, so the
+    // column total changes by exactly the top sources and the bottom
+    // drainage.  (Applying d_k sat_k directly loses conservation in
+    // proportion to |a| |d|, which for the stiff, highly conductive soils is
+    // ~1e-3 mm per step.)
+    float H[CG_MS + 1];
+    H[0] = dels * fluxh[0];
+    H[CG_MS] = dels * fluxh[CG_MS];
+#pragma unroll
+    for (int k = 1; k < CG_MS; ++k) H[k] = dels * (fluxh[k] + z3[k] * (dx[k] + r[k - 1] - r[k]));
 #pragma unroll
     for (int k = 0; k < CG_MS; ++k) {
-      wb[k] = df_add(wb[k], dwd[k] + r[k] * sat[k]);
+      float net = H[k] - H[k + 1];
+      if (k < 3) net = net + dels * fwtop[k] / DLIQ;
+      wb[k] = df_add(wb[k], net / zse[k]);
       wbf[k] = wb[k].hi;
     }
     const float dfactor = 1.0f - DICE / DLIQ;
@@ -1694,8 +1710,9 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   // surfbv remainder
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) {
-    rnof1 = rnof1 + fmaxf(wbf[k] - ssat, 0.0f) * DLIQ * zse[k];
     if (wbf[k] > ssat) {
+      // the excess over saturation, low word included, leaves as runoff
+      rnof1 = rnof1 + df_sub(wb[k], df32{ssat, 0.f}) * (DLIQ * zse[k]);
       wb[k] = df32{ssat, 0.f};
       wbf[k] = ssat;
     } else if (wbf[k] < swilt / 4.0f) {

@@ -249,3 +249,33 @@ def test_pipelined_host_io_step_equals_set_forcing_step_get(runtime):
         assert np.array_equal(a.get(k), b.get(k)), k
     a.close()
     b.close()
+
+
+def test_site5_full_year_against_oracle(oracle, runtime):
+    """The benchmark's site configuration over a full year (5 tiles, PFTs
+    1, 2, 5, 6, 9, soil type 2, 17,520 half-hour steps, replayed as CUDA
+    graphs) against the FP64 oracle on the same synthetic forcing: no drift
+    in soil temperature or moisture from the FP32 correction-form solves and
+    the double-FP32 soil water, and the cumulative energy and water balance
+    residuals stay as closed as the oracle's."""
+    R = runtime
+    ts = W.site5(nsteps=17520)
+    g = R.from_tileset(ts)
+    g.run(1, 17520)
+    g.synchronize()
+    gs = {k: g.get(k) for k in ("wb", "wbice", "tgg", "snowd", "ebal_tot", "wbal_tot", "cansto", "csoil", "cplant")}
+    g.close()
+    st = oracle.init_state(ts, 0)
+    oracle.run(ts, st, 17520, precision=0)
+    os_ = oracle.split_state(st)
+    # measured over the year: tgg 0.005 K, wb 8e-7, ebal_tot 1.5, wbal_tot 8e-5,
+    # csoil 0.14 (of 623) -- the same size as the REAL=FP32 oracle's own drift
+    assert np.abs(gs["tgg"] - os_["tgg"]).max() < 0.02                  # K after a year
+    assert np.abs(gs["wb"] - os_["wb"]).max() < 1e-5                    # m3/m3 after a year
+    assert np.abs(gs["wbice"] - os_["wbice"]).max() < 1e-5
+    assert np.abs(gs["cansto"] - os_["cansto"]).max() < 1e-4            # mm
+    # cumulative balance residuals (W/m2 and mm summed over the year)
+    assert np.abs(gs["ebal_tot"] - os_["ebal_tot"]).max() < 5.0
+    assert np.abs(gs["wbal_tot"] - os_["wbal_tot"]).max() < 1e-3
+    np.testing.assert_allclose(gs["csoil"], os_["csoil"], rtol=1e-3, atol=0.5)   # g C/m2
+    np.testing.assert_allclose(gs["cplant"], os_["cplant"], rtol=1e-3, atol=0.5)
