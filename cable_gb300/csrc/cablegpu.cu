@@ -182,10 +182,10 @@ struct cablegpu_ctx {
   unsigned int* h_status = nullptr;
   bool host_forcing = false;
   CgForcingSpec forc{12345ull, 1, 1800.f};
-  int medlyn = 0, diag = 0, capture_forcing = 0;
+  int medlyn = 0, diag = 0, capture_forcing = 0, thermal_fix = 0;
   cudaGraphExec_t graph = nullptr;
   float graph_dels = -1.f;
-  int graph_diag = -1, graph_medlyn = -1, graph_hostforc = -1, graph_capture = -1;
+  int graph_diag = -1, graph_medlyn = -1, graph_hostforc = -1, graph_capture = -1, graph_thermal = -1;
   unsigned long long graph_seed = 0;
   int graph_doy0 = -1;
   long long launches = 0;
@@ -314,6 +314,7 @@ StepParams make_params(cablegpu_ctx* c, int ktau, float dels) {
   p.ktau = ktau;
   p.dels = dels;
   p.medlyn = c->medlyn;
+  p.thermal_fix = c->thermal_fix;
   p.forc = c->forc;
   p.forc.dels = dels;
   p.step_index = ktau - 1;
@@ -322,7 +323,7 @@ StepParams make_params(cablegpu_ctx* c, int ktau, float dels) {
 
 int ensure_graph(cablegpu_ctx* c, float dels) {
   if (c->graph && c->graph_dels == dels && c->graph_diag == c->diag && c->graph_medlyn == c->medlyn &&
-      c->graph_hostforc == (int)c->host_forcing && c->graph_capture == c->capture_forcing &&
+      c->graph_thermal == c->thermal_fix && c->graph_hostforc == (int)c->host_forcing && c->graph_capture == c->capture_forcing &&
       c->graph_seed == c->forc.seed && c->graph_doy0 == c->forc.doy0 && c->graph_sur == c->sur_enabled &&
       c->graph_gate == c->sur_gate && std::equal(c->block, c->block + 5, c->graph_block))
     return CABLEGPU_OK;
@@ -340,7 +341,7 @@ int ensure_graph(cablegpu_ctx* c, float dels) {
   CG_CUDA(c, cudaStreamEndCapture(c->stream, &g));
   CG_CUDA(c, cudaGraphInstantiate(&c->graph, g, 0));
   cudaGraphDestroy(g);
-  c->graph_dels = dels; c->graph_diag = c->diag; c->graph_medlyn = c->medlyn;
+  c->graph_dels = dels; c->graph_diag = c->diag; c->graph_medlyn = c->medlyn; c->graph_thermal = c->thermal_fix;
   c->graph_hostforc = (int)c->host_forcing; c->graph_capture = c->capture_forcing;
   c->graph_seed = c->forc.seed; c->graph_doy0 = c->forc.doy0;
   c->graph_sur = c->sur_enabled; c->graph_gate = c->sur_gate;
@@ -601,9 +602,22 @@ int cablegpu_set_synthetic_forcing(cablegpu_ctx* c, unsigned long long seed, int
   return CABLEGPU_OK;
 }
 
-int cablegpu_set_options(cablegpu_ctx* c, int medlyn, int diag, int capture_forcing) {
+int cablegpu_set_options(cablegpu_ctx* c, int switches, int diag, int capture_forcing) {
   if (!c) return CABLEGPU_ERR_ARG;
-  c->medlyn = medlyn ? 1 : 0;
+  if (switches & ~(CABLEGPU_SW_MEDLYN | CABLEGPU_SW_SOIL_THERMAL_FIX))
+    return fail(c, CABLEGPU_ERR_ARG, "set_options: unknown switch bit");
+  c->medlyn = (switches & CABLEGPU_SW_MEDLYN) ? 1 : 0;
+  const int fix = (switches & CABLEGPU_SW_SOIL_THERMAL_FIX) ? 1 : 0;
+  if (fix != c->thermal_fix) {
+    // the switch changes the soil heat capacity and dry conductivity
+    // parameters: upload the matching tables, ordered after earlier steps
+    CgTables h{};
+    cg_build_tables(&h.pft, &h.soil);
+    if (fix) cg_apply_soil_thermal_fix(&h.soil);
+    CG_CUDA(c, cudaMemcpyAsync(c->d_tables, &h, sizeof(CgTables), cudaMemcpyHostToDevice, c->stream));
+    CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->thermal_fix = fix;
+  }
   c->diag = diag ? 1 : 0;
   c->capture_forcing = capture_forcing ? 1 : 0;
   return CABLEGPU_OK;
@@ -973,11 +987,15 @@ int cablegpu_param_table(int table, const char* name, float* out, int n) {
     CG_T(taul2) CG_T(rw) CG_T(tfcl) CG_T(tvclst)
 #undef CG_T
     if (!std::strcmp(name, "froot")) { src = &P.froot[0][0]; len = CG_MS * CG_NPFT; }
-  } else if (table == 1) {
-    const CgSoilTable& S = tab.soil;
+  } else if (table == 1 || table == 2) {
+    static CgSoilTable fixed;
+    static bool fixed_built = false;
+    if (!fixed_built) { fixed = tab.soil; cg_apply_soil_thermal_fix(&fixed); fixed_built = true; }
+    const CgSoilTable& S = table == 1 ? tab.soil : fixed;
 #define CG_T(x) if (!std::strcmp(name, #x)) { src = S.x; len = CG_NSOIL; }
     CG_T(bch) CG_T(css) CG_T(hyds) CG_T(rhosoil) CG_T(sfc) CG_T(ssat) CG_T(sucs) CG_T(swilt) CG_T(cnsd) CG_T(hsbh)
     CG_T(ibp2) CG_T(i2bp3) CG_T(pwb_min) CG_T(albsoil_vis) CG_T(albsoil_nir) CG_T(sand) CG_T(clay) CG_T(silt)
+    CG_T(cnsdv) CG_T(ktmp)
 #undef CG_T
   }
   if (!src || n < len) return CABLEGPU_ERR_ARG;

@@ -18,6 +18,7 @@ struct StepParams {
   int ktau;          // 1-based step counter of the run (mass_balance init / totals)
   float dels;        // step length (s)
   int medlyn;        // gs_switch: 0 leuning, 1 medlyn
+  int thermal_fix;   // cable_user%soil_thermal_fix
   CgForcingSpec forc;
   int step_index;    // 0-based counter for the synthetic forcing
 };
@@ -1321,12 +1322,33 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
     for (int k = 0; k < 3; ++k) { tggsn[k] = sp.tggsn[k]; ssdn[k] = sp.ssdn[k]; smass[k] = sp.smass[k]; sdepth[k] = sp.sdepth[k]; }
     return m;
   };
-  // stempv (cbl_stempv.F90:13-221) with old_soil_conductivity (cbl_Oldconductivity.F90:7-59)
+  // stempv (cbl_stempv.F90:13-221) with old_soil_conductivity
+  // (cbl_Oldconductivity.F90:7-59), or total_soil_conductivity
+  // (cbl_conductivity.F90:10-85) under soil_thermal_fix (cbl_stempv.F90:57-61)
   float ghflux, sghflux = 0.f;
   float gf[CG_MS];   // soil layer heat capacities (ssnow%gammzz), J/m2/K
   {
-    const float cnsd = ldf(S.cnsd, so);
     float ccnsw[CG_MS];
+    if (P.thermal_fix) {
+      const float ktmp = ldf(S.ktmp, so), cnsdv = ldf(S.cnsdv, so);
+      const bool snowy = isflag != 0 || snowd >= 0.1f;
+#pragma unroll
+      for (int k = 0; k < CG_MS; ++k) {
+        if (isoilm == 9) {
+          ccnsw[k] = SNOW_CCNSW;
+        } else {
+          const float w = wbf[k], wi = wbicef[k];
+          const float liq = (w >= 1.0e-15f) ? fminf(1.f, fmaxf(0.f, (w - wi) / w)) : 0.f;
+          // Ksat = Ktmp 2.2^(ssat (1 - liq)) 0.57^liq
+          const float ksat = ktmp * exp2f(ssat * (1.f - liq) * 1.13750352f + liq * -0.810966176f);
+          const float sr = fminf(0.9999f, fmaxf(0.f, w - 0.01f) / (ssat - 0.01f));
+          float ke = (sr >= 0.05f) ? 0.7f * log10f(sr) + 1.f : 0.f;
+          if (wi > 0.f || tgg[k] < TFRZ || snowy) ke = sr;
+          ccnsw[k] = fminf(ksat, fmaxf(cnsdv, ke * ksat + (1.f - ke) * cnsdv));
+        }
+      }
+    } else {
+    const float cnsd = ldf(S.cnsd, so);
 #pragma unroll
     for (int k = 0; k < CG_MS; ++k) {
       if (isoilm == 9) {
@@ -1337,6 +1359,7 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
         float f2 = fmaxf(1.0f, sqrtf(fminf(2.0f, 0.5f * ssat / fminf(ew, 0.5f * ssat))));
         ccnsw[k] = (exp_arg > 30.f) ? 1.5f * f2 : fminf(cnsd * __expf(exp_arg), 1.5f) * f2;
       }
+    }
     }
     float coeff[CG_MS + 1];   // coeff(1..ms+1) of the reference, coeff[ms] = 0
     float coefb;

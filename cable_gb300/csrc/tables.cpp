@@ -1,6 +1,7 @@
 // Host-side construction of the parameter tables declared in tables.h.
 #include "tables.h"
 
+#include <algorithm>
 #include <cmath>
 
 namespace {
@@ -126,9 +127,33 @@ void cg_build_tables(CgPftTable* P, CgSoilTable* S) {
     S->pwb_min[s] = std::pow(S->swilt[s] / S->ssat[s], S->ibp2[s]);
     S->albsoil_vis[s] = (float)alb_vis[s];
     S->albsoil_nir[s] = (float)alb_nir[s];
+    // soil_thermal_fix inputs, in double with the reference's default-REAL
+    // literals: the layer vectors hold the soil type's values
+    {
+      const double ssat_v = (double)S->ssat[s], sand_v = (double)S->sand[s];
+      const double sb = std::min((double)0.8f, std::max((double)0.1f, ssat_v));
+      S->cnsdv[s] = (float)(((double)0.135f * (1.0 - sb) + (double)64.7f / (double)S->rhosoil[s]) /
+                            (1.0 - (double)0.947f * (1.0 - sb)));
+      const double q = std::max(0.0, std::min((double)0.8f, sand_v * (double)0.92f));
+      const double ko = q > (double)0.2f ? 2.0 : 3.0;
+      S->ktmp[s] = (float)std::pow(std::pow((double)7.7f, q) * std::pow(ko, 1.0 - q), 1.0 - ssat_v);
+    }
   }
   for (int k = 0; k < CG_MS; ++k) S->zse[k] = (float)zse[k];
   S->zshh[0] = 0.5f * S->zse[0];
   S->zshh[CG_MS] = 0.5f * S->zse[CG_MS - 1];
   for (int k = 1; k < CG_MS; ++k) S->zshh[k] = 0.5f * (S->zse[k - 1] + S->zse[k]);
+}
+
+void cg_apply_soil_thermal_fix(CgSoilTable* S) {
+  for (int s = 0; s < CG_NSOIL; ++s) {
+    const double ssat_v = (double)S->ssat[s];
+    const double rho = (double)S->rhosoil[s] / (1.0 - ssat_v);
+    const double cs = std::max((double)910.6479f * (double)S->silt[s] + (double)916.4438f * (double)S->clay[s] +
+                                   (double)740.7491f * (double)S->sand[s],
+                               (double)800.0f);
+    S->rhosoil[s] = (float)rho;
+    S->css[s] = (float)cs;
+    S->cnsd[s] = S->cnsdv[s];
+  }
 }

@@ -13,6 +13,10 @@
 //   hsbh, ibp2, i2bp3, pwb_min                       cable_parameters.F90:2236-2245
 //   cnsd = 0.3 sand + 0.25 clay + 0.265 silt         cable_parameters.F90:2230
 //   zshh                                             cable_parameters.F90:1828-1831
+//   soil_thermal_fix set: cnsdv, and css, rhosoil,   cable_parameters.F90:2165-2227
+//   cnsd rewritten (cg_apply_soil_thermal_fix);
+//   ktmp, the saturated-conductivity factor of        cbl_conductivity.F90:36-43
+//   total_soil_conductivity
 // Soil albedo is not in the reference tables (it is read from the gridded
 // soil file); the VIS/NIR pair per soil type below is this library's choice.
 #pragma once
@@ -41,7 +45,14 @@ struct CgSoilTable {
   float pwb_min[CG_NSOIL], albsoil_vis[CG_NSOIL], albsoil_nir[CG_NSOIL];
   float sand[CG_NSOIL], clay[CG_NSOIL], silt[CG_NSOIL];
   float zse[CG_MS], zshh[CG_MS + 1];
+  // soil_thermal_fix: dry conductivity cnsd_vec and Ktmp = ((7.7^q Ko^(1-q))^(1-ssat),
+  // q the quartz fraction (both unused unless the switch is on)
+  float cnsdv[CG_NSOIL], ktmp[CG_NSOIL];
 };
 
 // Fills both tables; implemented in tables.cpp (host only).
 void cg_build_tables(CgPftTable* pft, CgSoilTable* soil);
+// Rewrites css, rhosoil and cnsd as the reference's parameter set-up does
+// under soil_thermal_fix (rhosoil / (1 - ssat), css from the texture
+// regression, cnsd = cnsd_vec).
+void cg_apply_soil_thermal_fix(CgSoilTable* soil);

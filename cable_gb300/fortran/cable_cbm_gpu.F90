@@ -19,9 +19,10 @@
 ! file and cbm_gpu_finalize at the end of the run.
 !
 ! Build: compile this file in place of cbl_model_driver_offline.F90 and link
-! cable_gb300/lib/libcablegpu.so.  Offline defaults only (soil_struc
-! 'default', fwsoil 'standard', ssnow_potev 'HDM', gs_switch 'leuning' or
-! 'medlyn'); other switches stay on the CPU path of the reference.
+! cable_gb300/lib/libcablegpu.so.  Offline defaults (soil_struc 'default',
+! fwsoil 'standard', ssnow_potev 'HDM') with gs_switch 'leuning' or 'medlyn'
+! and soil_thermal_fix on or off; other switches stay on the CPU path of the
+! reference.
 !==============================================================================
 
 MODULE cablegpu_c
@@ -75,10 +76,10 @@ MODULE cablegpu_c
       TYPE(c_ptr), VALUE :: host
     END FUNCTION cablegpu_set_forcing
 
-    INTEGER(c_int) FUNCTION cablegpu_set_options(ctx, medlyn, diag, capture) BIND(C, name="cablegpu_set_options")
+    INTEGER(c_int) FUNCTION cablegpu_set_options(ctx, switches, diag, capture) BIND(C, name="cablegpu_set_options")
       IMPORT :: c_int, c_ptr
       TYPE(c_ptr), VALUE :: ctx
-      INTEGER(c_int), VALUE :: medlyn, diag, capture
+      INTEGER(c_int), VALUE :: switches, diag, capture
     END FUNCTION cablegpu_set_options
 
     INTEGER(c_int) FUNCTION cablegpu_step(ctx, ktau, dels) BIND(C, name="cablegpu_step")
@@ -175,7 +176,7 @@ CONTAINS
     INTEGER(c_int), ALLOCATABLE, TARGET :: iveg(:), isoilm(:), flags(:)
     REAL(c_float), ALLOCATABLE, TARGET :: vlai(:), lat(:), r4(:, :)
     REAL(c_double), ALLOCATABLE, TARGET :: r8(:, :)
-    INTEGER(c_int) :: medlyn
+    INTEGER(c_int) :: switches
 
     mp_gpu = mp
     ALLOCATE(iveg(mp), isoilm(mp), vlai(mp), lat(mp), flags(mp))
@@ -193,9 +194,11 @@ CONTAINS
     tiles%swscale = c_null_ptr
     tiles%order = 0
     CALL check(cablegpu_create(tiles, 0_c_int, ctx), 'create')
-    medlyn = 0
-    IF (TRIM(cable_user%gs_switch) == 'medlyn') medlyn = 1
-    CALL check(cablegpu_set_options(ctx, medlyn, 0_c_int, 0_c_int), 'set_options')
+    ! science switch bits (CABLEGPU_SW_MEDLYN = 1, CABLEGPU_SW_SOIL_THERMAL_FIX = 2)
+    switches = 0
+    IF (TRIM(cable_user%gs_switch) == 'medlyn') switches = switches + 1
+    IF (cable_user%soil_thermal_fix) switches = switches + 2
+    CALL check(cablegpu_set_options(ctx, switches, 0_c_int, 0_c_int), 'set_options')
 
     ! prognostic state (soil_snow_type, canopy, bgc, bal)
     ALLOCATE(r8(mp, ms), r4(mp, ms))

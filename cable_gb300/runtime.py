@@ -40,6 +40,10 @@ EXPORTS = [
     "cablegpu_set_blocks", "cablegpu_get_config", "cablegpu_autotune", "cablegpu_step_host",
 ]
 NOALLOC_MAX_TILES = 65536
+# science switch bits of cablegpu_set_options (include/cablegpu.h)
+SW_MEDLYN = 1
+SW_SOIL_THERMAL_FIX = 2
+
 PHASES = ["radiation", "canopy", "snow_pack", "soil_heat", "soil_water", "surrogate_net"]
 
 _lib = None
@@ -264,8 +268,11 @@ class CableGPU:
         a = [np.ascontiguousarray(x, np.float64) for x in (snowd0, tgg0, wb0)]
         self._check(self.L.cablegpu_cold_start_noalloc(self.h, *[_ptr(x, C.c_double) for x in a]))
 
-    def set_options(self, medlyn=False, diag=False, capture_forcing=False):
-        self._check(self.L.cablegpu_set_options(self.h, int(medlyn), int(diag), int(capture_forcing)))
+    def set_options(self, medlyn=False, diag=False, capture_forcing=False, soil_thermal_fix=False):
+        """Science switches (``gs_switch='medlyn'``, ``soil_thermal_fix``) and
+        output options; every switch off is the reference's offline default."""
+        switches = (SW_MEDLYN if medlyn else 0) | (SW_SOIL_THERMAL_FIX if soil_thermal_fix else 0)
+        self._check(self.L.cablegpu_set_options(self.h, switches, int(diag), int(capture_forcing)))
 
     def set_synthetic_forcing(self, seed: int, doy0: int = 1):
         self._check(self.L.cablegpu_set_synthetic_forcing(self.h, int(seed), int(doy0)))

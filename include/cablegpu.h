@@ -130,10 +130,22 @@ int cablegpu_set_forcing(cablegpu_ctx* ctx, const float* host_forcing);
 /* Built-in seeded synthetic forcing generated inside the step kernel. */
 int cablegpu_set_synthetic_forcing(cablegpu_ctx* ctx, unsigned long long seed, int doy0);
 
-/* medlyn: 0 = gs_switch 'leuning' (offline cable.nml), 1 = 'medlyn'.
+/* switches: bit mask of the reference's science switches (cable_user,
+ * cable_runtime_opts_mod.F90:28-123); 0 = the offline defaults.
+ *   CABLEGPU_SW_MEDLYN            gs_switch = 'medlyn' instead of 'leuning'
+ *                                 (cbl_dryLeaf.F90:412-433)
+ *   CABLEGPU_SW_SOIL_THERMAL_FIX  soil_thermal_fix: total_soil_conductivity in
+ *                                 stempv (cbl_stempv.F90:57-61,
+ *                                 cbl_conductivity.F90:10-85) and the soil
+ *                                 heat parameters rewritten as
+ *                                 cable_parameters.F90:2165-2227 does
+ * (l_rev_corr acts only in the coupled model, cbl_soilsnow_main.F90 under
+ * cable_runtime%um: it has no offline effect.)  An unknown bit is an error.
  * diag: 1 = write the per-tile diagnostics fields every step.
  * capture_forcing: 1 = keep a copy of each step's forcing (field "forcing"). */
-int cablegpu_set_options(cablegpu_ctx* ctx, int medlyn, int diag, int capture_forcing);
+#define CABLEGPU_SW_MEDLYN 1
+#define CABLEGPU_SW_SOIL_THERMAL_FIX 2
+int cablegpu_set_options(cablegpu_ctx* ctx, int switches, int diag, int capture_forcing);
 
 /* One timestep, ktau 1-based (cbm(ktau, dels, ...) followed by the driver's
  * balance checks).  Asynchronous; errors of the step surface at the next
@@ -193,7 +205,9 @@ int cablegpu_autotune(const cablegpu_tiles* tiles, int device, int sample_tiles,
  * the per-plant-type table of pft_params.nml with derived entries "dleaf"
  * and "froot" (6 x 17, layer-major), table 1 the per-soil table of
  * cable_soilparm.nml with derived entries (hsbh, ibp2, i2bp3, pwb_min,
- * cnsd).  `n` is the capacity of `out`. */
+ * cnsd, and the soil_thermal_fix inputs cnsdv, ktmp), table 2 the same
+ * per-soil table with the soil_thermal_fix parameter set applied (css,
+ * rhosoil, cnsd rewritten).  `n` is the capacity of `out`. */
 int cablegpu_param_table(int table, const char* name, float* out, int n);
 
 /* ---------------------------------------------------------------- dryLeaf surrogate

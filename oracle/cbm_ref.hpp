@@ -53,6 +53,10 @@ struct Params {
   // soil (cable_parameters.F90:1511-1522 and derived_parameters :2236-2245)
   R bch, css, hyds, rhosoil, sfc, ssat, sucs, swilt, sand, clay, silt;
   R2 cnsd, pwb_min;
+  // soil_thermal_fix inputs of total_soil_conductivity (cbl_conductivity.F90:10-85):
+  // the layer vectors are the soil-type values spread over the layers
+  // (cable_parameters.F90:1689, :1516-1529), cnsd_vec rewritten at :2184-2186
+  R2 ssat_vec, sand_vec, cnsd_vec, watr;
   R hsbh, ibp2, i2bp3;
   R albsoil[3];
   R zse[MS], zshh[MS + 1];
@@ -101,6 +105,7 @@ struct CbmRef {
   using F = Forcing<R>;
   using D = Diag<R, R2>;
   bool medlyn = false;             // gs_switch; 'leuning' per cable.nml:62
+  bool soil_thermal_fix = false;   // cable_user%soil_thermal_fix (cable_runtime_opts_mod.F90:31)
 
   // ---- met / air working copies (met_type, air_type)
   struct Met { R fsd[3], fld, precip, precip_sn, tk, tvair, tvrad, pmb, ua, qv, qvair, dva, ca, coszen, doy; };
@@ -1366,7 +1371,26 @@ struct CbmRef {
     // ---- stempv (cbl_stempv.F90:13-221)
     {
       R2 ccnsw[MS];
-      for (int k = 0; k < MS; ++k) {   // old_soil_conductivity (cbl_Oldconductivity.F90:7-59)
+      // total_soil_conductivity (cbl_conductivity.F90:10-85), cbl_stempv.F90:57-61;
+      // r_2 arithmetic with default-REAL literals promoted
+      for (int k = 0; k < MS && soil_thermal_fix; ++k) {
+        if (p.isoilm == 9) {
+          ccnsw[k] = R2(R(SNOW_CCNSW));
+          continue;
+        }
+        const R2 quartz = mx(R2(0.0), mn(R2(0.8f), p.sand_vec * R2(0.92f)));
+        const R2 Ko = quartz > R2(0.2f) ? R2(2.0) : R2(3.0);
+        const R2 Ktmp = std::pow(std::pow(R2(7.7f), quartz) * std::pow(Ko, R2(1.0) - quartz), R2(1.0) - p.ssat_vec);
+        const R2 wbliq = s.wb[k] - s.wbice[k];   // cbl_soilsnow_main.F90:87
+        const R2 liq_frac = s.wb[k] >= R2(1.0e-15f) ? mn(R2(1.0), mx(R2(0.0), wbliq / s.wb[k])) : R2(0.0);
+        const R2 Ksat = Ktmp * std::pow(R2(2.2f), p.ssat_vec * (R2(1.0) - liq_frac)) * std::pow(R2(0.57f), liq_frac);
+        const R2 Sr = mn(R2(0.9999f), mx(R2(0.0), s.wb[k] - p.watr) / (p.ssat_vec - p.watr));
+        R2 Ke = Sr >= R2(0.05f) ? R2(0.7f) * std::log10(Sr) + R2(1.0) : R2(0.0);
+        if (s.wbice[k] > R2(0.0) || s.tgg[k] < R(TFRZ) || s.isflag != 0 || s.snowd >= R(0.1f)) Ke = Sr;
+        const R2 kk = Ke * Ksat + (R2(1.0) - Ke) * p.cnsd_vec;
+        ccnsw[k] = mn(Ksat, mx(p.cnsd_vec, kk));
+      }
+      for (int k = 0; k < MS && !soil_thermal_fix; ++k) {   // old_soil_conductivity (cbl_Oldconductivity.F90:7-59)
         if (p.isoilm == 9) {
           ccnsw[k] = R(SNOW_CCNSW);
         } else {

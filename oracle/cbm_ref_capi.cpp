@@ -97,7 +97,7 @@ void pack_diag(const Diag<R, R2>& d, double* dg, int mp, int t) {
 
 // ---------------------------------------------------------------- set-up
 template <class R, class R2>
-void make_params(Params<R, R2>& p, int iveg, int isoilm, double vlai, double lat) {
+void make_params(Params<R, R2>& p, int iveg, int isoilm, double vlai, double lat, bool thermal_fix = false) {
   const PftTable& V = pft_table();
   const SoilTable& T = soil_table();
   const int v = iveg - 1, s = isoilm - 1;
@@ -135,6 +135,22 @@ void make_params(Params<R, R2>& p, int iveg, int isoilm, double vlai, double lat
   p.sfc = R(T.sfc[s]); p.ssat = R(T.ssat[s]); p.sucs = R(-std::fabs(T.sucs[s])); p.swilt = R(T.swilt[s]);
   p.sand = R(T.sand[s]); p.clay = R(T.clay[s]); p.silt = R(T.silt[s]);
   p.cnsd = R2(p.sand * R(0.3) + p.clay * R(0.25) + p.silt * R(0.265));
+  // soil_thermal_fix parameter set (cable_parameters.F90:2165-2227, r_2 with
+  // default-REAL literals promoted): cnsd_vec from the bounded porosity and
+  // the table bulk density; then rhosoil_vec / (1 - ssat), css from the
+  // texture regression, and the scalar rhosoil, css, cnsd take the layer-3
+  // (= every layer's) values
+  p.ssat_vec = R2(p.ssat); p.sand_vec = R2(p.sand); p.watr = R2(0.01f);
+  {
+    const R2 sb = mn(R2(0.8f), mx(R2(0.1f), p.ssat_vec));
+    const R2 rhov = R2(p.rhosoil);
+    p.cnsd_vec = (R2(0.135f) * (R2(1.0) - sb) + R2(64.7f) / rhov) / (R2(1.0) - R2(0.947f) * (R2(1.0) - sb));
+    if (thermal_fix) {
+      p.rhosoil = R(rhov / (R2(1.0) - p.ssat_vec));
+      p.css = R(mx(R2(910.6479f) * R2(p.silt) + R2(916.4438f) * R2(p.clay) + R2(740.7491f) * R2(p.sand), R2(800.0f)));
+      p.cnsd = R2(R(p.cnsd_vec));
+    }
+  }
   p.hsbh = p.hyds * std::fabs(p.sucs) * p.bch;
   p.ibp2 = R(std::lround(p.bch) + 2);
   p.pwb_min = R2(std::pow(p.swilt / p.ssat, p.ibp2));
@@ -184,7 +200,7 @@ void make_state(State<R, R2>& s, const Params<R, R2>& p, int iveg, double snowd0
 }
 
 template <class R, class R2>
-int run_impl(int mp, int nsteps, int ktau0, double dels, int medlyn, const int* iveg, const int* isoilm,
+int run_impl(int mp, int nsteps, int ktau0, double dels, int switches, const int* iveg, const int* isoilm,
              const double* vlai, const double* lat, const float* forcing, const ForcingSpec* spec,
              const TileForcingParams* tfp, double* state, double* diag, int nthreads) {
   const int nslots = state_slots();
@@ -192,11 +208,12 @@ int run_impl(int mp, int nsteps, int ktau0, double dels, int medlyn, const int* 
 #pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads > 0 ? nthreads : 1)
   for (int t = 0; t < mp; ++t) {
     Params<R, R2> p;
-    make_params(p, iveg[t], isoilm[t], vlai[t], lat[t]);
+    make_params(p, iveg[t], isoilm[t], vlai[t], lat[t], (switches & 2) != 0);
     State<R, R2> s;
     unpack_state(s, state, mp, t);
     CbmRef<R, R2> model;
-    model.medlyn = medlyn != 0;
+    model.medlyn = (switches & 1) != 0;
+    model.soil_thermal_fix = (switches & 2) != 0;
     Diag<R, R2> d{};
     for (int n = 0; n < nsteps; ++n) {
       float fv[F_NFIELDS];
@@ -253,7 +270,8 @@ int cbmref_init(int mp, int precision, const int* iveg, const int* isoilm, const
 // with (seed, doy0) and the per-tile forcing parameters.  diag receives the
 // last step's diagnostics [ndiag][mp] (may be null).
 // precision: 0 = <double,double> oracle, 1 = <float,double> reference mix.
-int cbmref_run(int mp, int nsteps, int ktau0, double dels, int precision, int medlyn, const int* iveg,
+// switches: bit 0 gs_switch='medlyn', bit 1 soil_thermal_fix.
+int cbmref_run(int mp, int nsteps, int ktau0, double dels, int precision, int switches, const int* iveg,
                const int* isoilm, const double* vlai, const double* lat, const float* forcing, uint64_t seed,
                int doy0, const float* tf_lat, const float* tf_lonphase, const float* tf_tbase,
                const float* tf_swscale, double* state, double* diag, int nthreads) {
@@ -265,9 +283,9 @@ int cbmref_run(int mp, int nsteps, int ktau0, double dels, int precision, int me
     for (int t = 0; t < mp; ++t) tfp[t] = {tf_lat[t], tf_lonphase[t], tf_tbase[t], tf_swscale[t]};
   }
   if (precision == 0)
-    return run_impl<double, double>(mp, nsteps, ktau0, dels, medlyn, iveg, isoilm, vlai, lat, forcing, &spec,
+    return run_impl<double, double>(mp, nsteps, ktau0, dels, switches, iveg, isoilm, vlai, lat, forcing, &spec,
                                     tfp.data(), state, diag, nthreads);
-  return run_impl<float, double>(mp, nsteps, ktau0, dels, medlyn, iveg, isoilm, vlai, lat, forcing, &spec,
+  return run_impl<float, double>(mp, nsteps, ktau0, dels, switches, iveg, isoilm, vlai, lat, forcing, &spec,
                                  tfp.data(), state, diag, nthreads);
 }
 
@@ -322,6 +340,19 @@ double cbmref_soil_value(const char* name, int isoilm) {
   F(bch) F(clay) F(css) F(hyds) F(rhosoil) F(sand) F(sfc) F(silt) F(ssat) F(sucs) F(swilt) F(albsoil_vis) F(albsoil_nir)
 #undef F
   return NAN;
+}
+// soil_thermal_fix parameter set of one soil type, for comparison with the
+// product's tables: css, rhosoil, cnsd_vec and the saturated-conductivity
+// factor Ktmp of total_soil_conductivity (cbl_conductivity.F90:36-43)
+int cbmref_soil_thermal_fix(int isoilm, double* css, double* rhosoil, double* cnsd_vec, double* ktmp) {
+  if (isoilm < 1 || isoilm > NSOIL) return -1;
+  Params<double, double> p;
+  make_params(p, 1, isoilm, 1.0, 0.0, true);
+  *css = p.css; *rhosoil = p.rhosoil; *cnsd_vec = p.cnsd_vec;
+  const double quartz = mx(0.0, mn(double(0.8f), p.sand_vec * double(0.92f)));
+  const double Ko = quartz > double(0.2f) ? 2.0 : 3.0;
+  *ktmp = std::pow(std::pow(double(7.7f), quartz) * std::pow(Ko, 1.0 - quartz), 1.0 - p.ssat_vec);
+  return 0;
 }
 // derived per-tile parameters (froot etc.), for comparison with the product
 int cbmref_params(int iveg, int isoilm, double* froot6, double* dleaf, double* pwb_min, double* hsbh) {

@@ -50,6 +50,7 @@ def lib():
         L.cbmref_soil_value.restype = C.c_double
         L.cbmref_soil_value.argtypes = [C.c_char_p, C.c_int]
         L.cbmref_params.argtypes = [C.c_int, C.c_int, dp, dp, dp, dp]
+        L.cbmref_soil_thermal_fix.argtypes = [C.c_int, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -94,7 +95,7 @@ def init_state(ts, precision=0):
     return st
 
 
-def run(ts, state, nsteps, ktau0=1, forcing=None, precision=0, nthreads=None, medlyn=False):
+def run(ts, state, nsteps, ktau0=1, forcing=None, precision=0, nthreads=None, medlyn=False, soil_thermal_fix=False):
     """Advance ``state`` (modified in place) by ``nsteps``; return the last
     step's diagnostics as {name: array[mp]}."""
     L = lib()
@@ -115,7 +116,7 @@ def run(ts, state, nsteps, ktau0=1, forcing=None, precision=0, nthreads=None, me
     if nthreads is None:
         nthreads = os.cpu_count() or 1
     assert state.flags["C_CONTIGUOUS"] and state.dtype == np.float64
-    rc = L.cbmref_run(mp, nsteps, ktau0, float(ts.dels), precision, int(medlyn), _p(iveg, C.c_int),
+    rc = L.cbmref_run(mp, nsteps, ktau0, float(ts.dels), precision, int(bool(medlyn)) | (2 if soil_thermal_fix else 0), _p(iveg, C.c_int),
                       _p(isoil, C.c_int), _p(vlai, C.c_double), _p(lat, C.c_double), fptr, ts.seed, ts.doy0,
                       _p(tl, C.c_float), _p(tp, C.c_float), _p(tb, C.c_float), _p(tsw, C.c_float),
                       _p(state, C.c_double), _p(diag, C.c_double), nthreads)

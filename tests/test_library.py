@@ -127,3 +127,30 @@ def test_fortran_shim_binds_exported_symbols_and_registry_fields():
     assert names == R.FORCING_FIELDS
     outs = re.findall(r"(?:canopy|rad)%(\w+) = outb\(:, (\d)\)", src)
     assert [o[0] for o in sorted(outs, key=lambda x: int(x[1]))] == R.OUTPUT_FIELDS
+
+
+def test_soil_thermal_fix_tables_match_the_oracle(oracle):
+    """The soil_thermal_fix parameter set (css, rhosoil, dry conductivity and
+    the saturated-conductivity factor of total_soil_conductivity) equals the
+    oracle's restatement of cable_parameters.F90:2165-2227 and
+    cbl_conductivity.F90:36-43; table 1 keeps the default values."""
+    L = R.load()
+    got = {}
+    for name in ("css", "rhosoil", "cnsd", "cnsdv", "ktmp"):
+        b = (C.c_float * 9)()
+        assert L.cablegpu_param_table(2, name.encode(), b, 9) == 0
+        got[name] = np.frombuffer(b, np.float32).copy()
+    d = [C.c_double() for _ in range(4)]
+    for s in range(1, 10):
+        assert oracle.lib().cbmref_soil_thermal_fix(s, *[C.byref(x) for x in d]) == 0
+        css, rho, cnsdv, ktmp = (x.value for x in d)
+        assert got["css"][s - 1] == pytest.approx(css, rel=1e-6)
+        assert got["rhosoil"][s - 1] == pytest.approx(rho, rel=1e-6)
+        assert got["cnsdv"][s - 1] == pytest.approx(cnsdv, rel=1e-6)
+        assert got["cnsd"][s - 1] == got["cnsdv"][s - 1]
+        assert got["ktmp"][s - 1] == pytest.approx(ktmp, rel=1e-6)
+    # rhosoil / (1 - ssat) for the table's first soil (1600 kg/m3, ssat .398)
+    assert got["rhosoil"][0] == pytest.approx(1600.0 / (1 - 0.398), rel=1e-6)
+    b = (C.c_float * 9)()
+    assert L.cablegpu_param_table(1, b"css", b, 9) == 0
+    assert np.frombuffer(b, np.float32)[0] == 850.0

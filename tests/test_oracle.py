@@ -172,3 +172,22 @@ def test_forcing_generator_statistics(oracle):
     assert np.all((f["hod"] >= 0) & (f["hod"] < 24))
     # same seed -> same forcing
     assert np.array_equal(F, oracle.forcing(ts, 0, 48))
+
+
+def test_soil_thermal_fix_switch_is_live_and_conserves(oracle):
+    """With soil_thermal_fix the soil temperatures follow the new
+    conductivity and heat-capacity parameters (the switch changes them), and
+    the energy and leaf balances still close every step."""
+    ts = W.snow_grid(mp=400, nsteps=48)
+    res = {}
+    for fix in (False, True):
+        st = oracle.init_state(ts, 0)
+        d = oracle.run(ts, st, 48, soil_thermal_fix=fix)
+        res[fix] = (oracle.split_state(st), d)
+    (s0, d0), (s1, d1) = res[False], res[True]
+    assert np.abs(d1["ebal"]).max() < 1e-8
+    assert np.abs(d1["drybal"]).max() < 1e-6
+    dt = np.abs(np.asarray(s1["tgg"]) - np.asarray(s0["tgg"]))
+    assert dt.max() > 0.05                       # the switch changes soil temperatures
+    assert np.isfinite(np.asarray(s1["tgg"])).all()
+    assert 200.0 < np.asarray(s1["tgg"]).min() and np.asarray(s1["tgg"]).max() < 340.0
