@@ -182,10 +182,11 @@ struct cablegpu_ctx {
   unsigned int* h_status = nullptr;
   bool host_forcing = false;
   CgForcingSpec forc{12345ull, 1, 1800.f};
-  int medlyn = 0, diag = 0, capture_forcing = 0, thermal_fix = 0;
+  int medlyn = 0, diag = 0, capture_forcing = 0, thermal_fix = 0, litter = 0, rev_corr = 0;
+  int switches = 0;                // the CABLEGPU_SW_* mask the fields above come from
   cudaGraphExec_t graph = nullptr;
   float graph_dels = -1.f;
-  int graph_diag = -1, graph_medlyn = -1, graph_hostforc = -1, graph_capture = -1, graph_thermal = -1;
+  int graph_diag = -1, graph_switches = -1, graph_hostforc = -1, graph_capture = -1;
   unsigned long long graph_seed = 0;
   int graph_doy0 = -1;
   long long launches = 0;
@@ -315,6 +316,8 @@ StepParams make_params(cablegpu_ctx* c, int ktau, float dels) {
   p.dels = dels;
   p.medlyn = c->medlyn;
   p.thermal_fix = c->thermal_fix;
+  p.litter = c->litter;
+  p.rev_corr = c->rev_corr;
   p.forc = c->forc;
   p.forc.dels = dels;
   p.step_index = ktau - 1;
@@ -322,8 +325,8 @@ StepParams make_params(cablegpu_ctx* c, int ktau, float dels) {
 }
 
 int ensure_graph(cablegpu_ctx* c, float dels) {
-  if (c->graph && c->graph_dels == dels && c->graph_diag == c->diag && c->graph_medlyn == c->medlyn &&
-      c->graph_thermal == c->thermal_fix && c->graph_hostforc == (int)c->host_forcing && c->graph_capture == c->capture_forcing &&
+  if (c->graph && c->graph_dels == dels && c->graph_diag == c->diag && c->graph_switches == c->switches &&
+      c->graph_hostforc == (int)c->host_forcing && c->graph_capture == c->capture_forcing &&
       c->graph_seed == c->forc.seed && c->graph_doy0 == c->forc.doy0 && c->graph_sur == c->sur_enabled &&
       c->graph_gate == c->sur_gate && std::equal(c->block, c->block + 5, c->graph_block))
     return CABLEGPU_OK;
@@ -341,7 +344,7 @@ int ensure_graph(cablegpu_ctx* c, float dels) {
   CG_CUDA(c, cudaStreamEndCapture(c->stream, &g));
   CG_CUDA(c, cudaGraphInstantiate(&c->graph, g, 0));
   cudaGraphDestroy(g);
-  c->graph_dels = dels; c->graph_diag = c->diag; c->graph_medlyn = c->medlyn; c->graph_thermal = c->thermal_fix;
+  c->graph_dels = dels; c->graph_diag = c->diag; c->graph_switches = c->switches;
   c->graph_hostforc = (int)c->host_forcing; c->graph_capture = c->capture_forcing;
   c->graph_seed = c->forc.seed; c->graph_doy0 = c->forc.doy0;
   c->graph_sur = c->sur_enabled; c->graph_gate = c->sur_gate;
@@ -604,9 +607,11 @@ int cablegpu_set_synthetic_forcing(cablegpu_ctx* c, unsigned long long seed, int
 
 int cablegpu_set_options(cablegpu_ctx* c, int switches, int diag, int capture_forcing) {
   if (!c) return CABLEGPU_ERR_ARG;
-  if (switches & ~(CABLEGPU_SW_MEDLYN | CABLEGPU_SW_SOIL_THERMAL_FIX))
+  if (switches & ~(CABLEGPU_SW_MEDLYN | CABLEGPU_SW_SOIL_THERMAL_FIX | CABLEGPU_SW_LITTER | CABLEGPU_SW_L_REV_CORR))
     return fail(c, CABLEGPU_ERR_ARG, "set_options: unknown switch bit");
   c->medlyn = (switches & CABLEGPU_SW_MEDLYN) ? 1 : 0;
+  c->litter = (switches & CABLEGPU_SW_LITTER) ? 1 : 0;
+  c->rev_corr = (switches & CABLEGPU_SW_L_REV_CORR) ? 1 : 0;
   const int fix = (switches & CABLEGPU_SW_SOIL_THERMAL_FIX) ? 1 : 0;
   if (fix != c->thermal_fix) {
     // the switch changes the soil heat capacity and dry conductivity
@@ -618,6 +623,7 @@ int cablegpu_set_options(cablegpu_ctx* c, int switches, int diag, int capture_fo
     CG_CUDA(c, cudaStreamSynchronize(c->stream));
     c->thermal_fix = fix;
   }
+  c->switches = switches;
   c->diag = diag ? 1 : 0;
   c->capture_forcing = capture_forcing ? 1 : 0;
   return CABLEGPU_OK;
@@ -984,7 +990,7 @@ int cablegpu_param_table(int table, const char* name, float* out, int n) {
     CG_T(canst1) CG_T(dleaf) CG_T(ejmax) CG_T(frac4) CG_T(hc) CG_T(vbeta) CG_T(rp20) CG_T(vegcf) CG_T(extkn)
     CG_T(a1gs) CG_T(d0gs) CG_T(alpha) CG_T(convex) CG_T(cfrd) CG_T(gswmin) CG_T(conkc0) CG_T(conko0) CG_T(ekc)
     CG_T(eko) CG_T(g0) CG_T(g1) CG_T(vcmax) CG_T(xfang) CG_T(shelrb) CG_T(refl1) CG_T(refl2) CG_T(taul1)
-    CG_T(taul2) CG_T(rw) CG_T(tfcl) CG_T(tvclst)
+    CG_T(taul2) CG_T(rw) CG_T(tfcl) CG_T(tvclst) CG_T(clitt)
 #undef CG_T
     if (!std::strcmp(name, "froot")) { src = &P.froot[0][0]; len = CG_MS * CG_NPFT; }
   } else if (table == 1 || table == 2) {

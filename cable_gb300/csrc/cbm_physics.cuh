@@ -27,6 +27,8 @@ namespace cg {
 
 // physical constants (src/params/cable_phys_constants_mod.F90 and friends)
 constexpr float TFRZ = 273.16f, SBOLTZ = 5.67e-8f, EMSOIL = 1.0f, EMLEAF = 1.0f, CAPP = 1004.64f;
+// litter conductivity (W/m/K) and vapour diffusivity (m2/s) of cable_canopy.F90:203-204
+constexpr float KTH_LITT = 0.3f, DV_LITT = 3.1415841138194147e-05f;
 constexpr float HL = 2.5014e6f, HLF = 0.334e6f, DHEAT = 21.5e-6f, GRAV = 9.8086f, RGAS = 8.3143f;
 constexpr float RMAIR = 0.02897f, RMH2O = 0.018016f, CGSNOW = 2090.0f, CSICE = 2.100e3f, CSWAT = 4.218e3f;
 constexpr float DLIQ = 1000.0f, DICE = 921.0f, TETENA = 6.106f, TETENB = 17.27f, TETENC = 237.3f;

@@ -19,6 +19,8 @@ struct StepParams {
   float dels;        // step length (s)
   int medlyn;        // gs_switch: 0 leuning, 1 medlyn
   int thermal_fix;   // cable_user%soil_thermal_fix
+  int litter;        // cable_user%litter
+  int rev_corr;      // cable_user%l_rev_corr
   CgForcingSpec forc;
   int step_index;    // 0-based counter for the synthetic forcing
 };
@@ -403,6 +405,18 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
   const float sum_rad_gradis = gradis[0] + gradis[1];
   const float tss4 = pow4(tss);
   const float tvrad = tk;
+  // litter resistances to heat and vapour (cable_canopy.F90:471-476,
+  // :987-988), zero unless the litter switch is on; rho is fixed over the
+  // iteration, so they are too.  Recomputed where used rather than kept
+  // live through the dryLeaf iteration.
+  auto litter_resist = [&](float& rhlitt, float& relitt) {
+    rhlitt = 0.f; relitt = 0.f;
+    if (P.litter) {
+      const float cl = (float)(1 - (D.flags[t] & 1)) * ldf(V.clitt, v) * 0.003f;
+      rhlitt = cl / KTH_LITT / (rho * CAPP);
+      relitt = cl / DV_LITT;
+    }
+  };
   // state read by define_canopy
   const float oldcansto = D.cansto[t], ortsoil = D.rtsoil[t], snowd = D.snowd[t], pudsto = D.pudsto[t];
   const float tgg[1] = {D.tgg[t]};
@@ -719,7 +733,9 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
       // Humidity_deficit_method (cbl_pot_evap_snow.F90:79-167)
       float dq = qstss - (pass == 0 ? qv : qvair);
       if (snowd > 1.0f || tgg[0] == TFRZ) dq = fmaxf(-0.1e-3f, dq);
-      potev = rho * rlam * dq / rtsoil;
+      float rhlitt, relitt;
+      litter_resist(rhlitt, relitt);
+      potev = rho * rlam * dq / (rtsoil + relitt);
       // Latent_heat_flux (cbl_latent_heat.F90:15-285)
       {
         if (potev < 0.f) wetfac = 1.0f;
@@ -741,16 +757,19 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
         fesp = fminf(pudsto / dels * rlam, fmaxf(pwet * potev, 0.f));
         fes = fess + fesp;
       }
-      fhs = rho * CAPP * (tss - tvair) / rtsoil;
+      // the litter branch's first soil sensible heat uses the
+      // reference-height air temperature (cable_canopy.F90:521-534)
+      fhs = rho * CAPP * (tss - ((P.litter && pass == 0) ? tk : tvair)) / (rtsoil + rhlitt);
       if (pass == 0) {
         // within_canopy (cbl_within_canopy.F90:10-159)
         float rrbw = (gbhu[0] + gbhf[0] + gbhu[1] + gbhf[1]) / cmolar;
         float rrsw = (gswx[0] + gswx[1]) / cmolar;
-        float fix_eqn = cls;
+        float fix_eqn = cls, fix_eqn2 = 1.f;
+        if (P.litter) { fix_eqn = cls * rt0 / (rt0 + relitt); fix_eqn2 = rt0 / (rt0 + rhlitt); }
         if (potev > 0.f) fix_eqn = fix_eqn * wetfac;
         if (veg_mask && hruff > z0soilsn) {
           float r01 = rt0 * rt1, bs = rrbw * rrsw, g = (1.f + epsi) * rrsw + rrbw;
-          float dmah = (rt0 + rt1) * g + epsi * r01 * bs;
+          float dmah = (rt0 + fix_eqn2 * rt1) * g + epsi * r01 * bs;
           float dmbh = (-rlam / CAPP) * r01 * bs;
           float dmch = g * r01 * (fhv + fhs) / (rho * CAPP);
           float dmae = (-epsi * CAPP / rlam) * r01 * bs;
@@ -817,8 +836,16 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
                (logf((zscl - disp) / fmaxf(zruffs - disp, z0soilsn)) - psis((zscl - disp) * z4 / zref_tq) +
                 psis((zruffs - disp) * z4 / zref_tq)) / VONK;
       }
-      rsum = fminf(1.f, r_sc / fmaxf(1.f, rt0us + rt1usa + rt1usb + rt1usc));
-      tscrn = tss + (tk - tss) * rsum - TFRZ;
+      const float rsum0 = rt0us + rt1usa + rt1usb + rt1usc;
+      rsum = fminf(1.f, r_sc / fmaxf(1.f, rsum0));
+      float rsum_h = rsum;
+      if (P.litter) {   // :808-812, :848-854
+        float rhlitt, relitt;
+        litter_resist(rhlitt, relitt);
+        rsum_h = fminf(1.f, (r_sc + rhlitt * us) / fmaxf(1.f, rsum0 + rhlitt * us));
+        rsum = fminf(1.f, (r_sc + relitt * us) / fmaxf(1.f, rsum0 + relitt * us));
+      }
+      tscrn = tss + (tk - tss) * rsum_h - TFRZ;
     }
     float rsts = qsatfjh(tscrn, pmb);
     float qtgnet = rsts * wetfac - qv;
@@ -836,12 +863,18 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
   }
   const float precis0 = fmaxf(0.f, through);
   const float delwc = cansto - oldcansto;
-  // soil-coupling derivative (:913-1027, default branch)
+  // soil-coupling derivative (:913-1027, default and litter branches, with
+  // the l_rev_corr revisions :916-922, :993-1014)
   float dgdtg;
   {
     float dfn_dtg = -4.f * EMSOIL * SBOLTZ * tss4 / tss;
-    float dfh_dtg = rho * CAPP / rtsoil;
-    float dfe_ddq = wetfac * rho * rlam * cls / rtsoil;
+    float rttsoil = rtsoil;
+    if (P.rev_corr && veg_mask) rttsoil = rttsoil + rt1;
+    float rhlitt, relitt;
+    litter_resist(rhlitt, relitt);
+    float dfh_dtg = rho * CAPP / (rttsoil + rhlitt);
+    float dfe_ddq = wetfac * rho * rlam * cls / (rttsoil + relitt);
+    if (P.rev_corr && potev < 0.f) dfe_ddq = rho * rlam * cls / (rttsoil + relitt);
     float tc = tss - TFRZ;
     float ddq_dtg = (RMH2O / RMAIR) / pmb * TETENA * TETENB * TETENC / sqf(TETENC + tc) * expf(TETENB * tc / (TETENC + tc));
     dgdtg = dfn_dtg - dfh_dtg - dfe_ddq * ddq_dtg;

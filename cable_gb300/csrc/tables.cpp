@@ -37,6 +37,8 @@ const double xfang[] = {.01,.1,.01,.25,.01,-.3,-.3,-.3,-.3,-.3,-.3,.1,0,0,0,0,0}
 const double rw[] = {16,16,18,8.7,12.5,15.1,10.4,7.5,6.1,6.1,.001,5.8,.001,5.8,.001,9.0,.001};
 const double tfcl[] = {.42,.248,.38,.345,.31,.73,2.4,.35,.997,.997,.95,.55,.95,.55,.95,2.4,.95};
 const double tvclst[] = {235,283,268,278,278,235,278,278,278,278,278,278,278,278,268,278,278};
+// litter carbon (t C / ha), pft_params.nml:9 (vegin%clitt)
+const double clitt[] = {20,6,10,13,2,2,.3,.3,0,0,2,2,0,0,0,0,0};
 // cable_soilparm.nml
 const double bch[] = {4.2,7.1,11.4,5.15,10.4,10.4,7.12,5.83,7.1};
 const double clay[] = {.09,.3,.67,.2,.42,.48,.27,.17,.3};
@@ -87,6 +89,7 @@ void cg_build_tables(CgPftTable* P, CgSoilTable* S) {
     P->rw[v] = (float)rw[v];
     P->tfcl[v] = (float)tfcl[v];
     P->tvclst[v] = (float)tvclst[v];
+    P->clitt[v] = (float)clitt[v];
     P->cplant0[0][v] = (float)cplant1[v];
     P->cplant0[1][v] = (float)cplant2[v];
     P->cplant0[2][v] = (float)cplant3[v];

@@ -35,6 +35,7 @@ struct CgPftTable {
   float refl1[CG_NPFT], refl2[CG_NPFT], taul1[CG_NPFT], taul2[CG_NPFT];
   float froot[CG_MS][CG_NPFT];
   float rw[CG_NPFT], tfcl[CG_NPFT], tvclst[CG_NPFT];
+  float clitt[CG_NPFT];   // litter carbon, used by the litter switch
   float cplant0[3][CG_NPFT], csoil0[2][CG_NPFT];
   float ratecp[3], ratecs[2];
 };

@@ -21,8 +21,8 @@
 ! Build: compile this file in place of cbl_model_driver_offline.F90 and link
 ! cable_gb300/lib/libcablegpu.so.  Offline defaults (soil_struc 'default',
 ! fwsoil 'standard', ssnow_potev 'HDM') with gs_switch 'leuning' or 'medlyn'
-! and soil_thermal_fix on or off; other switches stay on the CPU path of the
-! reference.
+! and soil_thermal_fix, litter and l_rev_corr each on or off; other switches
+! stay on the CPU path of the reference.
 !==============================================================================
 
 MODULE cablegpu_c
@@ -194,10 +194,13 @@ CONTAINS
     tiles%swscale = c_null_ptr
     tiles%order = 0
     CALL check(cablegpu_create(tiles, 0_c_int, ctx), 'create')
-    ! science switch bits (CABLEGPU_SW_MEDLYN = 1, CABLEGPU_SW_SOIL_THERMAL_FIX = 2)
+    ! science switch bits (CABLEGPU_SW_MEDLYN = 1, CABLEGPU_SW_SOIL_THERMAL_FIX = 2,
+    ! CABLEGPU_SW_LITTER = 4, CABLEGPU_SW_L_REV_CORR = 8)
     switches = 0
     IF (TRIM(cable_user%gs_switch) == 'medlyn') switches = switches + 1
     IF (cable_user%soil_thermal_fix) switches = switches + 2
+    IF (cable_user%litter) switches = switches + 4
+    IF (cable_user%l_rev_corr) switches = switches + 8
     CALL check(cablegpu_set_options(ctx, switches, 0_c_int, 0_c_int), 'set_options')
 
     ! prognostic state (soil_snow_type, canopy, bgc, bal)

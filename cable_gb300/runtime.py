@@ -43,6 +43,13 @@ NOALLOC_MAX_TILES = 65536
 # science switch bits of cablegpu_set_options (include/cablegpu.h)
 SW_MEDLYN = 1
 SW_SOIL_THERMAL_FIX = 2
+SW_LITTER = 4
+SW_L_REV_CORR = 8
+
+
+def switch_mask(medlyn=False, soil_thermal_fix=False, litter=False, l_rev_corr=False) -> int:
+    return ((SW_MEDLYN if medlyn else 0) | (SW_SOIL_THERMAL_FIX if soil_thermal_fix else 0) |
+            (SW_LITTER if litter else 0) | (SW_L_REV_CORR if l_rev_corr else 0))
 
 PHASES = ["radiation", "canopy", "snow_pack", "soil_heat", "soil_water", "surrogate_net"]
 
@@ -268,11 +275,13 @@ class CableGPU:
         a = [np.ascontiguousarray(x, np.float64) for x in (snowd0, tgg0, wb0)]
         self._check(self.L.cablegpu_cold_start_noalloc(self.h, *[_ptr(x, C.c_double) for x in a]))
 
-    def set_options(self, medlyn=False, diag=False, capture_forcing=False, soil_thermal_fix=False):
-        """Science switches (``gs_switch='medlyn'``, ``soil_thermal_fix``) and
-        output options; every switch off is the reference's offline default."""
-        switches = (SW_MEDLYN if medlyn else 0) | (SW_SOIL_THERMAL_FIX if soil_thermal_fix else 0)
-        self._check(self.L.cablegpu_set_options(self.h, switches, int(diag), int(capture_forcing)))
+    def set_options(self, medlyn=False, diag=False, capture_forcing=False, soil_thermal_fix=False, litter=False,
+                    l_rev_corr=False):
+        """Science switches (``gs_switch='medlyn'``, ``soil_thermal_fix``,
+        ``litter``, ``l_rev_corr``) and output options; every switch off is the
+        reference's offline default."""
+        self._check(self.L.cablegpu_set_options(self.h, switch_mask(medlyn, soil_thermal_fix, litter, l_rev_corr),
+                                                int(diag), int(capture_forcing)))
 
     def set_synthetic_forcing(self, seed: int, doy0: int = 1):
         self._check(self.L.cablegpu_set_synthetic_forcing(self.h, int(seed), int(doy0)))

@@ -139,12 +139,24 @@ int cablegpu_set_synthetic_forcing(cablegpu_ctx* ctx, unsigned long long seed, i
  *                                 cbl_conductivity.F90:10-85) and the soil
  *                                 heat parameters rewritten as
  *                                 cable_parameters.F90:2165-2227 does
- * (l_rev_corr acts only in the coupled model, cbl_soilsnow_main.F90 under
- * cable_runtime%um: it has no offline effect.)  An unknown bit is an error.
+ *   CABLEGPU_SW_LITTER            litter: litter resistances to soil heat and
+ *                                 vapour transfer in define_canopy
+ *                                 (cable_canopy.F90:471-476, :521-530,
+ *                                 :808-854, :979-997; cbl_pot_evap_snow.F90
+ *                                 :155-157; cbl_within_canopy.F90:80-84) with
+ *                                 the static litter carbon of pft_params.nml
+ *   CABLEGPU_SW_L_REV_CORR        l_rev_corr: revised soil-coupling
+ *                                 derivatives (cable_canopy.F90:916-922,
+ *                                 :993-1014); its other uses act only in the
+ *                                 coupled model (cable_runtime%um) or on
+ *                                 fns_cor, which is 0 offline
+ * An unknown bit is an error.
  * diag: 1 = write the per-tile diagnostics fields every step.
  * capture_forcing: 1 = keep a copy of each step's forcing (field "forcing"). */
 #define CABLEGPU_SW_MEDLYN 1
 #define CABLEGPU_SW_SOIL_THERMAL_FIX 2
+#define CABLEGPU_SW_LITTER 4
+#define CABLEGPU_SW_L_REV_CORR 8
 int cablegpu_set_options(cablegpu_ctx* ctx, int switches, int diag, int capture_forcing);
 
 /* One timestep, ktau 1-based (cbm(ktau, dels, ...) followed by the driver's

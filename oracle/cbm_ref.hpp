@@ -49,6 +49,7 @@ struct Params {
   R a1gs, d0gs, alpha, convex, cfrd, gswmin, conkc0, conko0, ekc, eko, g0, g1, vcmax, xfang;
   R refl[3], taul[3], froot[MS], meth;
   R rw, tfcl, tvclst;             // carbon tables (cable_carbon.F90:129-140)
+  R2 clitt;                       // litter carbon (veg%clitt, cable_parameters.F90:3330)
   R ratecp[3], ratecs[2];
   // soil (cable_parameters.F90:1511-1522 and derived_parameters :2236-2245)
   R bch, css, hyds, rhosoil, sfc, ssat, sucs, swilt, sand, clay, silt;
@@ -106,6 +107,10 @@ struct CbmRef {
   using D = Diag<R, R2>;
   bool medlyn = false;             // gs_switch; 'leuning' per cable.nml:62
   bool soil_thermal_fix = false;   // cable_user%soil_thermal_fix (cable_runtime_opts_mod.F90:31)
+  bool litter = false;             // cable_user%litter: litter resistances in define_canopy
+  bool l_rev_corr = false;         // cable_user%l_rev_corr (cable_runtime_opts_mod.F90:28)
+  // litter conductivity / vapour diffusivity (cable_canopy.F90:203-204)
+  static constexpr double KTH_LITT = 0.3, DV_LITT = 3.1415841138194147e-05;
 
   // ---- met / air working copies (met_type, air_type)
   struct Met { R fsd[3], fld, precip, precip_sn, tk, tvair, tvrad, pmb, ua, qv, qvair, dva, ca, coszen, doy; };
@@ -708,6 +713,17 @@ struct CbmRef {
     if (snowd > R(1.0) || tgg1 == R(TFRZ)) dq = mx(R(-0.1e-3), dq);
     return rho * rlam * dq / rtsoil;
   }
+  // litter branch of Humidity_deficit_method (cbl_pot_evap_snow.F90:155-157):
+  // the litter vapour resistance added in default-REAL arithmetic
+  static R hdm_litter(R rho, R rlam, R dq, R rtsoil, R snowd, R tgg1, int isflag, R2 clitt) {
+    if (snowd > R(1.0) || tgg1 == R(TFRZ)) dq = mx(R(-0.1e-3), dq);
+    return rho * rlam * dq / (rtsoil + R(1 - isflag) * R(clitt) * R(0.003f) / R(DV_LITT));
+  }
+  // litter resistances to heat and vapour (cable_canopy.F90:471-476, :987-988)
+  static void litter_resist(R2 clitt, int isflag, R rho, R& rhlitt, R& relitt) {
+    rhlitt = R(R2(R(1 - isflag)) * clitt * R2(0.003f) / R2(KTH_LITT) / R2(rho * R(CAPP)));
+    relitt = R(R2(R(1 - isflag)) * clitt * R2(0.003f) / R2(DV_LITT));
+  }
 
   // ======================================================================
   // one cbm() timestep for one tile, followed by the offline driver's
@@ -815,6 +831,7 @@ struct CbmRef {
     const R sum_rad_rniso = rad.rniso[0] + rad.rniso[1];
     const R sum_rad_gradis = rad.gradis[0] + rad.gradis[1];
     R us = 0, rt0 = 0, rt1usc = 0, rtsoil = s.rtsoil, cls = R(1);
+    R rhlitt = 0, relitt = 0;   // cable_canopy.F90:239-240
     R fev = 0, fhv = 0, fnv = 0, fns = 0, fhs = 0, fe = 0, fh = 0, ga = 0, rnet = 0, epot = 0, qstss = 0;
     R fevw = 0, fhvw = 0;
     R2 ghwet = 0;
@@ -895,19 +912,23 @@ struct CbmRef {
       fns = rad.qssabs + rad.transd * met.fld + (R(1.0) - rad.transd) * R(EMLEAF) * R(SBOLTZ) * std::pow(tv, 4) -
             R(EMSOIL) * R(SBOLTZ) * tss4;
       qstss = qsatfjh(s.tss - R(TFRZ), met.pmb);
+      if (litter) litter_resist(p.clitt, s.isflag, air.rho, rhlitt, relitt);
       {
         R dq = qstss - met.qv;
-        potev = hdm(air.rho, air.rlam, dq, rtsoil, s.snowd, s.tgg[0]);
+        potev = litter ? hdm_litter(air.rho, air.rlam, dq, rtsoil, s.snowd, s.tgg[0], s.isflag, p.clitt)
+                       : hdm(air.rho, air.rlam, dq, rtsoil, s.snowd, s.tgg[0]);
       }
       latent_heat_flux(dels, p, air.rlam, s, potev, wetfac, evapfbl[0], cls, s.tss, fes, fess, fesp, pwet);
-      fhs = air.rho * R(CAPP) * (s.tss - met.tvair) / rtsoil;
+      // :521-534: the litter branch uses the reference-height air temperature
+      if (litter) fhs = air.rho * R(CAPP) * (s.tss - met.tk) / (rtsoil + rhlitt);
+      else fhs = air.rho * R(CAPP) * (s.tss - met.tvair) / rtsoil;
       // within_canopy (cbl_within_canopy.F90:10-159)
       {
         R rrbw = R(L.gbhu[0] + L.gbhf[0] + L.gbhu[1] + L.gbhf[1]) / air.cmolar;
         R rrsw = (L.gswx[0] + L.gswx[1]) / air.cmolar;
-        R fix_eqn = cls * rt0 / (rt0 + R(0));
+        R fix_eqn = cls * rt0 / (rt0 + relitt);
         if (potev > R(0.)) fix_eqn = fix_eqn * wetfac;
-        R fix_eqn2 = rt0 / (rt0 + R(0));
+        R fix_eqn2 = rt0 / (rt0 + rhlitt);
         if (p.meth > R(0) && vlaiw > R(LAI_THRESH) && rough.hruff > rough.z0soilsn) {
           const R rt1 = rough.rt1;
           R dmah = (rt0 + fix_eqn2 * rt1) * ((R(1.) + air.epsi) * rrsw + rrbw) + air.epsi * (rt0 * rt1) * (rrbw * rrsw);
@@ -932,10 +953,12 @@ struct CbmRef {
       qstss = qsatfjh(s.tss - R(TFRZ), met.pmb);
       {
         R dq = qstss - met.qvair;
-        potev = hdm(air.rho, air.rlam, dq, rtsoil, s.snowd, s.tgg[0]);
+        potev = litter ? hdm_litter(air.rho, air.rlam, dq, rtsoil, s.snowd, s.tgg[0], s.isflag, p.clitt)
+                       : hdm(air.rho, air.rlam, dq, rtsoil, s.snowd, s.tgg[0]);
       }
       latent_heat_flux(dels, p, air.rlam, s, potev, wetfac, evapfbl[0], cls, s.tss, fes, fess, fesp, pwet);
-      fhs = air.rho * R(CAPP) * (s.tss - met.tvair) / rtsoil;
+      if (litter) fhs = air.rho * R(CAPP) * (s.tss - met.tvair) / (rtsoil + rhlitt);
+      else fhs = air.rho * R(CAPP) * (s.tss - met.tvair) / rtsoil;
       ga = fns - fhs - R(fes);
       fe = R(fev + fes);
       fh = fhv + fhs;
@@ -991,15 +1014,25 @@ struct CbmRef {
                 psis((zscl - rough.disp) * zip / rough.zref_tq) + psis((rough.zruffs - rough.disp) * zip / rough.zref_tq)) /
                    R(VONK);
       }
-      tscrn = s.tss + (met.tk - s.tss) *
-                          mn(R(1.), (r_sc / mx(R(1.), rough.rt0us + rough.rt1usa + rough.rt1usb + rt1usc))) -
-              R(TFRZ);
+      if (litter)   // :808-812
+        tscrn = s.tss + (met.tk - s.tss) *
+                            mn(R(1.), ((r_sc + rhlitt * us) /
+                                       mx(R(1.), rough.rt0us + rough.rt1usa + rough.rt1usb + rt1usc + rhlitt * us))) -
+                R(TFRZ);
+      else
+        tscrn = s.tss + (met.tk - s.tss) *
+                            mn(R(1.), (r_sc / mx(R(1.), rough.rt0us + rough.rt1usa + rough.rt1usb + rt1usc))) -
+                R(TFRZ);
     }
     R rsts = qsatfjh(tscrn, met.pmb);
     R qtgnet = rsts * wetfac - met.qv;
     R qsurf = (qtgnet > R(0.)) ? rsts * wetfac : R(0.1) * rsts * wetfac + R(0.9) * met.qv;
     R qscrn = met.qv - qstar * ftemp;
-    if (screen_canopy)
+    if (screen_canopy && litter)   // :848-854
+      qscrn = qsurf + (met.qv - qsurf) *
+                          mn(R(1.), ((r_sc + relitt * us) /
+                                     mx(R(1.), rough.rt0us + rough.rt1usa + rough.rt1usb + rt1usc + relitt * us)));
+    else if (screen_canopy)
       qscrn = qsurf + (met.qv - qsurf) * mn(R(1.), (r_sc / mx(R(1.), rough.rt0us + rough.rt1usa + rough.rt1usb + rt1usc)));
     // canopy water budget (:881-906)
     R dewmm = R(-(mn(R(0.0), fevw) + mn(R2(0.0), L.fevc)) * dels / air.rlam);
@@ -1010,11 +1043,21 @@ struct CbmRef {
     R precis = mx(R(0.), through);
     cansto = cansto - spill;
     R delwc = cansto - oldcansto;
-    // soil-coupling derivatives (:913-1027), default branch
+    // soil-coupling derivatives (:913-1027): default and litter branches,
+    // with the l_rev_corr revisions (:916-922, :993-1014)
     R dfn_dtg = R(-1.) * R(4.) * R(EMSOIL) * R(SBOLTZ) * tss4 / s.tss;
     R rttsoil = rtsoil;
-    R dfh_dtg = air.rho * R(CAPP) / rttsoil;
-    R dfe_ddq = wetfac * air.rho * air.rlam * cls / rttsoil;
+    if (l_rev_corr && vlaiw > R(LAI_THRESH)) rttsoil = rttsoil + rough.rt1;
+    R dfh_dtg, dfe_ddq;
+    if (litter) {
+      litter_resist(p.clitt, s.isflag, air.rho, rhlitt, relitt);
+      dfh_dtg = air.rho * R(CAPP) / (rttsoil + rhlitt);
+      dfe_ddq = wetfac * air.rho * air.rlam * cls / (rttsoil + relitt);
+    } else {
+      dfh_dtg = air.rho * R(CAPP) / rttsoil;
+      dfe_ddq = wetfac * air.rho * air.rlam * cls / rttsoil;
+    }
+    if (l_rev_corr && potev < R(0.)) dfe_ddq = air.rho * air.rlam * cls / (rttsoil + relitt);
     R ddq_dtg = (R(RMH2O) / R(RMAIR)) / met.pmb * R(TETENA) * R(TETENB) * R(TETENC) / (sq(R(TETENC) + s.tss - R(TFRZ))) *
                 std::exp(R(TETENB) * (s.tss - R(TFRZ)) / (R(TETENC) + s.tss - R(TFRZ)));
     R dfe_dtg = dfe_ddq * ddq_dtg;

@@ -117,6 +117,7 @@ void make_params(Params<R, R2>& p, int iveg, int isoilm, double vlai, double lat
   p.taul[0] = R(V.taul1[v]); p.taul[1] = R(V.taul2[v]); p.taul[2] = R(0.01);
   p.meth = R(1);
   p.rw = R(V.rw[v]); p.tfcl = R(V.tfcl[v]); p.tvclst = R(V.tvclst[v]);
+  p.clitt = R2(R(V.clitt[v]));
   for (int k = 0; k < 3; ++k) p.ratecp[k] = R(V.ratecp[k]);
   for (int k = 0; k < 2; ++k) p.ratecs[k] = R(V.ratecs[k]);
   for (int k = 0; k < MS; ++k) p.zse[k] = R(ZSE[k]);
@@ -214,6 +215,8 @@ int run_impl(int mp, int nsteps, int ktau0, double dels, int switches, const int
     CbmRef<R, R2> model;
     model.medlyn = (switches & 1) != 0;
     model.soil_thermal_fix = (switches & 2) != 0;
+    model.litter = (switches & 4) != 0;
+    model.l_rev_corr = (switches & 8) != 0;
     Diag<R, R2> d{};
     for (int n = 0; n < nsteps; ++n) {
       float fv[F_NFIELDS];
@@ -270,7 +273,8 @@ int cbmref_init(int mp, int precision, const int* iveg, const int* isoilm, const
 // with (seed, doy0) and the per-tile forcing parameters.  diag receives the
 // last step's diagnostics [ndiag][mp] (may be null).
 // precision: 0 = <double,double> oracle, 1 = <float,double> reference mix.
-// switches: bit 0 gs_switch='medlyn', bit 1 soil_thermal_fix.
+// switches: bit 0 gs_switch='medlyn', bit 1 soil_thermal_fix, bit 2 litter,
+// bit 3 l_rev_corr.
 int cbmref_run(int mp, int nsteps, int ktau0, double dels, int precision, int switches, const int* iveg,
                const int* isoilm, const double* vlai, const double* lat, const float* forcing, uint64_t seed,
                int doy0, const float* tf_lat, const float* tf_lonphase, const float* tf_tbase,
@@ -328,7 +332,7 @@ double cbmref_pft_value(const char* name, int iveg) {
   F(a1gs) F(alpha) F(canst1) F(cfrd) F(conkc0) F(conko0) F(convex) F(cplant1) F(cplant2) F(cplant3) F(csoil1)
   F(csoil2) F(d0gs) F(ekc) F(eko) F(extkn) F(frac4) F(g0) F(g1) F(gswmin) F(hc) F(length) F(refl1) F(refl2)
   F(taul1) F(taul2) F(rootbeta) F(rp20) F(rs20) F(shelrb) F(vbeta) F(vcmax) F(vegcf) F(width) F(xfang) F(rw) F(tfcl)
-  F(tvclst)
+  F(tvclst) F(clitt)
 #undef F
   return NAN;
 }

@@ -66,6 +66,8 @@ struct PftTable {
   double width[NPFT], xfang[NPFT];
   // cable_carbon.F90 CASE(17)
   double rw[NPFT], tfcl[NPFT], tvclst[NPFT];
+  // litter carbon (t C / ha), pft_params.nml:9, used by the litter switch
+  double clitt[NPFT];
 };
 
 inline const PftTable& pft_table() {
@@ -110,6 +112,7 @@ inline const PftTable& pft_table() {
     /*rw*/ {16,16,18,8.7,12.5,15.1,10.4,7.5,6.1,6.1,.001,5.8,.001,5.8,.001,9.0,.001},
     /*tfcl*/ {.42,.248,.38,.345,.31,.73,2.4,.35,.997,.997,.95,.55,.95,.55,.95,2.4,.95},
     /*tvclst*/ {235,283,268,278,278,235,278,278,278,278,278,278,278,278,268,278,278},
+    /*clitt*/ {20,6,10,13,2,2,.3,.3,0,0,2,2,0,0,0,0,0},
   };
   return t;
 }

@@ -312,23 +312,37 @@ def test_snow_grid_full_year_against_oracle(oracle, runtime):
         assert np.mean(np.abs(gs[k] - o[k]) <= np.maximum(1e-3 * np.abs(o[k]), 0.5)) >= 0.95, k
 
 
-def test_soil_thermal_fix_switch_matches_oracle(oracle, runtime):
-    """soil_thermal_fix (total_soil_conductivity and its parameter set) on
-    snowy, freezing tiles against the FP64 oracle with the same switch, with
-    the same criterion as the default configuration: RMS and fraction of
-    tiles within tolerance against the reference's own FP32 build with the
-    switch on."""
+SWITCH_SETS = {
+    "soil_thermal_fix": dict(soil_thermal_fix=True),
+    "litter": dict(litter=True),
+    "l_rev_corr": dict(l_rev_corr=True),
+    "all": dict(medlyn=True, soil_thermal_fix=True, litter=True, l_rev_corr=True),
+}
+
+
+@pytest.mark.parametrize("which", list(SWITCH_SETS))
+def test_science_switches_match_oracle(oracle, runtime, which):
+    """The alternative science switches (soil_thermal_fix: conductivity and
+    soil heat parameters; litter: litter resistances in define_canopy;
+    l_rev_corr: revised soil-coupling derivatives; and all of them with
+    medlyn) on snowy, freezing tiles against the FP64 oracle with the same
+    switches, with the default configuration's criterion: RMS and fraction
+    of tiles within tolerance against the reference's own FP32 build with
+    the same switches.  Each switch is live on the GPU (results move)."""
+    sw = SWITCH_SETS[which]
     ts = W.snow_grid(8000, nsteps=24)
-    gs, gd, os_, od, F = H.run_pair(ts, 24, soil_thermal_fix=True)
+    gs, gd, os_, od, F = H.run_pair(ts, 24, **sw)
     rep = H.parity_report(gs, gd, os_, od)
     st32 = oracle.init_state(ts, 1)
-    od32 = oracle.run(ts, st32, 24, forcing=F, precision=1, soil_thermal_fix=True)
+    od32 = oracle.run(ts, st32, 24, forcing=F, precision=1, **sw)
     os32 = oracle.split_state(st32)
     ref = H.parity_report({k: os32[k] for k in H.STATE_FIELDS}, {gk: od32[ok] for gk, ok in H.DIAG_MAP.items()},
                           os_, od)
-    for k in ("tgg", "tggsn", "wb", "wbice", "ga_d", "fe_d", "fh_d", "tv_d"):
+    for k in ("tgg", "tggsn", "wb", "wbice", "ga_d", "fe_d", "fh_d", "tv_d", "fes"):
         assert rep[k]["rms"] <= max(rep[k]["tol"], 3 * ref[k]["rms"]), (k, rep[k], ref[k])
         assert rep[k]["frac_within"] >= min(0.995, ref[k]["frac_within"] - 0.005), (k, rep[k], ref[k])
-    # and the switch is live on the GPU: the default run differs
-    g0, _, o0, _, _ = H.run_pair(ts, 24)
-    assert np.abs(np.asarray(g0["tgg"]) - np.asarray(gs["tgg"])).max() > 0.05
+    assert np.abs(gd["ebal"]).max() < 0.05
+    g0, d0, _, _, _ = H.run_pair(ts, 24)
+    moved = np.abs(np.asarray(g0["tgg"]) - np.asarray(gs["tgg"])).max()
+    moved_fh = np.abs(np.asarray(d0["fhs"]) - np.asarray(gd["fhs"])).max()
+    assert max(moved, moved_fh) > 0.05, (which, moved, moved_fh)

@@ -191,3 +191,23 @@ def test_soil_thermal_fix_switch_is_live_and_conserves(oracle):
     assert dt.max() > 0.05                       # the switch changes soil temperatures
     assert np.isfinite(np.asarray(s1["tgg"])).all()
     assert 200.0 < np.asarray(s1["tgg"]).min() and np.asarray(s1["tgg"]).max() < 340.0
+
+
+@pytest.mark.parametrize("switch", ["litter", "l_rev_corr"])
+def test_canopy_switches_are_live_and_conserve(oracle, switch):
+    """litter (litter resistances to soil heat and vapour transfer) and
+    l_rev_corr (revised soil-coupling derivatives) change the soil fluxes
+    and temperatures, and the energy and leaf balances still close."""
+    ts = W.snow_grid(mp=400, nsteps=48)
+    res = {}
+    for on in (False, True):
+        st = oracle.init_state(ts, 0)
+        d = oracle.run(ts, st, 48, **{switch: on})
+        res[on] = (oracle.split_state(st), d)
+    (s0, d0), (s1, d1) = res[False], res[True]
+    assert np.abs(d1["ebal"]).max() < 1e-8
+    assert np.abs(d1["drybal"]).max() < 1e-6
+    assert np.abs(np.asarray(s1["tgg"]) - np.asarray(s0["tgg"])).max() > 0.01
+    if switch == "litter":
+        # the litter resistance moves the soil sensible heat flux
+        assert np.abs(d1["fhs"] - d0["fhs"]).max() > 1.0
