@@ -14,7 +14,7 @@ LIB = os.path.join(LIBDIR, "libcablegpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["cablegpu.cu", "phase_a.cu", "phase_b.cu", "phase_c1.cu", "phase_c2.cu", "phase_c3.cu", "tables.cpp",
-           "surrogate.cu"]
+           "surrogate.cu", "cgio.cpp"]
 # Per-file extra flags: the canopy phase is FP32-only and division-heavy, so
 # it uses the approximate division / exp intrinsics; the phases that carry
 # FP64 state keep IEEE semantics.  CG_MAXNREG caps registers per thread,

@@ -4,14 +4,17 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <condition_variable>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/cablegpu.h"
 #include "phase_kernels.cuh"
 #include "surrogate.cuh"
 #include "surrogate_host.h"
+#include "cgio.h"
 
 using namespace cg;
 
@@ -976,6 +979,245 @@ int cablegpu_autotune(const cablegpu_tiles* tiles, int device, int sample_tiles,
 }
 
 long long cablegpu_launch_count(cablegpu_ctx* c) { return c ? c->launches : -1; }
+
+// ---------------------------------------------------------------- files
+namespace {
+
+cgio::Entry file_entry(const char* name, uint32_t dtype, uint32_t width) {
+  cgio::Entry e{};
+  std::strncpy(e.name, name, sizeof(e.name) - 1);
+  e.dtype = dtype;
+  e.width = width;
+  return e;
+}
+
+// the registry fields a restart file carries: tile description and state
+bool in_restart(const FieldDef& f) { return f.kind == CABLEGPU_KIND_PARAM || f.kind == CABLEGPU_KIND_STATE; }
+uint32_t file_dtype(const FieldDef& f) { return f.st == S_DF ? cgio::kDF32 : (uint32_t)f.dtype; }
+
+}  // namespace
+
+int cablegpu_restart_write(cablegpu_ctx* c, const char* path, int ktau) {
+  if (!c || !path) return fail(c, CABLEGPU_ERR_ARG, "restart_write: null argument");
+  const auto& reg = registry();
+  std::vector<cgio::Entry> entries;
+  std::vector<int> ids;
+  for (int i = 0; i < (int)reg.size(); ++i)
+    if (in_restart(reg[i])) { entries.push_back(file_entry(reg[i].name, file_dtype(reg[i]), reg[i].nlayer)); ids.push_back(i); }
+  cgio::File f;
+  if (cgio::create(f, path, CABLEGPU_FILE_RESTART, (uint64_t)c->mp, entries, 1, ktau, c->forc.doy0, c->forc.dels))
+    return fail(c, CABLEGPU_ERR_IO, "restart_write: " + f.err);
+  std::vector<char> host((size_t)c->mp * CG_MS * 8);
+  int rc = CABLEGPU_OK;
+  for (size_t j = 0; j < ids.size() && rc == CABLEGPU_OK; ++j) {
+    const FieldDef& fd = reg[ids[j]];
+    if (fd.st == S_DF) {
+      // the exact word pairs: high rows then low rows, as stored
+      const int grid = (c->mp + 255) / 256;
+      gather_out_kernel<float, float><<<grid, 256, 0, c->stream>>>((float*)c->d_stage, (const float*)c->field_ptr[ids[j]],
+                                                                   c->d_order, c->mp, c->ld, 2 * fd.nlayer);
+      CG_CUDA(c, cudaGetLastError());
+      CG_CUDA(c, cudaMemcpyAsync(host.data(), c->d_stage, (size_t)c->mp * 2 * fd.nlayer * sizeof(float),
+                                 cudaMemcpyDeviceToHost, c->stream));
+      CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    } else {
+      rc = cablegpu_get_field(c, ids[j], host.data());
+    }
+    if (rc == CABLEGPU_OK && cgio::write_block(f, 0, (int)j, host.data()))
+      rc = fail(c, CABLEGPU_ERR_IO, "restart_write: " + f.err);
+  }
+  cgio::close(f);
+  return rc;
+}
+
+int cablegpu_restart_read(cablegpu_ctx* c, const char* path, int* ktau) {
+  if (!c || !path) return fail(c, CABLEGPU_ERR_ARG, "restart_read: null argument");
+  cgio::File f;
+  if (cgio::open_read(f, path)) return fail(c, CABLEGPU_ERR_IO, "restart_read: " + f.err);
+  struct Closer { cgio::File& f; ~Closer() { cgio::close(f); } } closer{f};
+  if (f.h.kind != CABLEGPU_FILE_RESTART || f.h.nrecords != 1)
+    return fail(c, CABLEGPU_ERR_IO, "restart_read: not a restart file");
+  if (f.h.mp != (uint64_t)c->mp) return fail(c, CABLEGPU_ERR_ARG, "restart_read: the file's tile count differs");
+  const auto& reg = registry();
+  std::vector<char> host((size_t)c->mp * CG_MS * 8), mine((size_t)c->mp * 4);
+  // the tiles must be the context's
+  for (const char* name : {"iveg", "isoilm"}) {
+    const int id = cablegpu_field_id(name), k = cgio::find(f, name);
+    if (k < 0 || f.fields[k].dtype != cgio::kI32 || f.fields[k].width != 1)
+      return fail(c, CABLEGPU_ERR_IO, std::string("restart_read: no valid field ") + name);
+    if (cgio::read_block(f, 0, k, host.data())) return fail(c, CABLEGPU_ERR_IO, "restart_read: read failed");
+    int rc = cablegpu_get_field(c, id, mine.data());
+    if (rc) return rc;
+    if (std::memcmp(host.data(), mine.data(), (size_t)c->mp * 4) != 0)
+      return fail(c, CABLEGPU_ERR_ARG, std::string("restart_read: the file's ") + name + " differs from the context's");
+  }
+  for (int i = 0; i < (int)reg.size(); ++i) {
+    const FieldDef& fd = reg[i];
+    if (fd.kind != CABLEGPU_KIND_STATE) continue;
+    const int k = cgio::find(f, fd.name);
+    if (k < 0) return fail(c, CABLEGPU_ERR_IO, std::string("restart_read: missing field ") + fd.name);
+    if (f.fields[k].dtype != file_dtype(fd) || f.fields[k].width != (uint32_t)fd.nlayer)
+      return fail(c, CABLEGPU_ERR_IO, std::string("restart_read: wrong type or width of ") + fd.name);
+    if (cgio::read_block(f, 0, k, host.data())) return fail(c, CABLEGPU_ERR_IO, "restart_read: read failed");
+    if (fd.st == S_DF) {
+      const int grid = (c->mp + 255) / 256;
+      CG_CUDA(c, cudaMemcpyAsync(c->d_stage, host.data(), (size_t)c->mp * 2 * fd.nlayer * sizeof(float),
+                                 cudaMemcpyHostToDevice, c->stream));
+      scatter_in_kernel<float, float><<<grid, 256, 0, c->stream>>>((float*)c->field_ptr[i], (const float*)c->d_stage,
+                                                                   c->d_order, c->mp, c->ld, 2 * fd.nlayer);
+      CG_CUDA(c, cudaGetLastError());
+      CG_CUDA(c, cudaStreamSynchronize(c->stream));
+    } else {
+      int rc = cablegpu_set_field(c, i, host.data());
+      if (rc) return rc;
+    }
+  }
+  if (ktau) *ktau = f.h.ktau;
+  return CABLEGPU_OK;
+}
+
+int cablegpu_forcing_file_write(const char* path, int mp, int nsteps, int doy0, float dels, const float* forcing) {
+  if (!path || mp < 1 || nsteps < 1 || !forcing || !(dels > 0.f)) return CABLEGPU_ERR_ARG;
+  cgio::File f;
+  if (cgio::create(f, path, CABLEGPU_FILE_FORCING, (uint64_t)mp, {file_entry("met", cgio::kF32, CG_NFORC)},
+                   (uint32_t)nsteps, 1, doy0, dels))
+    return CABLEGPU_ERR_IO;
+  int rc = CABLEGPU_OK;
+  for (int n = 0; n < nsteps && rc == CABLEGPU_OK; ++n)
+    if (cgio::write_block(f, (uint32_t)n, 0, forcing + (size_t)n * CG_NFORC * mp)) rc = CABLEGPU_ERR_IO;
+  cgio::close(f);
+  return rc;
+}
+
+int cablegpu_file_info(const char* path, int* kind, long long* mp, int* nrecords, int* nfields, int* ktau, int* doy0,
+                       float* dels) {
+  cgio::File f;
+  if (cgio::open_read(f, path)) { cgio::close(f); return CABLEGPU_ERR_IO; }
+  if (kind) *kind = (int)f.h.kind;
+  if (mp) *mp = (long long)f.h.mp;
+  if (nrecords) *nrecords = (int)f.h.nrecords;
+  if (nfields) *nfields = (int)f.h.nfields;
+  if (ktau) *ktau = f.h.ktau;
+  if (doy0) *doy0 = f.h.doy0;
+  if (dels) *dels = f.h.dels;
+  cgio::close(f);
+  return CABLEGPU_OK;
+}
+
+int cablegpu_run_forcing_file(cablegpu_ctx* c, const char* forcing_path, int record0, int ktau0, int nsteps,
+                              const char* output_path) {
+  if (!c || !forcing_path || record0 < 0 || ktau0 < 1 || nsteps < 0)
+    return fail(c, CABLEGPU_ERR_ARG, "run_forcing_file: bad argument");
+  cgio::File in, out;
+  if (cgio::open_read(in, forcing_path)) return fail(c, CABLEGPU_ERR_IO, "run_forcing_file: " + in.err);
+  struct Closer { cgio::File& a; cgio::File& b; ~Closer() { cgio::close(a); cgio::close(b); } } closer{in, out};
+  if (in.h.kind != CABLEGPU_FILE_FORCING || in.h.mp != (uint64_t)c->mp || in.fields.size() != 1 ||
+      cgio::find(in, "met") != 0 || in.fields[0].dtype != cgio::kF32 || in.fields[0].width != CG_NFORC ||
+      in.fields[0].offset != 0 || !(in.h.dels > 0.f))
+    return fail(c, CABLEGPU_ERR_IO, "run_forcing_file: not a forcing file for this context's tiles");
+  if ((long long)record0 + nsteps > (long long)in.h.nrecords)
+    return fail(c, CABLEGPU_ERR_ARG, "run_forcing_file: the file holds fewer records than asked for");
+  if (nsteps == 0) return CABLEGPU_OK;
+  const float dels = in.h.dels;
+  if (output_path &&
+      cgio::create(out, output_path, CABLEGPU_FILE_OUTPUT, (uint64_t)c->mp, {file_entry("out", cgio::kF32, CG_NOUT)},
+                   (uint32_t)nsteps, ktau0, in.h.doy0, dels))
+    return fail(c, CABLEGPU_ERR_IO, "run_forcing_file: " + out.err);
+  constexpr int NB = 3;   // host buffers in flight
+  const size_t fbytes = sizeof(float) * CG_NFORC * (size_t)c->mp, obytes = sizeof(float) * CG_NOUT * (size_t)c->mp;
+  float* fin[NB] = {};
+  float* fout[NB] = {};
+  cudaEvent_t ev_in[NB] = {}, ev_out[NB] = {};
+  auto release = [&]() {
+    for (int b = 0; b < NB; ++b) {
+      if (fin[b]) cudaFreeHost(fin[b]);
+      if (fout[b]) cudaFreeHost(fout[b]);
+      if (ev_in[b]) cudaEventDestroy(ev_in[b]);
+      if (ev_out[b]) cudaEventDestroy(ev_out[b]);
+    }
+  };
+  for (int b = 0; b < NB; ++b) {
+    if (cudaMallocHost(&fin[b], fbytes) != cudaSuccess || cudaMallocHost(&fout[b], obytes) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev_in[b], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev_out[b], cudaEventDisableTiming) != cudaSuccess) {
+      release();
+      return fail(c, CABLEGPU_ERR_CUDA, "run_forcing_file: cannot allocate pinned buffers");
+    }
+  }
+  std::mutex m;
+  std::condition_variable cv;
+  int filled = 0, submitted = 0, written = 0;
+  bool abort = false;
+  std::string err;
+  auto stop = [&](const std::string& why) {
+    std::lock_guard<std::mutex> g(m);
+    if (!abort) { abort = true; err = why; }
+    cv.notify_all();
+  };
+  // reader: record n into buffer n % NB once the upload of step n - NB is done
+  std::thread reader([&]() {
+    cudaSetDevice(c->device);
+    for (int n = 0; n < nsteps; ++n) {
+      const int b = n % NB;
+      if (n >= NB) {
+        std::unique_lock<std::mutex> lk(m);
+        cv.wait(lk, [&] { return abort || submitted > n - NB; });
+        if (abort) return;
+        lk.unlock();
+        if (cudaEventSynchronize(ev_in[b]) != cudaSuccess) { stop("run_forcing_file: upload failed"); return; }
+      }
+      if (cgio::read_record_prefix(in, (uint32_t)(record0 + n), fin[b], fbytes)) {
+        stop("run_forcing_file: reading forcing record " + std::to_string(record0 + n) + " failed");
+        return;
+      }
+      std::lock_guard<std::mutex> g(m);
+      filled = n + 1;
+      cv.notify_all();
+    }
+  });
+  // writer: output of step n once its download is done
+  std::thread writer([&]() {
+    if (!output_path) return;
+    cudaSetDevice(c->device);
+    for (int n = 0; n < nsteps; ++n) {
+      const int b = n % NB;
+      {
+        std::unique_lock<std::mutex> lk(m);
+        cv.wait(lk, [&] { return abort || submitted > n; });
+        if (abort && submitted <= n) return;
+      }
+      if (cudaEventSynchronize(ev_out[b]) != cudaSuccess) { stop("run_forcing_file: download failed"); return; }
+      if (cgio::write_block(out, (uint32_t)n, 0, fout[b])) { stop("run_forcing_file: " + out.err); return; }
+      std::lock_guard<std::mutex> g(m);
+      written = n + 1;
+      cv.notify_all();
+    }
+  });
+  int rc = CABLEGPU_OK;
+  for (int n = 0; n < nsteps; ++n) {
+    const int b = n % NB;
+    {
+      std::unique_lock<std::mutex> lk(m);
+      cv.wait(lk, [&] { return abort || (filled > n && (!output_path || n < NB || written > n - NB)); });
+      if (abort) break;
+    }
+    rc = cablegpu_step_host(c, ktau0 + n, dels, fin[b], fout[b]);
+    if (rc == CABLEGPU_OK && (cudaEventRecord(ev_in[b], c->cstream) != cudaSuccess ||
+                              cudaEventRecord(ev_out[b], c->dstream) != cudaSuccess))
+      rc = fail(c, CABLEGPU_ERR_CUDA, "run_forcing_file: event record failed");
+    if (rc) { stop("run_forcing_file: step failed"); break; }
+    std::lock_guard<std::mutex> g(m);
+    submitted = n + 1;
+    cv.notify_all();
+  }
+  reader.join();
+  writer.join();
+  const int rs = cablegpu_synchronize(c);
+  release();
+  if (rc) return rc;
+  if (abort) return fail(c, CABLEGPU_ERR_IO, err);
+  return rs;
+}
 
 int cablegpu_param_table(int table, const char* name, float* out, int n) {
   if (!name || !out) return CABLEGPU_ERR_ARG;

@@ -25,7 +25,8 @@ FORCING_FIELDS = ["fsd_vis", "fsd_nir", "fld", "precip", "precip_sn", "tk", "pmb
 OUTPUT_FIELDS = ["fe", "fh", "fgpp", "frday", "tv", "rnet", "ga", "trad"]
 _NP = {F32: np.float32, F64: np.float64, I32: np.int32}
 
-ERRORS = {-1: "CABLEGPU_ERR_ARG", -2: "CABLEGPU_ERR_CUDA", -3: "CABLEGPU_ERR_NONFINITE", -4: "CABLEGPU_ERR_STATE"}
+ERRORS = {-1: "CABLEGPU_ERR_ARG", -2: "CABLEGPU_ERR_CUDA", -3: "CABLEGPU_ERR_NONFINITE", -4: "CABLEGPU_ERR_STATE",
+          -5: "CABLEGPU_ERR_IO"}
 
 # Every symbol include/cablegpu.h declares.
 EXPORTS = [
@@ -38,6 +39,8 @@ EXPORTS = [
     "cablegpu_surrogate_weights", "cablegpu_set_surrogate", "cablegpu_surrogate_stats", "cablegpu_mlp_sizes",
     "cablegpu_mlp_forward", "cablegpu_mlp_grad", "cablegpu_mlp_fit", "cablegpu_mlp_last_error",
     "cablegpu_set_blocks", "cablegpu_get_config", "cablegpu_autotune", "cablegpu_step_host",
+    "cablegpu_restart_write", "cablegpu_restart_read", "cablegpu_forcing_file_write", "cablegpu_file_info",
+    "cablegpu_run_forcing_file",
 ]
 NOALLOC_MAX_TILES = 65536
 # science switch bits of cablegpu_set_options (include/cablegpu.h)
@@ -50,6 +53,30 @@ SW_L_REV_CORR = 8
 def switch_mask(medlyn=False, soil_thermal_fix=False, litter=False, l_rev_corr=False) -> int:
     return ((SW_MEDLYN if medlyn else 0) | (SW_SOIL_THERMAL_FIX if soil_thermal_fix else 0) |
             (SW_LITTER if litter else 0) | (SW_L_REV_CORR if l_rev_corr else 0))
+
+
+def forcing_file_write(path, forcing, doy0: int = 1, dels: float = 1800.0):
+    """Binary forcing file from [nsteps][13][mp] float32 met forcing."""
+    f = np.ascontiguousarray(forcing, np.float32)
+    assert f.ndim == 3 and f.shape[1] == NFORCING
+    L = load()
+    rc = L.cablegpu_forcing_file_write(os.fsencode(path), f.shape[2], f.shape[0], int(doy0), float(dels),
+                                       _ptr(f, C.c_float))
+    if rc != 0:
+        raise CableGPUError(rc, "forcing_file_write failed for %s" % path)
+
+
+def file_info(path) -> dict:
+    """Header of a restart, forcing or output file."""
+    L = load()
+    kind, nrec, nf, ktau, doy0 = (C.c_int() for _ in range(5))
+    mp, dels = C.c_longlong(), C.c_float()
+    rc = L.cablegpu_file_info(os.fsencode(path), C.byref(kind), C.byref(mp), C.byref(nrec), C.byref(nf),
+                              C.byref(ktau), C.byref(doy0), C.byref(dels))
+    if rc != 0:
+        raise CableGPUError(rc, "not a readable CABLEGPU file: %s" % path)
+    return {"kind": kind.value, "mp": mp.value, "nrecords": nrec.value, "nfields": nf.value, "ktau": ktau.value,
+            "doy0": doy0.value, "dels": dels.value}
 
 PHASES = ["radiation", "canopy", "snow_pack", "soil_heat", "soil_water", "surrogate_net"]
 
@@ -124,6 +151,12 @@ def load(build_if_missing: bool = True):
     L.cablegpu_launch_count.argtypes = [vp]
     L.cablegpu_launch_count.restype = C.c_longlong
     L.cablegpu_param_table.argtypes = [ip, C.c_char_p, C.POINTER(C.c_float), ip]
+    L.cablegpu_restart_write.argtypes = [vp, C.c_char_p, ip]
+    L.cablegpu_restart_read.argtypes = [vp, C.c_char_p, C.POINTER(ip)]
+    L.cablegpu_forcing_file_write.argtypes = [C.c_char_p, ip, ip, ip, C.c_float, C.POINTER(C.c_float)]
+    L.cablegpu_file_info.argtypes = [C.c_char_p, C.POINTER(ip), C.POINTER(C.c_longlong), C.POINTER(ip), C.POINTER(ip),
+                                     C.POINTER(ip), C.POINTER(ip), C.POINTER(C.c_float)]
+    L.cablegpu_run_forcing_file.argtypes = [vp, C.c_char_p, ip, ip, ip, C.c_char_p]
     L.cablegpu_last_error.argtypes = [vp]
     L.cablegpu_last_error.restype = C.c_char_p
     _lib = L
@@ -329,6 +362,23 @@ class CableGPU:
 
     def synchronize(self):
         self._check(self.L.cablegpu_synchronize(self.h))
+
+    # ------------------------------------------------------------------ files
+    def restart_write(self, path, ktau: int):
+        """Binary restart file of the state after step ``ktau``."""
+        self._check(self.L.cablegpu_restart_write(self.h, os.fsencode(path), int(ktau)))
+
+    def restart_read(self, path) -> int:
+        """Loads a restart file's state; returns the step it was written after."""
+        k = C.c_int()
+        self._check(self.L.cablegpu_restart_read(self.h, os.fsencode(path), C.byref(k)))
+        return k.value
+
+    def run_forcing_file(self, forcing_path, ktau0: int, nsteps: int, record0: int = 0, output_path=None):
+        """Steps ktau0.. on the records record0.. of a forcing file, with file
+        reads and output writes overlapping the steps."""
+        self._check(self.L.cablegpu_run_forcing_file(self.h, os.fsencode(forcing_path), int(record0), int(ktau0),
+                                                     int(nsteps), os.fsencode(output_path) if output_path else None))
 
     def run_timed(self, ktau0, nsteps, dels=1800.0) -> float:
         ms = C.c_float()

@@ -42,10 +42,12 @@ extern "C" {
 #define CABLEGPU_ERR_CUDA (-2)       /* a CUDA runtime call failed */
 #define CABLEGPU_ERR_NONFINITE (-3)  /* a step produced a non-finite output flux */
 #define CABLEGPU_ERR_STATE (-4)      /* call not valid in the context's current state */
+#define CABLEGPU_ERR_IO (-5)         /* a file could not be read or written, or is not a valid file */
 
 #define CABLEGPU_F32 0
 #define CABLEGPU_F64 1
 #define CABLEGPU_I32 2
+#define CABLEGPU_DF32 3   /* files only: double-FP32 pairs, `width` high rows then `width` low rows */
 
 #define CABLEGPU_KIND_PARAM 0   /* static per-tile parameter (veg / soil / forcing jitter) */
 #define CABLEGPU_KIND_STATE 1   /* prognostic state carried between steps */
@@ -212,6 +214,56 @@ int cablegpu_get_config(cablegpu_ctx* ctx, int* order, int* block5);
  * choice. */
 int cablegpu_autotune(const cablegpu_tiles* tiles, int device, int sample_tiles, int nsteps, int* order_out,
                       int* block5_out, float* ms_out);
+
+/* ---- Binary restart, forcing and output files ------------------------------
+ * Binary equivalents of the reference's netCDF files: the restart file
+ * (cable_output_impl.F90 write_restart :278-311, cable_initialise.F90
+ * get_restart_data :163-664), the met file read every step
+ * (cable_input.F90 get_met_data) and the per-step output file.  One
+ * container, little-endian: a 128-byte header (magic "CABLEGPU", version 1,
+ * kind, mp, field and record counts, ktau, doy0, dels, record size), a
+ * directory of 48-byte entries (name[32], dtype, width, offset), then from
+ * byte 4096 the records, 4096-byte aligned; a record holds every field as
+ * one [width][mp] block in caller tile order, 64-byte aligned.
+ *   restart: 1 record; the tile description (KIND_PARAM fields) and every
+ *            prognostic field (KIND_STATE), named as the field registry, the
+ *            double-FP32 soil water and ice as their exact word pairs
+ *            (CABLEGPU_DF32), so a resumed run is bitwise the
+ *            uninterrupted one
+ *   forcing: one record per step, one field "met" of width
+ *            CABLEGPU_NFORCING ([CABLEGPU_NFORCING][mp] float, rows as for
+ *            cablegpu_set_forcing)
+ *   output:  one record per step, one field "out" ([8][mp] float, the rows of
+ *            the field "out") */
+#define CABLEGPU_FILE_RESTART 1
+#define CABLEGPU_FILE_FORCING 2
+#define CABLEGPU_FILE_OUTPUT 3
+
+/* Writes the context's state after step `ktau` to `path`.  Synchronous. */
+int cablegpu_restart_write(cablegpu_ctx* ctx, const char* path, int ktau);
+/* Loads the prognostic state of a restart file into the context; the file's
+ * tiles must be the context's (same mp, iveg and isoilm in the same caller
+ * order; CABLEGPU_ERR_ARG otherwise) and hold every prognostic field.
+ * *ktau (may be NULL) receives the step the file was written after: the
+ * run continues with ktau + 1. */
+int cablegpu_restart_read(cablegpu_ctx* ctx, const char* path, int* ktau);
+/* Writes a forcing file of `nsteps` records from host memory
+ * ([nsteps][CABLEGPU_NFORCING][mp] float).  No context or GPU needed. */
+int cablegpu_forcing_file_write(const char* path, int mp, int nsteps, int doy0, float dels, const float* forcing);
+/* Header of any of the three files (each pointer may be NULL).  No context or
+ * GPU needed. */
+int cablegpu_file_info(const char* path, int* kind, long long* mp, int* nrecords, int* nfields, int* ktau, int* doy0,
+                       float* dels);
+/* Runs steps ktau0 .. ktau0+nsteps-1 on the records record0 .. of a forcing
+ * file (its dels), through the pipelined host path of cablegpu_step_host: a
+ * reader thread fills three pinned buffers from the file ahead of the GPU, and
+ * when `output_path` is not NULL a writer thread appends each step's output
+ * record to a new output file behind it.  Returns when every step is done and
+ * written: the offline driver's time loop (cable_serial.F90:493-738:
+ * get_met_data, cbm, cable_output_write) with the file I/O overlapping the
+ * steps. */
+int cablegpu_run_forcing_file(cablegpu_ctx* ctx, const char* forcing_path, int record0, int ktau0, int nsteps,
+                              const char* output_path);
 
 /* Copies a built-in parameter table (no context or GPU needed): table 0 is
  * the per-plant-type table of pft_params.nml with derived entries "dleaf"
