@@ -287,8 +287,9 @@ def test_snow_grid_full_year_against_oracle(oracle, runtime):
     threshold events: two FP32 builds of the reference algorithm (the
     REAL=FP32 / r_2=FP64 mix compiled with and without FMA contraction)
     each flip a different 2-4 tiles by tens of kg/m2 of snow over the
-    year, so snow depth is checked as the fraction of tiles within
-    1 kg/m2.  The water balance stays as closed as the FP64 oracle's
+    year, and 0-2 tiles by more than 0.1 K of soil temperature, so snow
+    depth is checked as the fraction of tiles within 1 kg/m2 and soil
+    temperature as a count of flipped tiles plus the RMS of the others.  The water balance stays as closed as the FP64 oracle's
     (flux-form soil water update) and soil moisture and temperature do not
     drift."""
     R = runtime
@@ -303,10 +304,15 @@ def test_snow_grid_full_year_against_oracle(oracle, runtime):
     o = {k: np.asarray(v, np.float64).reshape(gs[k].shape) for k, v in oracle.split_state(st).items() if k in gs}
     rms = lambda k: float(np.sqrt(np.mean((gs[k] - o[k]) ** 2)))
     # measured: wbal_tot rms 0.011 mm (the REAL=FP32 oracle: 0.011), wb rms
-    # 2.2e-4, tgg rms 0.02 K, snow depth within 1 kg/m2 on 252 of 256 tiles
+    # 2.2e-4, snow depth within 1 kg/m2 on 252 of 256 tiles; soil
+    # temperature: 0-2 tiles flipped beyond 0.1 K (the FP32 oracle builds:
+    # 0-2), the rest within 0.01 K RMS
     assert rms("wbal_tot") < 0.05                                       # mm over the year
     assert rms("wb") < 5e-4                                             # m3/m3
-    assert rms("tgg") < 0.05                                            # K
+    dt = np.abs(gs["tgg"] - o["tgg"])
+    flipped = dt.max(axis=0) > 0.1                                      # K, per tile
+    assert flipped.sum() <= 4, np.where(flipped)[0]
+    assert np.sqrt(np.mean(dt[:, ~flipped] ** 2)) < 0.02                # K
     assert np.mean(np.abs(gs["snowd"] - o["snowd"]) <= 1.0) >= 0.95     # kg/m2
     for k in ("csoil", "cplant"):
         assert np.mean(np.abs(gs[k] - o[k]) <= np.maximum(1e-3 * np.abs(o[k]), 0.5)) >= 0.95, k
