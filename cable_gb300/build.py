@@ -49,7 +49,7 @@ def sources():
 
 
 def _deps():
-    deps = sources()
+    deps = sources() + [os.path.abspath(__file__)]   # compiler flags live here
     for d in (CSRC, INCLUDE):
         deps += [os.path.join(d, f) for f in os.listdir(d) if f.endswith((".h", ".cuh", ".hpp"))]
     return deps
