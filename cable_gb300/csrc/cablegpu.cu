@@ -321,6 +321,11 @@ StepParams make_params(cablegpu_ctx* c, int ktau, float dels) {
   p.thermal_fix = c->thermal_fix;
   p.litter = c->litter;
   p.rev_corr = c->rev_corr;
+  p.fwsoil_mode = (c->switches & CABLEGPU_SW_FWSOIL_NONLINEAR) ? 1 : ((c->switches & CABLEGPU_SW_FWSOIL_LAI_KTAUL) ? 2 : 0);
+  p.potev_pm = (c->switches & CABLEGPU_SW_POTEV_PM) ? 1 : 0;
+  p.reduce_soilevp = (c->switches & CABLEGPU_SW_NEW_REDUCE_SOILEVP) ? 1 : 0;
+  p.runoff_speed = (c->switches & CABLEGPU_SW_NEW_RUNOFF_SPEED) ? 1 : 0;
+  p.soil_resp_off = (c->switches & CABLEGPU_SW_DIAG_SOIL_RESP_OFF) ? 1 : 0;
   p.forc = c->forc;
   p.forc.dels = dels;
   p.step_index = ktau - 1;
@@ -610,8 +615,12 @@ int cablegpu_set_synthetic_forcing(cablegpu_ctx* c, unsigned long long seed, int
 
 int cablegpu_set_options(cablegpu_ctx* c, int switches, int diag, int capture_forcing) {
   if (!c) return CABLEGPU_ERR_ARG;
-  if (switches & ~(CABLEGPU_SW_MEDLYN | CABLEGPU_SW_SOIL_THERMAL_FIX | CABLEGPU_SW_LITTER | CABLEGPU_SW_L_REV_CORR))
-    return fail(c, CABLEGPU_ERR_ARG, "set_options: unknown switch bit");
+  const int known = CABLEGPU_SW_MEDLYN | CABLEGPU_SW_SOIL_THERMAL_FIX | CABLEGPU_SW_LITTER | CABLEGPU_SW_L_REV_CORR |
+                    CABLEGPU_SW_FWSOIL_NONLINEAR | CABLEGPU_SW_FWSOIL_LAI_KTAUL | CABLEGPU_SW_POTEV_PM |
+                    CABLEGPU_SW_NEW_REDUCE_SOILEVP | CABLEGPU_SW_NEW_RUNOFF_SPEED | CABLEGPU_SW_DIAG_SOIL_RESP_OFF;
+  if (switches & ~known) return fail(c, CABLEGPU_ERR_ARG, "set_options: unknown switch bit");
+  if ((switches & CABLEGPU_SW_FWSOIL_NONLINEAR) && (switches & CABLEGPU_SW_FWSOIL_LAI_KTAUL))
+    return fail(c, CABLEGPU_ERR_ARG, "set_options: two fwsoil_switch values");
   c->medlyn = (switches & CABLEGPU_SW_MEDLYN) ? 1 : 0;
   c->litter = (switches & CABLEGPU_SW_LITTER) ? 1 : 0;
   c->rev_corr = (switches & CABLEGPU_SW_L_REV_CORR) ? 1 : 0;
@@ -991,8 +1000,12 @@ cgio::Entry file_entry(const char* name, uint32_t dtype, uint32_t width) {
   return e;
 }
 
-// the registry fields a restart file carries: tile description and state
-bool in_restart(const FieldDef& f) { return f.kind == CABLEGPU_KIND_PARAM || f.kind == CABLEGPU_KIND_STATE; }
+// the registry fields a restart file carries: tile description, state and
+// the last step's outputs (the reference's restart holds ga and trad; ga is
+// read again by ssnow_potev = 'P-M')
+bool in_restart(const FieldDef& f) {
+  return f.kind == CABLEGPU_KIND_PARAM || f.kind == CABLEGPU_KIND_STATE || f.kind == CABLEGPU_KIND_OUTPUT;
+}
 uint32_t file_dtype(const FieldDef& f) { return f.st == S_DF ? cgio::kDF32 : (uint32_t)f.dtype; }
 
 }  // namespace
@@ -1053,7 +1066,7 @@ int cablegpu_restart_read(cablegpu_ctx* c, const char* path, int* ktau) {
   }
   for (int i = 0; i < (int)reg.size(); ++i) {
     const FieldDef& fd = reg[i];
-    if (fd.kind != CABLEGPU_KIND_STATE) continue;
+    if (fd.kind != CABLEGPU_KIND_STATE && fd.kind != CABLEGPU_KIND_OUTPUT) continue;
     const int k = cgio::find(f, fd.name);
     if (k < 0) return fail(c, CABLEGPU_ERR_IO, std::string("restart_read: missing field ") + fd.name);
     if (f.fields[k].dtype != file_dtype(fd) || f.fields[k].width != (uint32_t)fd.nlayer)

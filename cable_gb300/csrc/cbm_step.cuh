@@ -21,6 +21,11 @@ struct StepParams {
   int thermal_fix;   // cable_user%soil_thermal_fix
   int litter;        // cable_user%litter
   int rev_corr;      // cable_user%l_rev_corr
+  int fwsoil_mode;   // fwsoil_switch: 0 standard, 1 non-linear extrapolation, 2 Lai and Ktaul 2000
+  int potev_pm;      // ssnow_potev = 'P-M'
+  int reduce_soilevp;  // cable_user%l_new_reduce_soilevp
+  int runoff_speed;  // cable_user%l_new_runoff_speed
+  int soil_resp_off; // diag_soil_resp = 'OFF'
   CgForcingSpec forc;
   int step_index;    // 0-based counter for the synthetic forcing
 };
@@ -443,13 +448,53 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
 
   float zetar[NITER] = {0.0f, ZETPOS + 1.f, 0.f, 0.f};
   float us = 0.f, rt0 = 0.f, rt1 = 0.f, rt1usc = 0.f, rtsoil = ortsoil, cls = 1.f;
-  float fev = 0.f, fhv = 0.f, fnv = 0.f, fns = 0.f, fhs = 0.f, fe = 0.f, fh = 0.f, ga = 0.f, potev = 0.f;
+  float fev = 0.f, fhv = 0.f, fnv = 0.f, fns = 0.f, fhs = 0.f, fe = 0.f, fh = 0.f, potev = 0.f;
+  // canopy%ga persists between steps; read before it is set only by ssnow_potev = 'P-M' (the
+  // output row "ga" holds the last step's value)
+  float ga = P.potev_pm ? D.out[6 * ld + t] : 0.f;
   float fes = 0.f, fess = 0.f, fesp = 0.f, fevw = 0.f, fhvw = 0.f, fevw_pot = 0.f, fevc = 0.f, epot = 0.f;
   float ecy = 0.f, hcy = 0.f, rny = 0.f, frday = 0.f, fpn = 0.f, fwsoil = 1.0f, qstss = 0.f;
   int passes_total = 0;
   // surrogate and harvest bookkeeping
   unsigned int sur_tried = 0, sur_accepted = 0;
   const bool harvesting = kHarvest && D.harvest != nullptr;
+  // soil water limitation of stomatal conductance, computed once in the
+  // first Monin-Obukhov iteration of the reference (cbl_dryLeaf.F90:168-181)
+  if (P.fwsoil_mode == 0) {   // fwsoil_calc_std (cbl_fwsoil.F90:13-38)
+    float rwater = 0.f;
+#pragma unroll
+    for (int k = 0; k < CG_MS; ++k)
+      rwater += froot[k] * fmaxf(1.0e-9f, fminf(1.0f, (wbliq0[k] - swilt) / (sfc - swilt)));
+    rwater = fmaxf(1.0e-9f, rwater);
+    fwsoil = P.medlyn ? fmaxf(1.0e-4f, fminf(1.0f, rwater)) : fmaxf(1.0e-9f, fminf(1.0f, vbeta * rwater));
+  } else if (P.fwsoil_mode == 1) {
+    // fwsoil_calc_non_linear (cbl_fwsoil.F90:44-88): quadratic through
+    // (swilt, 0), (midpoint, 0.9), (sfc, 1) of the root-weighted water
+    float sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < CG_MS; ++k) sum += froot[k] * fmaxf(0.0f, fminf(1.0f, wbliq0[k] - swilt));
+    float rwater = fmaxf(1.0e-9f, sum / (sfc - swilt));
+    rwater = swilt + rwater * (sfc - swilt);
+    const float x1 = swilt, x2 = swilt + (sfc - swilt) / 2.0f, x3 = sfc;
+    const float s2 = (rwater - x1) / (x2 - x1) * (rwater - x3) / (x2 - x3);
+    const float s3 = (rwater - x1) / (x3 - x1) * (rwater - x2) / (x3 - x2);
+    fwsoil = (rwater < sfc - 0.02f) ? fmaxf(0.f, fminf(1.f, 0.9f * s2 + s3)) : 1.0f;
+  } else {
+    // fwsoil_calc_Lai_Ktaul (cbl_fwsoil.F90:90-112); a layer drier than
+    // wilting takes the 1e-4 floor (a negative base to a non-integer
+    // power in the reference, compiler-dependent there)
+    const float ssat = ldf(S.ssat, so);
+    float fw = 0.f;
+#pragma unroll
+    for (int k = 0; k < CG_MS; ++k) {
+      const float avail = wbliq0[k] - swilt;
+      const float dummy = 0.01f / fmaxf(1.0e-3f, avail);
+      const float base = avail / ssat;
+      const float frw = (base > 0.f) ? fmaxf(1.0e-4f, __powf(base, dummy)) : 1.0e-4f;
+      fw = fminf(1.0f, fmaxf(fw, frw));
+    }
+    fwsoil = fw;
+  }
   for (int iter = 1; iter <= NITER; ++iter) {
     const float zi = zetar[iter - 1];
     // comp_friction_vel (cbl_friction_vel.F90:19-108)
@@ -482,14 +527,6 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
 
     // ------------------------------------------------ dryLeaf (cbl_dryLeaf.F90:10-666)
     {
-      if (iter == 1) {   // fwsoil_calc_std (cbl_fwsoil.F90:13-38)
-        float rwater = 0.f;
-#pragma unroll
-        for (int k = 0; k < CG_MS; ++k)
-          rwater += froot[k] * fmaxf(1.0e-9f, fminf(1.0f, (wbliq0[k] - swilt) / (sfc - swilt)));
-        rwater = fmaxf(1.0e-9f, rwater);
-        fwsoil = P.medlyn ? fmaxf(1.0e-4f, fminf(1.0f, rwater)) : fmaxf(1.0e-9f, fminf(1.0f, vbeta * rwater));
-      }
       // surrogate inputs: the state the first iteration starts from
       const float tlf_entry = tlfx;
       bool sampled = false;
@@ -735,7 +772,16 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
       if (snowd > 1.0f || tgg[0] == TFRZ) dq = fmaxf(-0.1e-3f, dq);
       float rhlitt, relitt;
       litter_resist(rhlitt, relitt);
-      potev = rho * rlam * dq / (rtsoil + relitt);
+      if (P.potev_pm) {
+        // Penman_Monteith (cbl_pot_evap_snow.F90:9-78): soil available
+        // energy fns - ga (ga of the previous iteration or step) and the
+        // canopy-air humidity deficit
+        const float cc1 = dsatdk / (dsatdk + psyc), cc2 = psyc / (dsatdk + psyc);
+        const float qsatfvar = qsatfjh(tvair - TFRZ, pmb);
+        potev = cc1 * (fns - ga) + cc2 * rho * rlam * (qsatfvar - qvair) / (rtsoil + relitt);
+      } else {
+        potev = rho * rlam * dq / (rtsoil + relitt);
+      }
       // Latent_heat_flux (cbl_latent_heat.F90:15-285)
       {
         if (potev < 0.f) wetfac = 1.0f;
@@ -744,7 +790,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
         fess = fess * (1.f - pwet);
         float frescale = zse[0] * DLIQ * rlam / dels;
         if (snowd < 0.1f && fess > 0.0f) {
-          float flower = wb[0].hi - swilt / 2.0f;
+          float flower = P.reduce_soilevp ? wb[0].hi - swilt : wb[0].hi - swilt / 2.0f;
           float fupper = fmaxf(0.f, flower * frescale - evapfbl[0] * rlam / dels);
           fess = fminf(fess, fupper);
           fupper = fmaxf(((wb[0].hi - wbice[0].hi / FROZEN_LIMIT) + (wb[0].lo - wbice[0].lo / FROZEN_LIMIT)) * frescale, 0.f);
@@ -1651,9 +1697,11 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     fluxh[0] = 0.f; fluxh[CG_MS] = 0.f;
     float delt_prev = 0.f;
 #pragma unroll
+    const float wbl_min = P.runoff_speed ? 0.001f : 0.01f;   // l_new_runoff_speed (cbl_smoisturev.F90:112)
+#pragma unroll
     for (int k = 1; k <= CG_MS - 1; ++k) {
-      float wbl_k = fmaxf(0.01f, wbf[k - 1] - wbicef[k - 1]);
-      float wbl_kp = fmaxf(0.01f, wbf[k] - wbicef[k]);
+      float wbl_k = fmaxf(wbl_min, wbf[k - 1] - wbicef[k - 1]);
+      float wbl_kp = fmaxf(wbl_min, wbf[k] - wbicef[k]);
       float delt = wbl_kp - wbl_k;
       float wh = fminf(wbl_k, wbl_kp);
       if (wbicef[k - 1] > 0.05f || wbicef[k] > 0.01f) wh = 0.9f * wbl_k + 0.1f * wbl_kp;
@@ -1670,8 +1718,13 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
       float wh = fminf(wbl_k, wbl_kp);
       if (wbicef[CG_MS - 1] > 0.05f) wh = 0.9f * wbl_k + 0.1f * wbl_kp;
       float speed_k = hyds * __powf(wh / ssat, i2bp3 - 1.f);
-      speed_k = 0.5f * speed_k / (1.f - fminf(0.5f, 10.f * wbicef[CG_MS - 1]));
-      speed_k = fminf(0.5f * speed_k, 0.5f * zse[CG_MS - 1] / dels);
+      if (P.runoff_speed) {   // cbl_smoisturev.F90:180-197
+        speed_k = speed_k / (1.f - fminf(0.5f, 10.f * wbicef[CG_MS - 1]));
+        speed_k = fminf(speed_k, 0.5f * zse[CG_MS - 1] / dels);
+      } else {
+        speed_k = 0.5f * speed_k / (1.f - fminf(0.5f, 10.f * wbicef[CG_MS - 1]));
+        speed_k = fminf(0.5f * speed_k, 0.5f * zse[CG_MS - 1] / dels);
+      }
       fluxh[CG_MS] = fmaxf(0.0f, speed_k * wbl_k);
     }
     // drainage step (cbl_smoisturev.F90, nmeth = -1 explicit part); its
@@ -1863,7 +1916,20 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     float c = ldf(V.rp20, v) * tmp3 / 31536000.0f;
     frp = c * pc1; frpw = c * pc1w; frpr = c * pc1r;
   }
-  {
+  if (P.soil_resp_off) {
+    // diag_soil_resp = 'OFF' (cable_carbon.F90:256-276): rs20 scheme
+    float avgwrs = 0.f, sumt = 0.f;
+#pragma unroll
+    for (int k = 0; k < CG_MS; ++k) { avgwrs += froot[k] * wbf[k]; sumt += froot[k] * tgg[k]; }
+    const float avgtrs = fmaxf(0.0f, sumt - TFRZ);
+    frs = ldf(V.rs20, v) *
+          fminf(1.0f, fmaxf(0.0f, fminf(-0.0178f + 0.2883f * avgwrs + 5.0176f * avgwrs * avgwrs -
+                                             4.5128f * avgwrs * avgwrs * avgwrs,
+                                         0.3320f + 22.6726f * __expf(-5.8184f * avgwrs)))) *
+          fminf(1.0f, fmaxf(0.0f, fminf(0.0104f * __powf(avgtrs, 1.3053f), 5.5956f - 0.1189f * avgtrs)));
+    frs = frs * (V.ratecs[0] * csoil[0] + V.ratecs[1] * csoil[1]) / (365.0f * 24.0f * 3600.0f);
+    if (snowd > 1.f) frs = frs / fmaxf(0.001f, fminf(100.f, snowd));
+  } else {
     float den = fmaxf(0.07f, sfc - swilt);
     float rswc = fmaxf(0.0001f, froot[0] * (wbf[1] - swilt)) / den;
     float tsoil = froot[0] * tgg[1] - TFRZ;

@@ -28,6 +28,7 @@ const double taul1[] = {.09,.09,.075,.09,.09,.11,.11,.075,.11,.11,.075,.023,.059
 const double taul2[] = {.3,.29,.3,.29,.3,.34,.34,.32,.34,.34,.146,.198,.163,.189,.113,.113,.113};
 const double rootbeta[] = {.943,.962,.966,.961,.964,.943,.943,.943,.961,.961,.943,.975,.961,.961,.961,.961,.961};
 const double rp20[] = {3,.6,3,2.2,1,1.5,2.8,2.5,1.5,1,1.5,1,1,1,1,1,1};
+const double rs20[] = {1,1,1,1,1,1,1,1,1,1,1,0,1,0,0,0,0};
 const double vbeta[] = {2,2,2,2,4,4,4,4,2,2,4,4,2,4,4,4,4};
 const double vcmax[] = {.00004,.000055,.00004,.00006,.00004,.00006,.00001,.00004,.00008,.00008,.00006,.000017,
                         .000001,.000017,.000017,.000017,.000017};
@@ -66,6 +67,7 @@ void cg_build_tables(CgPftTable* P, CgSoilTable* S) {
     P->hc[v] = (float)hc[v];
     P->vbeta[v] = (float)vbeta[v];
     P->rp20[v] = (float)rp20[v];
+    P->rs20[v] = (float)rs20[v];
     P->vegcf[v] = (float)vegcf[v];
     P->extkn[v] = 0.001f;
     P->a1gs[v] = (float)a1gs[v];

@@ -36,6 +36,7 @@ struct CgPftTable {
   float froot[CG_MS][CG_NPFT];
   float rw[CG_NPFT], tfcl[CG_NPFT], tvclst[CG_NPFT];
   float clitt[CG_NPFT];   // litter carbon, used by the litter switch
+  float rs20[CG_NPFT];    // soil respiration at 20 C, used by diag_soil_resp = 'OFF'
   float cplant0[3][CG_NPFT], csoil0[2][CG_NPFT];
   float ratecp[3], ratecs[2];
 };

@@ -19,10 +19,12 @@
 ! file and cbm_gpu_finalize at the end of the run.
 !
 ! Build: compile this file in place of cbl_model_driver_offline.F90 and link
-! cable_gb300/lib/libcablegpu.so.  Offline defaults (soil_struc 'default',
-! fwsoil 'standard', ssnow_potev 'HDM') with gs_switch 'leuning' or 'medlyn'
-! and soil_thermal_fix, litter and l_rev_corr each on or off; other switches
-! stay on the CPU path of the reference.
+! cable_gb300/lib/libcablegpu.so.  soil_struc 'default' with the science
+! switches gs_switch, fwsoil_switch ('standard', 'non-linear extrapolation',
+! 'Lai and Ktaul 2000'), ssnow_potev ('HDM', 'P-M'), soil_thermal_fix,
+! litter, l_rev_corr, l_new_reduce_soilevp, l_new_runoff_speed and
+! diag_soil_resp; other configurations stay on the CPU path of the
+! reference.
 !==============================================================================
 
 MODULE cablegpu_c
@@ -194,13 +196,19 @@ CONTAINS
     tiles%swscale = c_null_ptr
     tiles%order = 0
     CALL check(cablegpu_create(tiles, 0_c_int, ctx), 'create')
-    ! science switch bits (CABLEGPU_SW_MEDLYN = 1, CABLEGPU_SW_SOIL_THERMAL_FIX = 2,
-    ! CABLEGPU_SW_LITTER = 4, CABLEGPU_SW_L_REV_CORR = 8)
+    ! science switch bits (CABLEGPU_SW_* in cablegpu.h)
     switches = 0
     IF (TRIM(cable_user%gs_switch) == 'medlyn') switches = switches + 1
     IF (cable_user%soil_thermal_fix) switches = switches + 2
     IF (cable_user%litter) switches = switches + 4
     IF (cable_user%l_rev_corr) switches = switches + 8
+    IF (TRIM(cable_user%fwsoil_switch) == 'non-linear extrapolation') switches = switches + 16
+    IF (TRIM(cable_user%fwsoil_switch) == 'Lai and Ktaul 2000') switches = switches + 32
+    IF (TRIM(cable_user%ssnow_potev) == 'P-M') switches = switches + 64
+    IF (cable_user%l_new_reduce_soilevp) switches = switches + 128
+    IF (cable_user%l_new_runoff_speed) switches = switches + 256
+    IF (TRIM(cable_user%diag_soil_resp) == 'OFF' .OR. TRIM(cable_user%diag_soil_resp) == 'off') &
+      switches = switches + 512
     CALL check(cablegpu_set_options(ctx, switches, 0_c_int, 0_c_int), 'set_options')
 
     ! prognostic state (soil_snow_type, canopy, bgc, bal)

@@ -48,11 +48,31 @@ SW_MEDLYN = 1
 SW_SOIL_THERMAL_FIX = 2
 SW_LITTER = 4
 SW_L_REV_CORR = 8
+SW_FWSOIL_NONLINEAR = 16
+SW_FWSOIL_LAI_KTAUL = 32
+SW_POTEV_PM = 64
+SW_NEW_REDUCE_SOILEVP = 128
+SW_NEW_RUNOFF_SPEED = 256
+SW_DIAG_SOIL_RESP_OFF = 512
+FWSOIL_SWITCH = {"standard": 0, "non-linear extrapolation": SW_FWSOIL_NONLINEAR,
+                 "Lai and Ktaul 2000": SW_FWSOIL_LAI_KTAUL}
 
 
-def switch_mask(medlyn=False, soil_thermal_fix=False, litter=False, l_rev_corr=False) -> int:
+def switch_mask(medlyn=False, soil_thermal_fix=False, litter=False, l_rev_corr=False, fwsoil_switch="standard",
+                ssnow_potev="HDM", l_new_reduce_soilevp=False, l_new_runoff_speed=False, diag_soil_resp="ON") -> int:
+    """cablegpu_set_options mask of the reference's science switches
+    (``cable_user`` names and values; the defaults are the offline ones)."""
+    if fwsoil_switch not in FWSOIL_SWITCH:
+        raise ValueError("fwsoil_switch %r: one of %s" % (fwsoil_switch, list(FWSOIL_SWITCH)))
+    if ssnow_potev not in ("HDM", "P-M"):
+        raise ValueError("ssnow_potev %r: 'HDM' or 'P-M'" % ssnow_potev)
+    if diag_soil_resp.strip().upper() not in ("ON", "OFF"):
+        raise ValueError("diag_soil_resp %r: 'ON' or 'OFF'" % diag_soil_resp)
     return ((SW_MEDLYN if medlyn else 0) | (SW_SOIL_THERMAL_FIX if soil_thermal_fix else 0) |
-            (SW_LITTER if litter else 0) | (SW_L_REV_CORR if l_rev_corr else 0))
+            (SW_LITTER if litter else 0) | (SW_L_REV_CORR if l_rev_corr else 0) | FWSOIL_SWITCH[fwsoil_switch] |
+            (SW_POTEV_PM if ssnow_potev == "P-M" else 0) | (SW_NEW_REDUCE_SOILEVP if l_new_reduce_soilevp else 0) |
+            (SW_NEW_RUNOFF_SPEED if l_new_runoff_speed else 0) |
+            (SW_DIAG_SOIL_RESP_OFF if diag_soil_resp.strip().upper() == "OFF" else 0))
 
 
 def forcing_file_write(path, forcing, doy0: int = 1, dels: float = 1800.0):
@@ -308,13 +328,11 @@ class CableGPU:
         a = [np.ascontiguousarray(x, np.float64) for x in (snowd0, tgg0, wb0)]
         self._check(self.L.cablegpu_cold_start_noalloc(self.h, *[_ptr(x, C.c_double) for x in a]))
 
-    def set_options(self, medlyn=False, diag=False, capture_forcing=False, soil_thermal_fix=False, litter=False,
-                    l_rev_corr=False):
-        """Science switches (``gs_switch='medlyn'``, ``soil_thermal_fix``,
-        ``litter``, ``l_rev_corr``) and output options; every switch off is the
-        reference's offline default."""
-        self._check(self.L.cablegpu_set_options(self.h, switch_mask(medlyn, soil_thermal_fix, litter, l_rev_corr),
-                                                int(diag), int(capture_forcing)))
+    def set_options(self, diag=False, capture_forcing=False, **switches):
+        """Output options and the reference's science switches, by their
+        ``cable_user`` names (see :func:`switch_mask`; unset = the offline
+        defaults)."""
+        self._check(self.L.cablegpu_set_options(self.h, switch_mask(**switches), int(diag), int(capture_forcing)))
 
     def set_synthetic_forcing(self, seed: int, doy0: int = 1):
         self._check(self.L.cablegpu_set_synthetic_forcing(self.h, int(seed), int(doy0)))

@@ -152,13 +152,34 @@ int cablegpu_set_synthetic_forcing(cablegpu_ctx* ctx, unsigned long long seed, i
  *                                 :993-1014); its other uses act only in the
  *                                 coupled model (cable_runtime%um) or on
  *                                 fns_cor, which is 0 offline
- * An unknown bit is an error.
+ *   CABLEGPU_SW_FWSOIL_NONLINEAR  fwsoil_switch = 'non-linear extrapolation'
+ *                                 (cbl_fwsoil.F90:44-88)
+ *   CABLEGPU_SW_FWSOIL_LAI_KTAUL  fwsoil_switch = 'Lai and Ktaul 2000'
+ *                                 (cbl_fwsoil.F90:90-112)
+ *   CABLEGPU_SW_POTEV_PM          ssnow_potev = 'P-M': Penman-Monteith soil
+ *                                 potential evaporation
+ *                                 (cbl_pot_evap_snow.F90:9-78), which reads
+ *                                 canopy%ga of the last step (output row 6)
+ *   CABLEGPU_SW_NEW_REDUCE_SOILEVP  l_new_reduce_soilevp
+ *                                 (cbl_latent_heat.F90:205-210)
+ *   CABLEGPU_SW_NEW_RUNOFF_SPEED  l_new_runoff_speed (cbl_smoisturev.F90:112,
+ *                                 :153-197)
+ *   CABLEGPU_SW_DIAG_SOIL_RESP_OFF  diag_soil_resp = 'OFF': the rs20 soil
+ *                                 respiration scheme (cable_carbon.F90:256-276;
+ *                                 the offline cable.nml sets 'ON')
+ * An unknown bit, or both fwsoil bits, is an error.
  * diag: 1 = write the per-tile diagnostics fields every step.
  * capture_forcing: 1 = keep a copy of each step's forcing (field "forcing"). */
 #define CABLEGPU_SW_MEDLYN 1
 #define CABLEGPU_SW_SOIL_THERMAL_FIX 2
 #define CABLEGPU_SW_LITTER 4
 #define CABLEGPU_SW_L_REV_CORR 8
+#define CABLEGPU_SW_FWSOIL_NONLINEAR 16
+#define CABLEGPU_SW_FWSOIL_LAI_KTAUL 32
+#define CABLEGPU_SW_POTEV_PM 64
+#define CABLEGPU_SW_NEW_REDUCE_SOILEVP 128
+#define CABLEGPU_SW_NEW_RUNOFF_SPEED 256
+#define CABLEGPU_SW_DIAG_SOIL_RESP_OFF 512
 int cablegpu_set_options(cablegpu_ctx* ctx, int switches, int diag, int capture_forcing);
 
 /* One timestep, ktau 1-based (cbm(ktau, dels, ...) followed by the driver's
@@ -225,8 +246,10 @@ int cablegpu_autotune(const cablegpu_tiles* tiles, int device, int sample_tiles,
  * directory of 48-byte entries (name[32], dtype, width, offset), then from
  * byte 4096 the records, 4096-byte aligned; a record holds every field as
  * one [width][mp] block in caller tile order, 64-byte aligned.
- *   restart: 1 record; the tile description (KIND_PARAM fields) and every
- *            prognostic field (KIND_STATE), named as the field registry, the
+ *   restart: 1 record; the tile description (KIND_PARAM fields), every
+ *            prognostic field (KIND_STATE) and the last step's outputs
+ *            (KIND_OUTPUT: ga and trad are restart variables of the
+ *            reference too), named as the field registry, the
  *            double-FP32 soil water and ice as their exact word pairs
  *            (CABLEGPU_DF32), so a resumed run is bitwise the
  *            uninterrupted one
@@ -243,7 +266,8 @@ int cablegpu_autotune(const cablegpu_tiles* tiles, int device, int sample_tiles,
 int cablegpu_restart_write(cablegpu_ctx* ctx, const char* path, int ktau);
 /* Loads the prognostic state of a restart file into the context; the file's
  * tiles must be the context's (same mp, iveg and isoilm in the same caller
- * order; CABLEGPU_ERR_ARG otherwise) and hold every prognostic field.
+ * order; CABLEGPU_ERR_ARG otherwise) and hold every prognostic and output
+ * field.
  * *ktau (may be NULL) receives the step the file was written after: the
  * run continues with ktau + 1. */
 int cablegpu_restart_read(cablegpu_ctx* ctx, const char* path, int* ktau);

@@ -73,6 +73,7 @@ struct State {
   int isflag = 0;
   R snowd, osnowd, ssdnn, snage, pudsto, pudsmx, owetfac, rtsoil, tss, wb_lake, wbtot1, wbtot2;
   R cansto;
+  R ga = 0;                        // canopy%ga of the last step (read by ssnow_potev='P-M')
   R cplant[3], csoil[2];
   // balances (cable_checks.F90 mass_balance SAVE owb; energy/water totals)
   R2 owb, ebal_tot, wbal_tot;
@@ -109,6 +110,12 @@ struct CbmRef {
   bool soil_thermal_fix = false;   // cable_user%soil_thermal_fix (cable_runtime_opts_mod.F90:31)
   bool litter = false;             // cable_user%litter: litter resistances in define_canopy
   bool l_rev_corr = false;         // cable_user%l_rev_corr (cable_runtime_opts_mod.F90:28)
+  int fwsoil_mode = 0;             // fwsoil_switch: 0 'standard', 1 'non-linear extrapolation',
+                                   // 2 'Lai and Ktaul 2000' (cbl_dryLeaf.F90:170-181)
+  bool potev_pm = false;           // ssnow_potev = 'P-M' (cable_canopy.F90:480, :553)
+  bool new_reduce_soilevp = false; // cable_user%l_new_reduce_soilevp (cbl_latent_heat.F90:205-210)
+  bool new_runoff_speed = false;   // cable_user%l_new_runoff_speed (cbl_smoisturev.F90:112, :153)
+  bool diag_soil_resp_off = false; // diag_soil_resp = 'OFF' (cable_carbon.F90:256-276)
   // litter conductivity / vapour diffusivity (cable_canopy.F90:203-204)
   static constexpr double KTH_LITT = 0.3, DV_LITT = 3.1415841138194147e-05;
 
@@ -523,7 +530,7 @@ struct CbmRef {
                const R2 wbliq[MS], LeafIter& L, int iter, R sum_rad_gradis, R sum_rad_rniso) const {
     const R co2cp3 = R(0.0), jtomol = R(4.6e-6);
     R gs_coeff[2] = {0, 0};
-    if (iter == 1) {
+    if (iter == 1 && fwsoil_mode == 0) {
       // fwsoil_calc_std (cbl_fwsoil.F90:13-38)
       R rwater = 0;
       for (int k = 0; k < MS; ++k)
@@ -531,6 +538,35 @@ struct CbmRef {
       rwater = mx(R(1.0e-9), rwater);
       if (medlyn) L.fwsoil = mx(R(1.0e-4), mn(R(1.0), rwater));
       else L.fwsoil = mx(R(1.0e-9), mn(R(1.0), p.vbeta * rwater));
+    } else if (iter == 1 && fwsoil_mode == 1) {
+      // fwsoil_calc_non_linear (cbl_fwsoil.F90:44-88): the root-weighted
+      // available water mapped through a quadratic through (swilt, 0),
+      // (midpoint, 0.9), (sfc, 1)
+      R sum = 0;
+      for (int k = 0; k < MS; ++k) sum += p.froot[k] * mx(R(0.0), mn(R(1.0), R(wbliq[k] - R2(p.swilt))));
+      R rwater = mx(R(1.0e-9), sum / (p.sfc - p.swilt));
+      L.fwsoil = R(1.);
+      rwater = p.swilt + rwater * (p.sfc - p.swilt);
+      const R x1 = p.swilt, x2 = p.swilt + (p.sfc - p.swilt) / R(2.0), x3 = p.sfc;
+      const R s1 = (rwater - x2) / (x1 - x2) * (rwater - x3) / (x1 - x3);
+      const R s2 = (rwater - x1) / (x2 - x1) * (rwater - x3) / (x2 - x3);
+      const R s3 = (rwater - x1) / (x3 - x1) * (rwater - x2) / (x3 - x2);
+      if (rwater < p.sfc - R(0.02)) L.fwsoil = mx(R(0.), mn(R(1.), R(0.) * s1 + R(0.9) * s2 + R(1.0) * s3));
+    } else if (iter == 1 && fwsoil_mode == 2) {
+      // fwsoil_calc_Lai_Ktaul (cbl_fwsoil.F90:90-112), r_2 arithmetic.  A
+      // layer drier than wilting raises a negative base to a non-integer
+      // power (NaN in IEEE arithmetic) whose MAX with the 1e-4 floor is
+      // compiler-dependent in the reference; here it takes the floor.
+      const R2 rootgamma = R2(0.01f);
+      R fw = R(0.0);
+      for (int k = 0; k < MS; ++k) {
+        const R2 avail = wbliq[k] - p.swilt_vec[k];
+        const R dummy = R(rootgamma / mx(R2(1.0e-3), avail));
+        const R2 base = avail / p.ssat_vec;
+        const R2 frwater = base > R2(0.0) ? mx(R2(1.0e-4), std::pow(base, R2(dummy))) : R2(1.0e-4);
+        fw = mn(R(1.0), mx(fw, R(frwater)));
+      }
+      L.fwsoil = fw;
     }
     const R fwsoil = L.fwsoil;
     R gswmin[2];
@@ -681,15 +717,15 @@ struct CbmRef {
 
   // ------------------------------------------------------- Latent_heat_flux
   // cbl_latent_heat.F90:15-285
-  static void latent_heat_flux(R dels, const P& p, R rlam, const S& s, R potev, R& wetfac, R2 evapfbl1, R& cls,
-                               R tss, R2& fes, R2& fess, R2& fesp, R& pwet) {
+  void latent_heat_flux(R dels, const P& p, R rlam, const S& s, R potev, R& wetfac, R2 evapfbl1, R& cls,
+                               R tss, R2& fes, R2& fess, R2& fesp, R& pwet) const {
     if (potev < R(0.)) wetfac = R(1.0);
     fess = wetfac * potev;
     pwet = mx(R(0.), mn(R(0.2), s.pudsto / mx(R(1.), s.pudsmx)));
     fess = fess * (R(1.) - pwet);
     R frescale = p.zse[0] * R(DENSITY_LIQ) * rlam / dels;
     if (s.snowd < R(0.1) && fess > 0.0) {
-      R flower = R(s.wb[0]) - p.swilt / R(2.0);
+      R flower = new_reduce_soilevp ? R(s.wb[0]) - p.swilt : R(s.wb[0]) - p.swilt / R(2.0);
       R fupper = R(mx(R2(0.), flower * frescale - evapfbl1 * rlam / dels));
       fess = mn(fess, R2(fupper));
       fupper = R(s.wb[0] - s.wbice[0] / R(FROZEN_LIMIT)) * frescale;
@@ -718,6 +754,16 @@ struct CbmRef {
   static R hdm_litter(R rho, R rlam, R dq, R rtsoil, R snowd, R tgg1, int isflag, R2 clitt) {
     if (snowd > R(1.0) || tgg1 == R(TFRZ)) dq = mx(R(-0.1e-3), dq);
     return rho * rlam * dq / (rtsoil + R(1 - isflag) * R(clitt) * R(0.003f) / R(DV_LITT));
+  }
+  // Penman_Monteith (cbl_pot_evap_snow.F90:9-78): the latent heat of soil
+  // potential evaporation from the soil available energy (fns - ga, ga the
+  // latest value of canopy%ga) and the canopy-air humidity deficit
+  R penman_monteith(const Air& air, const Met& met, R ga_prev, R fns, R rtsoil, int isflag, R2 clitt) const {
+    const R sss = air.dsatdk;
+    const R cc1 = sss / (sss + air.psyc), cc2 = air.psyc / (sss + air.psyc);
+    const R qsatfvar = qsatfjh(met.tvair - R(TFRZ), met.pmb);
+    const R rs = litter ? rtsoil + R(1 - isflag) * R(clitt) * R(0.003f) / R(DV_LITT) : rtsoil;
+    return cc1 * (fns - ga_prev) + cc2 * air.rho * air.rlam * (qsatfvar - met.qvair) / rs;
   }
   // litter resistances to heat and vapour (cable_canopy.F90:471-476, :987-988)
   static void litter_resist(R2 clitt, int isflag, R rho, R& rhlitt, R& relitt) {
@@ -832,7 +878,8 @@ struct CbmRef {
     const R sum_rad_gradis = rad.gradis[0] + rad.gradis[1];
     R us = 0, rt0 = 0, rt1usc = 0, rtsoil = s.rtsoil, cls = R(1);
     R rhlitt = 0, relitt = 0;   // cable_canopy.F90:239-240
-    R fev = 0, fhv = 0, fnv = 0, fns = 0, fhs = 0, fe = 0, fh = 0, ga = 0, rnet = 0, epot = 0, qstss = 0;
+    R fev = 0, fhv = 0, fnv = 0, fns = 0, fhs = 0, fe = 0, fh = 0, rnet = 0, epot = 0, qstss = 0;
+    R ga = s.ga;   // canopy%ga persists between steps (read before it is set only by P-M)
     R fevw = 0, fhvw = 0;
     R2 ghwet = 0;
     int iterplus = 1;
@@ -913,7 +960,9 @@ struct CbmRef {
             R(EMSOIL) * R(SBOLTZ) * tss4;
       qstss = qsatfjh(s.tss - R(TFRZ), met.pmb);
       if (litter) litter_resist(p.clitt, s.isflag, air.rho, rhlitt, relitt);
-      {
+      if (potev_pm) {
+        potev = penman_monteith(air, met, ga, fns, rtsoil, s.isflag, p.clitt);
+      } else {
         R dq = qstss - met.qv;
         potev = litter ? hdm_litter(air.rho, air.rlam, dq, rtsoil, s.snowd, s.tgg[0], s.isflag, p.clitt)
                        : hdm(air.rho, air.rlam, dq, rtsoil, s.snowd, s.tgg[0]);
@@ -951,7 +1000,9 @@ struct CbmRef {
         }
       }
       qstss = qsatfjh(s.tss - R(TFRZ), met.pmb);
-      {
+      if (potev_pm) {
+        potev = penman_monteith(air, met, ga, fns, rtsoil, s.isflag, p.clitt);
+      } else {
         R dq = qstss - met.qvair;
         potev = litter ? hdm_litter(air.rho, air.rlam, dq, rtsoil, s.snowd, s.tgg[0], s.isflag, p.clitt)
                        : hdm(air.rho, air.rlam, dq, rtsoil, s.snowd, s.tgg[0]);
@@ -1069,6 +1120,7 @@ struct CbmRef {
     s.rtsoil = rtsoil;
     R2 fevc = L.fevc;
     s.cansto = cansto;
+    s.ga = ga;
     // ================= end define_canopy
     s.owetfac = wetfac;                    // cbm:192
 
@@ -1107,7 +1159,19 @@ struct CbmRef {
       frpw = p.rp20 * tmp3 * pc1w / spy;
       frpr = p.rp20 * tmp3 * pc1r / spy;
     }
-    {
+    if (diag_soil_resp_off) {
+      // diag_soil_resp = 'OFF' (cable_carbon.F90:256-276): rs20 scheme
+      R avgwrs = 0, sumt = 0;
+      for (int k = 0; k < MS; ++k) { avgwrs += p.froot[k] * R(s.wb[k]); sumt += p.froot[k] * s.tgg[k]; }
+      const R avgtrs = mx(R(0.0), sumt - R(TFRZ));
+      frs = p.rs20 *
+            mn(R(1.0), mx(R(0.0), mn(R(-0.0178) + R(0.2883) * avgwrs + R(5.0176) * avgwrs * avgwrs -
+                                         R(4.5128) * avgwrs * avgwrs * avgwrs,
+                                     R(0.3320) + R(22.6726) * std::exp(R(-5.8184) * avgwrs)))) *
+            mn(R(1.0), mx(R(0.0), mn(R(0.0104) * std::pow(avgtrs, R(1.3053)), R(5.5956) - R(0.1189) * avgtrs)));
+      frs = frs * (p.ratecs[0] * s.csoil[0] + p.ratecs[1] * s.csoil[1]) / (R(365.0) * R(24.0) * R(3600.0));
+      if (s.snowd > R(1.)) frs = frs / mx(R(0.001), mn(R(100.), s.snowd));
+    } else {
       const R rswch = R(0.16), soilcf = R(1.0), t0 = R(-46.0);
       R den = mx(R(0.07), p.sfc - p.swilt);
       R rswc = mx(R(0.0001), p.froot[0] * (R(s.wb[1]) - p.swilt)) / den;
@@ -1566,9 +1630,10 @@ struct CbmRef {
       R2 at[MS], bt[MS], ct[MS], fluxh[MS + 1], delt[MS + 1], dtt[MS];
       for (int k = 0; k < MS; ++k) { at[k] = 0.0; bt[k] = 1.0; ct[k] = 0.0; }
       delt[0] = 0.0; fluxh[0] = 0.0; fluxh[MS] = 0.0;
+      const R2 wbl_min = new_runoff_speed ? R2(0.001) : R2(0.01);
       for (int k = 1; k <= MS - 1; ++k) {
-        R2 wbl_k = mx(R2(0.01), s.wb[k - 1] - s.wbice[k - 1]);
-        R2 wbl_kp = mx(R2(0.01), s.wb[k] - s.wbice[k]);
+        R2 wbl_k = mx(wbl_min, s.wb[k - 1] - s.wbice[k - 1]);
+        R2 wbl_kp = mx(wbl_min, s.wb[k] - s.wbice[k]);
         delt[k] = wbl_kp - wbl_k;
         R2 wh = mn(wbl_k, wbl_kp);
         if (s.wbice[k - 1] > 0.05 || s.wbice[k] > 0.01) wh = 0.9 * wbl_k + 0.1 * wbl_kp;
@@ -1586,9 +1651,14 @@ struct CbmRef {
         R2 wh = mn(wbl_k, wbl_kp);
         if (s.wbice[MS - 1] > 0.05) wh = 0.9 * wbl_k + 0.1 * wbl_kp;
         R2 speed_k = p.hyds * std::pow(wh / p.ssat, R2(p.i2bp3 - R(1)));
-        speed_k = 0.5 * speed_k / (1. - mn(R2(0.5), 10. * s.wbice[MS - 1]));
+        if (new_runoff_speed) {   // :180-197
+          speed_k = speed_k / (1. - mn(R2(0.5), 10. * s.wbice[MS - 1]));
+          speed_k = mn(speed_k, R2(R(0.5) * p.zse[MS - 1] / dels));
+        } else {
+          speed_k = 0.5 * speed_k / (1. - mn(R2(0.5), 10. * s.wbice[MS - 1]));
+          speed_k = mn(0.5 * speed_k, R2(0.5) * p.zse[MS - 1] / dels);
+        }
         R2 fluxlo = wbl_k;
-        speed_k = mn(0.5 * speed_k, R2(0.5) * p.zse[MS - 1] / dels);
         fluxh[MS] = mx(R2(0.0), speed_k * fluxlo);
       }
       for (int k = MS; k >= 1; --k) {

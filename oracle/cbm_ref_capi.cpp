@@ -29,7 +29,7 @@ const Slot kState[] = {
   {"wb", MS}, {"wbice", MS}, {"gammzz", MS}, {"tgg", MS}, {"tggsn", MSN}, {"ssdn", MSN}, {"smass", MSN},
   {"sdepth", MSN}, {"isflag", 1}, {"snowd", 1}, {"ssdnn", 1}, {"snage", 1}, {"pudsto", 1}, {"owetfac", 1},
   {"rtsoil", 1}, {"tss", 1}, {"wb_lake", 1}, {"wbtot1", 1}, {"wbtot2", 1}, {"cansto", 1}, {"cplant", 3},
-  {"csoil", 2}, {"owb", 1}, {"ebal_tot", 1}, {"wbal_tot", 1}, {"first_call", 1},
+  {"csoil", 2}, {"owb", 1}, {"ebal_tot", 1}, {"wbal_tot", 1}, {"first_call", 1}, {"ga", 1},
 };
 constexpr int kNState = sizeof(kState) / sizeof(kState[0]);
 int state_slots() { int n = 0; for (auto& s : kState) n += s.width; return n; }
@@ -59,7 +59,7 @@ void pack_state(const State<R, R2>& s, double* st, int mp, int t) {
   put(s.tss); put(s.wb_lake); put(s.wbtot1); put(s.wbtot2); put(s.cansto);
   for (int k = 0; k < 3; ++k) put(s.cplant[k]);
   for (int k = 0; k < 2; ++k) put(s.csoil[k]);
-  put(s.owb); put(s.ebal_tot); put(s.wbal_tot); put(s.first_soilsnow_call ? 1.0 : 0.0);
+  put(s.owb); put(s.ebal_tot); put(s.wbal_tot); put(s.first_soilsnow_call ? 1.0 : 0.0); put(s.ga);
 }
 
 template <class R, class R2>
@@ -80,6 +80,7 @@ void unpack_state(State<R, R2>& s, const double* st, int mp, int t) {
   for (int k = 0; k < 3; ++k) s.cplant[k] = R(get());
   for (int k = 0; k < 2; ++k) s.csoil[k] = R(get());
   s.owb = R2(get()); s.ebal_tot = R2(get()); s.wbal_tot = R2(get()); s.first_soilsnow_call = get() != 0.0;
+  s.ga = R(get());
   s.pudsmx = 0; s.osnowd = s.snowd;
 }
 
@@ -217,6 +218,11 @@ int run_impl(int mp, int nsteps, int ktau0, double dels, int switches, const int
     model.soil_thermal_fix = (switches & 2) != 0;
     model.litter = (switches & 4) != 0;
     model.l_rev_corr = (switches & 8) != 0;
+    model.fwsoil_mode = (switches & 16) ? 1 : ((switches & 32) ? 2 : 0);
+    model.potev_pm = (switches & 64) != 0;
+    model.new_reduce_soilevp = (switches & 128) != 0;
+    model.new_runoff_speed = (switches & 256) != 0;
+    model.diag_soil_resp_off = (switches & 512) != 0;
     Diag<R, R2> d{};
     for (int n = 0; n < nsteps; ++n) {
       float fv[F_NFIELDS];
@@ -274,7 +280,9 @@ int cbmref_init(int mp, int precision, const int* iveg, const int* isoilm, const
 // last step's diagnostics [ndiag][mp] (may be null).
 // precision: 0 = <double,double> oracle, 1 = <float,double> reference mix.
 // switches: bit 0 gs_switch='medlyn', bit 1 soil_thermal_fix, bit 2 litter,
-// bit 3 l_rev_corr.
+// bit 3 l_rev_corr, bit 4 fwsoil_switch='non-linear extrapolation', bit 5
+// fwsoil_switch='Lai and Ktaul 2000', bit 6 ssnow_potev='P-M', bit 7
+// l_new_reduce_soilevp, bit 8 l_new_runoff_speed, bit 9 diag_soil_resp='OFF'.
 int cbmref_run(int mp, int nsteps, int ktau0, double dels, int precision, int switches, const int* iveg,
                const int* isoilm, const double* vlai, const double* lat, const float* forcing, uint64_t seed,
                int doy0, const float* tf_lat, const float* tf_lonphase, const float* tf_tbase,

@@ -55,15 +55,13 @@ def compare(name, gpu, ref):
     return out
 
 
-def run_pair(ts, nsteps, ktau0=1, diag=True, host_forcing=False, medlyn=False, precision=0, soil_thermal_fix=False,
-             litter=False, l_rev_corr=False):
+def run_pair(ts, nsteps, ktau0=1, diag=True, host_forcing=False, precision=0, **switches):
     """Advance the GPU and the oracle ``nsteps`` from a cold start on
     identical forcing.  Returns (gpu_state, gpu_diag, oracle_state, oracle_diag,
     forcing [nsteps, 13, mp])."""
     from cable_gb300 import runtime as R
     g = R.from_tileset(ts)
-    g.set_options(medlyn=medlyn, diag=diag, capture_forcing=not host_forcing, soil_thermal_fix=soil_thermal_fix,
-                  litter=litter, l_rev_corr=l_rev_corr)
+    g.set_options(diag=diag, capture_forcing=not host_forcing, **switches)
     forc = []
     if host_forcing:
         F = O.forcing(ts, ktau0 - 1, nsteps)
@@ -80,8 +78,7 @@ def run_pair(ts, nsteps, ktau0=1, diag=True, host_forcing=False, medlyn=False, p
     gdiag = {k: g.get(k)[0] for k in DIAG_MAP} if diag else {}
     g.close()
     st = O.init_state(ts, precision)
-    od = O.run(ts, st, nsteps, ktau0=ktau0, forcing=F, precision=precision, medlyn=medlyn,
-               soil_thermal_fix=soil_thermal_fix, litter=litter, l_rev_corr=l_rev_corr)
+    od = O.run(ts, st, nsteps, ktau0=ktau0, forcing=F, precision=precision, **switches)
     ostate = O.split_state(st)
     return gstate, gdiag, ostate, od, F
 

@@ -55,6 +55,12 @@ def lib():
     return _lib
 
 
+def _switch_mask(**switches):
+    """The science-switch bits (the same as the library's, cable_gb300.runtime.switch_mask)."""
+    from cable_gb300.runtime import switch_mask
+    return switch_mask(**switches)
+
+
 def _p(a, t):
     return a.ctypes.data_as(C.POINTER(t))
 
@@ -95,8 +101,7 @@ def init_state(ts, precision=0):
     return st
 
 
-def run(ts, state, nsteps, ktau0=1, forcing=None, precision=0, nthreads=None, medlyn=False, soil_thermal_fix=False,
-        litter=False, l_rev_corr=False):
+def run(ts, state, nsteps, ktau0=1, forcing=None, precision=0, nthreads=None, **switches):
     """Advance ``state`` (modified in place) by ``nsteps``; return the last
     step's diagnostics as {name: array[mp]}."""
     L = lib()
@@ -117,9 +122,7 @@ def run(ts, state, nsteps, ktau0=1, forcing=None, precision=0, nthreads=None, me
     if nthreads is None:
         nthreads = os.cpu_count() or 1
     assert state.flags["C_CONTIGUOUS"] and state.dtype == np.float64
-    rc = L.cbmref_run(mp, nsteps, ktau0, float(ts.dels), precision,
-                     int(bool(medlyn)) | (2 if soil_thermal_fix else 0) | (4 if litter else 0) | (8 if l_rev_corr else 0),
-                     _p(iveg, C.c_int),
+    rc = L.cbmref_run(mp, nsteps, ktau0, float(ts.dels), precision, _switch_mask(**switches), _p(iveg, C.c_int),
                       _p(isoil, C.c_int), _p(vlai, C.c_double), _p(lat, C.c_double), fptr, ts.seed, ts.doy0,
                       _p(tl, C.c_float), _p(tp, C.c_float), _p(tb, C.c_float), _p(tsw, C.c_float),
                       _p(state, C.c_double), _p(diag, C.c_double), nthreads)

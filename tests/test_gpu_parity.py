@@ -322,8 +322,21 @@ SWITCH_SETS = {
     "soil_thermal_fix": dict(soil_thermal_fix=True),
     "litter": dict(litter=True),
     "l_rev_corr": dict(l_rev_corr=True),
-    "all": dict(medlyn=True, soil_thermal_fix=True, litter=True, l_rev_corr=True),
+    "fwsoil_nonlinear": dict(fwsoil_switch="non-linear extrapolation"),
+    "fwsoil_lai_ktaul": dict(fwsoil_switch="Lai and Ktaul 2000"),
+    "potev_pm": dict(ssnow_potev="P-M"),
+    "reduce_soilevp": dict(l_new_reduce_soilevp=True),
+    "runoff_speed": dict(l_new_runoff_speed=True),
+    "soil_resp_off": dict(diag_soil_resp="OFF"),
+    "all": dict(medlyn=True, soil_thermal_fix=True, litter=True, l_rev_corr=True,
+                fwsoil_switch="non-linear extrapolation", ssnow_potev="P-M", l_new_reduce_soilevp=True,
+                l_new_runoff_speed=True, diag_soil_resp="OFF"),
 }
+# the field each switch must move on the GPU, and by how much
+SWITCH_LIVE = {"soil_thermal_fix": ("tgg", 0.05), "litter": ("fhs", 0.5), "l_rev_corr": ("tgg", 0.01),
+               "fwsoil_nonlinear": ("fevc", 1.0), "fwsoil_lai_ktaul": ("fevc", 1.0), "potev_pm": ("fes", 1.0),
+               "reduce_soilevp": ("fes", 1.0), "runoff_speed": ("wb", 1e-4), "soil_resp_off": ("frs", 1e-8),
+               "all": ("tgg", 0.05)}
 
 
 @pytest.mark.parametrize("which", list(SWITCH_SETS))
@@ -348,7 +361,15 @@ def test_science_switches_match_oracle(oracle, runtime, which):
         assert rep[k]["rms"] <= max(rep[k]["tol"], 3 * ref[k]["rms"]), (k, rep[k], ref[k])
         assert rep[k]["frac_within"] >= min(0.995, ref[k]["frac_within"] - 0.005), (k, rep[k], ref[k])
     assert np.abs(gd["ebal"]).max() < 0.05
+    # soil respiration (frs) and transpiration (fevc) against the oracle too
+    rms = lambda e: float(np.sqrt(np.mean(e ** 2)))
+    for k in ("frs", "fevc"):
+        ref = np.asarray(od[H.DIAG_MAP[k]], np.float64)
+        err = np.abs(np.asarray(gd[k], np.float64) - ref)
+        err32 = np.abs(np.asarray(od32[H.DIAG_MAP[k]], np.float64) - ref)
+        assert rms(err) <= max(3 * rms(err32), 1e-3 * np.abs(ref).max() + 1e-12), (k, rms(err), rms(err32))
     g0, d0, _, _, _ = H.run_pair(ts, 24)
-    moved = np.abs(np.asarray(g0["tgg"]) - np.asarray(gs["tgg"])).max()
-    moved_fh = np.abs(np.asarray(d0["fhs"]) - np.asarray(gd["fhs"])).max()
-    assert max(moved, moved_fh) > 0.05, (which, moved, moved_fh)
+    field, thr = SWITCH_LIVE[which]
+    a0 = np.asarray(g0[field] if field in g0 else d0[field], np.float64)
+    a1 = np.asarray(gs[field] if field in gs else gd[field], np.float64)
+    assert np.abs(a1 - a0).max() > thr, (which, field, np.abs(a1 - a0).max())

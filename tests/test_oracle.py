@@ -193,21 +193,44 @@ def test_soil_thermal_fix_switch_is_live_and_conserves(oracle):
     assert 200.0 < np.asarray(s1["tgg"]).min() and np.asarray(s1["tgg"]).max() < 340.0
 
 
-@pytest.mark.parametrize("switch", ["litter", "l_rev_corr"])
-def test_canopy_switches_are_live_and_conserve(oracle, switch):
-    """litter (litter resistances to soil heat and vapour transfer) and
-    l_rev_corr (revised soil-coupling derivatives) change the soil fluxes
-    and temperatures, and the energy and leaf balances still close."""
+SWITCH_CASES = {
+    # switch set, diagnostic or state field the switch must move, threshold
+    "litter": (dict(litter=True), "fhs", 1.0),
+    "l_rev_corr": (dict(l_rev_corr=True), "tgg", 0.01),
+    "fwsoil_nonlinear": (dict(fwsoil_switch="non-linear extrapolation"), "fevc", 1.0),
+    "fwsoil_lai_ktaul": (dict(fwsoil_switch="Lai and Ktaul 2000"), "fevc", 1.0),
+    "potev_pm": (dict(ssnow_potev="P-M"), "fes", 1.0),
+    "reduce_soilevp": (dict(l_new_reduce_soilevp=True), "fes", 1.0),
+    "runoff_speed": (dict(l_new_runoff_speed=True), "wb", 1e-4),
+    "soil_resp_off": (dict(diag_soil_resp="OFF"), "frs", 1e-8),
+}
+
+
+@pytest.mark.parametrize("case", list(SWITCH_CASES))
+def test_canopy_and_soil_switches_are_live_and_conserve(oracle, case):
+    """Each alternative science switch changes what it should (the named
+    field moves by more than the threshold over 48 steps of snowy gridded
+    tiles) and the energy and leaf balances still close every step."""
+    sw, field, thr = SWITCH_CASES[case]
     ts = W.snow_grid(mp=400, nsteps=48)
     res = {}
     for on in (False, True):
         st = oracle.init_state(ts, 0)
-        d = oracle.run(ts, st, 48, **{switch: on})
+        d = oracle.run(ts, st, 48, **(sw if on else {}))
         res[on] = (oracle.split_state(st), d)
     (s0, d0), (s1, d1) = res[False], res[True]
     assert np.abs(d1["ebal"]).max() < 1e-8
     assert np.abs(d1["drybal"]).max() < 1e-6
-    assert np.abs(np.asarray(s1["tgg"]) - np.asarray(s0["tgg"])).max() > 0.01
-    if switch == "litter":
-        # the litter resistance moves the soil sensible heat flux
-        assert np.abs(d1["fhs"] - d0["fhs"]).max() > 1.0
+    a0 = np.asarray(s0[field] if field in s0 else d0[field], np.float64)
+    a1 = np.asarray(s1[field] if field in s1 else d1[field], np.float64)
+    assert np.all(np.isfinite(a1))
+    assert np.abs(a1 - a0).max() > thr, (case, np.abs(a1 - a0).max())
+
+
+def test_switch_mask_rejects_unknown_values():
+    from cable_gb300 import runtime as R
+    assert R.switch_mask() == 0
+    assert R.switch_mask(fwsoil_switch="Lai and Ktaul 2000", ssnow_potev="P-M", diag_soil_resp="OFF ") == 32 | 64 | 512
+    for bad in (dict(fwsoil_switch="Haverd2013"), dict(ssnow_potev="PM"), dict(diag_soil_resp="maybe")):
+        with pytest.raises(ValueError):
+            R.switch_mask(**bad)
