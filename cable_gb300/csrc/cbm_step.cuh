@@ -367,6 +367,26 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
 // its converged result) to D.harvest.  kSur: the first
 // iteration's dryLeaf starts from the network's leaf temperature (the
 // surrogate; see the comment at its use).
+// transp_soil_water (cbl_remove_trans.F90:43-93): root-weighted extraction of
+// fe_mm (mm of transpiration over the step) from the layers, each layer's
+// deficit carried to the next; returns the total.  Explicitly rounded
+// operations, so a given fe_mm yields the same layer amounts wherever this is
+// evaluated: the canopy iteration keeps only fe_mm of the latest extracting
+// pass and of its best iterate, and rebuilds both layer arrays afterwards.
+__device__ __forceinline__ float transp_extract(float fe_mm, const float (&froot)[CG_MS], const float (&avail)[CG_MS],
+                                                float (&ev)[CG_MS]) {
+  float diffp = 0.f, se = 0.f;
+#pragma unroll
+  for (int kk = 0; kk < CG_MS; ++kk) {
+    const float xx = __fadd_rn(__fmul_rn(fe_mm, froot[kk]), diffp);
+    const float xxd = __fsub_rn(xx, avail[kk]);
+    if (xxd > 0.0f) { ev[kk] = avail[kk]; diffp = xxd; }
+    else { ev[kk] = xx; diffp = 0.0f; }
+    se = __fadd_rn(se, ev[kk]);
+  }
+  return se;
+}
+
 template <bool kDiag, bool kHarvest = false, bool kSur = false>
 __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
   const int ld = D.ld;
@@ -495,6 +515,11 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
     }
     fwsoil = fw;
   }
+  // water each layer can give to transpiration, fixed over the step
+  // (transp_soil_water, cbl_remove_trans.F90:62-63)
+  float dk_avail[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) dk_avail[k] = fmaxf(0.0f, wbliq0[k] - 1.1f * swilt) * zse[k] * DLIQ;
   for (int iter = 1; iter <= NITER; ++iter) {
     const float zi = zetar[iter - 1];
     // comp_friction_vel (cbl_friction_vel.F90:19-108)
@@ -555,12 +580,10 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
       float abs_deltlf = 999.0f, deltlf = 0.f;
       float tlfxx = tlfx;
       fevc = 0.f;
-#pragma unroll
-      for (int k = 0; k < CG_MS; ++k) evapfbl[k] = 0.f;
+      float fe_mm_last = 0.f, fe_mm_best = 0.f;   // transpiration (mm) of the latest extracting pass / best iterate
       hcy = 0.f;
       if (!veg_mask) { rnx = 0.f; ecx = 0.f; ecy = 0.f; abs_deltlf = 0.f; rny = 0.f; }
       float deltlfy = abs_deltlf;
-      float oldevapfbl[CG_MS];
       // With the surrogate the first iteration starts from the network's
       // leaf temperature.  The first pass is the closure test of the
       // prediction: when the leaf energy balance evaluated there moves the
@@ -648,19 +671,12 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
                 (dsatdk * (rniso[1] - cpr * (tvair - tk) * gradis[1]) + cpr * dva * ghr[1]) / (dsatdk + psycst[1]);
           float local_fevc = (1.0f - fwet) * ecx;
           if (local_fevc > 0.0f) {
-            // transp_soil_water (cbl_remove_trans.F90:43-93)
-            float diffp = 0.f, se = 0.f;
-#pragma unroll
-            for (int kk = 0; kk < CG_MS; ++kk) {
-              float xx = local_fevc * dels / HL * froot[kk] + diffp;
-              float dk = fmaxf(0.0f, wbliq0[kk] - 1.1f * swilt) * zse[kk] * DLIQ;
-              float xxd = xx - dk;
-              if (xxd > 0.0f) { evapfbl[kk] = dk; diffp = xxd; }
-              else { evapfbl[kk] = xx; diffp = 0.0f; }
-              se += evapfbl[kk];
-            }
+            const float fe_mm = local_fevc * dels / HL;
+            float ev[CG_MS];
+            const float se = transp_extract(fe_mm, froot, dk_avail, ev);
             fevc = se * rlam / dels;
             ecx = fevc / (1.0f - fwet);
+            fe_mm_last = fe_mm;
           }
           float sgh = gh[0] + gh[1];
           hcx = (sum_rad_rniso - ecx - cpr * (tvair - tk) * sum_rad_gradis) * sgh / (ghr[0] + ghr[1]);
@@ -677,8 +693,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
           if (abs_deltlf < fabsf(deltlfy)) deltlfy = deltlf;
           rny = rnx; hcy = hcx; ecy = ecx;
           rdy[0] = rdx[0]; rdy[1] = rdx[1]; an_y[0] = anx[0]; an_y[1] = anx[1];
-#pragma unroll
-          for (int kk = 0; kk < CG_MS; ++kk) oldevapfbl[kk] = evapfbl[kk];
+          fe_mm_best = fe_mm_last;
           tlfy = tlfx;   // damping below is a no-op for k == 1
         }
         // damping once k > 5 (:584-590)
@@ -700,8 +715,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
             rnx = sum_rad_rniso; ecx = sum_rad_rniso; hcx = 0.f;
             abs_deltlf = 999.0f; deltlf = 0.f; deltlfy = abs_deltlf;
             fevc = 0.f; hcy = 0.f;
-#pragma unroll
-            for (int kk = 0; kk < CG_MS; ++kk) evapfbl[kk] = 0.f;
+            fe_mm_last = 0.f; fe_mm_best = 0.f;
             rdx[0] = rdx[1] = anx[0] = anx[1] = rdy[0] = rdy[1] = an_y[0] = an_y[1] = 0.f;
             conv = 0.1f;
             sur_try = false;
@@ -712,11 +726,19 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
         // a tile that has stopped iterating never changes again: leave now
         if (!(veg_mask && abs_deltlf > conv)) break;
       }
+      // the layer amounts of the latest extracting pass (zero if none)
+      if (fe_mm_last > 0.f) {
+        transp_extract(fe_mm_last, froot, dk_avail, evapfbl);
+      } else {
+#pragma unroll
+        for (int kk = 0; kk < CG_MS; ++kk) evapfbl[kk] = 0.f;
+      }
       fevc = (1.0f - fwet) * ecy;
       if (ecy > 0.0f && fwet < 1.0f && fabsf(ecy - ecx) > 1.0e-6f) {
-        float so2 = 0.f;
-#pragma unroll
-        for (int kk = 0; kk < CG_MS; ++kk) so2 += oldevapfbl[kk];
+        // the best iterate's layer amounts replace them when they match its
+        // transpiration (cbl_dryLeaf.F90:626-645)
+        float oldevapfbl[CG_MS] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        const float so2 = (fe_mm_best > 0.f) ? transp_extract(fe_mm_best, froot, dk_avail, oldevapfbl) : 0.f;
         if (!(fabsf(fevc - so2 * rlam / dels) > 1.0e-4f)) {
 #pragma unroll
           for (int kk = 0; kk < CG_MS; ++kk) evapfbl[kk] = oldevapfbl[kk];
