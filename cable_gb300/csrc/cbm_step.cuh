@@ -575,7 +575,8 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
       }
       float gswmin[2] = {fmaxf(1.e-6f, scalex[0] * gswmin_p), fmaxf(1.e-6f, scalex[1] * gswmin_p)};
       float gh[2] = {1e-3f, 1e-3f}, ghr[2] = {1e-3f, 1e-3f}, psycst[2] = {psyc, psyc};
-      float rdx[2] = {0.f, 0.f}, anx[2] = {0.f, 0.f}, rdy[2] = {0.f, 0.f}, an_y[2] = {0.f, 0.f};
+      float rdx[2] = {0.f, 0.f}, anx[2] = {0.f, 0.f};
+      float rdy_sum = 0.f, an_y_sum = 0.f;   // the best iterate's leaf respiration / net assimilation, both leaves
       float rnx = sum_rad_rniso, ecx = sum_rad_rniso, hcx = 0.f;
       float abs_deltlf = 999.0f, deltlf = 0.f;
       float tlfxx = tlfx;
@@ -692,7 +693,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
         if (abs_deltlf < fabsf(deltlfy) || k == 1) {
           if (abs_deltlf < fabsf(deltlfy)) deltlfy = deltlf;
           rny = rnx; hcy = hcx; ecy = ecx;
-          rdy[0] = rdx[0]; rdy[1] = rdx[1]; an_y[0] = anx[0]; an_y[1] = anx[1];
+          rdy_sum = rdx[0] + rdx[1]; an_y_sum = anx[0] + anx[1];
           fe_mm_best = fe_mm_last;
           tlfy = tlfx;   // damping below is a no-op for k == 1
         }
@@ -716,7 +717,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
             abs_deltlf = 999.0f; deltlf = 0.f; deltlfy = abs_deltlf;
             fevc = 0.f; hcy = 0.f;
             fe_mm_last = 0.f; fe_mm_best = 0.f;
-            rdx[0] = rdx[1] = anx[0] = anx[1] = rdy[0] = rdy[1] = an_y[0] = an_y[1] = 0.f;
+            rdx[0] = rdx[1] = anx[0] = anx[1] = rdy_sum = an_y_sum = 0.f;
             conv = 0.1f;
             sur_try = false;
             k = 0;
@@ -744,8 +745,8 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
           for (int kk = 0; kk < CG_MS; ++kk) evapfbl[kk] = oldevapfbl[kk];
         }
       }
-      frday = 12.0f * (rdy[0] + rdy[1]);
-      fpn = fminf(-12.0f * (an_y[0] + an_y[1]), frday);
+      frday = 12.0f * rdy_sum;
+      fpn = fminf(-12.0f * an_y_sum, frday);
       // training row: features at entry, converged stomatal conductance,
       // net assimilation and leaf temperature change
       if (sampled) {
@@ -755,7 +756,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
           r[0] = make_float4(feat[0], feat[1], feat[2], feat[3]);
           r[1] = make_float4(feat[4], feat[5], feat[6], feat[7]);
           r[2] = make_float4(feat[8], feat[9], feat[10], feat[11]);
-          r[3] = make_float4(gswx[0] + gswx[1], an_y[0] + an_y[1], tlfy - tlf_entry, 0.f);
+          r[3] = make_float4(gswx[0] + gswx[1], an_y_sum, tlfy - tlf_entry, 0.f);
         }
       }
     }
