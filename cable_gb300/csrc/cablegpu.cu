@@ -16,6 +16,12 @@
 #include "surrogate_host.h"
 #include "cgio.h"
 
+// tile order 3: caller tiles per chunk (log2), sized so a chunk's forcing
+// (13 rows) and outputs (8 rows) fit the L2 cache together
+#ifndef CG_ORDER3_CHUNK_LOG2
+#define CG_ORDER3_CHUNK_LOG2 18
+#endif
+
 using namespace cg;
 
 namespace {
@@ -438,13 +444,15 @@ int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out)
       // sort key, most significant first: plant type, soil type (order 0);
       // plant type, local solar hour, 5-degree latitude band, LAI (order 2),
       // so a warp's tiles share radiation and hence iteration counts; order 3
-      // is order 2 applied within consecutive chunks of 2^18 caller tiles,
-      // so host-order forcing and outputs of a chunk stay L2-resident while
-      // they are gathered into device order (cablegpu_step_host)
+      // is order 2 applied within consecutive chunks of 2^CG_ORDER3_CHUNK_LOG2
+      // caller tiles, so host-order forcing and outputs of a chunk stay
+      // L2-resident while they are gathered into device order
+      // (cablegpu_step_host)
       std::vector<std::pair<unsigned long long, int>> key(c->mp);
       for (int i = 0; i < c->mp; ++i) {
         unsigned long long k = (unsigned long long)(tiles->iveg[i] & 0xff) << 56;
-        if (tiles->order == 3) k = (unsigned long long)(i >> 18) << 51 | (unsigned long long)(tiles->iveg[i] & 0xff) << 43;
+        if (tiles->order == 3)
+          k = (unsigned long long)(i >> CG_ORDER3_CHUNK_LOG2) << 51 | (unsigned long long)(tiles->iveg[i] & 0xff) << 43;
         if (tiles->order == 0) {
           k |= (unsigned long long)(tiles->isoilm[i] & 0xff) << 48;
         } else {

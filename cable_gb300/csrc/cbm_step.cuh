@@ -466,7 +466,9 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
   const float a1gs = ldf(V.a1gs, v), d0gs = ldf(V.d0gs, v), gswmin_p = ldf(V.gswmin, v);
   const float g0 = ldf(V.g0, v), g1 = ldf(V.g1, v), vbeta = ldf(V.vbeta, v), shelrb = ldf(V.shelrb, v);
 
-  float zetar[NITER] = {0.0f, ZETPOS + 1.f, 0.f, 0.f};
+  // stability parameter of the current Monin-Obukhov iteration (canopy%zetar:
+  // 0 for the first, then each iteration's update_zetar result)
+  float zeta = 0.0f;
   float us = 0.f, rt0 = 0.f, rt1 = 0.f, rt1usc = 0.f, rtsoil = ortsoil, cls = 1.f;
   float fev = 0.f, fhv = 0.f, fnv = 0.f, fns = 0.f, fhs = 0.f, fe = 0.f, fh = 0.f, potev = 0.f;
   // canopy%ga persists between steps; read before it is set only by ssnow_potev = 'P-M' (the
@@ -521,7 +523,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) dk_avail[k] = fmaxf(0.0f, wbliq0[k] - 1.1f * swilt) * zse[k] * DLIQ;
   for (int iter = 1; iter <= NITER; ++iter) {
-    const float zi = zetar[iter - 1];
+    const float zi = zeta;
     // comp_friction_vel (cbl_friction_vel.F90:19-108)
     {
       float psim_1 = psim(zi * zref_uv / zref_tq);
@@ -863,12 +865,12 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
     // update_zetar (cbl_zetar.F90:13-159)
     if (iter < NITER) {
       float z = -(VONK * GRAV * zref_tq * (fh + 0.07f * fe)) / (rho * CAPP * tk * us * us * us);
-      zetar[iter] = fmaxf(ZETNEG, fminf(ZETPOS, z));
+      zeta = fmaxf(ZETNEG, fminf(ZETPOS, z));
     }
   }
 
   // ---------------------------------------------------------------- post-loop (:684-1038)
-  const float z4 = zetar[NITER - 1];
+  const float z4 = zeta;   // the last iteration's
   const float cduv = us * us / sqf(fmaxf(ua, UMIN));
   float cdtq = 0.f;
   if (kDiag)

@@ -23,27 +23,34 @@ def runtime():
     return R
 
 
-def test_restart_file_resumes_bitwise(runtime, tmp_path):
+@pytest.mark.parametrize("switches", [{}, {"ssnow_potev": "P-M", "litter": True}])
+def test_restart_file_resumes_bitwise(runtime, tmp_path, switches):
+    """Also with Penman-Monteith soil evaporation, which reads the last
+    step's canopy%ga: the restart file carries the output rows."""
     R = runtime
     ts = W.snow_grid(6000, nsteps=48)
     path = str(tmp_path / "restart.cgf")
     a = R.from_tileset(ts)
+    a.set_options(**switches)
     a.run(1, 24)
     a.restart_write(path, 24)
     a.run(25, 24)
     a.synchronize()
     sa = {k: a.get(k) for k in STATE}
+    out_a = a.get("out")
     a.close()
     b = R.from_tileset(ts)
+    b.set_options(**switches)
     assert b.restart_read(path) == 24
     b.run(25, 24)
     b.synchronize()
     for k in STATE:
         np.testing.assert_array_equal(b.get(k), sa[k], err_msg=k)
+    np.testing.assert_array_equal(b.get("out"), out_a)
     b.close()
     # the file: tile description plus state, the soil water as exact word pairs
     f = cgfile.read(path)
-    assert f.kind == "restart" and f.header["ktau"] == 24 and f.mp == ts.mp
+    assert f.kind == "restart" and f.header["ktau"] == 24 and f.mp == ts.mp and "out" in f.fields
     assert f.fields["wb"][0] == cgfile.DF32 and f.fields["tgg"][:2] == (cgfile.F32, 6)
     np.testing.assert_array_equal(f.read("iveg")[0], ts.iveg)
     hi, lo = f.read_pairs("wb")
