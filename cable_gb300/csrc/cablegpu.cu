@@ -82,6 +82,7 @@ std::vector<FieldDef> make_registry() {
     {"ebal_tot", 1, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
     {"wbal_tot", 1, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
     {"out", CG_NOUT, CABLEGPU_F32, CABLEGPU_KIND_OUTPUT, S_F32},
+    {"tile_status", 1, CABLEGPU_I32, CABLEGPU_KIND_OUTPUT, S_U8},
   };
   for (int i = 0; i < CG_NDIAG; ++i) f.push_back({kDiagNames[i], 1, CABLEGPU_F32, CABLEGPU_KIND_DIAG, S_F32});
   f.push_back({"forcing", CG_NFORC, CABLEGPU_F32, CABLEGPU_KIND_FORCING, S_F32});
@@ -264,6 +265,7 @@ void bind_device_view(cablegpu_ctx* c) {
   D.cansto = (float*)P("cansto"); D.cplant = (float*)P("cplant"); D.csoil = (float*)P("csoil");
   D.owb = (double*)P("owb"); D.ebal_tot = (double*)P("ebal_tot"); D.wbal_tot = (double*)P("wbal_tot");
   D.out = (float*)P("out");
+  D.tile_status = (uint8_t*)P("tile_status");
   D.diag = c->diag ? (float*)P(kDiagNames[0]) : nullptr;
   D.forcing_in = c->host_forcing ? (const float*)P("forcing_in") : nullptr;
   D.forcing_caller_order = 0;

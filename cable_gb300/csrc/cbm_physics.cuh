@@ -40,6 +40,11 @@ constexpr float COSZEN_TOLS = 1.0e-4f, PI_C = 3.1415927f, MAX_GLACIER_SNOWD = 11
 constexpr float MAX_SSDN = 750.0f, MAX_SCONDS = 2.51f, FROZEN_LIMIT = 0.85f, SNMIN = 1.0f;
 constexpr float GW0 = 0.308f, GW1 = 0.514f, GW2 = 0.178f;
 constexpr int LAKES = 16, ICE_SURF = 17, ICE_SOIL = 9, MAXITER = 20, NITER = 4;
+// per-tile status bits (the public CABLEGPU_TILE_* values)
+constexpr uint8_t CG_TS_NONFINITE = 1, CG_TS_DRYLEAF_NOCONV = 2, CG_TS_FORCING_RANGE = 4, CG_TS_OUTPUT_RANGE = 8,
+                  CG_TS_EVAPFBL = 16;
+// x outside [lo, hi], or not a number (the range checks of cable_checks.F90)
+__device__ __forceinline__ bool out_of(float x, float lo, float hi) { return !(x >= lo && x <= hi); }
 
 // Number / order of the optional per-tile diagnostics (debug output).
 #define CG_NDIAG 59
@@ -86,6 +91,7 @@ struct CgDev {
   double* wbal_tot;
   // outputs
   float* out;              // [CG_NOUT]
+  uint8_t* tile_status;    // per-tile status bits (CG_TS_*), OR-ed by the kernels, cleared by the caller
   float* out_caller;       // [CG_NOUT][mp] copy of out in the caller's tile order (host-I/O steps), or null
   float* diag;             // [CG_NDIAG] or null
   float* work_a;           // phase A -> B, C handoff record

@@ -106,6 +106,12 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
   const float precip_sn = F[CGF_PRECIP_SN], tk = F[CGF_TK], pmb = F[CGF_PMB], ua = F[CGF_UA], qv = F[CGF_QV];
   const float ca = F[CGF_CA], coszen = F[CGF_COSZEN], doy = F[CGF_DOY];
   const float tvrad = tk;
+  // the driver's forcing checks (cable_input.F90:2683-2689; ranges
+  // cable_checks.F90:60-70): SWdown, LWdown, Qair, Rainf, Wind, Tair, PSurf
+  if (out_of(fsd0 + fsd1, 0.f, 1360.f) || out_of(fld, 0.f, 950.f) || out_of(qv, 0.f, 0.1f) ||
+      out_of(precip / P.dels, 0.f, 0.1f) || out_of(ua, 0.f, 75.f) || out_of(tk, 200.f, 333.f) ||
+      out_of(pmb, 500.f, 1100.f))
+    D.tile_status[t] |= CG_TS_FORCING_RANGE;
 
   // wbliq as left by the previous soil_snow call
   float wbliq0[CG_MS];
@@ -729,6 +735,10 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
         // a tile that has stopped iterating never changes again: leave now
         if (!(veg_mask && abs_deltlf > conv)) break;
       }
+      // status bits of this iteration, recorded with diagnostics on (they cost
+      // the fast kernel registers in its hottest loop): pass limit reached
+      // unconverged; the reference's 'oldevapfbl not right' condition
+      uint8_t it_bits = (kDiag && veg_mask && abs_deltlf > conv) ? CG_TS_DRYLEAF_NOCONV : 0;
       // the layer amounts of the latest extracting pass (zero if none)
       if (fe_mm_last > 0.f) {
         transp_extract(fe_mm_last, froot, dk_avail, evapfbl);
@@ -745,8 +755,11 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
         if (!(fabsf(fevc - so2 * rlam / dels) > 1.0e-4f)) {
 #pragma unroll
           for (int kk = 0; kk < CG_MS; ++kk) evapfbl[kk] = oldevapfbl[kk];
+        } else {
+          if (kDiag) it_bits |= CG_TS_EVAPFBL;
         }
       }
+      if (kDiag && it_bits) D.tile_status[t] |= it_bits;
       frday = 12.0f * rdy_sum;
       fpn = fminf(-12.0f * an_y_sum, frday);
       // training row: features at entry, converged stomatal conductance,
@@ -991,7 +1004,16 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
 #pragma unroll
     for (int i = 0; i < 7; ++i) D.out_caller[(size_t)i * D.mp + o] = outv[i];
   }
-  if (!finite) atomicOr(D.status, 1u);
+  {
+    // output ranges of the reference's output checks (cable_checks.F90:71-123):
+    // Qle, Qh, Qg, Rnet, VegT
+    uint8_t bits = finite ? 0 : CG_TS_NONFINITE;
+    if (!finite) atomicOr(D.status, 1u);
+    if (out_of(fe, -2500.f, 2500.f) || out_of(fh, -2000.f, 2000.f) || out_of(ga, -4000.f, 4000.f) ||
+        out_of(rnet, -500.f, 1250.f) || out_of(tv, 213.f, 353.f))
+      bits |= CG_TS_OUTPUT_RANGE;
+    if (bits) D.tile_status[t] |= bits;
+  }
   if (kDiag) {
     const int idx[37] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 18, 20, 21, 22, 32, 33, 34, 35,
                          36, 43, 44, 45, 50, 51, 52, 53, 55, 56, 57, 58};
@@ -2028,7 +2050,17 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   D.owb[t] = wbtot; D.wbal_tot[t] = wbal_tot;
   D.out[7 * ld + t] = trad;
   if (D.out_caller) D.out_caller[(size_t)7 * D.mp + D.tile_id[t]] = trad;
-  if (!isfinite(trad)) atomicOr(D.status, 1u);
+  {
+    uint8_t bits = 0;
+    if (!isfinite(trad)) { atomicOr(D.status, 1u); bits |= CG_TS_NONFINITE; }
+    // RadT and SoilTemp ranges (cable_checks.F90:81-104)
+    float tlo = tgg[0], thi = tgg[0];
+#pragma unroll
+    for (int k = 1; k < CG_MS; ++k) { tlo = fminf(tlo, tgg[k]); thi = fmaxf(thi, tgg[k]); }
+    if (out_of(trad, 200.f, 373.f) || out_of(tlo, 213.f, 353.f) || out_of(thi, 213.f, 353.f))
+      bits |= CG_TS_OUTPUT_RANGE;
+    if (bits) D.tile_status[t] |= bits;
+  }
   if (kDiag) {
     const int idx[16] = {17, 19, 23, 24, 25, 26, 27, 28, 37, 38, 39, 40, 41, 42, 46, 54};
     const float val[16] = {fevc, fevw, -fpn - frp, fpn + frs + frp, frp + frday, frp, frs, trad, runoff_mm,

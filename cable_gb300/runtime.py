@@ -54,6 +54,12 @@ SW_POTEV_PM = 64
 SW_NEW_REDUCE_SOILEVP = 128
 SW_NEW_RUNOFF_SPEED = 256
 SW_DIAG_SOIL_RESP_OFF = 512
+# per-tile status bits of the field "tile_status" (include/cablegpu.h)
+TILE_NONFINITE = 1
+TILE_DRYLEAF_NOCONV = 2
+TILE_FORCING_RANGE = 4
+TILE_OUTPUT_RANGE = 8
+TILE_EVAPFBL = 16
 FWSOIL_SWITCH = {"standard": 0, "non-linear extrapolation": SW_FWSOIL_NONLINEAR,
                  "Lai and Ktaul 2000": SW_FWSOIL_LAI_KTAUL}
 

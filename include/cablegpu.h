@@ -200,7 +200,35 @@ int cablegpu_run(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels);
  * of the offline driver (cable_serial.F90:594-640). */
 int cablegpu_step_host(cablegpu_ctx* ctx, int ktau, float dels, const float* host_forcing, float* host_out);
 /* Waits for all queued work; returns CABLEGPU_ERR_NONFINITE if any step
- * since the last call produced a non-finite output flux. */
+ * since the last call produced a non-finite output flux.  Which tiles, and
+ * what else went wrong where, is in the per-tile field "tile_status" (one
+ * byte per tile, read with cablegpu_get_field as int): the kernels OR these
+ * bits into it every step and never clear it (the caller clears it with
+ * cablegpu_set_field); nothing traps.
+ *   CABLEGPU_TILE_NONFINITE       an output flux or the radiative temperature
+ *                                 was not finite
+ *   CABLEGPU_TILE_DRYLEAF_NOCONV  a dryLeaf iteration ended at its 20-pass
+ *                                 limit without meeting its 0.1 K criterion
+ *                                 (the best iterate is kept, as the
+ *                                 reference does); recorded with
+ *                                 diagnostics on
+ *   CABLEGPU_TILE_FORCING_RANGE   a forcing value outside the driver's
+ *                                 check ranges (SWdown, LWdown, Qair, Rainf,
+ *                                 Wind, Tair, PSurf: cable_input.F90:2683-2689,
+ *                                 cable_checks.F90:60-70), or not finite
+ *   CABLEGPU_TILE_OUTPUT_RANGE    an output outside the reference's output
+ *                                 ranges (Qle, Qh, Qg, Rnet, VegT, RadT,
+ *                                 SoilTemp: cable_checks.F90:71-123)
+ *   CABLEGPU_TILE_EVAPFBL         the condition under which the reference
+ *                                 prints 'oldevapfbl not right'
+ *                                 (cbl_dryLeaf.F90:626-641) and keeps the
+ *                                 latest layer extraction; recorded with
+ *                                 diagnostics on */
+#define CABLEGPU_TILE_NONFINITE 1
+#define CABLEGPU_TILE_DRYLEAF_NOCONV 2
+#define CABLEGPU_TILE_FORCING_RANGE 4
+#define CABLEGPU_TILE_OUTPUT_RANGE 8
+#define CABLEGPU_TILE_EVAPFBL 16
 int cablegpu_synchronize(cablegpu_ctx* ctx);
 
 /* Timing helpers for benchmarks: CUDA events on the context's stream.

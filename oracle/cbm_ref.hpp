@@ -97,6 +97,8 @@ struct Diag {
   R2 wbtot;
   R gswx[2], fwsoil;
   int dryleaf_passes;            // total dryLeaf passes over the 4 MO iterations
+  int dryleaf_noconv;            // MO iterations whose dryLeaf loop ended unconverged at the pass limit
+  int evapfbl_err;               // MO iterations with the reference's 'oldevapfbl not right' message
 };
 
 // ==========================================================================
@@ -524,6 +526,8 @@ struct CbmRef {
     R frday, fpn;
     R2 evapfbl[MS];
     int passes;
+    int noconv = 0;     // MO iterations whose dryLeaf loop hit the pass limit unconverged
+    int evapfbl_err = 0;  // MO iterations where the reference prints 'oldevapfbl not right'
   };
 
   void dryLeaf(R dels, const P& p, const Rad& rad, const Met& met, const Air& air, R vlaiw, R cansto, R fwet,
@@ -699,6 +703,7 @@ struct CbmRef {
       // tiles are exact no-ops), so leaving the loop early is exact.
       if (!(vlaiw > R(LAI_THRESH) && abs_deltlf > R(0.1))) break;
     }
+    if (vlaiw > R(LAI_THRESH) && abs_deltlf > R(0.1)) L.noconv++;
     L.fevc = (R(1.0) - fwet) * L.ecy;
     if (L.ecy > 0.0 && fwet < R(1.0)) {
       if (std::fabs(L.ecy - ecx) > 1.0e-6) {
@@ -706,6 +711,7 @@ struct CbmRef {
         for (int kk = 0; kk < MS; ++kk) so += oldevapfbl[kk];
         if (std::fabs(L.fevc - (so * air.rlam / dels)) > 1.0e-4) {
           // the reference prints a diagnostic and keeps evapfbl
+          L.evapfbl_err++;
         } else {
           for (int kk = 0; kk < MS; ++kk) L.evapfbl[kk] = oldevapfbl[kk];
         }
@@ -1255,6 +1261,8 @@ struct CbmRef {
     d.tvair = met.tvair; d.qvair = met.qvair; d.swnet = rad.swnet; d.lwnet = rad.lwnet;
     d.wbtot = so.wbtot; d.gswx[0] = L.gswx[0]; d.gswx[1] = L.gswx[1]; d.fwsoil = L.fwsoil;
     d.dryleaf_passes = passes_total;
+    d.dryleaf_noconv = L.noconv;
+    d.evapfbl_err = L.evapfbl_err;
   }
 
   // ====================================================================

@@ -164,6 +164,9 @@ def test_nonfinite_input_is_reported_not_trapped(runtime):
     with pytest.raises(R.CableGPUError) as e:
         g.synchronize()
     assert e.value.code == -3
+    st = g.get("tile_status")[0]
+    assert st[17] & R.TILE_NONFINITE and st[17] & R.TILE_FORCING_RANGE
+    assert not np.any(np.delete(st, 17) & (R.TILE_NONFINITE | R.TILE_FORCING_RANGE))
     g.set_synthetic_forcing(ts.seed)
     ok = R.from_tileset(ts)
     ok.step(1)
@@ -373,3 +376,45 @@ def test_science_switches_match_oracle(oracle, runtime, which):
     a0 = np.asarray(g0[field] if field in g0 else d0[field], np.float64)
     a1 = np.asarray(gs[field] if field in gs else gd[field], np.float64)
     assert np.abs(a1 - a0).max() > thr, (which, field, np.abs(a1 - a0).max())
+
+
+def test_tile_status_matches_the_oracle_and_flags_bad_forcing(oracle, runtime):
+    """The per-tile status bits: dryLeaf non-convergence and the reference's
+    'oldevapfbl not right' condition agree with the oracle step by step
+    (up to the precision-noise tiles), the seeded forcing is inside the
+    driver's check ranges, and finite out-of-range forcing on two tiles sets
+    their forcing bit only.  (The two dryLeaf bits are recorded with
+    diagnostics on.)"""
+    R = runtime
+    ts = W.snow_grid(20000, nsteps=12)
+    n = 12
+    F = oracle.forcing(ts, 0, n)
+    g = R.from_tileset(ts)
+    g.set_options(diag=True)
+    st = oracle.init_state(ts, 0)
+    agree_nc, agree_ev, any_nc = [], [], 0
+    for k in range(n):
+        g.set("tile_status", 0)
+        g.set_forcing(F[k])
+        g.step(k + 1, ts.dels)
+        bits = g.get("tile_status")[0]
+        d = oracle.run(ts, st, 1, ktau0=k + 1, forcing=F[k:k + 1], precision=0)
+        assert not np.any(bits & (R.TILE_FORCING_RANGE | R.TILE_NONFINITE))
+        nc_o = np.asarray(d["dryleaf_noconv"]) > 0
+        ev_o = np.asarray(d["evapfbl_err"]) > 0
+        agree_nc.append(np.mean((bits & R.TILE_DRYLEAF_NOCONV > 0) == nc_o))
+        agree_ev.append(np.mean((bits & R.TILE_EVAPFBL > 0) == ev_o))
+        any_nc += int(nc_o.sum())
+    assert min(agree_nc) > 0.998 and min(agree_ev) > 0.998, (agree_nc, agree_ev)
+    # finite but out-of-range forcing: tile 17 at 340 K, tile 23 with 80 m/s wind
+    f = F[0].copy()
+    f[5, 17] = 340.0
+    f[7, 23] = 80.0
+    g.set("tile_status", 0)
+    g.set_forcing(f)
+    g.step(n + 1, ts.dels)
+    g.synchronize()
+    bits = g.get("tile_status")[0]
+    assert bits[17] & R.TILE_FORCING_RANGE and bits[23] & R.TILE_FORCING_RANGE
+    assert not np.any(np.delete(bits, [17, 23]) & R.TILE_FORCING_RANGE)
+    g.close()
