@@ -373,6 +373,15 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
 // its converged result) to D.harvest.  kSur: the first
 // iteration's dryLeaf starts from the network's leaf temperature (the
 // surrogate; see the comment at its use).
+// A read of a read-only table entry that the compiler may not hoist or keep
+// in a register: re-reading it where it is used costs an L1 hit, holding it
+// live through the dryLeaf iteration costs the canopy kernel registers.
+__device__ __forceinline__ float ldv(const float* p) {
+  float r;
+  asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(r) : "l"(p));
+  return r;
+}
+
 // transp_soil_water (cbl_remove_trans.F90:43-93): root-weighted extraction of
 // fe_mm (mm of transpiration over the step) from the layers, each layer's
 // deficit carried to the next; returns the total.  Explicitly rounded
@@ -402,7 +411,6 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
   (void)isoilm;
   const CgPftTable& V = T->pft;
   const CgSoilTable& S = T->soil;
-  const float dleaf = ldf(V.dleaf, v);
   float froot[CG_MS];
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
@@ -466,11 +474,9 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) evapfbl[k] = 0.0f;
   // per-PFT photosynthesis parameters (gathered once)
-  const float vcmax = ldf(V.vcmax, v), ejmax = ldf(V.ejmax, v), frac4 = ldf(V.frac4, v);
-  const float conkc0 = ldf(V.conkc0, v), conko0 = ldf(V.conko0, v), ekc = ldf(V.ekc, v), eko = ldf(V.eko, v);
-  const float alpha = ldf(V.alpha, v), convex = ldf(V.convex, v), cfrd = ldf(V.cfrd, v);
-  const float a1gs = ldf(V.a1gs, v), d0gs = ldf(V.d0gs, v), gswmin_p = ldf(V.gswmin, v);
-  const float g0 = ldf(V.g0, v), g1 = ldf(V.g1, v), vbeta = ldf(V.vbeta, v), shelrb = ldf(V.shelrb, v);
+  // per-PFT photosynthesis parameters: re-read from the (L1-resident) table
+  // where used instead of being held in registers through the iteration
+  const float vbeta = ldf(V.vbeta, v), shelrb = ldf(V.shelrb, v);
 
   // stability parameter of the current Monin-Obukhov iteration (canopy%zetar:
   // 0 for the first, then each iteration's update_zetar result)
@@ -550,7 +556,8 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
     }
     // boundary-layer conductance (:374-397)
     if (veg_mask) {
-      float gbvtop = cmolar * APOL * visc / PRANDT / dleaf * sqrtf(us / fmaxf(usuh, 1.e-6f) * dleaf / visc) *
+      const float dl = ldv(V.dleaf + v);
+      float gbvtop = cmolar * APOL * visc / PRANDT / dl * sqrtf(us / fmaxf(usuh, 1.e-6f) * dl / visc) *
                      0.89194175f /* prandt**(1/3) */ / shelrb;
       gbvtop = fmaxf(0.05f, gbvtop);
       gbhu[0] = gbvtop * (1.0f - expf(-fminf(vlaiw * (0.5f * coexp + extkb), 20.0f))) / (extkb + 0.5f * coexp);
@@ -572,7 +579,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
       if (sampled) {
         const float sc = scalex[0] + scalex[1];
         feat[0] = qcan_par[0]; feat[1] = qcan_par[1]; feat[2] = tlfx; feat[3] = dsx; feat[4] = ca;
-        feat[5] = vcmax * sc; feat[6] = ejmax * (1.0f - frac4) * sc; feat[7] = P.medlyn ? g1 : a1gs;
+        feat[5] = ldv(V.vcmax + v) * sc; feat[6] = ldv(V.ejmax + v) * (1.0f - ldv(V.frac4 + v)) * sc; feat[7] = P.medlyn ? ldv(V.g1 + v) : ldv(V.a1gs + v);
         feat[8] = fwsoil; feat[9] = vlaiw; feat[10] = us; feat[11] = tvair;
       }
       bool sur_try = false;
@@ -581,6 +588,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
         const float dt = D.sur_dt[t];
         if (isfinite(dt)) { sur_try = true; tlf_sur = tlf_entry + dt; }
       }
+      const float gswmin_p = ldv(V.gswmin + v);
       float gswmin[2] = {fmaxf(1.e-6f, scalex[0] * gswmin_p), fmaxf(1.e-6f, scalex[1] * gswmin_p)};
       float gh[2] = {1e-3f, 1e-3f}, ghr[2] = {1e-3f, 1e-3f}, psycst[2] = {psyc, psyc};
       float rdx[2] = {0.f, 0.f}, anx[2] = {0.f, 0.f};
@@ -615,6 +623,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
         const bool active = veg_mask && abs_deltlf > conv;
         if (active) {
           ++passes_total;
+          const float dleaf = ldv(V.dleaf + v);
           float gras = fmaxf(1.0e-6f, 1.595E8f * fabsf(tlfx - tvair) * (dleaf * dleaf * dleaf));
           float gr4 = sqrtf(sqrtf(gras));
 #pragma unroll
@@ -624,35 +633,37 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
             ghr[l] = gradis[l] + gh[l];
           }
           float vcmxt3[2], vcmxt4[2], vx3[2], vx4[2], gs_coeff[2];
+          const float vcmax = ldv(V.vcmax + v), frac4 = ldv(V.frac4 + v);
           float temp = xvcmxt3(tlfx) * vcmax * (1.0f - frac4);
           vcmxt3[0] = scalex[0] * temp; vcmxt3[1] = scalex[1] * temp;
           temp = xvcmxt4(tlfx - TFRZ) * vcmax * frac4;
           vcmxt4[0] = scalex[0] * temp; vcmxt4[1] = scalex[1] * temp;
-          temp = xejmxt3(tlfx) * ejmax * (1.0f - frac4);
+          temp = xejmxt3(tlfx) * ldv(V.ejmax + v) * (1.0f - frac4);
           float ejmxt3[2] = {scalex[0] * temp, scalex[1] * temp};
           float tdiff = tlfx - TREFK;
           float arr = (1.0f - TREFK / tlfx) / (RGAS * TREFK);
-          float conkct = conkc0 * expf(ekc * arr);
-          float conkot = conko0 * expf(eko * arr);
+          float conkct = ldv(V.conkc0 + v) * expf(ldv(V.ekc + v) * arr);
+          float conkot = ldv(V.conko0 + v) * expf(ldv(V.eko + v) * arr);
           tlfxx = tlfx;
           float cx1 = conkct * (1.0f + 0.21f / conkot);
           float cx2 = 2.0f * GAM0 * (1.0f + GAM1 * tdiff + GAM2 * tdiff * tdiff);
 #pragma unroll
           for (int l = 0; l < 2; ++l) {
             float par = qcan_par[l] * 4.6e-6f;
+            const float alpha = ldv(V.alpha + v), convex = ldv(V.convex + v), cfrd = ldv(V.cfrd + v);
             vx3[l] = ej3x(par * (1.0f - frac4), alpha, convex, ejmxt3[l]);
             vx4[l] = ej4x(par * frac4, alpha, convex, vcmxt4[l]);
             rdx[l] = cfrd * vcmxt3[l] + cfrd * vcmxt4[l];
           }
           if (!P.medlyn) {
-            float f = a1gs / (1.0f + dsx / d0gs);
+            float f = ldv(V.a1gs + v) / (1.0f + dsx / ldv(V.d0gs + v));
             gs_coeff[0] = (fwsoil / csx[0]) * f;
             gs_coeff[1] = (fwsoil / csx[1]) * f;
           } else {
-            gswmin[0] = g0; gswmin[1] = g0;
+            gswmin[0] = gswmin[1] = ldv(V.g0 + v);
             float vpd = (dsx < 50.0f) ? 0.05f : dsx * 1e-3f;
             float num = (fwsoil <= 0.05f) ? fwsoil / 0.05f : 1.0f;
-            float t2 = (g1 * fwsoil) * rsqrtf(vpd);
+            float t2 = (ldv(V.g1 + v) * fwsoil) * rsqrtf(vpd);
             gs_coeff[0] = (num + t2) / csx[0];
             gs_coeff[1] = (num + t2) / csx[1];
           }
