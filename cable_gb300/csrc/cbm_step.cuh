@@ -61,9 +61,9 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
   for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
   const float ssat = ldf(S.ssat, so), sfc = ldf(S.sfc, so), swilt = ldf(S.swilt, so), css = ldf(S.css, so);
   const float rhosoil = ldf(S.rhosoil, so);
-  float zse[CG_MS];
-#pragma unroll
-  for (int k = 0; k < CG_MS; ++k) zse[k] = S.zse[k];
+  // soil layer thicknesses (m), cable_parameters.F90:1241: model constants,
+  // the same values as the table's, as immediates rather than registers
+  constexpr float zse[CG_MS] = {0.022f, 0.058f, 0.154f, 0.409f, 1.085f, 2.872f};
 
   // ---------------------------------------------------------------- state
   df32 wb[CG_MS], wbice[CG_MS];
@@ -415,9 +415,9 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
   const float sfc = ldf(S.sfc, so), swilt = ldf(S.swilt, so);
-  float zse[CG_MS];
-#pragma unroll
-  for (int k = 0; k < CG_MS; ++k) zse[k] = S.zse[k];
+  // soil layer thicknesses (m), cable_parameters.F90:1241: model constants,
+  // the same values as the table's, as immediates rather than registers
+  constexpr float zse[CG_MS] = {0.022f, 0.058f, 0.154f, 0.409f, 1.085f, 2.872f};
   // phase A record
   const float* WA = D.work_a;
   auto A = [&](int i) { return WA[i * ld + t]; };
@@ -1049,9 +1049,9 @@ __device__ __forceinline__ void phase_c1(const CgDev& D, const CgTables* __restr
   for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
   const float ssat = ldf(S.ssat, so), sfc = ldf(S.sfc, so), swilt = ldf(S.swilt, so), css = ldf(S.css, so);
   const float rhosoil = ldf(S.rhosoil, so);
-  float zse[CG_MS];
-#pragma unroll
-  for (int k = 0; k < CG_MS; ++k) zse[k] = S.zse[k];
+  // soil layer thicknesses (m), cable_parameters.F90:1241: model constants,
+  // the same values as the table's, as immediates rather than registers
+  constexpr float zse[CG_MS] = {0.022f, 0.058f, 0.154f, 0.409f, 1.085f, 2.872f};
   // state
   df32 wb[CG_MS], wbice[CG_MS];
 #pragma unroll
@@ -1396,9 +1396,9 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
   for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
   const float ssat = ldf(S.ssat, so), sfc = ldf(S.sfc, so), swilt = ldf(S.swilt, so), css = ldf(S.css, so);
   const float rhosoil = ldf(S.rhosoil, so);
-  float zse[CG_MS];
-#pragma unroll
-  for (int k = 0; k < CG_MS; ++k) zse[k] = S.zse[k];
+  // soil layer thicknesses (m), cable_parameters.F90:1241: model constants,
+  // the same values as the table's, as immediates rather than registers
+  constexpr float zse[CG_MS] = {0.022f, 0.058f, 0.154f, 0.409f, 1.085f, 2.872f};
   // state
   df32 wb[CG_MS], wbice[CG_MS];
 #pragma unroll
@@ -1674,9 +1674,9 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
   const float ssat = ldf(S.ssat, so), sfc = ldf(S.sfc, so), swilt = ldf(S.swilt, so), css = ldf(S.css, so);
   const float rhosoil = ldf(S.rhosoil, so);
-  float zse[CG_MS];
-#pragma unroll
-  for (int k = 0; k < CG_MS; ++k) zse[k] = S.zse[k];
+  // soil layer thicknesses (m), cable_parameters.F90:1241: model constants,
+  // the same values as the table's, as immediates rather than registers
+  constexpr float zse[CG_MS] = {0.022f, 0.058f, 0.154f, 0.409f, 1.085f, 2.872f};
   // state
   df32 wb[CG_MS], wbice[CG_MS];
 #pragma unroll
