@@ -33,6 +33,14 @@ struct StepParams {
 __device__ __forceinline__ float ldf(const float* p, int i) { return __ldg(p + i); }
 
 
+// half-depths between layer centres (cable_parameters.F90:1828-1831) of the
+// constant layer thicknesses, as immediates: zshh(1) = zse(1)/2,
+// zshh(k) = (zse(k-1) + zse(k))/2, zshh(ms+1) = zse(ms)/2 (the table's values)
+__device__ constexpr float ZSE_C[CG_MS] = {0.022f, 0.058f, 0.154f, 0.409f, 1.085f, 2.872f};
+__device__ constexpr float ZSHH[CG_MS + 1] = {0.5f * ZSE_C[0], 0.5f * (ZSE_C[0] + ZSE_C[1]), 0.5f * (ZSE_C[1] + ZSE_C[2]),
+                                   0.5f * (ZSE_C[2] + ZSE_C[3]), 0.5f * (ZSE_C[3] + ZSE_C[4]),
+                                   0.5f * (ZSE_C[4] + ZSE_C[5]), 0.5f * ZSE_C[5]};
+
 // Phase A record (per tile, [CG_NA][ld]): forcing, roughness, air, radiation,
 // interception and the soil liquid water seen by dryLeaf.
 #define CG_NA 52
@@ -1669,9 +1677,6 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   const CgPftTable& V = T->pft;
   const CgSoilTable& S = T->soil;
   const float vlai = (iveg >= 14) ? 0.0f : D.vlai[t];
-  float froot[CG_MS];
-#pragma unroll
-  for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
   const float ssat = ldf(S.ssat, so), sfc = ldf(S.sfc, so), swilt = ldf(S.swilt, so), css = ldf(S.css, so);
   const float rhosoil = ldf(S.rhosoil, so);
   // soil layer thicknesses (m), cable_parameters.F90:1241: model constants,
@@ -1829,7 +1834,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
       float fact = __powf(wbh_k, ibp2 - 1.f);
       float icef = fmaxf(wbicef[k - 2] / fmaxf(0.01f, wbf[k - 2]), wbicef[k - 1] / fmaxf(0.01f, wbf[k - 1]));
       float pwb_wbh = (hsbh * (1.f - fminf(2.f * fminf(0.1f, icef), 0.1f))) * fmaxf(pwb_min, wbh_k * fact);
-      z3[k - 1] = pwb_wbh / ldf(S.zshh, k - 1);
+      z3[k - 1] = pwb_wbh / ZSHH[k - 1];
       a[k - 1] = -dtt[k - 1] * z3[k - 1];
       c[k - 2] = -dtt[k - 2] * z3[k - 1];
     }
@@ -1958,6 +1963,10 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   const float trad = sqrtf(sqrtf((1.f - transd) * pow4(tv) + transd * pow4(tss)));
 
   // carbon, icycle == 0 (cable_carbon.F90:38-360, cbm:214-229)
+  // root fractions, used only by the carbon routines below
+  float froot[CG_MS];
+#pragma unroll
+  for (int k = 0; k < CG_MS; ++k) froot[k] = ldf(V.froot[k], v);
   float frp, frpw, frpr, frs;
   float cplant[3], csoil[2];
 #pragma unroll
