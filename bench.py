@@ -239,7 +239,7 @@ def surrogate_arm(args, d, ts, plain_value, tuned):
     whose closure pass moves the leaf temperature by more than 0.1 K fall
     back to the plain iteration from its usual start), and measure its
     error against the plain kernel run side by side from the same state
-    (the plain iteration is the judge; the plain kernel's own agreement with
+    (the plain iteration is the reference for its error; the plain kernel's own agreement with
     the FP64 oracle is what the GPU tests check)."""
     import numpy as np
     from cable_gb300 import runtime as R

@@ -124,7 +124,7 @@ struct SoilTable {
   double sfc[NSOIL], silt[NSOIL], ssat[NSOIL], sucs[NSOIL], swilt[NSOIL];
   // Soil albedo is not part of the reference tables (it comes from the gridded
   // soil file, which is not available); these VIS/NIR values are a stated
-  // choice of this build, one pair per soil type.
+  // choice of this library, one pair per soil type.
   double albsoil_vis[NSOIL], albsoil_nir[NSOIL];
 };
 
