@@ -8,9 +8,12 @@ seeded synthetic forcing generated inside the kernels, 30-minute steps.
 Lines printed (one JSON line on rank 0):
   value  device-resident throughput: state and forcing generator in HBM, the
          timestep's kernels replayed from CUDA graphs, timed with CUDA events
-  e2e    the same steps through the C ABI with host buffers: each step
-         uploads its met forcing from pinned host memory (cablegpu_set_forcing)
-         and downloads the 8 output fluxes (cablegpu_get_field)
+  e2e    the same steps through the C ABI with host buffers
+         (cablegpu_step_host): each step uploads its met forcing from pinned
+         host memory and downloads the 8 output fluxes, the copies
+         overlapping neighbouring steps; host arrays in the context's device
+         tile order (cablegpu_tile_order), with the caller-order figure
+         beside it (e2e.caller_order)
   roofline  the timestep's algorithmic HBM bytes per step / measured step time
   cpu_baseline  the CPU restatement of the reference cbm() (REAL = FP32,
          r_2 = FP64, the reference's own precision mix) on all host cores, on a
@@ -358,43 +361,53 @@ def run_gb300(args):
             "scope": "one timestep (its 5 kernels, CUDA events around each step), %d algorithmic B per tile-step"
                      % ALGO_BYTES_PER_TILE_STEP,
             "kernels_ms": {k: round(v, 4) for k, v in phase_ms.items()}}
-    # --- end to end through the C ABI with host buffers.  Host arrays are in
-    # the caller's tile order, so this context uses tile order 3 (the
-    # climate-coherent order within 2^18-tile chunks of the caller's order),
-    # which keeps the reordering of each step's forcing and outputs L2-local.
-    e2e = None
-    try:
+    # --- end to end through the C ABI with host buffers: every step uploads
+    # its forcing from pinned host memory and downloads its 8 output fluxes,
+    # the copies overlapping the neighbouring steps (cablegpu_step_host).
+    # Headline: host buffers in the context's device tile order
+    # (cablegpu_set_host_layout(1); a driver fills its arrays through
+    # cablegpu_tile_order once), on the autotuned context.  Beside it: host
+    # buffers in the caller's order, which needs tile order 3 (the
+    # climate-coherent order within 2^18-tile chunks of the caller's order)
+    # to keep the per-step gather and scatter of caller positions L2-local.
+    def host_steps(gc, layout, ktau0):
         import torch
-        g.close()
-        g = R.from_tileset(ts, device=d.local, order=3)
-        g.set_blocks(blocks)
-        g.set_options(capture_forcing=True)
-        g.step(1, dels)
-        f0 = g.get("forcing")
-        g.step(2, dels)
-        f1 = g.get("forcing")
-        g.set_options(capture_forcing=False)
-        ktau = 3
+        gc.set_options(capture_forcing=True)
+        gc.step(ktau0, dels)
+        f0 = gc.get("forcing")
+        gc.step(ktau0 + 1, dels)
+        f1 = gc.get("forcing")
+        gc.set_options(capture_forcing=False)
+        gc.set_host_layout(layout)
+        if layout == 1:
+            perm = gc.tile_order()
+            f0, f1 = f0[:, perm], f1[:, perm]
+        k = ktau0 + 2
         pin = torch.cuda.is_available()
-        host_f = [torch.from_numpy(f).pin_memory() if pin else torch.from_numpy(f) for f in (f0, f1)]
-        host_f = [np.ascontiguousarray(h.numpy()) for h in host_f]
+        host_f = [np.ascontiguousarray(torch.from_numpy(np.ascontiguousarray(f)).pin_memory().numpy() if pin else f)
+                  for f in (f0, f1)]
         outs = [torch.empty((8, args.mp), dtype=torch.float32, pin_memory=pin).numpy() for _ in range(2)]
-        # warm the pipelined host path (staging buffers, copy streams)
-        for n in range(2):
-            g.step_host(ktau, host_f[n], outs[n], dels); ktau += 1
-        g.synchronize()
+        for n in range(2):   # warm the pipelined host path (staging buffers, copy streams)
+            gc.step_host(k, host_f[n], outs[n], dels); k += 1
+        gc.synchronize()
         d.barrier()
         t0 = time.perf_counter()
         for n in range(args.e2e_steps):
-            # every step uploads its forcing from pinned host memory and
-            # downloads its 8 output fluxes; copies overlap neighbouring steps
-            g.step_host(ktau, host_f[n % 2], outs[n % 2], dels); ktau += 1
-        g.synchronize()
+            gc.step_host(k, host_f[n % 2], outs[n % 2], dels); k += 1
+        gc.synchronize()
         secs = d.max(time.perf_counter() - t0)
-        e2e = {"value": d.world * args.mp * args.e2e_steps / secs, "unit": "tile-timesteps/s",
-               "h2d_bytes_per_step": int(f0.nbytes), "d2h_bytes_per_step": int(outs[0].nbytes),
-               "steps": args.e2e_steps, "tile_order": 3,
-               "path": "cablegpu_step_host: pinned host buffers, one copy stream per direction"}
+        return {"value": d.world * args.mp * args.e2e_steps / secs, "unit": "tile-timesteps/s",
+                "h2d_bytes_per_step": int(f0.nbytes), "d2h_bytes_per_step": int(outs[0].nbytes), "steps": args.e2e_steps}
+    e2e = None
+    try:
+        e2e = host_steps(g, 1, ktau + 8)
+        e2e.update({"tile_order": order, "host_layout": "device tile order (cablegpu_tile_order)",
+                    "path": "cablegpu_step_host: pinned host buffers, one copy stream per direction"})
+        g.close()
+        g = R.from_tileset(ts, device=d.local, order=3)
+        g.set_blocks(blocks)
+        cal = host_steps(g, 0, 1)
+        e2e["caller_order"] = {"value": cal["value"], "tile_order": 3, "host_layout": "caller tile order"}
     except Exception as exc:  # the line still prints; the failure is stated
         e2e = {"value": None, "unit": "tile-timesteps/s", "error": str(exc)[:200]}
     g.close()

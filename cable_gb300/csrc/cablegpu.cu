@@ -194,6 +194,7 @@ struct cablegpu_ctx {
   CgForcingSpec forc{12345ull, 1, 1800.f};
   int medlyn = 0, diag = 0, capture_forcing = 0, thermal_fix = 0, litter = 0, rev_corr = 0;
   int switches = 0;                // the CABLEGPU_SW_* mask the fields above come from
+  int host_layout = 0;             // host buffers of step_host / forcing files: 0 caller order, 1 device order
   cudaGraphExec_t graph = nullptr;
   float graph_dels = -1.f;
   int graph_diag = -1, graph_switches = -1, graph_hostforc = -1, graph_capture = -1;
@@ -271,9 +272,10 @@ void bind_device_view(cablegpu_ctx* c) {
   D.forcing_caller_order = 0;
   if (c->io_forcing) {
     D.forcing_in = c->io_forcing;
-    D.forcing_caller_order = 1;
+    D.forcing_caller_order = c->host_layout == 0 ? 1 : 2;
   }
   D.out_caller = c->io_out;
+  D.out_caller_order = c->host_layout == 0 ? 1 : 0;
   D.forcing_out = c->capture_forcing ? (float*)P("forcing") : nullptr;
   D.work_a = (float*)P("work_a");
   D.work_b = (float*)P("work_b");
@@ -720,6 +722,19 @@ int cablegpu_step_host(cablegpu_ctx* c, int ktau, float dels, const float* host_
   CG_CUDA(c, cudaMemcpyAsync(host_out, c->d_fout[slot], ob, cudaMemcpyDeviceToHost, c->dstream));
   CG_CUDA(c, cudaEventRecord(c->ev_d2h[slot], c->dstream));
   ++c->io_count;
+  return CABLEGPU_OK;
+}
+
+int cablegpu_set_host_layout(cablegpu_ctx* c, int layout) {
+  if (!c || (layout != 0 && layout != 1)) return fail(c, CABLEGPU_ERR_ARG, "set_host_layout: layout must be 0 or 1");
+  if (c->io_ready) CG_CUDA(c, cudaStreamSynchronize(c->stream));   // no step in flight changes layout
+  c->host_layout = layout;
+  return CABLEGPU_OK;
+}
+
+int cablegpu_tile_order(cablegpu_ctx* c, int* order_out) {
+  if (!c || !order_out) return fail(c, CABLEGPU_ERR_ARG, "tile_order: null argument");
+  CG_CUDA(c, cudaMemcpy(order_out, c->d_order, sizeof(int) * (size_t)c->mp, cudaMemcpyDeviceToHost));
   return CABLEGPU_OK;
 }
 

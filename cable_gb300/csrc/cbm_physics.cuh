@@ -92,13 +92,15 @@ struct CgDev {
   // outputs
   float* out;              // [CG_NOUT]
   uint8_t* tile_status;    // per-tile status bits (CG_TS_*), OR-ed by the kernels, cleared by the caller
-  float* out_caller;       // [CG_NOUT][mp] copy of out in the caller's tile order (host-I/O steps), or null
+  float* out_caller;       // [CG_NOUT][mp] copy of out for the host-I/O steps, or null
+  int out_caller_order;    // 1: out_caller in the caller's tile order, 0: in device order
   float* diag;             // [CG_NDIAG] or null
   float* work_a;           // phase A -> B, C handoff record
   float* work_b;           // phase B -> C handoff record
   float* work_c;           // phase C1 -> C2 -> C3 handoff record
   const float* forcing_in; // [CG_NFORC] host-provided forcing, or null (synthetic)
-  int forcing_caller_order; // 1: forcing_in is [CG_NFORC][mp] in the caller's tile order
+  int forcing_caller_order; // layout of forcing_in: 0 [CG_NFORC][ld] device order, 1 [CG_NFORC][mp]
+                            // in the caller's tile order, 2 [CG_NFORC][mp] in device order
   float* forcing_out;      // [CG_NFORC] copy of the forcing used, or null
   unsigned int* status;    // bit0: non-finite output seen, bit1: surrogate network failed
   // dryLeaf training-row harvest (null when off): rows of 12 features and 3

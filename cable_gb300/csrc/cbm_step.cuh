@@ -98,7 +98,7 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
   if (D.forcing_in) {
     // device tile order, or the caller's order straight from the host-I/O
     // staging buffer (one gather instead of a reordering pass)
-    const size_t base = D.forcing_caller_order ? (size_t)D.tile_id[t] : (size_t)t;
+    const size_t base = D.forcing_caller_order == 1 ? (size_t)D.tile_id[t] : (size_t)t;
     const size_t stride = D.forcing_caller_order ? (size_t)D.mp : (size_t)ld;
 #pragma unroll
     for (int i = 0; i < CG_NFORC; ++i) F[i] = D.forcing_in[i * stride + base];
@@ -1019,7 +1019,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
 #pragma unroll
   for (int i = 0; i < 7; ++i) { D.out[i * ld + t] = outv[i]; finite = finite && isfinite(outv[i]); }
   if (D.out_caller) {
-    const size_t o = (size_t)D.tile_id[t];
+    const size_t o = D.out_caller_order ? (size_t)D.tile_id[t] : (size_t)t;
 #pragma unroll
     for (int i = 0; i < 7; ++i) D.out_caller[(size_t)i * D.mp + o] = outv[i];
   }
@@ -2069,7 +2069,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   D.tss[t] = tss; D.wb_lake[t] = wb_lake;
   D.owb[t] = wbtot; D.wbal_tot[t] = wbal_tot;
   D.out[7 * ld + t] = trad;
-  if (D.out_caller) D.out_caller[(size_t)7 * D.mp + D.tile_id[t]] = trad;
+  if (D.out_caller) D.out_caller[(size_t)7 * D.mp + (D.out_caller_order ? (size_t)D.tile_id[t] : (size_t)t)] = trad;
   {
     uint8_t bits = 0;
     if (!isfinite(trad)) { atomicOr(D.status, 1u); bits |= CG_TS_NONFINITE; }

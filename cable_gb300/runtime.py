@@ -40,7 +40,7 @@ EXPORTS = [
     "cablegpu_mlp_forward", "cablegpu_mlp_grad", "cablegpu_mlp_fit", "cablegpu_mlp_last_error",
     "cablegpu_set_blocks", "cablegpu_get_config", "cablegpu_autotune", "cablegpu_step_host",
     "cablegpu_restart_write", "cablegpu_restart_read", "cablegpu_forcing_file_write", "cablegpu_file_info",
-    "cablegpu_run_forcing_file",
+    "cablegpu_run_forcing_file", "cablegpu_set_host_layout", "cablegpu_tile_order",
 ]
 NOALLOC_MAX_TILES = 65536
 # science switch bits of cablegpu_set_options (include/cablegpu.h)
@@ -183,6 +183,8 @@ def load(build_if_missing: bool = True):
     L.cablegpu_file_info.argtypes = [C.c_char_p, C.POINTER(ip), C.POINTER(C.c_longlong), C.POINTER(ip), C.POINTER(ip),
                                      C.POINTER(ip), C.POINTER(ip), C.POINTER(C.c_float)]
     L.cablegpu_run_forcing_file.argtypes = [vp, C.c_char_p, ip, ip, ip, C.c_char_p]
+    L.cablegpu_set_host_layout.argtypes = [vp, ip]
+    L.cablegpu_tile_order.argtypes = [vp, C.POINTER(ip)]
     L.cablegpu_last_error.argtypes = [vp]
     L.cablegpu_last_error.restype = C.c_char_p
     _lib = L
@@ -386,6 +388,16 @@ class CableGPU:
 
     def synchronize(self):
         self._check(self.L.cablegpu_synchronize(self.h))
+
+    def set_host_layout(self, layout: int):
+        """0: step_host buffers in the caller's tile order; 1: in device order."""
+        self._check(self.L.cablegpu_set_host_layout(self.h, int(layout)))
+
+    def tile_order(self) -> np.ndarray:
+        """The caller's index of the tile in each device slot."""
+        o = np.empty(self.mp, np.int32)
+        self._check(self.L.cablegpu_tile_order(self.h, _ptr(o, C.c_int)))
+        return o
 
     # ------------------------------------------------------------------ files
     def restart_write(self, path, ktau: int):

@@ -199,6 +199,16 @@ int cablegpu_run(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels);
  * only.  Replaces the per-step get_met_data -> cbm -> write_output sequence
  * of the offline driver (cable_serial.F90:594-640). */
 int cablegpu_step_host(cablegpu_ctx* ctx, int ktau, float dels, const float* host_forcing, float* host_out);
+/* Layout of the host buffers of cablegpu_step_host and of the records of
+ * cablegpu_run_forcing_file: 0 (default) the caller's tile order, 1 the
+ * context's device tile order (cablegpu_tile_order), which spares the kernels
+ * the per-step gather and scatter of caller positions and lets the context
+ * keep its fastest tile order; a driver fills its arrays through the order
+ * index once instead.  Applies to the steps issued after the call. */
+int cablegpu_set_host_layout(cablegpu_ctx* ctx, int layout);
+/* order_out[s] ([mp]) receives the caller's index of the tile in device
+ * slot s. */
+int cablegpu_tile_order(cablegpu_ctx* ctx, int* order_out);
 /* Waits for all queued work; returns CABLEGPU_ERR_NONFINITE if any step
  * since the last call produced a non-finite output flux.  Which tiles, and
  * what else went wrong where, is in the per-tile field "tile_status" (one

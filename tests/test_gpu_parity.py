@@ -418,3 +418,33 @@ def test_tile_status_matches_the_oracle_and_flags_bad_forcing(oracle, runtime):
     assert bits[17] & R.TILE_FORCING_RANGE and bits[23] & R.TILE_FORCING_RANGE
     assert not np.any(np.delete(bits, [17, 23]) & R.TILE_FORCING_RANGE)
     g.close()
+
+
+def test_host_layout_in_device_order_matches_caller_order(oracle, runtime):
+    """cablegpu_set_host_layout(1): host forcing and outputs in the device
+    tile order (cablegpu_tile_order) give bitwise the same steps as the
+    caller-order buffers."""
+    R = runtime
+    ts = W.snow_grid(5000, nsteps=6)
+    n, mp = 6, ts.mp
+    F = oracle.forcing(ts, 0, n)
+    runs = []
+    for layout in (0, 1):
+        g = R.from_tileset(ts, order=2)
+        g.set_host_layout(layout)
+        perm = g.tile_order()
+        assert sorted(perm.tolist()) == list(range(mp))
+        outs = []
+        for k in range(n):
+            f = np.ascontiguousarray(F[k] if layout == 0 else F[k][:, perm])
+            out = np.empty((8, mp), np.float32)
+            g.step_host(k + 1, f, out, ts.dels)
+            g.synchronize()
+            outs.append(out if layout == 0 else out[:, np.argsort(perm)])   # back to caller order
+        runs.append((outs, {k: g.get(k) for k in ("wb", "tgg", "snowd", "cansto", "out")}))
+        g.close()
+    (o0, s0), (o1, s1) = runs
+    for k in range(n):
+        np.testing.assert_array_equal(o1[k], o0[k], err_msg="step %d" % k)
+    for k in s0:
+        np.testing.assert_array_equal(s1[k], s0[k], err_msg=k)
