@@ -100,6 +100,26 @@ MODULE cablegpu_c
       IMPORT :: c_ptr
       TYPE(c_ptr), VALUE :: ctx
     END FUNCTION cablegpu_last_error
+
+    INTEGER(c_int) FUNCTION cablegpu_step_host(ctx, ktau, dels, forcing, out) BIND(C, name="cablegpu_step_host")
+      IMPORT :: c_int, c_float, c_ptr
+      TYPE(c_ptr), VALUE :: ctx
+      INTEGER(c_int), VALUE :: ktau
+      REAL(c_float), VALUE :: dels
+      TYPE(c_ptr), VALUE :: forcing, out
+    END FUNCTION cablegpu_step_host
+
+    INTEGER(c_int) FUNCTION cablegpu_set_host_layout(ctx, layout) BIND(C, name="cablegpu_set_host_layout")
+      IMPORT :: c_int, c_ptr
+      TYPE(c_ptr), VALUE :: ctx
+      INTEGER(c_int), VALUE :: layout
+    END FUNCTION cablegpu_set_host_layout
+
+    INTEGER(c_int) FUNCTION cablegpu_tile_order(ctx, order) BIND(C, name="cablegpu_tile_order")
+      IMPORT :: c_int, c_ptr
+      TYPE(c_ptr), VALUE :: ctx
+      TYPE(c_ptr), VALUE :: order
+    END FUNCTION cablegpu_tile_order
   END INTERFACE
 
 CONTAINS
@@ -129,6 +149,10 @@ MODULE cable_cbm_module
   INTEGER, SAVE :: mp_gpu = 0
   REAL(c_float), ALLOCATABLE, TARGET, SAVE :: forc(:, :)   ! (mp, 13)
   REAL(c_float), ALLOCATABLE, TARGET, SAVE :: outb(:, :)   ! (mp, 8)
+  ! caller tile (1-based) of each device slot: the per-step forcing and
+  ! outputs move in device order (cablegpu_set_host_layout), gathered and
+  ! scattered through this index on the host
+  INTEGER(c_int), ALLOCATABLE, TARGET, SAVE :: slot_tile(:)
 
 CONTAINS
 
@@ -210,6 +234,10 @@ CONTAINS
     IF (TRIM(cable_user%diag_soil_resp) == 'OFF' .OR. TRIM(cable_user%diag_soil_resp) == 'off') &
       switches = switches + 512
     CALL check(cablegpu_set_options(ctx, switches, 0_c_int, 0_c_int), 'set_options')
+    CALL check(cablegpu_set_host_layout(ctx, 1_c_int), 'set_host_layout')
+    ALLOCATE(slot_tile(mp))
+    CALL check(cablegpu_tile_order(ctx, C_LOC(slot_tile)), 'tile_order')
+    slot_tile = slot_tile + 1
 
     ! prognostic state (soil_snow_type, canopy, bgc, bal)
     ALLOCATE(r8(mp, ms), r4(mp, ms))
@@ -270,33 +298,35 @@ CONTAINS
     IF (.NOT. C_ASSOCIATED(ctx)) CALL gpu_setup(bal, bgc, canopy, rad, soil, ssnow, veg)
     IF (mp /= mp_gpu) STOP 'cablegpu: mp changed between calls'
 
-    ! met_type fields get_met_data filled for this step (cable_input.F90)
-    forc(:, 1) = met%fsd(:, 1)
-    forc(:, 2) = met%fsd(:, 2)
-    forc(:, 3) = met%fld
-    forc(:, 4) = met%precip
-    forc(:, 5) = met%precip_sn
-    forc(:, 6) = met%tk
-    forc(:, 7) = met%pmb
-    forc(:, 8) = met%ua
-    forc(:, 9) = met%qv
-    forc(:, 10) = met%ca
-    forc(:, 11) = met%coszen
-    forc(:, 12) = met%doy
-    forc(:, 13) = met%hod
-    CALL check(cablegpu_set_forcing(ctx, C_LOC(forc)), 'set_forcing')
-    CALL check(cablegpu_step(ctx, INT(ktau, c_int), REAL(dels, c_float)), 'step')
-    ! the per-step fluxes the driver writes (blocking copy; errors of the
+    ! met_type fields get_met_data filled for this step (cable_input.F90),
+    ! gathered into device order
+    forc(:, 1) = met%fsd(slot_tile, 1)
+    forc(:, 2) = met%fsd(slot_tile, 2)
+    forc(:, 3) = met%fld(slot_tile)
+    forc(:, 4) = met%precip(slot_tile)
+    forc(:, 5) = met%precip_sn(slot_tile)
+    forc(:, 6) = met%tk(slot_tile)
+    forc(:, 7) = met%pmb(slot_tile)
+    forc(:, 8) = met%ua(slot_tile)
+    forc(:, 9) = met%qv(slot_tile)
+    forc(:, 10) = met%ca(slot_tile)
+    forc(:, 11) = met%coszen(slot_tile)
+    forc(:, 12) = met%doy(slot_tile)
+    forc(:, 13) = met%hod(slot_tile)
+    ! one step with the forcing upload and the output download; the driver
+    ! writes the fluxes after every step, so wait for them (errors of the
     ! step surface here)
-    CALL get('out', C_LOC(outb))
-    canopy%fe = outb(:, 1)
-    canopy%fh = outb(:, 2)
-    canopy%fgpp = outb(:, 3)
-    canopy%frday = outb(:, 4)
-    canopy%tv = outb(:, 5)
-    canopy%rnet = outb(:, 6)
-    canopy%ga = outb(:, 7)
-    rad%trad = outb(:, 8)
+    CALL check(cablegpu_step_host(ctx, INT(ktau, c_int), REAL(dels, c_float), C_LOC(forc), C_LOC(outb)), &
+               'step_host')
+    CALL check(cablegpu_synchronize(ctx), 'synchronize')
+    canopy%fe(slot_tile) = outb(:, 1)
+    canopy%fh(slot_tile) = outb(:, 2)
+    canopy%fgpp(slot_tile) = outb(:, 3)
+    canopy%frday(slot_tile) = outb(:, 4)
+    canopy%tv(slot_tile) = outb(:, 5)
+    canopy%rnet(slot_tile) = outb(:, 6)
+    canopy%ga(slot_tile) = outb(:, 7)
+    rad%trad(slot_tile) = outb(:, 8)
   END SUBROUTINE cbm
 
   ! Copies the device-resident prognostic state back into the derived types
@@ -344,6 +374,7 @@ CONTAINS
     ctx = c_null_ptr
     IF (ALLOCATED(forc)) DEALLOCATE(forc)
     IF (ALLOCATED(outb)) DEALLOCATE(outb)
+    IF (ALLOCATED(slot_tile)) DEALLOCATE(slot_tile)
   END SUBROUTINE cbm_gpu_finalize
 
 END MODULE cable_cbm_module

@@ -120,13 +120,17 @@ def test_fortran_shim_binds_exported_symbols_and_registry_fields():
         buf = m.group(1)
         want = {R.F64: ("r8",), R.F32: ("r4", "outb"), R.I32: ("flags",)}[dt]
         assert buf in want, (name, buf, want)
-    order = re.findall(r"forc\(:, (\d+)\) = met%(\w+)(?:\(:, (\d)\))?", src)
+    # forcing gathered into device order through the slot -> tile index, the
+    # outputs scattered back through it
+    order = re.findall(r"forc\(:, (\d+)\) = met%(\w+)\(slot_tile(?:, (\d))?\)", src)
     names = []
     for idx, comp, band in order:
         names.append("fsd_" + ("vis" if band == "1" else "nir") if comp == "fsd" else comp)
     assert names == R.FORCING_FIELDS
-    outs = re.findall(r"(?:canopy|rad)%(\w+) = outb\(:, (\d)\)", src)
+    assert [int(o[0]) for o in order] == list(range(1, R.NFORCING + 1))
+    outs = re.findall(r"(?:canopy|rad)%(\w+)\(slot_tile\) = outb\(:, (\d)\)", src)
     assert [o[0] for o in sorted(outs, key=lambda x: int(x[1]))] == R.OUTPUT_FIELDS
+    assert "cablegpu_set_host_layout(ctx, 1_c_int)" in src and "cablegpu_tile_order(ctx, C_LOC(slot_tile))" in src
 
 
 def test_soil_thermal_fix_tables_match_the_oracle(oracle):
