@@ -43,7 +43,7 @@ const char* kDiagNames[CG_NDIAG] = {
   "fe_d", "fh_d", "fev", "fhv", "fhs", "fns", "fnv", "ga_d", "tv_d", "tscrn", "qscrn", "rnet_d", "us", "cduv", "cdtq",
   "epot", "fes", "fevc", "dgdtg", "fevw", "fpn", "frday_d", "fgpp_d", "fnpp", "fnee", "fra", "frp", "frs", "trad_d",
   "albedo_vis", "albedo_nir", "transd", "precis", "through", "fwet", "wetfac", "potev", "runoff", "rnof1", "rnof2",
-  "smelt", "ghflux", "sghflux", "drybal", "wetbal", "ebal", "wbal", "qssabs", "rniso", "vlaiw", "tvair", "qvair",
+  "smelt", "ghflux", "sghflux", "drybal", "wetbal", "ebal", "wbal", "qssabs", "rniso", "vlaiw_d", "tvair", "qvair",
   "swnet", "lwnet", "wbtot", "gswx_sun", "gswx_shd", "fwsoil", "dryleaf_passes",
 };
 
@@ -81,6 +81,7 @@ std::vector<FieldDef> make_registry() {
     {"owb", 1, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
     {"ebal_tot", 1, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
     {"wbal_tot", 1, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
+    {"vlaiw", 1, CABLEGPU_F32, CABLEGPU_KIND_STATE, S_F32},
     {"out", CG_NOUT, CABLEGPU_F32, CABLEGPU_KIND_OUTPUT, S_F32},
     {"tile_status", 1, CABLEGPU_I32, CABLEGPU_KIND_OUTPUT, S_U8},
   };
@@ -88,8 +89,8 @@ std::vector<FieldDef> make_registry() {
   f.push_back({"forcing", CG_NFORC, CABLEGPU_F32, CABLEGPU_KIND_FORCING, S_F32});
   f.push_back({"forcing_in", CG_NFORC, CABLEGPU_F32, CABLEGPU_KIND_FORCING, S_F32});
   f.push_back({"work_a", CG_NA, CABLEGPU_F32, CABLEGPU_KIND_WORK, S_F32});
-  f.push_back({"work_b", CG_NB, CABLEGPU_F32, CABLEGPU_KIND_WORK, S_F32});
-  f.push_back({"work_c", CG_NC, CABLEGPU_F32, CABLEGPU_KIND_WORK, S_F32});
+  f.push_back({"work_b", CG_NB_ALLOC, CABLEGPU_F32, CABLEGPU_KIND_WORK, S_F32});
+  f.push_back({"work_c", CG_NC_ALLOC, CABLEGPU_F32, CABLEGPU_KIND_WORK, S_F32});
   return f;
 }
 
@@ -102,6 +103,36 @@ size_t storage_bytes(Storage s) { return s == S_U8 ? 1 : (s == S_F32 ? 4 : 8); }
 
 // ---------------------------------------------------------------- kernels
 __global__ void advance_clock_kernel(int* clock) { clock[0] += 1; }
+
+// The prognostic bank of the coupled implicit call (cbl_prognostic_bank.F90:
+// 26-165): cable_store_prognostics saves these fields before each implicit
+// cycle and cable_reinstate_prognostics puts them back after every cycle but
+// the last (cable_implicit_main.F90:190-213).  Soil water and ice as their
+// double-FP32 word pairs; isflag is bit 0 of flags, while bit 1 (soil_snow's
+// first call, the reference's SAVE counter) is not in the bank.  Not banked,
+// as in the reference: gammzz, the balance totals and the outputs (ga).
+constexpr int kBankRows = CG_MS + 4 * CG_MS + 4 * 3 + 9 + 3 + 2 + 1;
+__global__ void bank_kernel(CgDev D, float* __restrict__ bank, int restore) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= D.mp) return;
+  const size_t ld = (size_t)D.ld;
+  int r = 0;
+  auto mv = [&](float* f, int rows) {
+    for (int k = 0; k < rows; ++k, ++r) {
+      float* a = f + k * ld + t;
+      float* b = bank + r * ld + t;
+      if (restore) *a = *b; else *b = *a;
+    }
+  };
+  mv(D.tgg, CG_MS); mv(D.wb, 2 * CG_MS); mv(D.wbice, 2 * CG_MS);
+  mv(D.sdepth, 3); mv(D.smass, 3); mv(D.tggsn, 3); mv(D.ssdn, 3);
+  mv(D.ssdnn, 1); mv(D.snage, 1); mv(D.snowd, 1); mv(D.pudsto, 1); mv(D.rtsoil, 1); mv(D.owetfac, 1);
+  mv(D.wb_lake, 1); mv(D.tss, 1); mv(D.cansto, 1);   // cansto: canopy%oldcansto of the next call
+  mv(D.cplant, 3); mv(D.csoil, 2);
+  float* b = bank + r * ld + t;
+  if (restore) D.flags[t] = (uint8_t)((D.flags[t] & 0xFEu) | ((unsigned)*b & 1u));
+  else *b = (float)(D.flags[t] & 1u);
+}
 
 // Cold start: the reference's initial state for a run without restart file.
 __global__ void cold_start_kernel(CgDev D, const CgTables* __restrict__ T, const double* snowd0, const double* tgg0,
@@ -216,6 +247,7 @@ struct cablegpu_ctx {
   float sur_gate = 0.1f;
   unsigned long long* d_sur_stats = nullptr;  // [2]
   float* d_sur_dt = nullptr;                  // [ld] predicted leaf-temperature change
+  float* d_bank = nullptr;                    // [kBankRows][ld] prognostic bank of the implicit coupled call
   int graph_sur = -1;
   float graph_gate = -1.f;
   // threads per block of the five step kernels (radiation, canopy, snow
@@ -265,6 +297,7 @@ void bind_device_view(cablegpu_ctx* c) {
   D.wb_lake = (float*)P("wb_lake"); D.wbtot1 = (float*)P("wbtot1"); D.wbtot2 = (float*)P("wbtot2");
   D.cansto = (float*)P("cansto"); D.cplant = (float*)P("cplant"); D.csoil = (float*)P("csoil");
   D.owb = (double*)P("owb"); D.ebal_tot = (double*)P("ebal_tot"); D.wbal_tot = (double*)P("wbal_tot");
+  D.vlaiw = (float*)P("vlaiw");
   D.out = (float*)P("out");
   D.tile_status = (uint8_t*)P("tile_status");
   D.diag = c->diag ? (float*)P(kDiagNames[0]) : nullptr;
@@ -315,10 +348,12 @@ int launch_step(cablegpu_ctx* c, const StepParams& p, const int* clock) {
   } else {
     launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, clock, bk[1]);
   }
-  launch_phase_c1(diag, c->stream, c->dev, c->d_tables, p, clock, bk[2]);
-  launch_phase_c2(diag, c->stream, c->dev, c->d_tables, p, clock, bk[3]);
-  launch_phase_c3(diag, c->stream, c->dev, c->d_tables, p, clock, bk[4]);
-  c->launches += kKernelsPerStep;
+  if (p.mode != 1) {   // the explicit coupled call stops after the canopy
+    launch_phase_c1(diag, c->stream, c->dev, c->d_tables, p, clock, bk[2]);
+    launch_phase_c2(diag, c->stream, c->dev, c->d_tables, p, clock, bk[3]);
+    launch_phase_c3(diag, c->stream, c->dev, c->d_tables, p, clock, bk[4]);
+  }
+  c->launches += p.mode == 1 ? 2 : kKernelsPerStep;
   CG_CUDA(c, cudaGetLastError());
   return CABLEGPU_OK;
 }
@@ -339,6 +374,9 @@ StepParams make_params(cablegpu_ctx* c, int ktau, float dels) {
   p.forc = c->forc;
   p.forc.dels = dels;
   p.step_index = ktau - 1;
+  p.mode = 0;
+  p.final_cycle = 1;
+  p.lai_refresh = 0;
   return p;
 }
 
@@ -528,6 +566,7 @@ int cablegpu_destroy(cablegpu_ctx* c) {
     cudaStreamDestroy(c->dstream);
   }
   if (c->d_sur_dt) cudaFree(c->d_sur_dt);
+  if (c->d_bank) cudaFree(c->d_bank);
   sur_free(c->net);
   cudaFreeHost(c->h_clock);
   cudaFreeHost(c->h_status);
@@ -656,6 +695,37 @@ int cablegpu_set_options(cablegpu_ctx* c, int switches, int diag, int capture_fo
 int cablegpu_step(cablegpu_ctx* c, int ktau, float dels) {
   if (!c || ktau < 1 || !(dels > 0.f)) return fail(c, CABLEGPU_ERR_ARG, "step: bad argument");
   return launch_step(c, make_params(c, ktau, dels), nullptr);
+}
+
+int cablegpu_step_explicit(cablegpu_ctx* c, int ktau, float dels, int lai_refresh) {
+  if (!c || ktau < 1 || !(dels > 0.f)) return fail(c, CABLEGPU_ERR_ARG, "step_explicit: bad argument");
+  StepParams p = make_params(c, ktau, dels);
+  p.mode = 1;
+  p.lai_refresh = lai_refresh ? 1 : 0;
+  return launch_step(c, p, nullptr);
+}
+
+int cablegpu_step_implicit(cablegpu_ctx* c, int ktau, float dels, int cycleno, int numcycles) {
+  if (!c || ktau < 1 || !(dels > 0.f) || numcycles < 1 || cycleno < 1 || cycleno > numcycles)
+    return fail(c, CABLEGPU_ERR_ARG, "step_implicit: bad argument");
+  StepParams p = make_params(c, ktau, dels);
+  p.mode = 2;
+  p.final_cycle = cycleno == numcycles ? 1 : 0;
+  const int block = 256, grid = (c->mp + block - 1) / block;
+  if (!p.final_cycle) {
+    if (!c->d_bank) CG_CUDA(c, cudaMalloc(&c->d_bank, sizeof(float) * kBankRows * (size_t)c->ld));
+    bind_device_view(c);
+    bank_kernel<<<grid, block, 0, c->stream>>>(c->dev, c->d_bank, 0);
+    ++c->launches;
+  }
+  int rc = launch_step(c, p, nullptr);
+  if (rc) return rc;
+  if (!p.final_cycle) {
+    bank_kernel<<<grid, block, 0, c->stream>>>(c->dev, c->d_bank, 1);
+    ++c->launches;
+    CG_CUDA(c, cudaGetLastError());
+  }
+  return CABLEGPU_OK;
 }
 
 int cablegpu_run(cablegpu_ctx* c, int ktau0, int nsteps, float dels) {

@@ -89,6 +89,7 @@ struct CgDev {
   double* owb;
   double* ebal_tot;
   double* wbal_tot;
+  float* vlaiw;      // snow-reduced LAI carried between coupled calls (canopy%vlaiw)
   // outputs
   float* out;              // [CG_NOUT]
   uint8_t* tile_status;    // per-tile status bits (CG_TS_*), OR-ed by the kernels, cleared by the caller

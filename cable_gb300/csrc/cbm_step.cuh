@@ -28,6 +28,13 @@ struct StepParams {
   int soil_resp_off; // diag_soil_resp = 'OFF'
   CgForcingSpec forc;
   int step_index;    // 0-based counter for the synthetic forcing
+  // ACCESS coupling (src/coupled/AM3/control/cable/CM3/cbl_cbm_mod.F90):
+  // 0 the offline cbm(), 1 cbm_expl (radiation and canopy; the canopy water,
+  // wetness factor and surface temperature are left as they were), 2 cbm_impl
+  int mode;
+  int final_cycle;   // cbm_impl: 1 on the last implicit cycle of the step (cycleno == numcycles)
+  int lai_refresh;   // cbm_expl: the host model's radiation call ran, so the
+                     // snow-reduced LAI is recomputed rather than carried
 };
 
 __device__ __forceinline__ float ldf(const float* p, int i) { return __ldg(p + i); }
@@ -46,10 +53,17 @@ __device__ constexpr float ZSHH[CG_MS + 1] = {0.5f * ZSE_C[0], 0.5f * (ZSE_C[0] 
 #define CG_NA 52
 // Phase B record (per tile, [CG_NB][ld]): what soil_snow, carbon and the
 // water balance need from define_canopy.
-#define CG_NB 20
+#define CG_NB 19
+// rows CG_NB.. of the same record, written only by the canopy kernel of an
+// implicit coupled call: dfh_dtg, dfe_dtg, dfn_dtg (the soil-surface flux
+// derivatives of the online energy-balance corrections)
+#define CG_NB_ALLOC 22
 // Soil-snow record (per tile, [CG_NC][ld]) handed from the snow-pack kernel
 // to the soil-heat kernel and on to the soil-water kernel.
 #define CG_NC 12
+// row CG_NC: ssnow%dtmlt(:,1) of an implicit coupled call, summed by the
+// snow-pack and soil-heat kernels, read by the soil-water kernel
+#define CG_NC_ALLOC 13
 
 template <bool kDiag>
 __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
@@ -126,13 +140,17 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) wbliq0[k] = df_sub(wb[k], wbice[k]);
 
-  // lakes top-layer fix (cbl_model_driver_offline.F90:116-121)
-  if (iveg == LAKES && df_lt(wb[0], df32{sfc, 0.f})) {
-    wbtot1 = wb[0].hi * DLIQ * zse[0];
-    wb[0] = df32{sfc, 0.f};
-    wbtot2 = wb[0].hi * DLIQ * zse[0];
+  // lakes top-layer fix (cbl_model_driver_offline.F90:116-121); the
+  // coupled cbm_expl / cbm_impl have none
+  const bool offline = P.mode == 0;
+  if (offline) {
+    if (iveg == LAKES && df_lt(wb[0], df32{sfc, 0.f})) {
+      wbtot1 = wb[0].hi * DLIQ * zse[0];
+      wb[0] = df32{sfc, 0.f};
+      wbtot2 = wb[0].hi * DLIQ * zse[0];
+    }
+    wb_lake = wb_lake + fmaxf(wbtot2 - wbtot1, 0.f);
   }
-  wb_lake = wb_lake + fmaxf(wbtot2 - wbtot1, 0.f);
 
   // ---------------------------------------------------------------- ruff_resist
   // cable_roughness.F90:64-332, roughnessHGT_effLAI_cbl.F90:42-149
@@ -141,6 +159,14 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
     float den_eff = fmaxf(100.0f, ssdnn);
     hruff = fmaxf(1.0e-6f, hc - (1.2f * snowd / den_eff));
     vlaiw = vlai * (hruff / fmaxf(0.01f, hc));
+    // coupled calls: ruff_resist leaves canopy%vlaiw alone
+    // (cable_roughness.F90:176-186); it holds the LAI_eff of the host
+    // model's last radiation call (cable_land_albedo_mod_cbl.F90:263,
+    // cbl_um_update_canopy.F90:27), the same function of the snow state
+    if (P.mode != 0) {
+      if (P.lai_refresh) D.vlaiw[t] = vlaiw;
+      else vlaiw = D.vlaiw[t];
+    }
     float z0soil = 0.0009f * fminf(1.0f, vlaiw) + 1.e-4f;
     z0soilsn = z0soil;
     if (snowd > 0.01f) z0soilsn = fmaxf(1.e-7f, z0soil - z0soil * fminf(snowd, 10.f) / 10.f);
@@ -368,8 +394,10 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
 #pragma unroll
     for (int i = 0; i < CG_NA; ++i) D.work_a[i * ld + t] = rec[i];
   }
-  if (iveg == LAKES) df_store(D.wb, CG_MS, ld, 0, t, wb[0]);
-  D.wb_lake[t] = wb_lake; D.wbtot1[t] = wbtot1; D.wbtot2[t] = wbtot2;
+  if (offline) {
+    if (iveg == LAKES) df_store(D.wb, CG_MS, ld, 0, t, wb[0]);
+    D.wb_lake[t] = wb_lake; D.wbtot1[t] = wbtot1; D.wbtot2[t] = wbtot2;
+  }
   if (kDiag) {
     D.diag[29 * ld + t] = albedo[0]; D.diag[30 * ld + t] = albedo[1]; D.diag[31 * ld + t] = transd;
     D.diag[47 * ld + t] = qssabs; D.diag[48 * ld + t] = sum_rad_rniso; D.diag[49 * ld + t] = vlaiw;
@@ -970,7 +998,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
   // the l_rev_corr revisions :916-922, :993-1014)
   float dgdtg;
   {
-    float dfn_dtg = -4.f * EMSOIL * SBOLTZ * tss4 / tss;
+    const float dfn_dtg = -4.f * EMSOIL * SBOLTZ * tss4 / tss;
     float rttsoil = rtsoil;
     if (P.rev_corr && veg_mask) rttsoil = rttsoil + rt1;
     float rhlitt, relitt;
@@ -981,6 +1009,11 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
     float tc = tss - TFRZ;
     float ddq_dtg = (RMH2O / RMAIR) / pmb * TETENA * TETENB * TETENC / sqf(TETENC + tc) * expf(TETENB * tc / (TETENC + tc));
     dgdtg = dfn_dtg - dfh_dtg - dfe_ddq * ddq_dtg;
+    if (P.mode == 2) {
+      D.work_b[CG_NB * ld + t] = dfh_dtg;
+      D.work_b[(CG_NB + 1) * ld + t] = dfe_ddq * ddq_dtg;   // ssnow%dfe_dtg (:1026)
+      D.work_b[(CG_NB + 2) * ld + t] = dfn_dtg;
+    }
   }
   const float drybal = (ecy + hcy) - sum_rad_rniso + CAPP * RMAIR * (tlfy - tk) * sum_rad_gradis;
   const float wetbal = fevw + fhvw - sum_rad_rniso * fwet + CAPP * RMAIR * (tlfy - tk) * sum_rad_gradis * fwet;
@@ -1002,26 +1035,38 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
       if (b) atomicAdd(&D.sur_stats[1], (unsigned long long)b);
     }
   }
-  D.ebal_tot[t] = D.ebal_tot[t] + (double)ebal;
-  D.cansto[t] = cansto;
+  // the coupled calls run no balance checks; cbm_expl restores the canopy
+  // water and wetness factor (cbl_cbm_mod.F90:150-152), so the step's
+  // state is what the implicit call leaves
+  if (P.mode == 0) D.ebal_tot[t] = D.ebal_tot[t] + (double)ebal;
+  if (P.mode != 1) {
+    D.cansto[t] = cansto;
+    D.owetfac[t] = owetfac_out;
+  }
   D.rtsoil[t] = rtsoil;
-  D.owetfac[t] = owetfac_out;
-  {
+  if (P.mode != 1) {
     const float rec[CG_NB] = {ga, dgdtg, fes, fess, fesp, fevc, fevw, cls, precis0, evapfbl[0], evapfbl[1], evapfbl[2],
-                              evapfbl[3], evapfbl[4], evapfbl[5], delwc, fpn, frday, tv, 0.f};
+                              evapfbl[3], evapfbl[4], evapfbl[5], delwc, fpn, frday, tv};
 #pragma unroll
     for (int i = 0; i < CG_NB; ++i) D.work_b[i * ld + t] = rec[i];
   }
   const float rnet = fns + fnv;
   const float fgpp = -fpn + frday;
-  const float outv[7] = {fe, fh, fgpp, frday, tv, rnet, ga};
+  // cbm_expl's radiative temperature (cbl_cbm_mod.F90:172-179): emissivities
+  // 1, the surface temperature of the start of the step, and no correction
+  // term (canopy%fns_cor is zeroed by define_canopy, :233)
+  const float trad_x = sqrtf(sqrtf((1.f - transd) * pow4(tv) + transd * tss4));
+  const float outv[8] = {fe, fh, fgpp, frday, tv, rnet, ga, trad_x};
+  const int nout = P.mode == 1 ? 8 : 7;
   bool finite = true;
 #pragma unroll
-  for (int i = 0; i < 7; ++i) { D.out[i * ld + t] = outv[i]; finite = finite && isfinite(outv[i]); }
+  for (int i = 0; i < 8; ++i)
+    if (i < nout) { D.out[i * ld + t] = outv[i]; finite = finite && isfinite(outv[i]); }
   if (D.out_caller) {
     const size_t o = D.out_caller_order ? (size_t)D.tile_id[t] : (size_t)t;
 #pragma unroll
-    for (int i = 0; i < 7; ++i) D.out_caller[(size_t)i * D.mp + o] = outv[i];
+    for (int i = 0; i < 8; ++i)
+      if (i < nout) D.out_caller[(size_t)i * D.mp + o] = outv[i];
   }
   {
     // output ranges of the reference's output checks (cable_checks.F90:71-123):
@@ -1242,6 +1287,7 @@ __device__ __forceinline__ void phase_c1(const CgDev& D, const CgTables* __restr
     if (snowd > 0.0f && isflag == 0 && tgg[0] >= TFRZ) {
       float snowflx = (tgg[0] - TFRZ) * g1f;
       snowmlt = fminf(snowflx / HLF, snowd);
+      dtmlt0 = dtmlt0 + snowmlt * HLF / g1f;
       snowd = snowd - snowmlt;
       tgg[0] = tgg[0] - snowmlt * HLF / g1f;
     }
@@ -1339,7 +1385,8 @@ __device__ __forceinline__ void phase_c1(const CgDev& D, const CgTables* __restr
   D.work_c[1 * ld + t] = precis;
   D.work_c[2 * ld + t] = segg;
   D.work_c[3 * ld + t] = smelt;
-  (void)dtmlt0; (void)sconds; (void)hcll; (void)wblf; (void)wbfice;
+  if (P.mode == 2) D.work_c[CG_NC * ld + t] = dtmlt0;
+  (void)sconds; (void)hcll; (void)wblf; (void)wbfice;
 }
 
 // snow pack state that snow_melting updates
@@ -1356,6 +1403,7 @@ static __device__ __noinline__ float cg_snow_melting(CgSnowPack& p, int isflag, 
   if (p.snowd > 0.0f && isflag == 0 && p.tgg0 >= TFRZ) {
     float snowflx = (p.tgg0 - TFRZ) * g1f;
     snowmlt = fminf(snowflx / HLF, p.snowd);
+    p.dtmlt0 = p.dtmlt0 + snowmlt * HLF / g1f;
     p.snowd = p.snowd - snowmlt;
     p.tgg0 = p.tgg0 - snowmlt * HLF / g1f;
   }
@@ -1442,7 +1490,9 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
   float tss;
   // soil_snow, heat part (cbl_soilsnow_main.F90:125-136)
   float hcll = fmaxf(0.01f, css * rhosoil);
-  float dtmlt0 = 0.f;
+  // dtmlt(:,1) so far this step (the snow-pack kernel's part); only the
+  // implicit coupled call uses it
+  float dtmlt0 = P.mode == 2 ? D.work_c[CG_NC * ld + t] : 0.f;
   float g1f = (float)gammzz1;
   float smelt = D.work_c[3 * ld + t];
   float wblf[CG_MS], wbfice[CG_MS];
@@ -1665,7 +1715,8 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
   D.work_c[5 * ld + t] = sghflux;
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) D.work_c[(6 + k) * ld + t] = gf[k];
-  (void)tss; (void)first_call; (void)dtmlt0;
+  if (P.mode == 2) D.work_c[CG_NC * ld + t] = dtmlt0;
+  (void)tss; (void)first_call;
 }
 
 template <bool kDiag>
@@ -1960,7 +2011,38 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     float dtau = 1.0e-6f * (__expf(ar1) + __expf(10.0f * ar1) + ar3) * dels;
     snage = fmaxf(0.0f, (snage + dtau) * (1.0f - dnsnow));
   }
-  const float trad = sqrtf(sqrtf((1.f - transd) * pow4(tv) + transd * pow4(tss)));
+  float trad;
+  if (P.mode != 2) {
+    trad = sqrtf(sqrtf((1.f - transd) * pow4(tv) + transd * pow4(tss)));
+  } else {
+    // implicit coupled call: the online energy-balance corrections of
+    // soil_snow (cbl_soilsnow_main.F90:164-183, melt-driven) and of cbm_impl
+    // (cbl_cbm_mod.F90:317-357, surface-temperature-driven; the temperature
+    // is reset to the start of the step first on a cycle that is not the
+    // last, :307-311), applied to the canopy kernel's fe, fh, rnet and ga;
+    // then cbm_impl's radiative temperature (:374-381): emissivities 1, the
+    // start-of-step surface temperature and the correction fns_cor / sigma
+    const float otss = D.tss[t];
+    if (!P.final_cycle) tss = otss;
+    const float dfh_dtg = Bv(CG_NB), dfe_dtg = Bv(CG_NB + 1), dfn_dtg = Bv(CG_NB + 2);
+    const float dtm = D.work_c[CG_NC * ld + t];
+    const float dT = tss - otss;
+    const size_t oc = D.out_caller_order ? (size_t)D.tile_id[t] : (size_t)t;
+    auto add_out = [&](int i, float dv) {
+      const float x = D.out[i * ld + t] + dv;
+      D.out[i * ld + t] = x;
+      if (D.out_caller) D.out_caller[(size_t)i * D.mp + oc] = x;
+    };
+    add_out(0, dtm * dfe_dtg + dT * dfe_dtg);   // fe = fev + fes
+    add_out(1, dtm * dfh_dtg + dT * dfh_dtg);   // fh = fhv + fhs
+    float fns_cor = 0.f;
+    if (P.rev_corr) {
+      fns_cor = dtm * dfn_dtg + dT * dfn_dtg;
+      add_out(5, fns_cor);                      // rnet = fns + fnv
+      add_out(6, dtm * dgdtg + dT * dgdtg);     // ga
+    }
+    trad = sqrtf(sqrtf((1.f - transd) * pow4(tv) + transd * pow4(otss) + fns_cor / SBOLTZ));
+  }
 
   // carbon, icycle == 0 (cable_carbon.F90:38-360, cbm:214-229)
   // root fractions, used only by the carbon routines below
@@ -2067,7 +2149,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   D.csoil[t] = csoil[0]; D.csoil[ld + t] = csoil[1];
   D.snowd[t] = snowd; D.ssdnn[t] = ssdnn; D.snage[t] = snage; D.pudsto[t] = pudsto;
   D.tss[t] = tss; D.wb_lake[t] = wb_lake;
-  D.owb[t] = wbtot; D.wbal_tot[t] = wbal_tot;
+  if (P.mode == 0) { D.owb[t] = wbtot; D.wbal_tot[t] = wbal_tot; }   // no balance checks in coupled calls
   D.out[7 * ld + t] = trad;
   if (D.out_caller) D.out_caller[(size_t)7 * D.mp + (D.out_caller_order ? (size_t)D.tile_id[t] : (size_t)t)] = trad;
   {

@@ -41,6 +41,7 @@ EXPORTS = [
     "cablegpu_set_blocks", "cablegpu_get_config", "cablegpu_autotune", "cablegpu_step_host",
     "cablegpu_restart_write", "cablegpu_restart_read", "cablegpu_forcing_file_write", "cablegpu_file_info",
     "cablegpu_run_forcing_file", "cablegpu_set_host_layout", "cablegpu_tile_order",
+    "cablegpu_step_explicit", "cablegpu_step_implicit",
 ]
 NOALLOC_MAX_TILES = 65536
 # science switch bits of cablegpu_set_options (include/cablegpu.h)
@@ -165,6 +166,8 @@ def load(build_if_missing: bool = True):
     L.cablegpu_set_synthetic_forcing.argtypes = [vp, C.c_ulonglong, ip]
     L.cablegpu_set_options.argtypes = [vp, ip, ip, ip]
     L.cablegpu_step.argtypes = [vp, ip, C.c_float]
+    L.cablegpu_step_explicit.argtypes = [vp, ip, C.c_float, ip]
+    L.cablegpu_step_implicit.argtypes = [vp, ip, C.c_float, ip, ip]
     L.cablegpu_run.argtypes = [vp, ip, ip, C.c_float]
     L.cablegpu_synchronize.argtypes = [vp]
     L.cablegpu_run_timed.argtypes = [vp, ip, ip, C.c_float, C.POINTER(C.c_float)]
@@ -374,6 +377,17 @@ class CableGPU:
     # ------------------------------------------------------------------ time
     def step(self, ktau: int, dels: float = 1800.0):
         self._check(self.L.cablegpu_step(self.h, int(ktau), float(dels)))
+
+    def step_explicit(self, ktau: int, dels: float = 1800.0, lai_refresh: bool = True):
+        """cbm_expl of the ACCESS coupling: radiation and canopy fluxes from
+        the current state, which is left unchanged but for rtsoil, ga and
+        (lai_refresh) the carried snow-reduced LAI."""
+        self._check(self.L.cablegpu_step_explicit(self.h, int(ktau), float(dels), 1 if lai_refresh else 0))
+
+    def step_implicit(self, ktau: int, dels: float = 1800.0, cycleno: int = 1, numcycles: int = 1):
+        """cbm_impl of the ACCESS coupling; only the last of numcycles cycles
+        advances the prognostic state."""
+        self._check(self.L.cablegpu_step_implicit(self.h, int(ktau), float(dels), int(cycleno), int(numcycles)))
 
     def run(self, ktau0: int, nsteps: int, dels: float = 1800.0):
         self._check(self.L.cablegpu_run(self.h, int(ktau0), int(nsteps), float(dels)))

@@ -186,6 +186,42 @@ int cablegpu_set_options(cablegpu_ctx* ctx, int switches, int diag, int capture_
  * balance checks).  Asynchronous; errors of the step surface at the next
  * synchronising call. */
 int cablegpu_step(cablegpu_ctx* ctx, int ktau, float dels);
+
+/* ACCESS coupling: the two halves of a coupled timestep, replacing
+ *   SUBROUTINE cbm_expl(mp, nrb, ktau, dels, air, bgc, canopy, met, bal, rad,
+ *                       rough, soil, ssnow, sum_flux, veg, climate)
+ *   SUBROUTINE cbm_impl(cycleno, numcycles, mp, nrb, ktau, dels, air, bgc,
+ *                       canopy, met, bal, rad, rough, soil, ssnow, sum_flux,
+ *                       veg, climate)
+ *   src/coupled/AM3/control/cable/CM3/cbl_cbm_mod.F90:10-182, :184-396
+ * called from cable_explicit_driver.F90:266 and cable_implicit_driver.F90:200.
+ * Forcing comes as for cablegpu_step (cablegpu_set_forcing / the synthetic
+ * generator); between the two calls the host model updates the air
+ * temperature and humidity (cable_implicit_driver.F90:189-198).
+ *
+ * cablegpu_step_explicit: radiation and canopy fluxes from the current state
+ * (two kernel launches).  The canopy water, soil wetness factor and surface
+ * temperature are left as they were (cbl_cbm_mod.F90:150-152); the canopy's
+ * soil resistance (rtsoil) and ga are kept, as in the reference.  Outputs:
+ * all eight rows of "out", trad from the start-of-step surface temperature
+ * (:172-179).  lai_refresh != 0 when the host model's radiation call ran since
+ * the last explicit call: the snow-reduced LAI (canopy%vlaiw, state field
+ * "vlaiw") is then recomputed from the current snow state
+ * (cable_land_albedo_mod_cbl.F90:263); otherwise the carried value is used
+ * (cable_roughness.F90:176-186 skips it in coupled calls).  The first
+ * explicit call of a run passes lai_refresh = 1.
+ *
+ * cablegpu_step_implicit: canopy, soil and snow, snow ageing and carbon (the
+ * five kernels), with the online energy-balance corrections of soil_snow
+ * (cbl_soilsnow_main.F90:164-183) and of cbm_impl (:317-357) applied to
+ * out's fe, fh and (with l_rev_corr) rnet and ga, and trad with the
+ * correction term (:374-381).  1 <= cycleno <= numcycles; on every cycle but
+ * the last the prognostic bank (cbl_prognostic_bank.F90) is restored after
+ * the call, as cable_implicit_main.F90:190-213 does, so only the last cycle
+ * advances the state.  The offline driver's lakes fix and balance checks do
+ * not run in either call (ebal_tot, wbal_tot and owb are left alone). */
+int cablegpu_step_explicit(cablegpu_ctx* ctx, int ktau, float dels, int lai_refresh);
+int cablegpu_step_implicit(cablegpu_ctx* ctx, int ktau, float dels, int cycleno, int numcycles);
 /* nsteps timesteps ktau0 .. ktau0+nsteps-1, replayed from a captured CUDA
  * graph.  Asynchronous. */
 int cablegpu_run(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels);

@@ -78,6 +78,7 @@ struct State {
   // balances (cable_checks.F90 mass_balance SAVE owb; energy/water totals)
   R2 owb, ebal_tot, wbal_tot;
   bool first_soilsnow_call = true;  // soil_snow SAVE ktau (cbl_soilsnow_main.F90:60-62)
+  R vlaiw = 0;                      // canopy%vlaiw carried between coupled calls
 };
 
 // Per-step forcing (met_type fields set by the driver, cable_input.F90).
@@ -180,7 +181,9 @@ struct CbmRef {
 
   // ------------------------------------------------------------ ruff_resist
   // cable_roughness.F90:64-332 (+ roughnessHGT_effLAI_cbl.F90:42-149)
-  static void ruff_resist(const P& p, const S& s, Rough& r, R& vlaiw, R& rghlai) {
+  // vlaiw_in: the coupled calls' carried canopy%vlaiw, which ruff_resist
+  // then leaves alone (cable_roughness.F90:176-186), or null
+  static void ruff_resist(const P& p, const S& s, Rough& r, R& vlaiw, R& rghlai, const R* vlaiw_in = nullptr) {
     const R z0soilsn_min = R(1.e-7), z0soilsn_min_PF = R(1.e-4);
     // HgtAboveSnow (roughnessHGT_effLAI_cbl.F90:71-95)
     R snowden_eff = mx(R(100.0), s.ssdnn);
@@ -190,6 +193,7 @@ struct CbmRef {
     r.hruff = has;
     // LAI_eff (:123-126)
     vlaiw = p.vlai * (has / mx(R(0.01), p.hc));
+    if (vlaiw_in) vlaiw = *vlaiw_in;
     rghlai = vlaiw;
     // :193-205
     r.z0soil = R(0.0009) * mn(R(1.0), vlaiw) + R(1.e-4);
@@ -780,7 +784,40 @@ struct CbmRef {
   // ======================================================================
   // one cbm() timestep for one tile, followed by the offline driver's
   // rescaling and balance checks (cable_serial.F90:573-728)
-  void step(const P& p, S& s, const F& f, D& d, int ktau, R dels) const {
+  // mode 0: the offline cbm() (cbl_model_driver_offline.F90:38-231).
+  // ACCESS coupling (src/coupled/AM3/control/cable/CM3/cbl_cbm_mod.F90):
+  // mode 1 cbm_expl (:10-182), lai_refresh when the host model's radiation
+  // call recomputed canopy%vlaiw (cable_land_albedo_mod_cbl.F90:263,
+  // cbl_um_update_canopy.F90:27); mode 2 cbm_impl (:184-396) for cycle
+  // cycleno of numcycles, with the driver's prognostic bank: stored before
+  // the call and reinstated after every cycle but the last
+  // (cable_implicit_main.F90:190-213, cbl_prognostic_bank.F90:26-165).
+  void step(const P& p, S& s, const F& f, D& d, int ktau, R dels, int mode = 0, bool final_cycle = true,
+            bool lai_refresh = false) const {
+    if (mode == 2 && !final_cycle) {
+      const S bank = s;
+      step_body(p, s, f, d, ktau, dels, mode, final_cycle, lai_refresh);
+      reinstate(s, bank);
+      return;
+    }
+    step_body(p, s, f, d, ktau, dels, mode, final_cycle, lai_refresh);
+  }
+
+  // cable_reinstate_prognostics (cbl_prognostic_bank.F90:119-165), default soil
+  static void reinstate(S& s, const S& pb) {
+    for (int k = 0; k < MS; ++k) { s.tgg[k] = pb.tgg[k]; s.wb[k] = pb.wb[k]; s.wbice[k] = pb.wbice[k]; }
+    for (int k = 0; k < MSN; ++k) {
+      s.sdepth[k] = pb.sdepth[k]; s.smass[k] = pb.smass[k]; s.tggsn[k] = pb.tggsn[k]; s.ssdn[k] = pb.ssdn[k];
+    }
+    s.ssdnn = pb.ssdnn; s.snage = pb.snage; s.isflag = pb.isflag; s.snowd = pb.snowd; s.pudsto = pb.pudsto;
+    s.rtsoil = pb.rtsoil; s.owetfac = pb.owetfac; s.wb_lake = pb.wb_lake; s.tss = pb.tss;
+    s.cansto = pb.cansto;   // canopy%oldcansto, the next call's starting canopy water
+    for (int k = 0; k < 3; ++k) s.cplant[k] = pb.cplant[k];
+    for (int k = 0; k < 2; ++k) s.csoil[k] = pb.csoil[k];
+  }
+
+  void step_body(const P& p, S& s, const F& f, D& d, int ktau, R dels, int mode, bool final_cycle,
+                 bool lai_refresh) const {
     Met met;
     met.fsd[0] = f.fsd[0]; met.fsd[1] = f.fsd[1]; met.fsd[2] = 0;
     met.fld = f.fld; met.precip = f.precip; met.precip_sn = f.precip_sn; met.tk = f.tk;
@@ -793,17 +830,22 @@ struct CbmRef {
     R2 wbliq0[MS];
     for (int k = 0; k < MS; ++k) wbliq0[k] = s.wb[k] - s.wbice[k];
 
-    // lakes top-layer fix (cbl_model_driver_offline.F90:116-121)
-    if (p.iveg == LAKES && s.wb[0] < p.sfc) {
-      s.wbtot1 = R(s.wb[0]) * R(DENSITY_LIQ) * p.zse[0];
-      s.wb[0] = p.sfc;
-      s.wbtot2 = R(s.wb[0]) * R(DENSITY_LIQ) * p.zse[0];
+    // lakes top-layer fix (cbl_model_driver_offline.F90:116-121); not in
+    // the coupled calls
+    if (mode == 0) {
+      if (p.iveg == LAKES && s.wb[0] < p.sfc) {
+        s.wbtot1 = R(s.wb[0]) * R(DENSITY_LIQ) * p.zse[0];
+        s.wb[0] = p.sfc;
+        s.wbtot2 = R(s.wb[0]) * R(DENSITY_LIQ) * p.zse[0];
+      }
+      s.wb_lake = s.wb_lake + mx(s.wbtot2 - s.wbtot1, R(0.));
     }
-    s.wb_lake = s.wb_lake + mx(s.wbtot2 - s.wbtot1, R(0.));
 
     Rough rough{};
     R vlaiw, rghlai;
-    ruff_resist(p, s, rough, vlaiw, rghlai);
+    const bool carried = mode != 0 && !(mode == 1 && lai_refresh);
+    ruff_resist(p, s, rough, vlaiw, rghlai, carried ? &s.vlaiw : nullptr);
+    if (mode == 1 && lai_refresh) s.vlaiw = vlaiw;
     Air air;
     define_air(met, air);
     const bool veg_mask = vlaiw > R(LAI_THRESH);
@@ -1125,16 +1167,19 @@ struct CbmRef {
     rad.lwnet = met.fld - R(SBOLTZ) * R(EMLEAF) * std::pow(tv, 4) * (R(1) - rad.transd) - rad.flws * rad.transd;
     s.rtsoil = rtsoil;
     R2 fevc = L.fevc;
-    s.cansto = cansto;
+    // cbm_expl puts back the canopy water and wetness factor
+    // (cbl_cbm_mod.F90:150-152)
+    if (mode != 1) s.cansto = cansto;
     s.ga = ga;
     // ================= end define_canopy
-    s.owetfac = wetfac;                    // cbm:192
+    if (mode != 1) s.owetfac = wetfac;     // cbm:192
 
     SoilOut so{};
-    soil_snow(p, s, dels, precis, fes, fess, fesp, fevc, fevw, ga, dgdtg, evapfbl, met, cls == R(1.1335), so);
+    if (mode != 1)
+      soil_snow(p, s, dels, precis, fes, fess, fesp, fevc, fevw, ga, dgdtg, evapfbl, met, cls == R(1.1335), so);
 
     // snow_aging (cbl_snow_aging.F90:11-83)
-    if (s.snowd > R(SNOW_DEPTH_THRESH)) {
+    if (mode != 1 && s.snowd > R(SNOW_DEPTH_THRESH)) {
       R dnsnow = mn(R(1.0), R(0.1) * mx(R(0.0), s.snowd - s.osnowd));
       R tmp = R(s.isflag) * s.tggsn[0] + R(1 - s.isflag) * s.tgg[0];
       tmp = mn(tmp, R(TFRZ));
@@ -1145,10 +1190,49 @@ struct CbmRef {
       R dtau = R(1.0e-6) * (std::exp(ar1) + std::exp(ar2) + ar3) * dels;
       s.snage = mx(R(0.0), (s.snage + dtau) * (R(1.0) - dnsnow));
     }
-    fev = R(fevc + fevw);
-    fe = R(fev + fes);
-    rnet = fns + fnv;
-    R trad = std::pow((R(1.) - rad.transd) * std::pow(tv, 4) + rad.transd * std::pow(s.tss, 4), R(0.25));
+    R trad;
+    if (mode == 0) {
+      fev = R(fevc + fevw);
+      fe = R(fev + fes);
+      rnet = fns + fnv;
+      trad = std::pow((R(1.) - rad.transd) * std::pow(tv, 4) + rad.transd * std::pow(s.tss, 4), R(0.25));
+    } else {
+      R fns_cor = 0;   // zeroed by define_canopy (cable_canopy.F90:233)
+      if (mode == 2) {
+        // soil_snow's online corrections (cbl_soilsnow_main.F90:164-183)
+        const R fhs_cor = so.dtmlt1 * dfh_dtg;
+        const R2 fes_cor = so.dtmlt1 * dfe_dtg;
+        fhs = fhs + fhs_cor;
+        fes = fes + fes_cor;
+        if (l_rev_corr) {
+          fns_cor = so.dtmlt1 * dfn_dtg;
+          fns = fns + fns_cor;
+          ga = R(ga + so.dtmlt1 * dgdtg);
+          fess = fess + fes_cor;
+        }
+        // cbm_impl (cbl_cbm_mod.F90:307-357): tss reset on a cycle that is
+        // not the last, then the corrections for the change of tss
+        if (!final_cycle) s.tss = otss;
+        const R dT = s.tss - otss;
+        fhs = fhs + dT * dfh_dtg;
+        fh = fhv + fhs;
+        fes = fes + dT * dfe_dtg;
+        if (l_rev_corr) {
+          fns_cor = fns_cor + dT * dfn_dtg;
+          fns = fns + dT * dfn_dtg;
+          ga = R(ga + dT * dgdtg);
+          fess = fess + dT * dfe_dtg;
+        }
+        s.ga = ga;
+      }
+      fev = R(fevc + fevw);
+      fe = R(fev + fes);
+      rnet = fns + fnv;
+      // emissivities 1 (cable_phys_constants_mod.F90:26-27), the surface
+      // temperature of the start of the step (cbl_cbm_mod.F90:172-179, :374-381)
+      trad = std::pow((R(1.) - rad.transd) * std::pow(tv, 4) + rad.transd * std::pow(otss, 4) + fns_cor / R(SBOLTZ),
+                      R(0.25));
+    }
 
     // carbon, icycle == 0 (cable_carbon.F90:38-360 and cbm:214-229)
     R frp, frpw, frpr, frs;
@@ -1196,7 +1280,7 @@ struct CbmRef {
       frs = p.vegcf * (R(144.0) / R(44.0e6)) * soilcf * mn(R(1.), R(1.4) * mx(R(.3), R(.0278) * tsoil + R(.5))) * ftsrs *
             rswc / (rswch + rswc);
     }
-    {
+    if (mode != 1) {   // carbon_pl; cbm_expl has no carbon
       const R beta = R(0.9);
       const R trnl = R(3.17e-8), trnr = R(4.53e-9), trnsf = R(1.057e-10), trnw = R(6.342e-10);
       R coef_cold = std::exp(mn(R(1.), -(tv - p.tvclst)));
@@ -1230,18 +1314,21 @@ struct CbmRef {
     const R smelt = so.smelt * dels;
     const R rnof1 = so.rnof1 * dels, rnof2 = so.rnof2 * dels, runoff = so.runoff * dels;
 
-    // mass_balance (cable_checks.F90:472-551)
-    if (ktau == 1) s.owb = so.wbtot;
-    R2 delwb = so.wbtot - s.owb;
-    s.owb = so.wbtot;
-    R wbal = R(met.precip - delwc - s.snowd + s.osnowd - runoff - (fevw + fevc + fes / cls) * dels / air.rlam - delwb - R(0));
-    if (ktau == 1) s.wbal_tot = 0;
-    if (ktau > 10) s.wbal_tot = s.wbal_tot + wbal;
-    // energy_balance (cable_checks.F90:565-618)
-    R ebal = rad.qcan[0][0] + rad.qcan[1][0] + rad.qcan[0][1] + rad.qcan[1][1] + rad.qssabs + met.fld -
+    // the offline driver's balance checks; the coupled calls run none
+    R wbal = 0, ebal = 0;
+    if (mode == 0) {
+      // mass_balance (cable_checks.F90:472-551)
+      if (ktau == 1) s.owb = so.wbtot;
+      R2 delwb = so.wbtot - s.owb;
+      s.owb = so.wbtot;
+      wbal = R(met.precip - delwc - s.snowd + s.osnowd - runoff - (fevw + fevc + fes / cls) * dels / air.rlam - delwb - R(0));
+      if (ktau == 1) s.wbal_tot = 0;
+      if (ktau > 10) s.wbal_tot = s.wbal_tot + wbal;
+      // energy_balance (cable_checks.F90:565-618)
+      ebal = rad.qcan[0][0] + rad.qcan[1][0] + rad.qcan[0][1] + rad.qcan[1][1] + rad.qssabs + met.fld -
              R(SBOLTZ) * R(EMLEAF) * std::pow(tv, 4) * (R(1) - rad.transd) - rad.flws * rad.transd - fev - R(fes) - fh - ga;
-    s.ebal_tot = s.ebal_tot + ebal;
-    (void)otss;
+      s.ebal_tot = s.ebal_tot + ebal;
+    }
 
     // ---- diagnostics
     d.fe = fe; d.fh = fh; d.fev = fev; d.fhv = fhv; d.fhs = fhs; d.fns = fns; d.fnv = fnv; d.ga = ga; d.tv = tv;
@@ -1267,7 +1354,7 @@ struct CbmRef {
 
   // ====================================================================
   // soil_snow (cbl_soilsnow_main.F90:28-207) and its callees
-  struct SoilOut { R smelt, rnof1, rnof2, runoff, ghflux, sghflux; R2 wbtot; };
+  struct SoilOut { R smelt, rnof1, rnof2, runoff, ghflux, sghflux; R2 wbtot; R dtmlt1; };
 
   static void trimb(const R2* a, const R2* b, const R2* c, R2* rhs, int kmax) {
     // cbl_trimb.F90:17-53
@@ -1761,6 +1848,7 @@ struct CbmRef {
       wbtot = wbtot + (wl * R(DENSITY_LIQ) + s.wbice[k] * R(DENSITY_ICE)) * p.zse[k];
     }
     o.wbtot = wbtot;
+    o.dtmlt1 = dtmlt[0];   // ssnow%dtmlt(:,1), read by the coupled corrections
   }
 
   // snow_melting (cbl_snowMelt.F90:9-120); returns snowmlt

@@ -29,7 +29,7 @@ const Slot kState[] = {
   {"wb", MS}, {"wbice", MS}, {"gammzz", MS}, {"tgg", MS}, {"tggsn", MSN}, {"ssdn", MSN}, {"smass", MSN},
   {"sdepth", MSN}, {"isflag", 1}, {"snowd", 1}, {"ssdnn", 1}, {"snage", 1}, {"pudsto", 1}, {"owetfac", 1},
   {"rtsoil", 1}, {"tss", 1}, {"wb_lake", 1}, {"wbtot1", 1}, {"wbtot2", 1}, {"cansto", 1}, {"cplant", 3},
-  {"csoil", 2}, {"owb", 1}, {"ebal_tot", 1}, {"wbal_tot", 1}, {"first_call", 1}, {"ga", 1},
+  {"csoil", 2}, {"owb", 1}, {"ebal_tot", 1}, {"wbal_tot", 1}, {"first_call", 1}, {"ga", 1}, {"vlaiw", 1},
 };
 constexpr int kNState = sizeof(kState) / sizeof(kState[0]);
 int state_slots() { int n = 0; for (auto& s : kState) n += s.width; return n; }
@@ -60,6 +60,7 @@ void pack_state(const State<R, R2>& s, double* st, int mp, int t) {
   for (int k = 0; k < 3; ++k) put(s.cplant[k]);
   for (int k = 0; k < 2; ++k) put(s.csoil[k]);
   put(s.owb); put(s.ebal_tot); put(s.wbal_tot); put(s.first_soilsnow_call ? 1.0 : 0.0); put(s.ga);
+  put(s.vlaiw);
 }
 
 template <class R, class R2>
@@ -81,6 +82,7 @@ void unpack_state(State<R, R2>& s, const double* st, int mp, int t) {
   for (int k = 0; k < 2; ++k) s.csoil[k] = R(get());
   s.owb = R2(get()); s.ebal_tot = R2(get()); s.wbal_tot = R2(get()); s.first_soilsnow_call = get() != 0.0;
   s.ga = R(get());
+  s.vlaiw = R(get());
   s.pudsmx = 0; s.osnowd = s.snowd;
 }
 
@@ -205,7 +207,7 @@ void make_state(State<R, R2>& s, const Params<R, R2>& p, int iveg, double snowd0
 template <class R, class R2>
 int run_impl(int mp, int nsteps, int ktau0, double dels, int switches, const int* iveg, const int* isoilm,
              const double* vlai, const double* lat, const float* forcing, const ForcingSpec* spec,
-             const TileForcingParams* tfp, double* state, double* diag, int nthreads) {
+             const TileForcingParams* tfp, double* state, double* diag, int nthreads, const int* calls = nullptr) {
   const int nslots = state_slots();
   (void)nslots;
 #pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads > 0 ? nthreads : 1)
@@ -231,13 +233,19 @@ int run_impl(int mp, int nsteps, int ktau0, double dels, int switches, const int
         const float* fs = forcing + (size_t)n * F_NFIELDS * mp;
         for (int i = 0; i < F_NFIELDS; ++i) fv[i] = fs[(size_t)i * mp + t];
       } else {
-        forcing_at(*spec, tfp[t], (uint32_t)t, (uint32_t)(ktau0 - 1 + n), fv);
+        const int k = calls ? calls[4 * n] : ktau0 + n;
+        forcing_at(*spec, tfp[t], (uint32_t)t, (uint32_t)(k - 1), fv);
       }
       Forcing<R> f;
       f.fsd[0] = R(fv[F_FSD1]); f.fsd[1] = R(fv[F_FSD2]); f.fld = R(fv[F_FLD]); f.precip = R(fv[F_PRECIP]);
       f.precip_sn = R(fv[F_PRECIP_SN]); f.tk = R(fv[F_TK]); f.pmb = R(fv[F_PMB]); f.ua = R(fv[F_UA]);
       f.qv = R(fv[F_QV]); f.ca = R(fv[F_CA]); f.coszen = R(fv[F_COSZEN]); f.doy = R(fv[F_DOY]); f.hod = R(fv[F_HOD]);
-      model.step(p, s, f, d, ktau0 + n, R(dels));
+      if (calls) {
+        const int* cl = calls + 4 * n;
+        model.step(p, s, f, d, cl[0], R(dels), cl[1], cl[2] != 0, cl[3] != 0);
+      } else {
+        model.step(p, s, f, d, ktau0 + n, R(dels));
+      }
     }
     pack_state(s, state, mp, t);
     if (diag) pack_diag(d, diag, mp, t);
@@ -300,6 +308,32 @@ int cbmref_run(int mp, int nsteps, int ktau0, double dels, int precision, int sw
                                     tfp.data(), state, diag, nthreads);
   return run_impl<float, double>(mp, nsteps, ktau0, dels, switches, iveg, isoilm, vlai, lat, forcing, &spec,
                                  tfp.data(), state, diag, nthreads);
+}
+
+// A sequence of ncalls cbm calls of the offline or the coupled kinds:
+// calls[n] = {ktau, mode, final_cycle, lai_refresh} with mode 0 the offline
+// cbm(), 1 cbm_expl, 2 cbm_impl (CbmRef::step).  forcing, if not null, is
+// [ncalls][13][mp], one record per call; else the synthetic generator's
+// record of step ktau.  Other arguments as for cbmref_run.
+int cbmref_run_calls(int mp, int ncalls, const int* calls, double dels, int precision, int switches,
+                     const int* iveg, const int* isoilm, const double* vlai, const double* lat, const float* forcing,
+                     uint64_t seed, int doy0, const float* tf_lat, const float* tf_lonphase, const float* tf_tbase,
+                     const float* tf_swscale, double* state, double* diag, int nthreads) {
+  if (!calls || ncalls < 0) return -1;
+  for (int n = 0; n < ncalls; ++n)
+    if (calls[4 * n] < 1 || calls[4 * n + 1] < 0 || calls[4 * n + 1] > 2) return -1;
+  ForcingSpec spec;
+  spec.seed = seed; spec.doy0 = doy0; spec.dels = (float)dels;
+  std::vector<TileForcingParams> tfp;
+  if (!forcing) {
+    tfp.resize(mp);
+    for (int t = 0; t < mp; ++t) tfp[t] = {tf_lat[t], tf_lonphase[t], tf_tbase[t], tf_swscale[t]};
+  }
+  if (precision == 0)
+    return run_impl<double, double>(mp, ncalls, 1, dels, switches, iveg, isoilm, vlai, lat, forcing, &spec,
+                                    tfp.data(), state, diag, nthreads, calls);
+  return run_impl<float, double>(mp, ncalls, 1, dels, switches, iveg, isoilm, vlai, lat, forcing, &spec,
+                                 tfp.data(), state, diag, nthreads, calls);
 }
 
 // Synthetic forcing for tiles [0, mp) and steps [step0, step0+nsteps):

@@ -16,7 +16,7 @@ DIAG_MAP = {
     "albedo_nir": "albedo_nir", "transd": "transd", "precis": "precis", "through": "through", "fwet": "fwet",
     "wetfac": "wetfac", "potev": "potev", "runoff": "runoff", "ghflux": "ghflux", "sghflux": "sghflux",
     "drybal": "drybal", "wetbal": "wetbal", "ebal": "ebal", "wbal": "wbal", "qssabs": "qssabs", "rniso": "rniso",
-    "vlaiw": "vlaiw", "tvair": "tvair", "qvair": "qvair", "swnet": "swnet", "lwnet": "lwnet", "wbtot": "wbtot",
+    "vlaiw_d": "vlaiw", "tvair": "tvair", "qvair": "qvair", "swnet": "swnet", "lwnet": "lwnet", "wbtot": "wbtot",
     "gswx_sun": "gswx_sun", "gswx_shd": "gswx_shd", "fwsoil": "fwsoil", "dryleaf_passes": "dryleaf_passes",
 }
 STATE_FIELDS = ["wb", "wbice", "tgg", "tggsn", "ssdn", "smass", "sdepth", "snowd", "ssdnn", "snage", "pudsto",

@@ -34,6 +34,8 @@ def lib():
         L.cbmref_init.argtypes = [C.c_int, C.c_int, ip, ip, dp, dp, dp, dp, dp, dp]
         L.cbmref_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, ip, ip, dp, dp, fp,
                                  C.c_uint64, C.c_int, fp, fp, fp, fp, dp, dp, C.c_int]
+        L.cbmref_run_calls.argtypes = [C.c_int, C.c_int, ip, C.c_double, C.c_int, C.c_int, ip, ip, dp, dp, fp,
+                                       C.c_uint64, C.c_int, fp, fp, fp, fp, dp, dp, C.c_int]
         L.cbmref_forcing.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_int, C.c_double, fp, fp, fp, fp, fp]
         for n in ("cbmref_psim", "cbmref_psis"):
             getattr(L, n).restype = C.c_double
@@ -126,6 +128,36 @@ def run(ts, state, nsteps, ktau0=1, forcing=None, precision=0, nthreads=None, **
                       _p(isoil, C.c_int), _p(vlai, C.c_double), _p(lat, C.c_double), fptr, ts.seed, ts.doy0,
                       _p(tl, C.c_float), _p(tp, C.c_float), _p(tb, C.c_float), _p(tsw, C.c_float),
                       _p(state, C.c_double), _p(diag, C.c_double), nthreads)
+    assert rc == 0
+    return dict(zip(diag_names(), diag))
+
+
+def run_calls(ts, state, calls, forcing=None, precision=0, nthreads=None, **switches):
+    """A sequence of offline / coupled calls on ``state`` (modified in place):
+    calls = [(ktau, mode, final_cycle, lai_refresh), ...] with mode 0 cbm(),
+    1 cbm_expl, 2 cbm_impl; forcing [ncalls][13][mp] or None (the synthetic
+    record of each call's ktau).  Returns the last call's diagnostics."""
+    L = lib()
+    mp = ts.mp
+    cl = np.ascontiguousarray(np.asarray(calls, np.int32).reshape(-1, 4))
+    diag = np.zeros((L.cbmref_num_diag(), mp), np.float64)
+    iveg = np.ascontiguousarray(ts.iveg, np.int32)
+    isoil = np.ascontiguousarray(ts.isoilm, np.int32)
+    vlai = np.ascontiguousarray(ts.vlai, np.float64)
+    lat = np.ascontiguousarray(ts.lat, np.float64)
+    f32 = lambda a: np.ascontiguousarray(a, np.float32)
+    tl, tp, tb, tsw = f32(ts.lat), f32(ts.lonphase), f32(ts.tbase), f32(ts.swscale)
+    fptr = None
+    if forcing is not None:
+        forcing = np.ascontiguousarray(forcing, np.float32)
+        assert forcing.shape == (len(cl), L.cbmref_num_forcing_fields(), mp)
+        fptr = _p(forcing, C.c_float)
+    assert state.flags["C_CONTIGUOUS"] and state.dtype == np.float64
+    rc = L.cbmref_run_calls(mp, len(cl), _p(cl, C.c_int), float(ts.dels), precision, _switch_mask(**switches),
+                            _p(iveg, C.c_int), _p(isoil, C.c_int), _p(vlai, C.c_double), _p(lat, C.c_double), fptr,
+                            ts.seed, ts.doy0, _p(tl, C.c_float), _p(tp, C.c_float), _p(tb, C.c_float),
+                            _p(tsw, C.c_float), _p(state, C.c_double), _p(diag, C.c_double),
+                            nthreads or os.cpu_count() or 1)
     assert rc == 0
     return dict(zip(diag_names(), diag))
 

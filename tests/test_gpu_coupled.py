@@ -1,0 +1,142 @@
+"""The coupled (ACCESS) calls on the GPU against the oracle: a run of
+cbm_expl / cbm_impl pairs with two implicit cycles per step, the host
+model's air temperature and humidity increments between the explicit and
+the implicit calls, and the snow-reduced LAI refreshed every third step."""
+import numpy as np
+import pytest
+
+import harness as H
+import oracle_lib as O
+from cable_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+OUT = ["fe", "fh", "fgpp", "frday", "tv", "rnet", "ga", "trad"]
+OUT_GPU = {"fe": "fe_d", "fh": "fh_d", "tv": "tv_d", "rnet": "rnet_d", "ga": "ga_d", "trad": "trad_d"}
+STATE = ["wb", "wbice", "tgg", "tggsn", "ssdn", "smass", "sdepth", "snowd", "ssdnn", "snage", "pudsto", "owetfac",
+         "rtsoil", "tss", "cansto", "cplant", "csoil"]
+BANKED = ["wb", "wbice", "tgg", "tggsn", "ssdn", "smass", "sdepth", "snowd", "ssdnn", "snage", "pudsto", "owetfac",
+          "rtsoil", "tss", "wb_lake", "cansto", "cplant", "csoil"]
+ALL_STATE = BANKED + ["gammzz1", "flags", "wbtot1", "wbtot2", "owb", "ebal_tot", "wbal_tot", "vlaiw"]
+
+
+@pytest.fixture(scope="module")
+def runtime():
+    from cable_gb300 import runtime as R
+    R.load()
+    return R
+
+
+def schedule(ts, nsteps, seed=5):
+    """calls [(ktau, mode, final, lai_refresh)] and their forcing: each step's
+    explicit call on the step's record, two implicit cycles on it with the
+    host model's increments dT ~ N(0, 0.4 K), dq/q ~ N(0, 2 %)."""
+    base = O.forcing(ts, 0, nsteps)
+    rng = np.random.default_rng(seed)
+    calls, forc = [], []
+    for k in range(1, nsteps + 1):
+        calls.append((k, 1, 1, 1 if k % 3 == 1 else 0))
+        forc.append(base[k - 1])
+        for cyc in (1, 2):
+            f = base[k - 1].copy()
+            f[5] += rng.normal(0.0, 0.4, ts.mp).astype(np.float32)                       # tk
+            f[8] *= (1.0 + rng.normal(0.0, 0.02, ts.mp)).astype(np.float32)              # qv
+            calls.append((k, 2, 1 if cyc == 2 else 0, 0))
+            forc.append(f)
+    return calls, np.stack(forc)
+
+
+def gpu_call(g, call, dels):
+    k, mode, final, lr = call
+    if mode == 1:
+        g.step_explicit(k, dels, lai_refresh=bool(lr))
+    else:
+        g.step_implicit(k, dels, cycleno=2 if final else 1, numcycles=2)
+
+
+def oracle_run(ts, calls, F, precision, **sw):
+    """Oracle over the calls; returns (outputs of the last explicit call,
+    outputs of the last implicit call, state)."""
+    st = O.init_state(ts, precision)
+    n = len(calls)
+    dx = O.run_calls(ts, st, calls[: n - 2], forcing=F[: n - 2], precision=precision, **sw)
+    di = O.run_calls(ts, st, calls[n - 2:], forcing=F[n - 2:], precision=precision, **sw)
+    return dx, di, O.split_state(st)
+
+
+def report(outx, outi, state, ox, oi, ostate):
+    rep = {}
+    for i, k in enumerate(OUT):
+        name = OUT_GPU.get(k, k)
+        rep["x_" + k] = H.compare(name, outx[i], ox[k])
+        rep["i_" + k] = H.compare(name, outi[i], oi[k])
+    for k in STATE:
+        rep[k] = H.compare(k, state[k], ostate[k][: state[k].shape[0]])
+    return rep
+
+
+@pytest.mark.parametrize("switches", [{}, {"l_rev_corr": True}])
+def test_coupled_sequence_matches_oracle(runtime, switches):
+    R = runtime
+    ts = W.snow_grid(6000, seed=23, nsteps=24)
+    calls, F = schedule(ts, 24)
+    g = R.from_tileset(ts)
+    g.set_options(**switches)
+    outx = None
+    for i, c in enumerate(calls):
+        g.set_forcing(F[i])
+        gpu_call(g, c, ts.dels)
+        if i == len(calls) - 3:
+            outx = g.get("out")
+    g.synchronize()
+    outi = g.get("out")
+    gstate = {k: g.get(k) for k in STATE}
+    g.close()
+    ox, oi, ostate = oracle_run(ts, calls, F, 0, **switches)
+    rep = report(outx, outi, gstate, ox, oi, ostate)
+    # the reference's own precision mix on the same calls
+    rx, ri, rstate = oracle_run(ts, calls, F, 1, **switches)
+    ref = report(np.stack([rx[k] for k in OUT]), np.stack([ri[k] for k in OUT]),
+                 {k: rstate[k] for k in STATE}, ox, oi, ostate)
+    for k, r in rep.items():
+        if "tol" not in r:
+            continue
+        assert r["rms"] <= max(r["tol"], 3 * ref[k]["rms"]), (k, r, ref[k])
+        assert r["frac_within"] >= min(0.995, ref[k]["frac_within"] - 0.005), (k, r, ref[k])
+
+
+def test_coupled_state_contract(runtime):
+    """Bitwise: the explicit call changes no state but rtsoil and the carried
+    LAI; a cycle that is not the last leaves every banked field, and the
+    balance totals, as they were before it."""
+    R = runtime
+    ts = W.snow_grid(4000, seed=29, nsteps=8)
+    calls, F = schedule(ts, 8)
+    g = R.from_tileset(ts)
+    g.set_options(l_rev_corr=True)
+    for i, c in enumerate(calls[:-3]):
+        g.set_forcing(F[i])
+        gpu_call(g, c, ts.dels)
+    g.synchronize()
+    before = {k: g.get(k) for k in ALL_STATE}
+    g.set_forcing(F[-3])
+    gpu_call(g, calls[-3], ts.dels)             # explicit
+    g.synchronize()
+    mid = {k: g.get(k) for k in ALL_STATE}
+    for k in ALL_STATE:
+        if k not in ("rtsoil", "vlaiw"):
+            np.testing.assert_array_equal(mid[k], before[k], err_msg=k)
+    g.set_forcing(F[-2])
+    gpu_call(g, calls[-2], ts.dels)             # implicit, cycle 1 of 2
+    g.synchronize()
+    after = {k: g.get(k) for k in ALL_STATE}
+    for k in BANKED + ["wbtot1", "wbtot2", "owb", "ebal_tot", "wbal_tot", "vlaiw"]:
+        np.testing.assert_array_equal(after[k], mid[k], err_msg=k)
+    np.testing.assert_array_equal(after["flags"] & 1, mid["flags"] & 1)
+    g.set_forcing(F[-1])
+    gpu_call(g, calls[-1], ts.dels)             # implicit, last cycle: the state advances
+    g.synchronize()
+    assert not np.array_equal(g.get("tgg"), mid["tgg"])
+    with pytest.raises(R.CableGPUError):
+        g.step_implicit(1, ts.dels, cycleno=3, numcycles=2)
+    g.close()
