@@ -104,6 +104,11 @@ size_t storage_bytes(Storage s) { return s == S_U8 ? 1 : (s == S_F32 ? 4 : 8); }
 // ---------------------------------------------------------------- kernels
 __global__ void advance_clock_kernel(int* clock) { clock[0] += 1; }
 
+__global__ void explicit_trad_kernel(CgDev D) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < D.mp) explicit_trad(D, t);
+}
+
 // The prognostic bank of the coupled implicit call (cbl_prognostic_bank.F90:
 // 26-165): cable_store_prognostics saves these fields before each implicit
 // cycle and cable_reinstate_prognostics puts them back after every cycle but
@@ -338,7 +343,11 @@ int launch_step(cablegpu_ctx* c, const StepParams& p, const int* clock) {
   const bool diag = c->diag != 0;
   const int* bk = c->block;
   launch_phase_a(diag, c->stream, c->dev, c->d_tables, p, clock, bk[0]);
-  if (c->sur_enabled) {
+  if (p.mode != 0) {
+    // coupled calls: the plain canopy iteration (the surrogate start and the
+    // training-row harvest are offline-driver features)
+    launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, clock, bk[1]);
+  } else if (c->sur_enabled) {
     int rc = launch_sur_net(c);
     if (rc) return rc;
     ++c->launches;
@@ -348,12 +357,15 @@ int launch_step(cablegpu_ctx* c, const StepParams& p, const int* clock) {
   } else {
     launch_phase_b(diag, c->stream, c->dev, c->d_tables, p, clock, bk[1]);
   }
-  if (p.mode != 1) {   // the explicit coupled call stops after the canopy
+  if (p.mode != 1) {
     launch_phase_c1(diag, c->stream, c->dev, c->d_tables, p, clock, bk[2]);
     launch_phase_c2(diag, c->stream, c->dev, c->d_tables, p, clock, bk[3]);
     launch_phase_c3(diag, c->stream, c->dev, c->d_tables, p, clock, bk[4]);
+  } else {
+    // the explicit coupled call stops after the canopy: its radiative temperature
+    explicit_trad_kernel<<<(c->mp + 255) / 256, 256, 0, c->stream>>>(c->dev);
   }
-  c->launches += p.mode == 1 ? 2 : kKernelsPerStep;
+  c->launches += p.mode == 1 ? 3 : kKernelsPerStep;
   CG_CUDA(c, cudaGetLastError());
   return CABLEGPU_OK;
 }

@@ -65,8 +65,10 @@ __device__ constexpr float ZSHH[CG_MS + 1] = {0.5f * ZSE_C[0], 0.5f * (ZSE_C[0] 
 // snow-pack and soil-heat kernels, read by the soil-water kernel
 #define CG_NC_ALLOC 13
 
-template <bool kDiag>
+template <bool kDiag, bool kCoupled = false>
 __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
+  // the coupled-call code exists only in the kCoupled instantiation
+  const int mode = kCoupled ? P.mode : 0;
   const int ld = D.ld;
   const float dels = P.dels;
   // ---------------------------------------------------------------- static
@@ -142,7 +144,7 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
 
   // lakes top-layer fix (cbl_model_driver_offline.F90:116-121); the
   // coupled cbm_expl / cbm_impl have none
-  const bool offline = P.mode == 0;
+  const bool offline = mode == 0;
   if (offline) {
     if (iveg == LAKES && df_lt(wb[0], df32{sfc, 0.f})) {
       wbtot1 = wb[0].hi * DLIQ * zse[0];
@@ -163,7 +165,7 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
     // (cable_roughness.F90:176-186); it holds the LAI_eff of the host
     // model's last radiation call (cable_land_albedo_mod_cbl.F90:263,
     // cbl_um_update_canopy.F90:27), the same function of the snow state
-    if (P.mode != 0) {
+    if (mode != 0) {
       if (P.lai_refresh) D.vlaiw[t] = vlaiw;
       else vlaiw = D.vlaiw[t];
     }
@@ -438,8 +440,10 @@ __device__ __forceinline__ float transp_extract(float fe_mm, const float (&froot
   return se;
 }
 
-template <bool kDiag, bool kHarvest = false, bool kSur = false>
+template <bool kDiag, bool kHarvest = false, bool kSur = false, bool kCoupled = false>
 __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
+  // the coupled-call code exists only in the kCoupled instantiation
+  const int mode = kCoupled ? P.mode : 0;
   const int ld = D.ld;
   const float dels = P.dels;
   const int iveg = D.iveg[t], isoilm = D.isoilm[t];
@@ -1009,7 +1013,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
     float tc = tss - TFRZ;
     float ddq_dtg = (RMH2O / RMAIR) / pmb * TETENA * TETENB * TETENC / sqf(TETENC + tc) * expf(TETENB * tc / (TETENC + tc));
     dgdtg = dfn_dtg - dfh_dtg - dfe_ddq * ddq_dtg;
-    if (P.mode == 2) {
+    if (mode == 2) {
       D.work_b[CG_NB * ld + t] = dfh_dtg;
       D.work_b[(CG_NB + 1) * ld + t] = dfe_ddq * ddq_dtg;   // ssnow%dfe_dtg (:1026)
       D.work_b[(CG_NB + 2) * ld + t] = dfn_dtg;
@@ -1038,13 +1042,13 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
   // the coupled calls run no balance checks; cbm_expl restores the canopy
   // water and wetness factor (cbl_cbm_mod.F90:150-152), so the step's
   // state is what the implicit call leaves
-  if (P.mode == 0) D.ebal_tot[t] = D.ebal_tot[t] + (double)ebal;
-  if (P.mode != 1) {
+  if (mode == 0) D.ebal_tot[t] = D.ebal_tot[t] + (double)ebal;
+  if (mode != 1) {
     D.cansto[t] = cansto;
     D.owetfac[t] = owetfac_out;
   }
   D.rtsoil[t] = rtsoil;
-  if (P.mode != 1) {
+  if (mode != 1) {
     const float rec[CG_NB] = {ga, dgdtg, fes, fess, fesp, fevc, fevw, cls, precis0, evapfbl[0], evapfbl[1], evapfbl[2],
                               evapfbl[3], evapfbl[4], evapfbl[5], delwc, fpn, frday, tv};
 #pragma unroll
@@ -1052,21 +1056,14 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
   }
   const float rnet = fns + fnv;
   const float fgpp = -fpn + frday;
-  // cbm_expl's radiative temperature (cbl_cbm_mod.F90:172-179): emissivities
-  // 1, the surface temperature of the start of the step, and no correction
-  // term (canopy%fns_cor is zeroed by define_canopy, :233)
-  const float trad_x = sqrtf(sqrtf((1.f - transd) * pow4(tv) + transd * tss4));
-  const float outv[8] = {fe, fh, fgpp, frday, tv, rnet, ga, trad_x};
-  const int nout = P.mode == 1 ? 8 : 7;
+  const float outv[7] = {fe, fh, fgpp, frday, tv, rnet, ga};
   bool finite = true;
 #pragma unroll
-  for (int i = 0; i < 8; ++i)
-    if (i < nout) { D.out[i * ld + t] = outv[i]; finite = finite && isfinite(outv[i]); }
+  for (int i = 0; i < 7; ++i) { D.out[i * ld + t] = outv[i]; finite = finite && isfinite(outv[i]); }
   if (D.out_caller) {
     const size_t o = D.out_caller_order ? (size_t)D.tile_id[t] : (size_t)t;
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
-      if (i < nout) D.out_caller[(size_t)i * D.mp + o] = outv[i];
+    for (int i = 0; i < 7; ++i) D.out_caller[(size_t)i * D.mp + o] = outv[i];
   }
   {
     // output ranges of the reference's output checks (cable_checks.F90:71-123):
@@ -1089,8 +1086,24 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
   }
 }
 
-template <bool kDiag>
+// cbm_expl's radiative temperature (cbl_cbm_mod.F90:172-179) after the
+// canopy kernel of an explicit call: emissivities 1, the surface temperature
+// of the start of the step, and no correction term (canopy%fns_cor is zeroed
+// by define_canopy, cable_canopy.F90:233).
+__device__ __forceinline__ void explicit_trad(const CgDev& D, int t) {
+  const int ld = D.ld;
+  const float tv = D.out[4 * ld + t];
+  const float transd = D.work_a[27 * ld + t], tss = D.work_a[45 * ld + t];
+  const float trad = sqrtf(sqrtf((1.f - transd) * pow4(tv) + transd * pow4(tss)));
+  D.out[7 * ld + t] = trad;
+  if (D.out_caller) D.out_caller[(size_t)7 * D.mp + (D.out_caller_order ? (size_t)D.tile_id[t] : (size_t)t)] = trad;
+  if (!isfinite(trad)) { atomicOr(D.status, 1u); D.tile_status[t] |= CG_TS_NONFINITE; }
+}
+
+template <bool kDiag, bool kCoupled = false>
 __device__ __forceinline__ void phase_c1(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
+  // the coupled-call code exists only in the kCoupled instantiation
+  const int mode = kCoupled ? P.mode : 0;
   const int ld = D.ld;
   const float dels = P.dels;
   const int iveg = D.iveg[t], isoilm = D.isoilm[t];
@@ -1385,7 +1398,7 @@ __device__ __forceinline__ void phase_c1(const CgDev& D, const CgTables* __restr
   D.work_c[1 * ld + t] = precis;
   D.work_c[2 * ld + t] = segg;
   D.work_c[3 * ld + t] = smelt;
-  if (P.mode == 2) D.work_c[CG_NC * ld + t] = dtmlt0;
+  if (mode == 2) D.work_c[CG_NC * ld + t] = dtmlt0;
   (void)sconds; (void)hcll; (void)wblf; (void)wbfice;
 }
 
@@ -1439,8 +1452,10 @@ static __device__ __noinline__ float cg_snow_melting(CgSnowPack& p, int isflag, 
   return snowmlt;
 }
 
-template <bool kDiag>
+template <bool kDiag, bool kCoupled = false>
 __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
+  // the coupled-call code exists only in the kCoupled instantiation
+  const int mode = kCoupled ? P.mode : 0;
   const int ld = D.ld;
   const float dels = P.dels;
   const int iveg = D.iveg[t], isoilm = D.isoilm[t];
@@ -1492,7 +1507,7 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
   float hcll = fmaxf(0.01f, css * rhosoil);
   // dtmlt(:,1) so far this step (the snow-pack kernel's part); only the
   // implicit coupled call uses it
-  float dtmlt0 = P.mode == 2 ? D.work_c[CG_NC * ld + t] : 0.f;
+  float dtmlt0 = mode == 2 ? D.work_c[CG_NC * ld + t] : 0.f;
   float g1f = (float)gammzz1;
   float smelt = D.work_c[3 * ld + t];
   float wblf[CG_MS], wbfice[CG_MS];
@@ -1715,12 +1730,14 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
   D.work_c[5 * ld + t] = sghflux;
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) D.work_c[(6 + k) * ld + t] = gf[k];
-  if (P.mode == 2) D.work_c[CG_NC * ld + t] = dtmlt0;
+  if (mode == 2) D.work_c[CG_NC * ld + t] = dtmlt0;
   (void)tss; (void)first_call;
 }
 
-template <bool kDiag>
+template <bool kDiag, bool kCoupled = false>
 __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
+  // the coupled-call code exists only in the kCoupled instantiation
+  const int mode = kCoupled ? P.mode : 0;
   const int ld = D.ld;
   const float dels = P.dels;
   const int iveg = D.iveg[t], isoilm = D.isoilm[t];
@@ -1810,7 +1827,6 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     float fluxh[CG_MS + 1];
     fluxh[0] = 0.f; fluxh[CG_MS] = 0.f;
     float delt_prev = 0.f;
-#pragma unroll
     const float wbl_min = P.runoff_speed ? 0.001f : 0.01f;   // l_new_runoff_speed (cbl_smoisturev.F90:112)
 #pragma unroll
     for (int k = 1; k <= CG_MS - 1; ++k) {
@@ -2012,7 +2028,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     snage = fmaxf(0.0f, (snage + dtau) * (1.0f - dnsnow));
   }
   float trad;
-  if (P.mode != 2) {
+  if (mode != 2) {
     trad = sqrtf(sqrtf((1.f - transd) * pow4(tv) + transd * pow4(tss)));
   } else {
     // implicit coupled call: the online energy-balance corrections of
@@ -2149,7 +2165,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   D.csoil[t] = csoil[0]; D.csoil[ld + t] = csoil[1];
   D.snowd[t] = snowd; D.ssdnn[t] = ssdnn; D.snage[t] = snage; D.pudsto[t] = pudsto;
   D.tss[t] = tss; D.wb_lake[t] = wb_lake;
-  if (P.mode == 0) { D.owb[t] = wbtot; D.wbal_tot[t] = wbal_tot; }   // no balance checks in coupled calls
+  if (mode == 0) { D.owb[t] = wbtot; D.wbal_tot[t] = wbal_tot; }   // no balance checks in coupled calls
   D.out[7 * ld + t] = trad;
   if (D.out_caller) D.out_caller[(size_t)7 * D.mp + (D.out_caller_order ? (size_t)D.tile_id[t] : (size_t)t)] = trad;
   {

@@ -1,7 +1,20 @@
 // Phase B of the cbm() timestep kernel set -- canopy: define_canopy (Monin-Obukhov loop with dryLeaf / wetLeaf, soil evaporation).
-#define CG_PHASE phase_b
+#include "cbm_step.cuh"
+
+namespace cg {
+// the plain canopy kernel's phase, in the <kDiag, kCoupled> form the shared
+// kernel wrapper instantiates
+template <bool kDiag, bool kCoupled>
+__device__ __forceinline__ void phase_b_plain(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P,
+                                              int t) {
+  phase_b<kDiag, false, false, kCoupled>(D, T, P, t);
+}
+}  // namespace cg
+
+#define CG_PHASE phase_b_plain
 #define CG_PHASE_KERNEL cbm_phase_b_kernel
 #define CG_PHASE_LAUNCH launch_phase_b
+#define CG_PHASE_COUPLED 1
 #include "phase_kernels.cuh"
 
 namespace cg {

@@ -34,21 +34,38 @@ void launch_phase_c3(bool diag, cudaStream_t s, const CgDev& D, const CgTables* 
                     const int* clock, int block = kPhaseBlock);
 
 #ifdef CG_PHASE
-template <bool kDiag>
+// CG_PHASE_COUPLED 1: the phase has a second instantiation for the coupled
+// calls (StepParams::mode != 0), so that the offline one carries none of
+// their code; 0: one instantiation that tests the mode at run time.
+#ifndef CG_PHASE_COUPLED
+#define CG_PHASE_COUPLED 0
+#endif
+template <bool kDiag, bool kCoupled>
 __global__ void __maxnreg__(CG_MAXNREG)
     CG_PHASE_KERNEL(CgDev D, const CgTables* __restrict__ T, StepParams P, const int* __restrict__ clock) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= D.mp) return;
   StepParams p = P;
   if (clock) { p.ktau = clock[0]; p.step_index = clock[0] - 1; }
+#if CG_PHASE_COUPLED
+  CG_PHASE<kDiag, kCoupled>(D, T, p, t);
+#else
   CG_PHASE<kDiag>(D, T, p, t);
+#endif
 }
 
 void CG_PHASE_LAUNCH(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
                      const int* clock, int block) {
   const int grid = (D.mp + block - 1) / block;
-  if (diag) CG_PHASE_KERNEL<true><<<grid, block, 0, s>>>(D, T, P, clock);
-  else CG_PHASE_KERNEL<false><<<grid, block, 0, s>>>(D, T, P, clock);
+#if CG_PHASE_COUPLED
+  if (P.mode != 0) {
+    if (diag) CG_PHASE_KERNEL<true, true><<<grid, block, 0, s>>>(D, T, P, clock);
+    else CG_PHASE_KERNEL<false, true><<<grid, block, 0, s>>>(D, T, P, clock);
+    return;
+  }
+#endif
+  if (diag) CG_PHASE_KERNEL<true, false><<<grid, block, 0, s>>>(D, T, P, clock);
+  else CG_PHASE_KERNEL<false, false><<<grid, block, 0, s>>>(D, T, P, clock);
 }
 #endif
 

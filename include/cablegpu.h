@@ -200,7 +200,7 @@ int cablegpu_step(cablegpu_ctx* ctx, int ktau, float dels);
  * temperature and humidity (cable_implicit_driver.F90:189-198).
  *
  * cablegpu_step_explicit: radiation and canopy fluxes from the current state
- * (two kernel launches).  The canopy water, soil wetness factor and surface
+ * (three kernel launches: radiation, canopy, radiative temperature).  The canopy water, soil wetness factor and surface
  * temperature are left as they were (cbl_cbm_mod.F90:150-152); the canopy's
  * soil resistance (rtsoil) and ga are kept, as in the reference.  Outputs:
  * all eight rows of "out", trad from the start-of-step surface temperature
@@ -219,7 +219,9 @@ int cablegpu_step(cablegpu_ctx* ctx, int ktau, float dels);
  * the last the prognostic bank (cbl_prognostic_bank.F90) is restored after
  * the call, as cable_implicit_main.F90:190-213 does, so only the last cycle
  * advances the state.  The offline driver's lakes fix and balance checks do
- * not run in either call (ebal_tot, wbal_tot and owb are left alone). */
+ * not run in either call (ebal_tot, wbal_tot and owb are left alone).  Both
+ * calls use the plain dryLeaf iteration (the surrogate start and the
+ * training-row harvest apply to cablegpu_step / cablegpu_run only). */
 int cablegpu_step_explicit(cablegpu_ctx* ctx, int ktau, float dels, int lai_refresh);
 int cablegpu_step_implicit(cablegpu_ctx* ctx, int ktau, float dels, int cycleno, int numcycles);
 /* nsteps timesteps ktau0 .. ktau0+nsteps-1, replayed from a captured CUDA
