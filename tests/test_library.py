@@ -92,8 +92,11 @@ def test_parameter_tables_match_the_oracle(oracle):
     assert abs(fr.sum(0) - 1).max() < 1e-5
 
 
-SHIM = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "cable_gb300", "fortran",
-                    "cable_cbm_gpu.F90")
+FORTRAN = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "cable_gb300", "fortran")
+SHIM = os.path.join(FORTRAN, "cable_cbm_gpu.F90")
+COUPLED_SHIM = os.path.join(FORTRAN, "cable_cbm_coupled_gpu.F90")
+SHIM_FILES = [os.path.join(FORTRAN, n) for n in ("cablegpu_c.F90", "cablegpu_shim.F90", "cable_cbm_gpu.F90",
+                                                  "cable_cbm_coupled_gpu.F90")]
 
 
 def test_fortran_shim_binds_exported_symbols_and_registry_fields():
@@ -101,7 +104,7 @@ def test_fortran_shim_binds_exported_symbols_and_registry_fields():
     textually: every BIND(C) name is an exported symbol declared in the
     header, every field it moves is in the registry with the width and type
     the shim's buffer assumes, and the forcing order matches the ABI's."""
-    src = open(SHIM).read()
+    src = "\n".join(open(f).read() for f in SHIM_FILES)
     lib = C.CDLL(B.build())
     binds = re.findall(r'BIND\(C,\s*name="(\w+)"\)', src)
     assert len(binds) >= 10
@@ -122,6 +125,7 @@ def test_fortran_shim_binds_exported_symbols_and_registry_fields():
         assert buf in want, (name, buf, want)
     # forcing gathered into device order through the slot -> tile index, the
     # outputs scattered back through it
+    src = open(SHIM).read() + open(SHIM_FILES[1]).read()
     order = re.findall(r"forc\(:, (\d+)\) = met%(\w+)\(slot_tile(?:, (\d))?\)", src)
     names = []
     for idx, comp, band in order:
@@ -131,6 +135,32 @@ def test_fortran_shim_binds_exported_symbols_and_registry_fields():
     outs = re.findall(r"(?:canopy|rad)%(\w+)\(slot_tile\) = outb\(:, (\d)\)", src)
     assert [o[0] for o in sorted(outs, key=lambda x: int(x[1]))] == R.OUTPUT_FIELDS
     assert "cablegpu_set_host_layout(ctx, 1_c_int)" in src and "cablegpu_tile_order(ctx, C_LOC(slot_tile))" in src
+
+
+def test_coupled_fortran_shim_matches_the_cm3_interface():
+    """The ACCESS (CM3) replacement of cable_cbm_module: cbm_expl and cbm_impl
+    with the reference's argument lists (cbl_cbm_mod.F90:10-11, :184-186),
+    the forcing in the ABI's field order, the eight outputs back into their
+    components, and the two coupled entry points."""
+    src = open(COUPLED_SHIM).read()
+    assert re.search(r"^MODULE cable_cbm_module", src, re.M)
+    assert re.search(r"PUBLIC cbm_expl, cbm_impl", src)
+
+    def args(name):
+        m = re.search(r"SUBROUTINE %s\(([^)]*)\)" % name, src, re.S)
+        return [a.strip() for a in m.group(1).replace("&", "").split(",")]
+
+    tail = ["air", "bgc", "canopy", "met", "bal", "rad", "rough", "soil", "ssnow", "sum_flux", "veg", "climate"]
+    assert args("cbm_expl") == ["mp", "nrb", "ktau", "dels"] + tail
+    assert args("cbm_impl") == ["cycleno", "numcycles", "mp", "nrb", "ktau", "dels"] + tail
+    order = re.findall(r"forc\(:, (\d+)\) = met%(\w+)(?:\(:, (\d)\))?", src)
+    names = ["fsd_" + ("vis" if band == "1" else "nir") if comp == "fsd" else comp for _, comp, band in order]
+    assert names == R.FORCING_FIELDS
+    assert [int(o[0]) for o in order] == list(range(1, R.NFORCING + 1))
+    outs = re.findall(r"(?:canopy|rad)%(\w+) = outb\(:, (\d)\)", src)
+    assert [o[0] for o in sorted(outs, key=lambda x: int(x[1]))] == R.OUTPUT_FIELDS
+    assert "cablegpu_step_explicit(ctx" in src and "cablegpu_step_implicit(ctx" in src
+    assert "CALL put('vlaiw', C_LOC(r4))" in src and R.fields()["vlaiw"][2] == R.F32
 
 
 def test_soil_thermal_fix_tables_match_the_oracle(oracle):
