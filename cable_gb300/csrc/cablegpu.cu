@@ -490,6 +490,8 @@ int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out)
   cg_build_tables(&h.pft, &h.soil);
   CG_CUDA(c, cudaMalloc(&c->d_tables, sizeof(CgTables)));
   CG_CUDA(c, cudaMemcpyAsync(c->d_tables, &h, sizeof(CgTables), cudaMemcpyHostToDevice, c->stream));
+  upload_canopy_pft_table(h.pft, c->stream);
+  CG_CUDA(c, cudaGetLastError());
   // device tile order
   {
     std::vector<int> order(c->mp);

@@ -406,6 +406,18 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
   }
 }
 
+// The plant-type table the canopy kernel re-reads inside its dryLeaf
+// iteration, in constant memory (one copy per translation unit that includes
+// this header; phase_b.cu uploads its copy, upload_canopy_pft_table).  Tiles
+// are grouped by plant type, so a warp's reads are almost always of one
+// address: a constant-cache broadcast rather than an L1 load on the
+// iteration's dependency chain.  The table is the same for every context.
+static __constant__ CgPftTable c_pft;
+// A read of c_pft.  Constant-bank loads are cheap for the compiler to
+// re-issue where a value is used, so unlike ldv's reads these need no
+// protection against being hoisted into registers.
+__device__ __forceinline__ float ldk(const float& x) { return x; }
+
 // kHarvest: sampled tiles append a training row for the surrogate network
 // (features at the start of the first Monin-Obukhov iteration's dryLeaf and
 // its converged result) to D.harvest.  kSur: the first
@@ -596,7 +608,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
     }
     // boundary-layer conductance (:374-397)
     if (veg_mask) {
-      const float dl = ldv(V.dleaf + v);
+      const float dl = ldk(c_pft.dleaf[v]);
       float gbvtop = cmolar * APOL * visc / PRANDT / dl * sqrtf(us / fmaxf(usuh, 1.e-6f) * dl / visc) *
                      0.89194175f /* prandt**(1/3) */ / shelrb;
       gbvtop = fmaxf(0.05f, gbvtop);
@@ -619,7 +631,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
       if (sampled) {
         const float sc = scalex[0] + scalex[1];
         feat[0] = qcan_par[0]; feat[1] = qcan_par[1]; feat[2] = tlfx; feat[3] = dsx; feat[4] = ca;
-        feat[5] = ldv(V.vcmax + v) * sc; feat[6] = ldv(V.ejmax + v) * (1.0f - ldv(V.frac4 + v)) * sc; feat[7] = P.medlyn ? ldv(V.g1 + v) : ldv(V.a1gs + v);
+        feat[5] = ldk(c_pft.vcmax[v]) * sc; feat[6] = ldk(c_pft.ejmax[v]) * (1.0f - ldk(c_pft.frac4[v])) * sc; feat[7] = P.medlyn ? ldk(c_pft.g1[v]) : ldk(c_pft.a1gs[v]);
         feat[8] = fwsoil; feat[9] = vlaiw; feat[10] = us; feat[11] = tvair;
       }
       bool sur_try = false;
@@ -628,7 +640,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
         const float dt = D.sur_dt[t];
         if (isfinite(dt)) { sur_try = true; tlf_sur = tlf_entry + dt; }
       }
-      const float gswmin_p = ldv(V.gswmin + v);
+      const float gswmin_p = ldk(c_pft.gswmin[v]);
       float gswmin[2] = {fmaxf(1.e-6f, scalex[0] * gswmin_p), fmaxf(1.e-6f, scalex[1] * gswmin_p)};
       float gh[2] = {1e-3f, 1e-3f}, ghr[2] = {1e-3f, 1e-3f}, psycst[2] = {psyc, psyc};
       float rdx[2] = {0.f, 0.f}, anx[2] = {0.f, 0.f};
@@ -663,7 +675,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
         const bool active = veg_mask && abs_deltlf > conv;
         if (active) {
           ++passes_total;
-          const float dleaf = ldv(V.dleaf + v);
+          const float dleaf = ldk(c_pft.dleaf[v]);
           float gras = fmaxf(1.0e-6f, 1.595E8f * fabsf(tlfx - tvair) * (dleaf * dleaf * dleaf));
           float gr4 = sqrtf(sqrtf(gras));
 #pragma unroll
@@ -673,37 +685,37 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
             ghr[l] = gradis[l] + gh[l];
           }
           float vcmxt3[2], vcmxt4[2], vx3[2], vx4[2], gs_coeff[2];
-          const float vcmax = ldv(V.vcmax + v), frac4 = ldv(V.frac4 + v);
+          const float vcmax = ldk(c_pft.vcmax[v]), frac4 = ldk(c_pft.frac4[v]);
           float temp = xvcmxt3(tlfx) * vcmax * (1.0f - frac4);
           vcmxt3[0] = scalex[0] * temp; vcmxt3[1] = scalex[1] * temp;
           temp = xvcmxt4(tlfx - TFRZ) * vcmax * frac4;
           vcmxt4[0] = scalex[0] * temp; vcmxt4[1] = scalex[1] * temp;
-          temp = xejmxt3(tlfx) * ldv(V.ejmax + v) * (1.0f - frac4);
+          temp = xejmxt3(tlfx) * ldk(c_pft.ejmax[v]) * (1.0f - frac4);
           float ejmxt3[2] = {scalex[0] * temp, scalex[1] * temp};
           float tdiff = tlfx - TREFK;
           float arr = (1.0f - TREFK / tlfx) / (RGAS * TREFK);
-          float conkct = ldv(V.conkc0 + v) * expf(ldv(V.ekc + v) * arr);
-          float conkot = ldv(V.conko0 + v) * expf(ldv(V.eko + v) * arr);
+          float conkct = ldk(c_pft.conkc0[v]) * expf(ldk(c_pft.ekc[v]) * arr);
+          float conkot = ldk(c_pft.conko0[v]) * expf(ldk(c_pft.eko[v]) * arr);
           tlfxx = tlfx;
           float cx1 = conkct * (1.0f + 0.21f / conkot);
           float cx2 = 2.0f * GAM0 * (1.0f + GAM1 * tdiff + GAM2 * tdiff * tdiff);
 #pragma unroll
           for (int l = 0; l < 2; ++l) {
             float par = qcan_par[l] * 4.6e-6f;
-            const float alpha = ldv(V.alpha + v), convex = ldv(V.convex + v), cfrd = ldv(V.cfrd + v);
+            const float alpha = ldk(c_pft.alpha[v]), convex = ldk(c_pft.convex[v]), cfrd = ldk(c_pft.cfrd[v]);
             vx3[l] = ej3x(par * (1.0f - frac4), alpha, convex, ejmxt3[l]);
             vx4[l] = ej4x(par * frac4, alpha, convex, vcmxt4[l]);
             rdx[l] = cfrd * vcmxt3[l] + cfrd * vcmxt4[l];
           }
           if (!P.medlyn) {
-            float f = ldv(V.a1gs + v) / (1.0f + dsx / ldv(V.d0gs + v));
+            float f = ldk(c_pft.a1gs[v]) / (1.0f + dsx / ldk(c_pft.d0gs[v]));
             gs_coeff[0] = (fwsoil / csx[0]) * f;
             gs_coeff[1] = (fwsoil / csx[1]) * f;
           } else {
-            gswmin[0] = gswmin[1] = ldv(V.g0 + v);
+            gswmin[0] = gswmin[1] = ldk(c_pft.g0[v]);
             float vpd = (dsx < 50.0f) ? 0.05f : dsx * 1e-3f;
             float num = (fwsoil <= 0.05f) ? fwsoil / 0.05f : 1.0f;
-            float t2 = (ldv(V.g1 + v) * fwsoil) * rsqrtf(vpd);
+            float t2 = (ldk(c_pft.g1[v]) * fwsoil) * rsqrtf(vpd);
             gs_coeff[0] = (num + t2) / csx[0];
             gs_coeff[1] = (num + t2) / csx[1];
           }

@@ -56,4 +56,8 @@ void launch_phase_b_sur(bool diag, cudaStream_t s, const CgDev& D, const CgTable
   else cbm_phase_b_sur_kernel<false><<<grid, block, 0, s>>>(D, T, P, clock);
 }
 
+void upload_canopy_pft_table(const CgPftTable& pft, cudaStream_t s) {
+  cudaMemcpyToSymbolAsync(c_pft, &pft, sizeof(CgPftTable), 0, cudaMemcpyHostToDevice, s);
+}
+
 }  // namespace cg

@@ -33,6 +33,9 @@ void launch_phase_c2(bool diag, cudaStream_t s, const CgDev& D, const CgTables* 
 void launch_phase_c3(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
                     const int* clock, int block = kPhaseBlock);
 
+// the canopy kernel's constant-memory copy of the plant-type table
+void upload_canopy_pft_table(const CgPftTable& pft, cudaStream_t s);
+
 #ifdef CG_PHASE
 // CG_PHASE_COUPLED 1: the phase has a second instantiation for the coupled
 // calls (StepParams::mode != 0), so that the offline one carries none of
