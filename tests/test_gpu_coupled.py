@@ -73,18 +73,26 @@ def oracle_run(ts, calls, F, precision, **sw):
 
 
 def report(outx, outi, state, ox, oi, ostate):
+    """Per-field comparison over the entries finite on both sides (the
+    non-finite ones are checked to coincide by the caller)."""
+    def cmp(name, a, b):
+        m = np.isfinite(a) & np.isfinite(b)
+        return H.compare(name, np.asarray(a)[m], np.asarray(b)[m])
     rep = {}
     for i, k in enumerate(OUT):
         name = OUT_GPU.get(k, k)
-        rep["x_" + k] = H.compare(name, outx[i], ox[k])
-        rep["i_" + k] = H.compare(name, outi[i], oi[k])
+        rep["x_" + k] = cmp(name, outx[i], ox[k])
+        rep["i_" + k] = cmp(name, outi[i], oi[k])
     for k in STATE:
         rep[k] = H.compare(k, state[k], ostate[k][: state[k].shape[0]])
     return rep
 
 
-@pytest.mark.parametrize("switches", [{}, {"l_rev_corr": True}])
+@pytest.mark.parametrize("switches", [{}, {"l_rev_corr": True},
+                                      {"l_rev_corr": True, "ssnow_potev": "P-M", "litter": True}])
 def test_coupled_sequence_matches_oracle(runtime, switches):
+    """The third set: the implicit call's corrected ga is what Penman-Monteith
+    soil evaporation reads in the next call, explicit or implicit."""
     R = runtime
     ts = W.snow_grid(6000, seed=23, nsteps=24)
     calls, F = schedule(ts, 24)
@@ -110,6 +118,9 @@ def test_coupled_sequence_matches_oracle(runtime, switches):
     outi = g.get("out")
     gstate = {k: g.get(k) for k in STATE}
     g.close()
+    for i, k in enumerate(OUT):
+        np.testing.assert_array_equal(np.isfinite(outx[i]), np.isfinite(ox[k]), err_msg="finite " + k)
+        np.testing.assert_array_equal(np.isfinite(outi[i]), np.isfinite(oi[k]), err_msg="finite " + k)
     rep = report(outx, outi, gstate, ox, oi, ostate)
     # the reference's own precision mix on the same calls
     rx, ri, rstate, _ = oracle_run(ts, calls, F, 1, **switches)
