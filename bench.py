@@ -58,6 +58,7 @@ def parse():
     p.add_argument("--cpu-sample-steps", type=int, default=48)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-surrogate", action="store_true", help="skip the surrogate arm")
+    p.add_argument("--no-coupled", action="store_true", help="skip the coupled (cbm_expl / cbm_impl) arm")
     p.add_argument("--order", type=int, default=-1, help="tile order; -1 = autotuned (default)")
     p.add_argument("--blocks", default=None, help="threads per block of the five step kernels, e.g. 64,64,64,64,256 "
                                                   "(with --order; default: autotuned)")
@@ -312,6 +313,28 @@ def surrogate_arm(args, d, ts, plain_value, tuned):
                          "loss_train_val_last": [float(x) for x in losses[-1]]}}
 
 
+def coupled_arm(args, d, ts, plain_value, tuned, steps=32, numcycles=2):
+    """The ACCESS coupling on the same workload: one coupled timestep is
+    cbm_expl followed by numcycles cbm_impl cycles (the last one advances
+    the state; the others restore the prognostic bank), timed with CUDA
+    events on the context's stream (cablegpu_coupled_timed)."""
+    from cable_gb300 import runtime as R
+    g = R.from_tileset(ts, device=d.local, order=tuned[0])
+    g.set_blocks(tuned[1])
+    g.coupled_timed(1, 4, ts.dels, numcycles)
+    g.synchronize()
+    l0 = g.launch_count()
+    ms = g.coupled_timed(5, steps, ts.dels, numcycles)
+    g.synchronize()
+    launches = g.launch_count() - l0
+    g.close()
+    value = d.world * args.mp * steps / (d.max(ms) / 1e3)
+    return {"value": value, "unit": "tile-timesteps/s", "vs_plain": value / plain_value,
+            "ms_per_step": d.max(ms) / steps, "steps": steps,
+            "calls_per_step": "cbm_expl (lai refreshed) + %d cbm_impl cycles" % numcycles,
+            "gpu_launches": int(launches)}
+
+
 def run_gb300(args):
     import numpy as np
     from cable_gb300 import runtime as R
@@ -417,6 +440,12 @@ def run_gb300(args):
             sur = surrogate_arm(args, d, ts, value, (order, blocks))
         except Exception as exc:  # the line still prints; the failure is stated
             sur = {"error": str(exc)[:300]}
+    coupled = None
+    if not args.no_coupled:
+        try:
+            coupled = coupled_arm(args, d, ts, value, (order, blocks))
+        except Exception as exc:  # the line still prints; the failure is stated
+            coupled = {"error": str(exc)[:300]}
     cpu = None
     if d.rank == 0 and d.world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, ts)
@@ -429,7 +458,7 @@ def run_gb300(args):
                                                                  "create_and_tune_s": round(t_create, 2)}),
                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
                "clocks": clk, "gpu_launches": int(launches),
-               "step_kernels_ms": step_ms, "surrogate": sur}
+               "step_kernels_ms": step_ms, "surrogate": sur, "coupled": coupled}
         print(json.dumps(out))
     d.close()
 

@@ -860,6 +860,30 @@ int cablegpu_run_timed(cablegpu_ctx* c, int ktau0, int nsteps, float dels, float
   return CABLEGPU_OK;
 }
 
+int cablegpu_coupled_timed(cablegpu_ctx* c, int ktau0, int nsteps, float dels, int numcycles, float* ms_total) {
+  if (!c || !ms_total || ktau0 < 1 || nsteps < 1 || numcycles < 1 || !(dels > 0.f))
+    return fail(c, CABLEGPU_ERR_ARG, "coupled_timed: bad argument");
+  cudaEvent_t a, b;
+  CG_CUDA(c, cudaEventCreate(&a));
+  CG_CUDA(c, cudaEventCreate(&b));
+  CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  CG_CUDA(c, cudaEventRecord(a, c->stream));
+  int rc = CABLEGPU_OK;
+  for (int n = 0; n < nsteps && rc == CABLEGPU_OK; ++n) {
+    rc = cablegpu_step_explicit(c, ktau0 + n, dels, 1);
+    for (int cyc = 1; cyc <= numcycles && rc == CABLEGPU_OK; ++cyc)
+      rc = cablegpu_step_implicit(c, ktau0 + n, dels, cyc, numcycles);
+  }
+  if (rc == CABLEGPU_OK) {
+    CG_CUDA(c, cudaEventRecord(b, c->stream));
+    CG_CUDA(c, cudaEventSynchronize(b));
+    CG_CUDA(c, cudaEventElapsedTime(ms_total, a, b));
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return rc;
+}
+
 int cablegpu_kernel_timed(cablegpu_ctx* c, int ktau0, int nsteps, float dels, float* ms_per_launch) {
   if (!c || !ms_per_launch || nsteps <= 0) return CABLEGPU_ERR_ARG;
   std::vector<cudaEvent_t> ev(2 * nsteps);

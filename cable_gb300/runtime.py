@@ -41,7 +41,7 @@ EXPORTS = [
     "cablegpu_set_blocks", "cablegpu_get_config", "cablegpu_autotune", "cablegpu_step_host",
     "cablegpu_restart_write", "cablegpu_restart_read", "cablegpu_forcing_file_write", "cablegpu_file_info",
     "cablegpu_run_forcing_file", "cablegpu_set_host_layout", "cablegpu_tile_order",
-    "cablegpu_step_explicit", "cablegpu_step_implicit",
+    "cablegpu_step_explicit", "cablegpu_step_implicit", "cablegpu_coupled_timed",
 ]
 NOALLOC_MAX_TILES = 65536
 # science switch bits of cablegpu_set_options (include/cablegpu.h)
@@ -167,6 +167,7 @@ def load(build_if_missing: bool = True):
     L.cablegpu_set_options.argtypes = [vp, ip, ip, ip]
     L.cablegpu_step.argtypes = [vp, ip, C.c_float]
     L.cablegpu_step_explicit.argtypes = [vp, ip, C.c_float, ip]
+    L.cablegpu_coupled_timed.argtypes = [vp, ip, ip, C.c_float, ip, C.POINTER(C.c_float)]
     L.cablegpu_step_implicit.argtypes = [vp, ip, C.c_float, ip, ip]
     L.cablegpu_run.argtypes = [vp, ip, ip, C.c_float]
     L.cablegpu_synchronize.argtypes = [vp]
@@ -433,6 +434,14 @@ class CableGPU:
     def run_timed(self, ktau0, nsteps, dels=1800.0) -> float:
         ms = C.c_float()
         self._check(self.L.cablegpu_run_timed(self.h, int(ktau0), int(nsteps), float(dels), C.byref(ms)))
+        return ms.value
+
+    def coupled_timed(self, ktau0, nsteps, dels=1800.0, numcycles=2) -> float:
+        """Milliseconds (CUDA events) of nsteps coupled timesteps: an explicit
+        call and numcycles implicit cycles each."""
+        ms = C.c_float()
+        self._check(self.L.cablegpu_coupled_timed(self.h, int(ktau0), int(nsteps), float(dels), int(numcycles),
+                                                  C.byref(ms)))
         return ms.value
 
     def kernel_timed(self, ktau0, nsteps, dels=1800.0) -> float:

@@ -224,6 +224,11 @@ int cablegpu_step(cablegpu_ctx* ctx, int ktau, float dels);
  * training-row harvest apply to cablegpu_step / cablegpu_run only). */
 int cablegpu_step_explicit(cablegpu_ctx* ctx, int ktau, float dels, int lai_refresh);
 int cablegpu_step_implicit(cablegpu_ctx* ctx, int ktau, float dels, int cycleno, int numcycles);
+/* Timing helper (no counterpart in the reference): nsteps coupled timesteps
+ * ktau0.. of cablegpu_step_explicit(lai_refresh = 1) followed by numcycles
+ * cablegpu_step_implicit cycles, timed with CUDA events on the context's
+ * stream; *ms_total receives the elapsed milliseconds. */
+int cablegpu_coupled_timed(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, int numcycles, float* ms_total);
 /* nsteps timesteps ktau0 .. ktau0+nsteps-1, replayed from a captured CUDA
  * graph.  Asynchronous. */
 int cablegpu_run(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels);

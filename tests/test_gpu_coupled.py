@@ -167,3 +167,22 @@ def test_coupled_state_contract(runtime):
     with pytest.raises(R.CableGPUError):
         g.step_implicit(1, ts.dels, cycleno=3, numcycles=2)
     g.close()
+
+
+def test_coupled_timed_runs_exactly_the_calls(runtime):
+    """The timing helper's steps are the direct calls' steps, bitwise."""
+    R = runtime
+    ts = W.snow_grid(3000, seed=41, nsteps=6)
+    a = R.from_tileset(ts)
+    assert a.coupled_timed(1, 3, ts.dels, 2) > 0.0
+    a.synchronize()
+    b = R.from_tileset(ts)
+    for k in range(1, 4):
+        b.step_explicit(k, ts.dels, lai_refresh=True)
+        b.step_implicit(k, ts.dels, cycleno=1, numcycles=2)
+        b.step_implicit(k, ts.dels, cycleno=2, numcycles=2)
+    b.synchronize()
+    for k in ("wb", "tgg", "tggsn", "snowd", "cansto", "vlaiw", "out"):
+        np.testing.assert_array_equal(a.get(k), b.get(k), err_msg=k)
+    a.close()
+    b.close()
