@@ -112,31 +112,20 @@ __global__ void explicit_trad_kernel(CgDev D) {
 // The prognostic bank of the coupled implicit call (cbl_prognostic_bank.F90:
 // 26-165): cable_store_prognostics saves these fields before each implicit
 // cycle and cable_reinstate_prognostics puts them back after every cycle but
-// the last (cable_implicit_main.F90:190-213).  Soil water and ice as their
-// double-FP32 word pairs; isflag is bit 0 of flags, while bit 1 (soil_snow's
-// first call, the reference's SAVE counter) is not in the bank.  Not banked,
-// as in the reference: gammzz, the balance totals and the outputs (ga).
-constexpr int kBankRows = CG_MS + 4 * CG_MS + 4 * 3 + 9 + 3 + 2 + 1;
-__global__ void bank_kernel(CgDev D, float* __restrict__ bank, int restore) {
+// the last (cable_implicit_main.F90:190-213).  Each field's [rows][ld] block
+// moves as one device-to-device copy (soil water and ice as their
+// double-FP32 word pairs); isflag is bit 0 of flags, while bit 1 (soil_snow's
+// first call, the reference's SAVE counter) is not in the bank, so flags
+// is saved whole and only its bit 0 put back (bank_flags_kernel).  Not
+// banked, as in the reference: gammzz, the balance totals and the outputs
+// (ga).
+const char* const kBankFields[] = {"tgg", "wb", "wbice", "sdepth", "smass", "tggsn", "ssdn", "ssdnn", "snage",
+                                   "snowd", "pudsto", "rtsoil", "owetfac", "wb_lake", "tss",
+                                   "cansto" /* canopy%oldcansto of the next call */, "cplant", "csoil"};
+constexpr int kBankWords = CG_MS + 4 * CG_MS + 4 * 3 + 9 + 3 + 2;   // 4-byte rows of the fields above
+__global__ void bank_flags_kernel(uint8_t* __restrict__ flags, const uint8_t* __restrict__ saved, int mp) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= D.mp) return;
-  const size_t ld = (size_t)D.ld;
-  int r = 0;
-  auto mv = [&](float* f, int rows) {
-    for (int k = 0; k < rows; ++k, ++r) {
-      float* a = f + k * ld + t;
-      float* b = bank + r * ld + t;
-      if (restore) *a = *b; else *b = *a;
-    }
-  };
-  mv(D.tgg, CG_MS); mv(D.wb, 2 * CG_MS); mv(D.wbice, 2 * CG_MS);
-  mv(D.sdepth, 3); mv(D.smass, 3); mv(D.tggsn, 3); mv(D.ssdn, 3);
-  mv(D.ssdnn, 1); mv(D.snage, 1); mv(D.snowd, 1); mv(D.pudsto, 1); mv(D.rtsoil, 1); mv(D.owetfac, 1);
-  mv(D.wb_lake, 1); mv(D.tss, 1); mv(D.cansto, 1);   // cansto: canopy%oldcansto of the next call
-  mv(D.cplant, 3); mv(D.csoil, 2);
-  float* b = bank + r * ld + t;
-  if (restore) D.flags[t] = (uint8_t)((D.flags[t] & 0xFEu) | ((unsigned)*b & 1u));
-  else *b = (float)(D.flags[t] & 1u);
+  if (t < mp) flags[t] = (uint8_t)((flags[t] & 0xFEu) | (saved[t] & 1u));
 }
 
 // Cold start: the reference's initial state for a run without restart file.
@@ -252,7 +241,7 @@ struct cablegpu_ctx {
   float sur_gate = 0.1f;
   unsigned long long* d_sur_stats = nullptr;  // [2]
   float* d_sur_dt = nullptr;                  // [ld] predicted leaf-temperature change
-  float* d_bank = nullptr;                    // [kBankRows][ld] prognostic bank of the implicit coupled call
+  void* d_bank = nullptr;                     // prognostic bank of the implicit coupled call (kBankFields)
   int graph_sur = -1;
   float graph_gate = -1.f;
   // threads per block of the five step kernels (radiation, canopy, snow
@@ -725,20 +714,39 @@ int cablegpu_step_implicit(cablegpu_ctx* c, int ktau, float dels, int cycleno, i
   StepParams p = make_params(c, ktau, dels);
   p.mode = 2;
   p.final_cycle = cycleno == numcycles ? 1 : 0;
-  const int block = 256, grid = (c->mp + block - 1) / block;
+  const size_t ld = (size_t)c->ld;
+  // bank layout: the fields' blocks one after another, then flags
+  auto bank_copies = [&](bool restore) -> int {
+    size_t off = 0;
+    for (const char* name : kBankFields) {
+      const int id = cablegpu_field_id(name);
+      const FieldDef& f = registry()[id];
+      const size_t bytes = storage_bytes(f.st) * (size_t)f.nlayer * ld;
+      char* field = (char*)c->field_ptr[id];
+      char* bank = (char*)c->d_bank + off;
+      CG_CUDA(c, cudaMemcpyAsync(restore ? field : bank, restore ? bank : field, bytes, cudaMemcpyDeviceToDevice,
+                                 c->stream));
+      off += bytes;
+    }
+    uint8_t* flags = (uint8_t*)c->field_ptr[cablegpu_field_id("flags")];
+    uint8_t* saved = (uint8_t*)c->d_bank + off;
+    if (restore) {
+      bank_flags_kernel<<<(c->mp + 255) / 256, 256, 0, c->stream>>>(flags, saved, c->mp);
+      ++c->launches;
+      CG_CUDA(c, cudaGetLastError());
+    } else {
+      CG_CUDA(c, cudaMemcpyAsync(saved, flags, ld, cudaMemcpyDeviceToDevice, c->stream));
+    }
+    return CABLEGPU_OK;
+  };
   if (!p.final_cycle) {
-    if (!c->d_bank) CG_CUDA(c, cudaMalloc(&c->d_bank, sizeof(float) * kBankRows * (size_t)c->ld));
-    bind_device_view(c);
-    bank_kernel<<<grid, block, 0, c->stream>>>(c->dev, c->d_bank, 0);
-    ++c->launches;
+    if (!c->d_bank) CG_CUDA(c, cudaMalloc(&c->d_bank, 4 * (size_t)kBankWords * ld + ld));
+    int rc = bank_copies(false);
+    if (rc) return rc;
   }
   int rc = launch_step(c, p, nullptr);
   if (rc) return rc;
-  if (!p.final_cycle) {
-    bank_kernel<<<grid, block, 0, c->stream>>>(c->dev, c->d_bank, 1);
-    ++c->launches;
-    CG_CUDA(c, cudaGetLastError());
-  }
+  if (!p.final_cycle) return bank_copies(true);
   return CABLEGPU_OK;
 }
 
