@@ -122,7 +122,6 @@ __global__ void explicit_trad_kernel(CgDev D) {
 const char* const kBankFields[] = {"tgg", "wb", "wbice", "sdepth", "smass", "tggsn", "ssdn", "ssdnn", "snage",
                                    "snowd", "pudsto", "rtsoil", "owetfac", "wb_lake", "tss",
                                    "cansto" /* canopy%oldcansto of the next call */, "cplant", "csoil"};
-constexpr int kBankWords = CG_MS + 4 * CG_MS + 4 * 3 + 9 + 3 + 2;   // 4-byte rows of the fields above
 __global__ void bank_flags_kernel(uint8_t* __restrict__ flags, const uint8_t* __restrict__ saved, int mp) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < mp) flags[t] = (uint8_t)((flags[t] & 0xFEu) | (saved[t] & 1u));
@@ -740,7 +739,14 @@ int cablegpu_step_implicit(cablegpu_ctx* c, int ktau, float dels, int cycleno, i
     return CABLEGPU_OK;
   };
   if (!p.final_cycle) {
-    if (!c->d_bank) CG_CUDA(c, cudaMalloc(&c->d_bank, 4 * (size_t)kBankWords * ld + ld));
+    if (!c->d_bank) {
+      size_t bytes = ld;   // flags
+      for (const char* name : kBankFields) {
+        const FieldDef& f = registry()[cablegpu_field_id(name)];
+        bytes += storage_bytes(f.st) * (size_t)f.nlayer * ld;
+      }
+      CG_CUDA(c, cudaMalloc(&c->d_bank, bytes));
+    }
     int rc = bank_copies(false);
     if (rc) return rc;
   }
