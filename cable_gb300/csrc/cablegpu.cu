@@ -1101,7 +1101,9 @@ int cablegpu_autotune(const cablegpu_tiles* tiles, int device, int sample_tiles,
     sw[i] = tiles->swscale ? tiles->swscale[j] : 1.f;
   }
   std::vector<double> sn(n, 0.0), tg(n, 285.0), wb(n, 0.25);
-  const int cand_block[3] = {64, 128, 256};
+  // 32: a block releases its registers when its last warp finishes, so
+  // one-warp blocks free a diverged warp's slot early (the canopy kernel)
+  const int cand_block[4] = {32, 64, 128, 256};
   float best = 1e30f;
   for (int order = 0; order <= 3; ++order) {
     cablegpu_tiles t = {n, iveg.data(), isoil.data(), vlai.data(), lat.data(), ph.data(), tb.data(), sw.data(), order};
@@ -1112,7 +1114,7 @@ int cablegpu_autotune(const cablegpu_tiles* tiles, int device, int sample_tiles,
     if (!rc) rc = cablegpu_run(c, 1, 4, 1800.f);
     float per[5] = {1e30f, 1e30f, 1e30f, 1e30f, 1e30f};
     int pick[5] = {128, 128, 128, 128, 128};
-    for (int b = 0; b < 3 && !rc; ++b) {
+    for (int b = 0; b < 4 && !rc; ++b) {
       int bb[5];
       std::fill(bb, bb + 5, cand_block[b]);
       rc = cablegpu_set_blocks(c, bb);

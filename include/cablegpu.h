@@ -307,7 +307,7 @@ long long cablegpu_launch_count(cablegpu_ctx* ctx);
  * the tile order the context was built with and the current block sizes. */
 int cablegpu_set_blocks(cablegpu_ctx* ctx, const int* block5);
 int cablegpu_get_config(cablegpu_ctx* ctx, int* order, int* block5);
-/* Autotuner: times tile orders 0-3 and block sizes 64, 128, 256 of each
+/* Autotuner: times tile orders 0-3 and block sizes 32, 64, 128, 256 of each
  * step kernel on an evenly strided sample of `sample_tiles` of the tiles
  * (synthetic forcing, nsteps timed steps per candidate) and returns the
  * fastest order, the fastest block size of each kernel and the step time
