@@ -112,19 +112,21 @@ __global__ void explicit_trad_kernel(CgDev D) {
 // The prognostic bank of the coupled implicit call (cbl_prognostic_bank.F90:
 // 26-165): cable_store_prognostics saves these fields before each implicit
 // cycle and cable_reinstate_prognostics puts them back after every cycle but
-// the last (cable_implicit_main.F90:190-213).  Each field's [rows][ld] block
-// moves as one device-to-device copy (soil water and ice as their
-// double-FP32 word pairs); isflag is bit 0 of flags, while bit 1 (soil_snow's
-// first call, the reference's SAVE counter) is not in the bank, so flags
-// is saved whole and only its bit 0 put back (bank_flags_kernel).  Not
-// banked, as in the reference: gammzz, the balance totals and the outputs
-// (ga).
+// the last (cable_implicit_main.F90:190-213).  Here the cycle runs on a
+// copy instead: each banked field's [rows][ld] block is copied device to
+// device (soil water and ice as their double-FP32 word pairs), the cycle's
+// kernels read and write the copies, and the fields' own blocks, untouched,
+// are the reinstated state.  isflag is bit 0 of flags, while bit 1
+// (soil_snow's first call, the reference's SAVE counter) is not in the
+// bank: the cycle's bit 1 is merged back (bank_flags_kernel).  Not banked,
+// as in the reference, and so updated in place by the cycle: gammzz, the
+// balance totals and the outputs (ga).
 const char* const kBankFields[] = {"tgg", "wb", "wbice", "sdepth", "smass", "tggsn", "ssdn", "ssdnn", "snage",
                                    "snowd", "pudsto", "rtsoil", "owetfac", "wb_lake", "tss",
                                    "cansto" /* canopy%oldcansto of the next call */, "cplant", "csoil"};
-__global__ void bank_flags_kernel(uint8_t* __restrict__ flags, const uint8_t* __restrict__ saved, int mp) {
+__global__ void bank_flags_kernel(uint8_t* __restrict__ flags, const uint8_t* __restrict__ cycle, int mp) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < mp) flags[t] = (uint8_t)((flags[t] & 0xFEu) | (saved[t] & 1u));
+  if (t < mp) flags[t] = (uint8_t)((flags[t] & 1u) | (cycle[t] & 0xFEu));
 }
 
 // Cold start: the reference's initial state for a run without restart file.
@@ -713,46 +715,43 @@ int cablegpu_step_implicit(cablegpu_ctx* c, int ktau, float dels, int cycleno, i
   StepParams p = make_params(c, ktau, dels);
   p.mode = 2;
   p.final_cycle = cycleno == numcycles ? 1 : 0;
+  if (p.final_cycle) return launch_step(c, p, nullptr);
+  // a cycle that is not the last runs on a copy of the banked fields
   const size_t ld = (size_t)c->ld;
-  // bank layout: the fields' blocks one after another, then flags
-  auto bank_copies = [&](bool restore) -> int {
-    size_t off = 0;
+  if (!c->d_bank) {
+    size_t bytes = ld;   // flags
     for (const char* name : kBankFields) {
-      const int id = cablegpu_field_id(name);
-      const FieldDef& f = registry()[id];
-      const size_t bytes = storage_bytes(f.st) * (size_t)f.nlayer * ld;
-      char* field = (char*)c->field_ptr[id];
-      char* bank = (char*)c->d_bank + off;
-      CG_CUDA(c, cudaMemcpyAsync(restore ? field : bank, restore ? bank : field, bytes, cudaMemcpyDeviceToDevice,
-                                 c->stream));
-      off += bytes;
+      const FieldDef& f = registry()[cablegpu_field_id(name)];
+      bytes += storage_bytes(f.st) * (size_t)f.nlayer * ld;
     }
-    uint8_t* flags = (uint8_t*)c->field_ptr[cablegpu_field_id("flags")];
-    uint8_t* saved = (uint8_t*)c->d_bank + off;
-    if (restore) {
-      bank_flags_kernel<<<(c->mp + 255) / 256, 256, 0, c->stream>>>(flags, saved, c->mp);
-      ++c->launches;
-      CG_CUDA(c, cudaGetLastError());
-    } else {
-      CG_CUDA(c, cudaMemcpyAsync(saved, flags, ld, cudaMemcpyDeviceToDevice, c->stream));
-    }
-    return CABLEGPU_OK;
-  };
-  if (!p.final_cycle) {
-    if (!c->d_bank) {
-      size_t bytes = ld;   // flags
-      for (const char* name : kBankFields) {
-        const FieldDef& f = registry()[cablegpu_field_id(name)];
-        bytes += storage_bytes(f.st) * (size_t)f.nlayer * ld;
-      }
-      CG_CUDA(c, cudaMalloc(&c->d_bank, bytes));
-    }
-    int rc = bank_copies(false);
-    if (rc) return rc;
+    CG_CUDA(c, cudaMalloc(&c->d_bank, bytes));
   }
-  int rc = launch_step(c, p, nullptr);
+  const int nbank = (int)(sizeof(kBankFields) / sizeof(kBankFields[0]));
+  int ids[sizeof(kBankFields) / sizeof(kBankFields[0]) + 1];
+  void* own[sizeof(kBankFields) / sizeof(kBankFields[0]) + 1];
+  size_t off = 0;
+  int nswapped = 0;
+  cudaError_t ce = cudaSuccess;
+  for (int i = 0; i <= nbank && ce == cudaSuccess; ++i) {
+    ids[i] = cablegpu_field_id(i < nbank ? kBankFields[i] : "flags");
+    const FieldDef& f = registry()[ids[i]];
+    const size_t bytes = storage_bytes(f.st) * (size_t)f.nlayer * ld;
+    own[i] = c->field_ptr[ids[i]];
+    void* copy = (char*)c->d_bank + off;
+    ce = cudaMemcpyAsync(copy, own[i], bytes, cudaMemcpyDeviceToDevice, c->stream);
+    if (ce == cudaSuccess) { c->field_ptr[ids[i]] = copy; nswapped = i + 1; }
+    off += bytes;
+  }
+  int rc = ce == cudaSuccess ? launch_step(c, p, nullptr) : CABLEGPU_OK;
+  // the fields' own blocks again, whatever happened
+  for (int i = 0; i < nswapped; ++i) c->field_ptr[ids[i]] = own[i];
+  bind_device_view(c);
+  CG_CUDA(c, ce);
   if (rc) return rc;
-  if (!p.final_cycle) return bank_copies(true);
+  bank_flags_kernel<<<(c->mp + 255) / 256, 256, 0, c->stream>>>((uint8_t*)own[nbank], (const uint8_t*)c->d_bank + off - ld,
+                                                              c->mp);
+  ++c->launches;
+  CG_CUDA(c, cudaGetLastError());
   return CABLEGPU_OK;
 }
 
