@@ -1,6 +1,7 @@
 /*
  * cablegpu.h - C ABI of the GB300 implementation of CABLE's per-timestep
- * tile physics (the offline cbm() call).
+ * tile physics (the offline cbm() call, and the ACCESS coupling's
+ * cbm_expl / cbm_impl: cablegpu_step_explicit / cablegpu_step_implicit).
  *
  * Replaces, for the offline driver, the reference interface
  *   SUBROUTINE cbm(ktau, dels, air, bgc, canopy, met, bal, rad, rough, soil,
