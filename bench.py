@@ -241,16 +241,39 @@ def run_reference(args):
     d.close()
 
 
-def traffic_per_step(mp):
-    """DRAM bytes per step from the committed ncu summary, scaled to mp tiles."""
+def profile_figure(key):
+    """A per-tile figure ("key: value" line) of the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "cbm_step_snow_grid.md")
     try:
         for ln in open(path):
-            if ln.startswith("traffic_bytes_per_tile_step:"):
-                return float(ln.split(":")[1]) * mp
+            if ln.startswith(key + ":"):
+                return float(ln.split(":")[1])
     except OSError:
         pass
     return None
+
+
+def traffic_per_step(mp):
+    """DRAM bytes per step from the committed ncu summary, scaled to mp tiles."""
+    b = profile_figure("traffic_bytes_per_tile_step")
+    return None if b is None else b * mp
+
+
+def canopy_issue(mp, canopy_ms, sm_mhz):
+    """The canopy kernel against its own bound, instruction issue: warp
+    instructions per tile-step from the committed ncu summary (a count
+    independent of the tile count: one thread per tile) times the tiles,
+    over its event-timed duration, against one warp instruction per cycle
+    per scheduler (152 SMs x 4) at the SM clock sampled during the run."""
+    n = profile_figure("canopy_warp_instructions_per_tile_step")
+    if n is None or not canopy_ms or not sm_mhz:
+        return None
+    achieved = n * mp / (canopy_ms / 1e3)
+    peak = 152 * 4 * sm_mhz * 1e6
+    return {"kernel": "canopy", "bound": "issue", "achieved": achieved, "peak": peak,
+            "unit": "warp instructions/s", "frac": achieved / peak,
+            "source": "ncu smsp__inst_executed.sum per tile (profiles/cbm_step_snow_grid.md) x tiles / "
+                      "CUDA-event kernel time; peak at the sampled median SM clock"}
 
 
 def surrogate_arm(args, d, ts, plain_value, tuned):
@@ -475,6 +498,7 @@ def run_gb300(args):
                                                                  "create_and_tune_s": round(t_create, 2)}),
                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
                "clocks": clk, "gpu_launches": int(launches),
+               "canopy_issue": canopy_issue(args.mp, roof["kernels_ms"].get("canopy"), (clk or {}).get("sm_mhz")),
                "step_kernels_ms": step_ms, "surrogate": sur, "coupled": coupled}
         print(json.dumps(out))
     d.close()
