@@ -88,15 +88,17 @@ def report(outx, outi, state, ox, oi, ostate):
     return rep
 
 
-@pytest.mark.parametrize("switches", [{}, {"l_rev_corr": True},
-                                      {"l_rev_corr": True, "ssnow_potev": "P-M", "litter": True}])
-def test_coupled_sequence_matches_oracle(runtime, switches):
+@pytest.mark.parametrize("switches,order", [({}, 0), ({"l_rev_corr": True}, 0),
+                                            ({"l_rev_corr": True, "ssnow_potev": "P-M", "litter": True}, 0),
+                                            ({"medlyn": True, "soil_thermal_fix": True}, 2)])
+def test_coupled_sequence_matches_oracle(runtime, switches, order):
     """The third set: the implicit call's corrected ga is what Penman-Monteith
-    soil evaporation reads in the next call, explicit or implicit."""
+    soil evaporation reads in the next call, explicit or implicit.  The
+    fourth runs in the climate-grouped tile order."""
     R = runtime
     ts = W.snow_grid(6000, seed=23, nsteps=24)
     calls, F = schedule(ts, 24)
-    g = R.from_tileset(ts)
+    g = R.from_tileset(ts, order=order)
     g.set_options(**switches)
     outx = None
     for i, c in enumerate(calls):
