@@ -242,3 +242,33 @@ def test_site5_coupled_year_against_oracle(runtime):
     np.testing.assert_allclose(gs["cplant"], o["cplant"], rtol=1e-3, atol=0.5)
     # no balance checks in the coupled calls: the totals stay at their start
     assert not np.any(gs["ebal_tot"]) and not np.any(gs["wbal_tot"])
+
+
+def test_snow_grid_coupled_year_against_oracle(runtime):
+    """256 snow tiles over a year of ACCESS timesteps (cbm_expl and two
+    cbm_impl cycles) against the FP64 oracle, with the offline snow year's
+    bounds: snow layering and melt are threshold events (the reference's
+    REAL=FP32 mix flips 1 tile beyond 0.1 K of soil temperature over this
+    year, keeps the rest within 0.005 K RMS and 98.4 % of tiles within
+    1 kg/m2 of snow)."""
+    R = runtime
+    ts = W.snow_grid(mp=256, nsteps=17520)
+    g = R.from_tileset(ts)
+    g.coupled_timed(1, 17520, ts.dels, 2)
+    g.synchronize()
+    gs = {k: np.asarray(g.get(k), np.float64) for k in ("wb", "tgg", "snowd", "csoil", "cplant")}
+    g.close()
+    calls = []
+    for k in range(1, 17521):
+        calls += [(k, 1, 1, 1), (k, 2, 0, 0), (k, 2, 1, 0)]
+    st = O.init_state(ts, 0)
+    O.run_calls(ts, st, calls)
+    o = {k: np.asarray(v, np.float64).reshape(gs[k].shape) for k, v in O.split_state(st).items() if k in gs}
+    assert float(np.sqrt(np.mean((gs["wb"] - o["wb"]) ** 2))) < 5e-4     # m3/m3
+    dt = np.abs(gs["tgg"] - o["tgg"])
+    flipped = dt.max(axis=0) > 0.1                                      # K, per tile
+    assert flipped.sum() <= 4, np.where(flipped)[0]
+    assert np.sqrt(np.mean(dt[:, ~flipped] ** 2)) < 0.02                # K
+    assert np.mean(np.abs(gs["snowd"] - o["snowd"]) <= 1.0) >= 0.95     # kg/m2
+    for k in ("csoil", "cplant"):
+        assert np.mean(np.abs(gs[k] - o[k]) <= np.maximum(1e-3 * np.abs(o[k]), 0.5)) >= 0.95, k
