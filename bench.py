@@ -160,17 +160,41 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU (oracle)
-def cpu_time(ts, steps, precision=1):
-    """Seconds of the CPU restatement (precision 1: REAL=FP32, r_2=FP64) on
-    every host core for ``ts`` tiles and ``steps`` steps."""
+def oracle_timing_build():
+    """The CPU restatement's timing build (oracle/libcbmref_timing.so: -O3
+    with FMA contraction and unrolling), the one the CPU legs time."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib as O
+    O.TIMING = True
+    return O
+
+
+def cpu_time(ts, steps, precision=1, nthreads=None):
+    """Seconds of the CPU restatement (precision 1: REAL=FP32, r_2=FP64; 0:
+    FP64) on ``nthreads`` host cores (default all) for ``ts`` tiles and
+    ``steps`` steps."""
+    O = oracle_timing_build()
     st = O.init_state(ts, precision)
-    O.run(ts, st, 2, ktau0=1, precision=precision)  # warm caches / threads
+    O.run(ts, st, 2, ktau0=1, precision=precision, nthreads=nthreads)  # warm caches / threads
     st = O.init_state(ts, precision)
     t0 = time.perf_counter()
-    O.run(ts, st, steps, ktau0=1, precision=precision)
+    O.run(ts, st, steps, ktau0=1, precision=precision, nthreads=nthreads)
     return time.perf_counter() - t0
+
+
+def cpu_site_year():
+    """The site configuration on one core: 5 tiles (PFT 1, 2, 5, 6, 9) on
+    soil type 2, 17,520 half-hour steps (a year), in FP64 and in the
+    reference's REAL=FP32 / r_2=FP64 mix."""
+    from cable_gb300 import workloads as W
+    ts = W.site5(nsteps=17520)
+    out = {}
+    for key, prec in (("fp64", 0), ("precision_mix", 1)):
+        secs = cpu_time(ts, 17520, precision=prec, nthreads=1)
+        out[key] = {"value": ts.mp * 17520 / secs, "unit": "tile-timesteps/s", "seconds": round(secs, 3)}
+    out.update({"cores": 1, "kind": "port",
+                "sample": "site5: 5 tiles x 17,520 steps of 1800 s (one year), one thread"})
+    return out
 
 
 def cpu_baseline(args, ts_full):
@@ -180,7 +204,9 @@ def cpu_baseline(args, ts_full):
     return {"value": n * args.cpu_sample_steps / secs, "unit": "tile-timesteps/s", "cores": os.cpu_count(),
             "kind": "port",
             "sample": "%d tiles of the %s workload x %d steps, CPU restatement of the reference cbm() "
-                      "(REAL FP32 / r_2 FP64), OpenMP over tiles, %.1f s" % (n, ts_full.name, args.cpu_sample_steps, secs)}
+                      "(REAL FP32 / r_2 FP64), OpenMP over tiles, %.1f s" % (n, ts_full.name, args.cpu_sample_steps, secs),
+            "build": "oracle/libcbmref_timing.so: g++ -O3 -ffp-contract=fast -funroll-loops -fopenmp",
+            "site_year_single_thread": cpu_site_year()}
 
 
 def workload(args, rank=0):
@@ -206,8 +232,7 @@ def run_reference(args):
     timestep over a bounded tile sample of the workload, sized by a short
     calibration so that the --warmup W untimed and --steps K timed steps
     take about two minutes together."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle_lib as O
+    O = oracle_timing_build()
     d = Dist(args.gpus)
     if d.rank != 0:
         d.close()
@@ -233,7 +258,8 @@ def run_reference(args):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
            "data": "synthetic (seeded generator)", "config": config(args, args.gpus),
            "cpu_baseline": {"value": value, "unit": "tile-timesteps/s", "cores": os.cpu_count(), "kind": "port",
-                            "sample": sample},
+                            "sample": sample,
+                            "build": "oracle/libcbmref_timing.so: g++ -O3 -ffp-contract=fast -funroll-loops -fopenmp"},
            "e2e": {"value": value, "unit": "tile-timesteps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "note": "the reference is Fortran and cannot be compiled here (no Fortran compiler); this arm times "
                    "the CPU restatement of its cbm() in the reference's REAL=FP32 / r_2=FP64 precision mix"}

@@ -119,8 +119,9 @@ __global__ void explicit_trad_kernel(CgDev D) {
 // are the reinstated state.  isflag is bit 0 of flags, while bit 1
 // (soil_snow's first call, the reference's SAVE counter) is not in the
 // bank: the cycle's bit 1 is merged back (bank_flags_kernel).  Not banked,
-// as in the reference, and so updated in place by the cycle: gammzz, the
-// balance totals and the outputs (ga).
+// as in the reference, and so updated in place by the cycle: gammzz and the
+// outputs (ga).  The coupled calls do not touch the balance totals (owb,
+// ebal_tot, wbal_tot) or the lakes fix's wbtot1 / wbtot2 at all.
 const char* const kBankFields[] = {"tgg", "wb", "wbice", "sdepth", "smass", "tggsn", "ssdn", "ssdnn", "snage",
                                    "snowd", "pudsto", "rtsoil", "owetfac", "wb_lake", "tss",
                                    "cansto" /* canopy%oldcansto of the next call */, "cplant", "csoil"};
@@ -640,17 +641,29 @@ int cablegpu_field_device_ptr(cablegpu_ctx* c, int id, void** dptr, int* ld) {
 
 int cablegpu_cold_start(cablegpu_ctx* c, const double* snowd0, const double* tgg0, const double* wb0) {
   if (!c || !snowd0 || !tgg0 || !wb0) return fail(c, CABLEGPU_ERR_ARG, "cold_start: null argument");
+  // the staging buffer belongs on the context's device, whichever device
+  // the calling thread has current
+  int prev = 0;
+  CG_CUDA(c, cudaGetDevice(&prev));
+  CG_CUDA(c, cudaSetDevice(c->device));
   const size_t n = (size_t)c->mp;
   double* tmp = nullptr;
-  CG_CUDA(c, cudaMalloc(&tmp, 3 * n * sizeof(double)));
-  CG_CUDA(c, cudaMemcpyAsync(tmp, snowd0, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  CG_CUDA(c, cudaMemcpyAsync(tmp + n, tgg0, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  CG_CUDA(c, cudaMemcpyAsync(tmp + 2 * n, wb0, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  bind_device_view(c);
-  cold_start_kernel<<<(c->mp + 255) / 256, 256, 0, c->stream>>>(c->dev, c->d_tables, tmp, tmp + n, tmp + 2 * n);
-  CG_CUDA(c, cudaGetLastError());
-  CG_CUDA(c, cudaStreamSynchronize(c->stream));
-  CG_CUDA(c, cudaFree(tmp));
+  cudaError_t e = cudaMalloc(&tmp, 3 * n * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tmp, snowd0, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tmp + n, tgg0, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tmp + 2 * n, wb0, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) {
+    bind_device_view(c);
+    cold_start_kernel<<<(c->mp + 255) / 256, 256, 0, c->stream>>>(c->dev, c->d_tables, tmp, tmp + n, tmp + 2 * n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (tmp) {
+    const cudaError_t ef = cudaFree(tmp);
+    if (e == cudaSuccess) e = ef;
+  }
+  cudaSetDevice(prev);
+  if (e != cudaSuccess) return fail(c, CABLEGPU_ERR_CUDA, std::string("cold_start: ") + cudaGetErrorString(e));
   return CABLEGPU_OK;
 }
 

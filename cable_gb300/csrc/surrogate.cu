@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -342,6 +343,7 @@ struct FwdArgs {
   float* y;            // [n][NOUT] raw outputs, may be null
   float* loss_part;    // [gridDim.x] sum of squared normalised errors, may be null
   unsigned int* err;
+  unsigned long long wait_ns;   // tensor-core wait limit (wait_limit_ns)
 };
 
 __global__ void __launch_bounds__(128, 1) mlp_forward_kernel(FwdArgs a) {
@@ -385,7 +387,7 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_kernel(FwdArgs a) {
 #pragma unroll
     for (int f = 0; f < NIN; ++f) xn[f] = valid ? (raw[f] - nrm[f]) * nrm[12 + f] : 0.f;
     float y[NOUT];
-    ok = forward128(smem, taddr, phase, xn, y);
+    ok = forward128(smem, taddr, phase, xn, y, a.wait_ns);
     if (!ok) break;
     if (valid) {
 #pragma unroll
@@ -431,6 +433,7 @@ struct InferArgs {
   const float* norm;
   float* dt;           // [ld]
   unsigned int* status;
+  unsigned long long wait_ns;   // tensor-core wait limit (wait_limit_ns)
 };
 
 __global__ void __launch_bounds__(128, 1) mlp_infer_soa_kernel(InferArgs a) {
@@ -504,7 +507,7 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_soa_kernel(InferArgs a) {
       for (int q = 0; q < NIN; ++q) xn[q] = 0.f;
     }
     fetch(c + gridDim.x, w, iv, so);
-    ok = forward128(smem, taddr, phase, xn, y);
+    ok = forward128(smem, taddr, phase, xn, y, a.wait_ns);
     if (!ok) break;
     if (valid) a.dt[t] = y[2] * nrm[29] + nrm[26];
   }
@@ -659,11 +662,20 @@ void sur_free(SurNet& n) {
   n = SurNet();
 }
 
+unsigned long long cg::sur::wait_limit_ns() {
+  const char* v = std::getenv("CABLEGPU_DEBUG_TC_WAIT_NS");
+  if (!v || !*v) return tc::kWaitNs;
+  char* end = nullptr;
+  const unsigned long long x = std::strtoull(v, &end, 10);
+  return (end && *end == 0) ? std::min(x, (unsigned long long)tc::kWaitNs) : tc::kWaitNs;
+}
+
 int sur_infer(const SurNet& n, const float* work_a, const uint8_t* iveg, const uint8_t* isoilm, const CgTables* tables,
               int medlyn, int mp, int ld, float* dt, unsigned int* status, cudaStream_t st, std::string& err) {
   InferArgs a;
   a.work_a = work_a; a.iveg = iveg; a.isoilm = isoilm; a.tables = tables; a.medlyn = medlyn; a.mp = mp; a.ld = ld; a.packed = n.packed; a.params = n.params; a.norm = n.norm; a.dt = dt;
   a.status = status;
+  a.wait_ns = wait_limit_ns();
   const int chunks = (mp + 127) / 128;
   const int grid = std::max(1, std::min(chunks, 8 * n.nblk));
   mlp_infer_soa_kernel<<<grid, 128, FW_SMEM, st>>>(a);
@@ -720,6 +732,7 @@ int sur_eval(SurNet& n, const float* d_rows, long long nrows, float* y_dev, doub
   FwdArgs f;
   f.rows = d_rows; f.n = nrows; f.packed = n.packed; f.params = n.params; f.norm = n.norm; f.y = y_dev;
   f.loss_part = n.loss_part; f.err = n.err;
+  f.wait_ns = wait_limit_ns();
   mlp_forward_kernel<<<n.nblk, 128, FW_SMEM, st>>>(f);
   SUR_CUDA(cudaGetLastError());
   std::vector<float> lp(n.nblk);

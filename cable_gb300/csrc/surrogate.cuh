@@ -65,10 +65,11 @@ constexpr uint32_t FW_TMEM_COLS = 64;      // D1, D2, D3 in turn at column 0
 // of the calling CTA (thread i = row i = tensor-memory lane i).  xn: this
 // thread's 12 normalised inputs; y: its 3 normalised outputs.  Every thread
 // of the CTA must call it (it synchronises the CTA).  Returns false if a
-// tensor-core completion did not arrive within the wait limit, in which case
-// the outputs are unusable: the caller must not call it again in this
-// kernel, and must call settle() before freeing the tensor memory.
-__device__ __forceinline__ bool forward128(uint8_t* smem, uint32_t taddr, uint32_t& phase, const float* xn, float* y) {
+// tensor-core completion did not arrive within wait_ns, in which case the
+// outputs are unusable: the caller must not call it again in this kernel,
+// and must call settle() before freeing the tensor memory.
+__device__ __forceinline__ bool forward128(uint8_t* smem, uint32_t taddr, uint32_t& phase, const float* xn, float* y,
+                                           uint64_t wait_ns = tc::kWaitNs) {
   using namespace tc;
   const int s = threadIdx.x;
   const uint32_t lane = taddr + ((uint32_t)(s & ~31) << 16);
@@ -98,7 +99,7 @@ __device__ __forceinline__ bool forward128(uint8_t* smem, uint32_t taddr, uint32
              idesc_bf16(128, 64), 0);
     mma_commit(bar);
   }
-  ok = mbar_wait(bar, phase);
+  ok = mbar_wait(bar, phase, wait_ns);
   phase ^= 1u;
   if (__syncthreads_or(!ok)) return false;
   fence_after_sync();
@@ -125,7 +126,7 @@ __device__ __forceinline__ bool forward128(uint8_t* smem, uint32_t taddr, uint32
                idesc_bf16(128, 64), j > 0);
     mma_commit(bar);
   }
-  ok = mbar_wait(bar, phase);
+  ok = mbar_wait(bar, phase, wait_ns);
   phase ^= 1u;
   if (__syncthreads_or(!ok)) return false;
   fence_after_sync();
@@ -152,7 +153,7 @@ __device__ __forceinline__ bool forward128(uint8_t* smem, uint32_t taddr, uint32
                idesc_bf16(128, NOUTP), j > 0);
     mma_commit(bar);
   }
-  ok = mbar_wait(bar, phase);
+  ok = mbar_wait(bar, phase, wait_ns);
   phase ^= 1u;
   if (__syncthreads_or(!ok)) return false;
   fence_after_sync();
@@ -169,11 +170,18 @@ __device__ __forceinline__ bool forward128(uint8_t* smem, uint32_t taddr, uint32
   return true;
 }
 
-// After a failed wait: waits once more (bounded) for the tensor-core pass
-// that did not report, so the tensor memory it writes can be freed.
+// After a failed wait: waits once more for the tensor-core pass that did not
+// report, so the tensor memory it writes can be freed.  Always with the
+// default limit (never the caller's debug limit): the pass was issued and
+// completes in microseconds, and the memory must not be freed under it.
 __device__ __forceinline__ void settle(uint8_t* smem, uint32_t phase) {
-  tc::mbar_wait(reinterpret_cast<uint64_t*>(smem + FW_BAR), phase ^ 1u);
+  tc::mbar_wait(reinterpret_cast<uint64_t*>(smem + FW_BAR), phase ^ 1u, tc::kWaitNs);
 }
+
+// Wait limit (ns) the host passes to the network kernels: the default, or
+// the value of the environment variable CABLEGPU_DEBUG_TC_WAIT_NS read at
+// each launch (0 makes every first wait give up, to test the fallback).
+unsigned long long wait_limit_ns();
 
 }  // namespace sur
 }  // namespace cg

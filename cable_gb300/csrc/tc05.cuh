@@ -56,10 +56,15 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
   asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
   return t;
 }
+// Default wait limit: 0.2 s of wall time (a tensor-core pass completes in
+// microseconds).
+constexpr uint64_t kWaitNs = 200000000ull;
 // Waits for the phase with parity `parity` to complete.  Gives up and
-// returns false after max_ns nanoseconds of wall time (a tensor-core pass
-// completes in microseconds), so no caller can wait forever.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t max_ns = 200000000ull) {
+// returns false after max_ns nanoseconds of wall time, so no caller can wait
+// forever.  max_ns == 0 gives up at once without polling: the debug setting
+// that exercises the callers' give-up path deterministically.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t max_ns = kWaitNs) {
+  if (max_ns == 0) return false;
   const uint32_t addr = smem_u32(bar);
   const uint64_t t0 = globaltimer_ns();
   while (true) {

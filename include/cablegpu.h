@@ -107,7 +107,10 @@ int cablegpu_cold_start(cablegpu_ctx* ctx, const double* snowd0, const double* t
  * the staging array is shared by all contexts on a device, so calls must not
  * overlap (from any thread); the call returns after its kernel ran.  The
  * first call on a device resolves the array's address and may load the
- * library's device code, so make it before any stream capture begins. */
+ * library's device code, so make it before any stream capture begins.  The
+ * address is kept for the life of the process: a cudaDeviceReset of that
+ * device invalidates it, so do not use this entry point on a device after
+ * resetting it (cablegpu_cold_start has no such restriction). */
 #define CABLEGPU_NOALLOC_MAX_TILES 65536
 int cablegpu_cold_start_noalloc(cablegpu_ctx* ctx, const double* snowd0, const double* tgg0, const double* wb0);
 
@@ -401,6 +404,16 @@ int cablegpu_param_table(int table, const char* name, float* out, int n);
  * air temperature (K).  Targets (columns 12-14): stomatal conductance to
  * water (mol/m2/s), net assimilation (mol/m2/s), leaf temperature change
  * over the iteration (K).  Column 15 is unused. */
+
+/* Failure handling: the network kernels wait on the tensor cores with a
+ * bounded wait (0.2 s of wall time).  A wait that gives up makes the kernel
+ * wait once more (bounded) for the pass it issued, free its tensor memory
+ * and return; in a step, every tile then runs the plain dryLeaf iteration
+ * and cablegpu_synchronize returns CABLEGPU_ERR_CUDA, and the context-free
+ * calls below return CABLEGPU_ERR_CUDA.  Debugging aid: the environment
+ * variable CABLEGPU_DEBUG_TC_WAIT_NS, read at each network-kernel launch,
+ * lowers the limit of the first waits (0: give up at once without
+ * polling), to exercise that path; the final wait keeps its full limit. */
 
 /* Runs nsteps plain steps that also append one training row for each
  * sampled (vegetated tile, Monin-Obukhov iteration), sampled with

@@ -23,9 +23,15 @@ STATE_FIELDS = ["wb", "wbice", "tgg", "tggsn", "ssdn", "smass", "sdepth", "snowd
                 "owetfac", "rtsoil", "tss", "cansto", "cplant", "csoil", "owb", "ebal_tot", "wbal_tot"]
 
 # Tolerances of the spec: fluxes 1e-3 relative with a 1 W/m2 floor,
-# temperatures 0.01 K, soil moisture 1e-5 m3/m3.
+# temperatures 0.01 K, soil moisture 1e-5 m3/m3.  The carbon fluxes (gross
+# primary production fgpp = -fpn + frday, cbl_model_driver_offline.F90:224;
+# net photosynthesis fpn and leaf respiration frday, cbl_dryLeaf.F90:659-661)
+# are fluxes too, in g C/m2/s: 1e-3 relative with a floor of 1e-7 g C/m2/s
+# (0.008 umol CO2/m2/s, 0.03 % of a midday canopy GPP of 3.7e-4).
 FLUX_FIELDS = {"fe_d", "fh_d", "fev", "fhv", "fhs", "fns", "fnv", "ga_d", "rnet_d", "fes", "fevc", "fevw", "swnet",
                "lwnet", "qssabs", "rniso"}
+CARBON_FLUX_FIELDS = {"fgpp_d", "fpn", "frday_d", "fgpp", "frday"}
+CARBON_FLUX_FLOOR = 1e-7
 TEMP_FIELDS = {"tv_d", "trad_d", "tgg", "tggsn", "tss", "tvair"}
 MOIST_FIELDS = {"wb", "wbice"}
 
@@ -34,6 +40,8 @@ def tolerance(name, ref):
     ref = np.abs(np.asarray(ref, np.float64))
     if name in FLUX_FIELDS:
         return np.maximum(1e-3 * ref, 1.0)
+    if name in CARBON_FLUX_FIELDS:
+        return np.maximum(1e-3 * ref, CARBON_FLUX_FLOOR)
     if name in TEMP_FIELDS:
         return np.full(ref.shape, 0.01)
     if name in MOIST_FIELDS:

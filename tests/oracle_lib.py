@@ -14,20 +14,28 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 LIB_PATH = os.path.join(ORACLE_DIR, "libcbmref.so")
+# the CPU-baseline build (FMA contraction, unrolling): timed by bench.py,
+# never used as the parity checker
+TIMING_LIB_PATH = os.path.join(ORACLE_DIR, "libcbmref_timing.so")
 
-_lib = None
+_libs = {}
+# which build init_state / run / run_calls / forcing use: False the parity
+# build, True the timing build (bench.py's CPU legs set it)
+TIMING = False
 
 
 def build():
     subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
 
 
-def lib():
-    global _lib
+def lib(timing=None):
+    timing = TIMING if timing is None else timing
+    path = TIMING_LIB_PATH if timing else LIB_PATH
+    _lib = _libs.get(path)
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
+        if not os.path.exists(path):
             build()
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(path)
         dp, ip, fp = C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_float)
         L.cbmref_state_field_name.restype = C.c_char_p
         L.cbmref_diag_name.restype = C.c_char_p
@@ -53,7 +61,7 @@ def lib():
         L.cbmref_soil_value.argtypes = [C.c_char_p, C.c_int]
         L.cbmref_params.argtypes = [C.c_int, C.c_int, dp, dp, dp, dp]
         L.cbmref_soil_thermal_fix.argtypes = [C.c_int, dp, dp, dp, dp]
-        _lib = L
+        _libs[path] = _lib = L
     return _lib
 
 

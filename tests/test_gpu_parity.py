@@ -14,7 +14,10 @@ from cable_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
 
-FIELDS = ["fe_d", "fh_d", "ga_d", "rnet_d", "fes", "fevc", "tv_d", "trad_d", "tgg", "tggsn", "wb", "wbice"]
+# the benchmark spec's outputs (latent and sensible heat, GPP, canopy and soil
+# temperature, soil moisture) and the fluxes that make them up
+FIELDS = ["fe_d", "fh_d", "ga_d", "rnet_d", "fes", "fevc", "tv_d", "trad_d", "tgg", "tggsn", "wb", "wbice",
+          "fgpp_d", "fpn", "frday_d"]
 
 
 @pytest.fixture(scope="module")
@@ -59,6 +62,41 @@ def test_gridded_parity_matches_reference_precision_noise(oracle, runtime, name)
     assert np.abs(gd["ebal"]).max() < 0.05
     assert np.array_equal(gs["flags"][0] & 1, os_["isflag"][0].astype(np.int32)) or \
         np.mean((gs["flags"][0] & 1) == os_["isflag"][0]) > 0.999
+
+
+def test_plain_kernels_equal_the_diagnostics_kernels(runtime):
+    """The benchmarked instantiations (diagnostics off) compute bitwise the
+    outputs and state of the diagnostics instantiations that the per-step
+    flux comparisons run: every output row every step, and the state after
+    24 steps, stepped directly and replayed as CUDA graphs."""
+    R = runtime
+    ts = W.snow_grid(20000, nsteps=24)
+    names = [n for n, v in R.fields().items() if v[3] == R.KIND_STATE] + ["tile_status"]
+    runs = []
+    for diag in (False, True):
+        g = R.from_tileset(ts, order=2)
+        g.set_options(diag=diag)
+        outs = []
+        for n in range(24):
+            g.step(1 + n, ts.dels)
+            outs.append(g.get("out"))
+        runs.append((outs, {k: g.get(k) for k in names}))
+        g.close()
+    g = R.from_tileset(ts, order=2)
+    g.run(1, 24, ts.dels)
+    g.synchronize()
+    graph = {k: g.get(k) for k in names}
+    g.close()
+    (o0, s0), (o1, s1) = runs
+    for n in range(24):
+        np.testing.assert_array_equal(o0[n], o1[n], err_msg="out, step %d" % (n + 1))
+    for k in names:
+        if k == "tile_status":   # the dryLeaf bits are recorded by the diagnostics kernel only
+            np.testing.assert_array_equal(s0[k] & ~(R.TILE_DRYLEAF_NOCONV | R.TILE_EVAPFBL),
+                                          s1[k] & ~(R.TILE_DRYLEAF_NOCONV | R.TILE_EVAPFBL), err_msg=k)
+            continue
+        np.testing.assert_array_equal(s0[k], s1[k], err_msg=k)
+        np.testing.assert_array_equal(s0[k], graph[k], err_msg="graph " + k)
 
 
 def test_host_forcing_path_matches_synthetic(runtime):
@@ -360,7 +398,7 @@ def test_science_switches_match_oracle(oracle, runtime, which):
     os32 = oracle.split_state(st32)
     ref = H.parity_report({k: os32[k] for k in H.STATE_FIELDS}, {gk: od32[ok] for gk, ok in H.DIAG_MAP.items()},
                           os_, od)
-    for k in ("tgg", "tggsn", "wb", "wbice", "ga_d", "fe_d", "fh_d", "tv_d", "fes"):
+    for k in ("tgg", "tggsn", "wb", "wbice", "ga_d", "fe_d", "fh_d", "tv_d", "fes", "fgpp_d", "frday_d"):
         assert rep[k]["rms"] <= max(rep[k]["tol"], 3 * ref[k]["rms"]), (k, rep[k], ref[k])
         assert rep[k]["frac_within"] >= min(0.995, ref[k]["frac_within"] - 0.005), (k, rep[k], ref[k])
     assert np.abs(gd["ebal"]).max() < 0.05
@@ -448,3 +486,25 @@ def test_host_layout_in_device_order_matches_caller_order(oracle, runtime):
         np.testing.assert_array_equal(o1[k], o0[k], err_msg="step %d" % k)
     for k in s0:
         np.testing.assert_array_equal(s1[k], s0[k], err_msg=k)
+
+
+def test_config2_full_size_against_fp64_oracle(runtime):
+    """The gridded workload at its full size, 1,000,000 tiles x 48 steps, on
+    the benchmarked kernels (diagnostics off), against the FP64 oracle on the
+    GPU's own forcing, every output every step and the soil profiles at the
+    end: each field's RMS error within its tolerance or within the
+    reference's own FP32/FP64 noise on the same inputs, and its fraction of
+    tile-steps within tolerance no lower than that noise's."""
+    import parity_full as P
+    rep = P.config2_report(mp=1_000_000, nsteps=48)
+    bad = []
+    for k, r in rep["fields"].items():
+        g, m = r["gpu"], r["precision_mix"]
+        assert "nonfinite" not in g, (k, g)
+        if r["tol"] is None:
+            continue
+        if not g["rms"] <= max(r["tol"], 1.5 * m["rms"]):
+            bad.append((k, "rms", g, m))
+        if not g["frac_within"] >= m["frac_within"] - 1e-3:
+            bad.append((k, "within", g, m))
+    assert not bad, bad

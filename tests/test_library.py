@@ -28,6 +28,23 @@ def test_library_builds_and_exports_every_declared_symbol():
     assert set(syms) == set(R.EXPORTS)   # the Python binding lists exactly the declared entry points
 
 
+def test_binding_constants_match_the_header():
+    """Values the Python binding copies from include/cablegpu.h: a change to
+    the header must not leave the binding (and the tests built on it)
+    checking a stale value."""
+    txt = open(HEADER).read()
+    defs = dict(re.findall(r"#define\s+(CABLEGPU_\w+)\s+\(?(-?\d+)\)?", txt))
+    assert int(defs["CABLEGPU_NOALLOC_MAX_TILES"]) == R.NOALLOC_MAX_TILES
+    assert int(defs["CABLEGPU_NFORCING"]) == R.NFORCING
+    for name in ("MEDLYN", "SOIL_THERMAL_FIX", "LITTER", "L_REV_CORR", "FWSOIL_NONLINEAR", "FWSOIL_LAI_KTAUL",
+                 "POTEV_PM", "NEW_REDUCE_SOILEVP", "NEW_RUNOFF_SPEED", "DIAG_SOIL_RESP_OFF"):
+        assert int(defs["CABLEGPU_SW_" + name]) == getattr(R, "SW_" + name), name
+    for name in ("NONFINITE", "DRYLEAF_NOCONV", "FORCING_RANGE", "OUTPUT_RANGE", "EVAPFBL"):
+        assert int(defs["CABLEGPU_TILE_" + name]) == getattr(R, "TILE_" + name), name
+    for code, name in R.ERRORS.items():
+        assert int(defs[name]) == code, name
+
+
 def test_field_registry_is_consistent():
     f = R.fields()
     assert len(f) == R.load().cablegpu_num_fields()

@@ -103,3 +103,44 @@ def test_strict_surrogate_error_against_fp64(oracle, trained):
     e_tv = np.sqrt(np.mean((d_sur["tv_d"] - od["tv"]) ** 2))
     assert e_le <= 2.0, e_le
     assert e_tv <= 0.05, e_tv
+
+
+def test_tensor_core_give_up_falls_back_and_is_reported(trained, monkeypatch):
+    """The network kernels' bounded tensor-core waits.  With the debug wait
+    limit CABLEGPU_DEBUG_TC_WAIT_NS=0 every first wait gives up at once: the
+    inference kernel then waits, with its full limit, for the pass it issued,
+    frees its tensor memory, marks every tile "no prediction" and flags the
+    failure.  The canopy kernel runs the plain iteration (the step is bitwise
+    the plain kernel's), cablegpu_synchronize reports the failure, and the
+    context-free forward pass returns an error.  With the limit restored the
+    next step uses the network again, so the tensor memory was freed."""
+    from cable_gb300 import runtime as R
+    rows, _, params, norm = trained
+    ts = W.snow_grid(8000, seed=81, nsteps=2)
+    plain = R.from_tileset(ts)
+    plain.step(1)
+    plain.synchronize()
+    ref = {k: plain.get(k) for k in ("out", "wb", "tgg", "tggsn", "snowd", "cansto", "rtsoil")}
+    plain.close()
+    g = R.from_tileset(ts)
+    g.surrogate_weights(params, norm)
+    g.set_surrogate(1, 0.1)
+    g.surrogate_stats(reset=True)
+    monkeypatch.setenv("CABLEGPU_DEBUG_TC_WAIT_NS", "0")
+    g.step(1)
+    with pytest.raises(R.CableGPUError) as e:
+        g.synchronize()
+    assert e.value.code == -2 and "surrogate" in str(e.value), e.value
+    assert g.surrogate_stats(reset=True)[0] == 0          # no tile started from a prediction
+    for k, v in ref.items():
+        np.testing.assert_array_equal(g.get(k), v, err_msg=k)
+    with pytest.raises(R.CableGPUError):
+        R.mlp_forward(params, norm, rows[:4096])
+    monkeypatch.delenv("CABLEGPU_DEBUG_TC_WAIT_NS")
+    g.step(2)
+    g.synchronize()
+    tried, _ = g.surrogate_stats(reset=True)
+    assert tried > 0
+    y = R.mlp_forward(params, norm, rows[:4096])
+    assert np.all(np.isfinite(y))
+    g.close()
