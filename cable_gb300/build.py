@@ -22,7 +22,8 @@ SOURCES = ["cablegpu.cu", "phase_a.cu", "phase_b.cu", "phase_c1.cu", "phase_c2.c
 # FP64, and the correction-form solves are insensitive to ulp-level
 # coefficient errors); the snow pack keeps IEEE division, since its layering
 # thresholds turn ulp differences into branch flips more often than the
-# reference's own FP32 build does.  CG_MAXNREG caps registers per thread,
+# reference's own FP32 build does.  CG_MAXNREG caps registers per thread
+# (CG_MAXNREG_S64: of the soil kernels' FP64-solve instantiations),
 # chosen per kernel from measured step times at 4M tiles (radiation 80, soil
 # heat 80, canopy 72, soil water 112, snow pack 128), trading a few hundred
 # bytes of spills for occupancy; the
@@ -31,8 +32,8 @@ EXTRA_FLAGS = {
     "phase_a.cu": ["-prec-div=false", "-DCG_MAXNREG=80"],
     "phase_b.cu": ["--use_fast_math", "-DCG_MAXNREG=72"],
     "phase_c1.cu": ["-DCG_MAXNREG=128"],
-    "phase_c2.cu": ["-prec-div=false", "-DCG_MAXNREG=80"],
-    "phase_c3.cu": ["-prec-div=false", "-DCG_MAXNREG=112"],
+    "phase_c2.cu": ["-prec-div=false", "-DCG_MAXNREG=80", "-DCG_MAXNREG_S64=128"],
+    "phase_c3.cu": ["-prec-div=false", "-DCG_MAXNREG=112", "-DCG_MAXNREG_S64=128"],
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

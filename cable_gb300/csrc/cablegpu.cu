@@ -221,10 +221,11 @@ struct cablegpu_ctx {
   CgForcingSpec forc{12345ull, 1, 1800.f};
   int medlyn = 0, diag = 0, capture_forcing = 0, thermal_fix = 0, litter = 0, rev_corr = 0;
   int switches = 0;                // the CABLEGPU_SW_* mask the fields above come from
+  int solve64 = 1;                 // soil Thomas solves: 1 FP64 direct form (default), 0 FP32 on the change
   int host_layout = 0;             // host buffers of step_host / forcing files: 0 caller order, 1 device order
   cudaGraphExec_t graph = nullptr;
   float graph_dels = -1.f;
-  int graph_diag = -1, graph_switches = -1, graph_hostforc = -1, graph_capture = -1;
+  int graph_diag = -1, graph_switches = -1, graph_hostforc = -1, graph_capture = -1, graph_solve64 = -1;
   unsigned long long graph_seed = 0;
   int graph_doy0 = -1;
   long long launches = 0;
@@ -380,6 +381,7 @@ StepParams make_params(cablegpu_ctx* c, int ktau, float dels) {
   p.mode = 0;
   p.final_cycle = 1;
   p.lai_refresh = 0;
+  p.solve64 = c->solve64;
   return p;
 }
 
@@ -387,7 +389,8 @@ int ensure_graph(cablegpu_ctx* c, float dels) {
   if (c->graph && c->graph_dels == dels && c->graph_diag == c->diag && c->graph_switches == c->switches &&
       c->graph_hostforc == (int)c->host_forcing && c->graph_capture == c->capture_forcing &&
       c->graph_seed == c->forc.seed && c->graph_doy0 == c->forc.doy0 && c->graph_sur == c->sur_enabled &&
-      c->graph_gate == c->sur_gate && std::equal(c->block, c->block + 5, c->graph_block))
+      c->graph_gate == c->sur_gate && c->graph_solve64 == c->solve64 &&
+      std::equal(c->block, c->block + 5, c->graph_block))
     return CABLEGPU_OK;
   if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   StepParams p = make_params(c, 0, dels);
@@ -406,7 +409,7 @@ int ensure_graph(cablegpu_ctx* c, float dels) {
   c->graph_dels = dels; c->graph_diag = c->diag; c->graph_switches = c->switches;
   c->graph_hostforc = (int)c->host_forcing; c->graph_capture = c->capture_forcing;
   c->graph_seed = c->forc.seed; c->graph_doy0 = c->forc.doy0;
-  c->graph_sur = c->sur_enabled; c->graph_gate = c->sur_gate;
+  c->graph_sur = c->sur_enabled; c->graph_gate = c->sur_gate; c->graph_solve64 = c->solve64;
   std::copy(c->block, c->block + 5, c->graph_block);
   return CABLEGPU_OK;
 }
@@ -678,6 +681,14 @@ int cablegpu_set_synthetic_forcing(cablegpu_ctx* c, unsigned long long seed, int
   c->host_forcing = false;
   c->forc.seed = seed;
   c->forc.doy0 = doy0;
+  return CABLEGPU_OK;
+}
+
+int cablegpu_set_soil_solve(cablegpu_ctx* c, int mode) {
+  if (!c) return CABLEGPU_ERR_ARG;
+  if (mode != CABLEGPU_SOLVE_FP64 && mode != CABLEGPU_SOLVE_FP32_CHANGE)
+    return fail(c, CABLEGPU_ERR_ARG, "set_soil_solve: unknown mode");
+  c->solve64 = mode == CABLEGPU_SOLVE_FP64 ? 1 : 0;
   return CABLEGPU_OK;
 }
 

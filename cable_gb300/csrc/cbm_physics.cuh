@@ -7,11 +7,14 @@
 //
 // Precision policy (GB300: FP64 runs at a small fraction of the FP32 rate):
 //   * FP32 for radiation, canopy energy balance, photosynthesis, snow, soil
-//     fluxes and carbon;
-//   * FP64 storage for soil water / ice (ssnow%wb, ssnow%wbice) and the layer-1
-//     heat capacity, with water increments accumulated in FP64;
-//   * FP64 for the two tridiagonal (Thomas) solves of soil heat and soil
-//     moisture and for the energy / water balance accumulators.
+//     fluxes, the coefficients of the soil systems, and carbon;
+//   * FP64-class storage for soil water / ice (ssnow%wb, ssnow%wbice:
+//     double-FP32 pairs, a 48-bit significand) and FP64 for the layer-1 heat
+//     capacity;
+//   * the two tridiagonal (Thomas) solves of soil heat and soil moisture in
+//     FP64 on the reference's direct form (trimb64, the default), or in FP32
+//     on the step's change (trid_correction, selectable); FP64 for the
+//     energy / water balance accumulators.
 //
 // Switch set: the reference offline defaults (cable.nml): soil_struc
 // 'default', fwsoil 'standard', ssnow_potev 'HDM', gs_switch 'leuning'
@@ -277,6 +280,40 @@ __device__ __forceinline__ float xejmxt3(float x) {
   float num = 1.16715f * expf((50300.0f / (RGAS * TREFK)) * (1.f - TREFK / x));
   float den = 1.0f + expf((495.0f * x - 152044.0f) / (RGAS * x));
   return fmaxf(0.0f, num / den);
+}
+
+// cbl_trimb.F90:17-53 in FP64, as the reference solves both soil systems,
+// for their diffusion form: the Thomas algorithm on
+//   a(k) u(k-1) + b(k) u(k) + c(k) u(k+1) = rhs(k),  b(k) = 1 - a(k) - c(k)
+// (cbl_stempv.F90:100-124, cbl_smoisturev.F90:256), plus db0 on the first
+// row (the surface coupling of the heat system, cbl_stempv.F90:129, :197).
+// The off-diagonals come as FP32 coefficients and are widened exactly; the
+// diagonal, the right-hand side and the elimination are FP64.  rhs is
+// replaced by the solution.  The reference's steps: e(1) = c(1)/b(1),
+// g(1) = rhs(1)/b(1); temp(k) = 1/(b(k) - a(k) e(k-1)), e(k) = c(k) temp(k),
+// g(k) = (rhs(k) - a(k) g(k-1)) temp(k) for k = 2..N-1; the last row
+// divided by its own pivot; back substitution.  Row 1's two divisions by
+// b(1) are one reciprocal here (the same value to an FP64 ulp), and g(k)
+// overwrites rhs(k), so only e and the solution are live in FP64.
+template <int N>
+__device__ __forceinline__ void trimb64(const float* a, const float* c, double db0, double* rhs) {
+  double e[N - 1];
+  const double ib = 1.0 / ((1.0 - (double)a[0] - (double)c[0]) + db0);
+  e[0] = (double)c[0] * ib;
+  rhs[0] = rhs[0] * ib;
+#pragma unroll
+  for (int k = 1; k < N - 1; ++k) {
+    const double ak = a[k], ck = c[k];
+    const double temp = 1.0 / ((1.0 - ak - ck) - ak * e[k - 1]);
+    e[k] = ck * temp;
+    rhs[k] = (rhs[k] - ak * rhs[k - 1]) * temp;
+  }
+  {
+    const double ak = a[N - 1], ck = c[N - 1];
+    rhs[N - 1] = (rhs[N - 1] - ak * rhs[N - 2]) / ((1.0 - ak - ck) - ak * e[N - 2]);
+  }
+#pragma unroll
+  for (int k = N - 2; k >= 0; --k) rhs[k] = rhs[k] - e[k] * rhs[k + 1];
 }
 
 // Tridiagonal solve in correction form (the elimination of cbl_trimb.F90:17-53

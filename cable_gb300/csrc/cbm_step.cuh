@@ -1,11 +1,16 @@
-// The cbm() timestep as three kernels per step, one thread per tile in each:
-//   phase A  ruff_resist, define_air, masks, init_radiation, albedo,
-//            Surf_wetness_fact, radiation
-//   phase B  define_canopy: 4 Monin-Obukhov iterations of dryLeaf / wetLeaf /
-//            within-canopy / soil evaporation, screen diagnostics, canopy
-//            water budget, soil-coupling derivatives, energy balance
-//   phase C  soil_snow (snow layering, FP64 heat and moisture solves),
-//            snow_aging, carbon, water balance
+// The cbm() timestep as five kernels per step, one thread per tile in each:
+//   phase A   ruff_resist, define_air, masks, init_radiation, albedo,
+//             Surf_wetness_fact, radiation
+//   phase B   define_canopy: 4 Monin-Obukhov iterations of dryLeaf / wetLeaf /
+//             within-canopy / soil evaporation, screen diagnostics, canopy
+//             water budget, soil-coupling derivatives, energy balance
+//   phase C1  soil_snow's snow pack: snowcheck, density, accumulation, melt,
+//             layer adjustment
+//   phase C2  soil heat: the stempv tridiagonal solve (FP64 on the direct
+//             form by default, or FP32 on the step's change), melt,
+//             remove_trans, soilfreeze
+//   phase C3  soil water: the smoisturev tridiagonal solve (likewise),
+//             surfbv, snow_aging, carbon, water balance
 // Splitting keeps each kernel's code and register footprint small enough
 // for the instruction cache and for several resident warps per scheduler;
 // the phases hand over per-tile records through HBM (structure of arrays).
@@ -33,6 +38,8 @@ struct StepParams {
   // wetness factor and surface temperature are left as they were), 2 cbm_impl
   int mode;
   int final_cycle;   // cbm_impl: 1 on the last implicit cycle of the step (cycleno == numcycles)
+  int solve64;       // 1: the soil heat and moisture Thomas solves in FP64 on the
+                     // reference's direct form; 0: in FP32 on the step's change
   int lai_refresh;   // cbm_expl: the host model's radiation call ran, so the
                      // snow-reduced LAI is recomputed rather than carried
 };
@@ -768,10 +775,13 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
           fe_mm_best = fe_mm_last;
           tlfy = tlfx;   // damping below is a no-op for k == 1
         }
-        // damping once k > 5 (:584-590)
+        // damping once k > 5 (:584-590).  Written with explicitly rounded
+        // operations: a*b + c*d leaves the compiler a choice of which product
+        // to fuse, and that choice may differ between instantiations of the
+        // kernel (diagnostics on or off), which must give identical results.
         if (abs_deltlf > conv) {
           float fac = 0.5f * ((float)max(0, k - 5) / ((float)k - 4.9999f));
-          tlfx = fac * tlfxx + (1.0f - fac) * tlfx;
+          tlfx = __fmaf_rn(fac, tlfxx, __fmul_rn(1.0f - fac, tlfx));
         }
         if (kSur && sur_try && k == 1) {
           if (abs_deltlf <= conv) {
@@ -1464,7 +1474,10 @@ static __device__ __noinline__ float cg_snow_melting(CgSnowPack& p, int isflag, 
   return snowmlt;
 }
 
-template <bool kDiag, bool kCoupled = false>
+// kS64: the heat solve in FP64 on the reference's direct form (trimb64, as
+// cbl_stempv.F90:201-214 calls cbl_trimb.F90); otherwise in FP32 on the
+// step's change (trid_correction).
+template <bool kDiag, bool kCoupled = false, bool kS64 = true>
 __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
   // the coupled-call code exists only in the kCoupled instantiation
   const int mode = kCoupled ? P.mode : 0;
@@ -1612,42 +1625,58 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
     for (int k = 0; k < CG_MS; ++k)
       gf[k] = fmaxf(hcll, (1.0f - ssat) * css * rhosoil + ssat * (wblf[k] * CSWAT * DLIQ + wbfice[k] * CSICE * DICE)) * zse[k];
     if (isflag == 0) gf[0] = gf[0] + CGSNOW * snowd;
-    // Implicit heat conduction (cbl_stempv.F90:98-217) solved for the
-    // temperature change of the step (trid_correction).  Row k of the
+    // Implicit heat conduction (cbl_stempv.F90:98-217).  Row k of the
     // reference's system is a_k T_{k-1} + b_k T_k + c_k T_{k+1} = rhs_k with
     // b_k = 1 - a_k - c_k, minus dgdtg * dtg on the surface row, and rhs the
     // old temperatures after the explicit surface update
-    // T_1 + (ga - T_1 dgdtg) dtg (:129-131, :201-204).  Subtracting A T_old
-    // leaves ga * dtg on the surface row and -a_k (T_{k-1} - T_k)
-    // - c_k (T_{k+1} - T_k) everywhere: the surface-coupling terms in dgdtg
-    // cancel exactly.
+    // T_1 + (ga - T_1 dgdtg) dtg (:129-131, :201-204).
+    //   kS64: that system in FP64 (coefficients formed in FP32 and widened,
+    //   b and the elimination in FP64), the explicit update in FP32 as the
+    //   reference's REAL arithmetic, the solution rounded to the FP32 state.
+    //   Otherwise: solved for the temperature change of the step
+    //   (trid_correction).  Subtracting A T_old leaves ga * dtg on the
+    //   surface row and -a_k (T_{k-1} - T_k) - c_k (T_{k+1} - T_k)
+    //   everywhere: the surface-coupling terms in dgdtg cancel exactly.
     if (isflag == 0) {
       // soil-only system: the snow rows of the reference's 9-row system are
       // identity rows decoupled from the soil (coeff(1) = 0), so the 6-row
       // solve gives the same soil temperatures
-      float a[CG_MS], b[CG_MS], c[CG_MS], r[CG_MS];
+      float a[CG_MS], c[CG_MS];
+      const float dtg0 = dels / gf[0];
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k) {
         const float dtg = dels / gf[k];
         a[k] = -dtg * coeff[k];
         c[k] = -dtg * coeff[k + 1];
-        b[k] = 1.0f - a[k] - c[k];
-        const float up = (k > 0) ? tgg[k - 1] - tgg[k] : 0.f;
-        const float dn = (k < CG_MS - 1) ? tgg[k + 1] - tgg[k] : 0.f;
-        r[k] = -(a[k] * up + c[k] * dn);
-        if (k == 0) {
-          b[0] = b[0] - dgdtg * dtg;
-          r[0] = r[0] + ga * dtg;
-        }
       }
-      trid_correction<CG_MS>(a, b, c, r);
+      if constexpr (kS64) {
+        double rd[CG_MS];
 #pragma unroll
-      for (int k = 0; k < CG_MS; ++k) tgg[k] = tgg[k] + r[k];
+        for (int k = 1; k < CG_MS; ++k) rd[k] = tgg[k];
+        rd[0] = (double)(tgg[0] + (ga - tgg[0] * dgdtg) * dtg0);
+        trimb64<CG_MS>(a, c, -(double)dgdtg * (double)dtg0, rd);
+#pragma unroll
+        for (int k = 0; k < CG_MS; ++k) tgg[k] = (float)rd[k];
+      } else {
+        float b[CG_MS], r[CG_MS];
+#pragma unroll
+        for (int k = 0; k < CG_MS; ++k) {
+          b[k] = 1.0f - a[k] - c[k];
+          const float up = (k > 0) ? tgg[k - 1] - tgg[k] : 0.f;
+          const float dn = (k < CG_MS - 1) ? tgg[k + 1] - tgg[k] : 0.f;
+          r[k] = -(a[k] * up + c[k] * dn);
+        }
+        b[0] = b[0] - dgdtg * dtg0;
+        r[0] = r[0] + ga * dtg0;
+        trid_correction<CG_MS>(a, b, c, r);
+#pragma unroll
+        for (int k = 0; k < CG_MS; ++k) tgg[k] = tgg[k] + r[k];
+      }
       ghflux = coefb * (tgg[0] - tgg[1]);
     } else {
       // rows 0-2 snow layers, 3-8 soil layers
       const float csnow[4] = {0.f, csn[0], csn[1], coeff[0]};   // coeff(-2..1)
-      float x[9], a[9], b[9], c[9], r[9];
+      float x[9], a[9], c[9];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         x[k] = tggsn[k];
@@ -1662,21 +1691,34 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
         a[3 + k] = -dtg * coeff[k];
         c[3 + k] = -dtg * coeff[k + 1];
       }
-#pragma unroll
-      for (int k = 0; k < 9; ++k) {
-        b[k] = 1.0f - a[k] - c[k];
-        const float up = (k > 0) ? x[k - 1] - x[k] : 0.f;
-        const float dn = (k < 8) ? x[k + 1] - x[k] : 0.f;
-        r[k] = -(a[k] * up + c[k] * dn);
-      }
       const float dtg0 = dels / (ssdn[0] * CGSNOW * sdepth[0]);
-      b[0] = b[0] - dgdtg * dtg0;
-      r[0] = r[0] + ga * dtg0;
-      trid_correction<9>(a, b, c, r);
+      if constexpr (kS64) {
+        double rd[9];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) tggsn[k] = x[k] + r[k];
+        for (int k = 1; k < 9; ++k) rd[k] = x[k];
+        rd[0] = (double)(x[0] + (ga - x[0] * dgdtg) * dtg0);
+        trimb64<9>(a, c, -(double)dgdtg * (double)dtg0, rd);
 #pragma unroll
-      for (int k = 0; k < CG_MS; ++k) tgg[k] = x[3 + k] + r[3 + k];
+        for (int k = 0; k < 3; ++k) tggsn[k] = (float)rd[k];
+#pragma unroll
+        for (int k = 0; k < CG_MS; ++k) tgg[k] = (float)rd[3 + k];
+      } else {
+        float b[9], r[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          b[k] = 1.0f - a[k] - c[k];
+          const float up = (k > 0) ? x[k - 1] - x[k] : 0.f;
+          const float dn = (k < 8) ? x[k + 1] - x[k] : 0.f;
+          r[k] = -(a[k] * up + c[k] * dn);
+        }
+        b[0] = b[0] - dgdtg * dtg0;
+        r[0] = r[0] + ga * dtg0;
+        trid_correction<9>(a, b, c, r);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) tggsn[k] = x[k] + r[k];
+#pragma unroll
+        for (int k = 0; k < CG_MS; ++k) tgg[k] = x[3 + k] + r[3 + k];
+      }
       sghflux = csn[0] * (tggsn[0] - tggsn[1]);
       ghflux = coefb * (tgg[0] - tgg[1]);
     }
@@ -1746,7 +1788,10 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
   (void)tss; (void)first_call;
 }
 
-template <bool kDiag, bool kCoupled = false>
+// kS64: the moisture solve in FP64 on the reference's direct form (trimb64
+// on wblf, as cbl_smoisturev.F90:422 calls cbl_trimb.F90); otherwise in FP32
+// on the step's change (trid_correction) with a flux-form state update.
+template <bool kDiag, bool kCoupled = false, bool kS64 = true>
 __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
   // the coupled-call code exists only in the kCoupled instantiation
   const int mode = kCoupled ? P.mode : 0;
@@ -1880,6 +1925,47 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
       wbf[k - 1] = wbf[k - 1] + dwd[k - 1];
     }
     rnof2 = dels * fluxh[CG_MS] * DLIQ;
+    if constexpr (kS64) {
+      // Implicit diffusion of the liquid fraction wblf = (wb - wbice) /
+      // (ssat - wbice) on the reference's direct form
+      // (cbl_smoisturev.F90:200-262, :422-427): the state after the explicit
+      // drainage and wblf in FP64, the matrix coefficients
+      // dtt z3 = dels / (zse (ssat - wbice)) z3 in FP32 (bulk arithmetic,
+      // widened exactly), the top layers' infiltration source and the
+      // elimination in FP64 (trimb64), then wb = wblf (ssat - wbice) + wbice
+      // in FP64, stored as double-FP32.
+      double wbid[CG_MS], satd[CG_MS], rd[CG_MS];
+      float xf[CG_MS], dtt[CG_MS];
+#pragma unroll
+      for (int k = 0; k < CG_MS; ++k) {
+        wbid[k] = df_to_double(wbice[k]);
+        const double wbd = df_to_double(wb[k]) + (double)dwd[k];
+        satd[k] = (double)ssat - wbid[k];
+        rd[k] = (wbd - wbid[k]) / satd[k];
+        xf[k] = (float)rd[k];
+        dtt[k] = dels / (zse[k] * (ssat - wbicef[k]));
+      }
+      float a[CG_MS], c[CG_MS];
+      a[0] = 0.f; c[CG_MS - 1] = 0.f;
+#pragma unroll
+      for (int k = 2; k <= CG_MS; ++k) {
+        float wbh_k = (zse[k - 1] * xf[k - 2] + zse[k - 2] * xf[k - 1]) / (zse[k - 1] + zse[k - 2]);
+        float fact = __powf(wbh_k, ibp2 - 1.f);
+        float icef = fmaxf(wbicef[k - 2] / fmaxf(0.01f, wbf[k - 2]), wbicef[k - 1] / fmaxf(0.01f, wbf[k - 1]));
+        float pwb_wbh = (hsbh * (1.f - fminf(2.f * fminf(0.1f, icef), 0.1f))) * fmaxf(pwb_min, wbh_k * fact);
+        const float z3 = pwb_wbh / ZSHH[k - 1];
+        a[k - 1] = -dtt[k - 1] * z3;
+        c[k - 2] = -dtt[k - 2] * z3;
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) rd[k] = rd[k] + (double)(dtt[k] * fwtop[k] / DLIQ);
+      trimb64<CG_MS>(a, c, 0.0, rd);
+#pragma unroll
+      for (int k = 0; k < CG_MS; ++k) {
+        wb[k] = df_from_double(rd[k] * satd[k] + wbid[k]);
+        wbf[k] = wb[k].hi;
+      }
+    } else {
     // Implicit diffusion of the liquid fraction x = (wb - wbice) /
     // (ssat - wbice) (cbl_smoisturev.F90, trimb on wblfsp), solved for the
     // change of x (trid_correction): the right-hand side is the top layers'
@@ -1944,6 +2030,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
       if (k < 3) net = net + dels * fwtop[k] / DLIQ;
       wb[k] = df_add(wb[k], net / zse[k]);
       wbf[k] = wb[k].hi;
+    }
     }
     const float dfactor = 1.0f - DICE / DLIQ;
 #pragma unroll

@@ -1,6 +1,8 @@
-// Phase C3 of the cbm() timestep kernel set -- soil water: infiltration, smoisturev (FP64 Thomas), surfbv, snow_aging, carbon, water balance.
+// Phase C3 of the cbm() timestep kernel set -- soil water: infiltration, smoisturev (Thomas solve in FP64 on the
+// reference's direct form, or in FP32 on the step's change), surfbv, snow_aging, carbon, water balance.
 #define CG_PHASE phase_c3
 #define CG_PHASE_KERNEL cbm_phase_c3_kernel
 #define CG_PHASE_LAUNCH launch_phase_c3
 #define CG_PHASE_COUPLED 1
+#define CG_PHASE_SOLVE 1
 #include "phase_kernels.cuh"

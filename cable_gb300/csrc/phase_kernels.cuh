@@ -13,6 +13,11 @@ constexpr int kPhaseBlock = 128;   // default threads per block; launches take a
 #ifndef CG_MAXNREG
 #define CG_MAXNREG 128
 #endif
+// the cap of the FP64-solve instantiations of the soil kernels (their FP64
+// elimination keeps more values live)
+#ifndef CG_MAXNREG_S64
+#define CG_MAXNREG_S64 CG_MAXNREG
+#endif
 
 // Launch one phase over D.mp tiles: a = radiation, b = canopy, c1 = snow
 // pack, c2 = soil heat, c3 = soil water, carbon and balances.  clock, when non-null, holds ktau on the device (graph replay).
@@ -43,32 +48,52 @@ void upload_canopy_pft_table(const CgPftTable& pft, cudaStream_t s);
 #ifndef CG_PHASE_COUPLED
 #define CG_PHASE_COUPLED 0
 #endif
-template <bool kDiag, bool kCoupled>
-__global__ void __maxnreg__(CG_MAXNREG)
+// CG_PHASE_SOLVE 1: the phase solves a soil tridiagonal system and has an
+// instantiation per solve precision (StepParams::solve64: FP64 on the
+// reference's direct form, or FP32 on the step's change).
+#ifndef CG_PHASE_SOLVE
+#define CG_PHASE_SOLVE 0
+#endif
+template <bool kDiag, bool kCoupled, bool kS64>
+__global__ void __maxnreg__(kS64 ? CG_MAXNREG_S64 : CG_MAXNREG)
     CG_PHASE_KERNEL(CgDev D, const CgTables* __restrict__ T, StepParams P, const int* __restrict__ clock) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= D.mp) return;
   StepParams p = P;
   if (clock) { p.ktau = clock[0]; p.step_index = clock[0] - 1; }
-#if CG_PHASE_COUPLED
+#if CG_PHASE_SOLVE
+  CG_PHASE<kDiag, kCoupled, kS64>(D, T, p, t);
+#elif CG_PHASE_COUPLED
   CG_PHASE<kDiag, kCoupled>(D, T, p, t);
 #else
   CG_PHASE<kDiag>(D, T, p, t);
 #endif
 }
 
-void CG_PHASE_LAUNCH(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
-                     const int* clock, int block) {
+template <bool kS64>
+void CG_PHASE_LAUNCH_S(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
+                       const int* clock, int block) {
   const int grid = (D.mp + block - 1) / block;
 #if CG_PHASE_COUPLED
   if (P.mode != 0) {
-    if (diag) CG_PHASE_KERNEL<true, true><<<grid, block, 0, s>>>(D, T, P, clock);
-    else CG_PHASE_KERNEL<false, true><<<grid, block, 0, s>>>(D, T, P, clock);
+    if (diag) CG_PHASE_KERNEL<true, true, kS64><<<grid, block, 0, s>>>(D, T, P, clock);
+    else CG_PHASE_KERNEL<false, true, kS64><<<grid, block, 0, s>>>(D, T, P, clock);
     return;
   }
 #endif
-  if (diag) CG_PHASE_KERNEL<true, false><<<grid, block, 0, s>>>(D, T, P, clock);
-  else CG_PHASE_KERNEL<false, false><<<grid, block, 0, s>>>(D, T, P, clock);
+  if (diag) CG_PHASE_KERNEL<true, false, kS64><<<grid, block, 0, s>>>(D, T, P, clock);
+  else CG_PHASE_KERNEL<false, false, kS64><<<grid, block, 0, s>>>(D, T, P, clock);
+}
+
+void CG_PHASE_LAUNCH(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
+                     const int* clock, int block) {
+#if CG_PHASE_SOLVE
+  if (P.solve64) {
+    CG_PHASE_LAUNCH_S<true>(diag, s, D, T, P, clock, block);
+    return;
+  }
+#endif
+  CG_PHASE_LAUNCH_S<false>(diag, s, D, T, P, clock, block);
 }
 #endif
 

@@ -186,6 +186,21 @@ int cablegpu_set_synthetic_forcing(cablegpu_ctx* ctx, unsigned long long seed, i
 #define CABLEGPU_SW_DIAG_SOIL_RESP_OFF 512
 int cablegpu_set_options(cablegpu_ctx* ctx, int switches, int diag, int capture_forcing);
 
+/* Arithmetic of the two soil tridiagonal (Thomas) solves, heat (stempv,
+ * cbl_stempv.F90:201-214) and moisture (smoisturev, cbl_smoisturev.F90:422):
+ *   CABLEGPU_SOLVE_FP64        (default) the reference's: each system in FP64
+ *                              on its direct form (cbl_trimb.F90:17-53), the
+ *                              coefficients formed in FP32
+ *   CABLEGPU_SOLVE_FP32_CHANGE the same systems solved in FP32 for the step's
+ *                              change of the state (right-hand side formed
+ *                              from differences of the old state), the soil
+ *                              water applied as interface fluxes; faster, and
+ *                              within the tolerances of the FP64 solve
+ * Applies to the steps issued after the call. */
+#define CABLEGPU_SOLVE_FP64 0
+#define CABLEGPU_SOLVE_FP32_CHANGE 1
+int cablegpu_set_soil_solve(cablegpu_ctx* ctx, int mode);
+
 /* One timestep, ktau 1-based (cbm(ktau, dels, ...) followed by the driver's
  * balance checks).  Asynchronous; errors of the step surface at the next
  * synchronising call. */

@@ -95,23 +95,25 @@ def test_gpu_matches_fixture(name):
                     continue
                 got = g.get(gn)[0].astype(np.float64)
                 if per_step:
-                    err.setdefault(j, []).append((got - ref[j]) / H.tolerance(gn, ref[j]))
+                    err.setdefault(j, []).append(got)
                     continue
                 rep = H.compare(gn, got, ref[j])
                 if rep["frac_within"] < 0.98:
                     fails.append((k, gn, rep))
     if per_step:
-        # every tile-step within tolerance, or within the reference's own
-        # precision noise on the same inputs (its REAL = FP32 build departs
-        # from FP64 by up to ~0.016 K in canopy temperature on this site when
-        # the dryLeaf iteration takes a different path); RMS within tolerance
+        # every tile-step against the fixture, held to the criterion of the
+        # gridded tests against the reference's own precision mix on the same
+        # inputs (its REAL = FP32 build departs from FP64 by up to ~0.016 K
+        # in canopy temperature on this site when the dryLeaf iteration takes
+        # a different path): out-of-tolerance count and unflipped RMS
         mix = z["diag_precision_mix"]
-        for j, e in err.items():
+        for j, got in err.items():
             gn = GPU_DIAG[names[j]]
-            e = np.abs(np.array(e))
-            noise = np.abs(mix[:, j] - z["diag"][:, j]) / np.stack([H.tolerance(gn, z["diag"][k, j]) for k in range(n)])
-            if e.max() > max(1.0, 1.25 * noise.max()) or np.sqrt(np.mean(e ** 2)) > 1.0:
-                fails.append((gn, float(e.max()), float(np.sqrt(np.mean(e ** 2))), float(noise.max())))
+            rep = H.compare(gn, np.stack(got), z["diag"][:, j])
+            noise = H.compare(gn, mix[:, j], z["diag"][:, j])
+            bad = H.noise_criterion(rep, noise)
+            if bad:
+                fails.append((gn, bad, rep, noise))
     if not per_step:
         fg = g.get("forcing")
         fc = z["forcing"][0]

@@ -128,11 +128,8 @@ def test_coupled_sequence_matches_oracle(runtime, switches, order):
     rx, ri, rstate, _ = oracle_run(ts, calls, F, 1, **switches)
     ref = report(np.stack([rx[k] for k in OUT]), np.stack([ri[k] for k in OUT]),
                  {k: rstate[k] for k in STATE}, ox, oi, ostate)
-    for k, r in rep.items():
-        if "tol" not in r:
-            continue
-        assert r["rms"] <= max(r["tol"], 3 * ref[k]["rms"]), (k, r, ref[k])
-        assert r["frac_within"] >= min(0.995, ref[k]["frac_within"] - 0.005), (k, r, ref[k])
+    bad = {k: H.noise_criterion(r, ref[k]) for k, r in rep.items() if "tol" in r}
+    assert not any(bad.values()), {k: (v, rep[k], ref[k]) for k, v in bad.items() if v}
 
 
 def test_coupled_state_contract(runtime):

@@ -1,11 +1,13 @@
 """GPU timestep against the FP64 CPU oracle on identical forcing.
 
-Tolerances (the benchmark spec): fluxes 1e-3 relative with a 1 W/m2 floor,
-temperatures 0.01 K, soil moisture 1e-5 m3/m3.  A few tiles per thousand can
-flip a branch of the iterative canopy solution in FP32 (as the reference's
-own FP32 build does against FP64), so on gridded workloads the check is the
-RMS error plus the fraction of tiles within tolerance, compared with the
-same statistics of the reference's REAL=FP32 / r_2=FP64 mix."""
+Tolerances (the benchmark spec): fluxes 1e-3 relative with a 1 W/m2 floor
+(carbon fluxes: a 1e-7 g C/m2/s floor), temperatures 0.01 K, soil moisture
+1e-5 m3/m3.  A few tiles per thousand can flip a branch of the iterative
+canopy solution or of the snow layering in FP32 (as the reference's own FP32
+build does against FP64), so on gridded workloads the check
+(harness.noise_criterion) counts the values out of tolerance against the
+count of the reference's REAL=FP32 / r_2=FP64 build on the same inputs, and
+holds the RMS error of the unflipped values to the tolerance."""
 import numpy as np
 import pytest
 
@@ -50,9 +52,8 @@ def test_gridded_parity_matches_reference_precision_noise(oracle, runtime, name)
     gs32 = {k: os32[k] for k in H.STATE_FIELDS}
     gd32 = {gk: od32[ok] for gk, ok in H.DIAG_MAP.items()}
     ref = H.parity_report(gs32, gd32, os_, od)
-    for k in FIELDS:
-        assert rep[k]["rms"] <= max(rep[k]["tol"], 3 * ref[k]["rms"]), (k, rep[k], ref[k])
-        assert rep[k]["frac_within"] >= min(0.995, ref[k]["frac_within"] - 0.005), (k, rep[k], ref[k])
+    bad = {k: H.noise_criterion(rep[k], ref[k]) for k in FIELDS}
+    assert not any(bad.values()), {k: (v, rep[k], ref[k]) for k, v in bad.items() if v}
     if name == "grid":
         # no snow: the RMS itself is inside the tolerance; with snow a few
         # tiles flip snow layering and dominate the RMS exactly as they do
@@ -224,12 +225,17 @@ def test_diagnostics_disabled_is_an_error(runtime):
     g.close()
 
 
-def test_medlyn_switch_matches_oracle(runtime):
+def test_medlyn_switch_matches_oracle(oracle, runtime):
     ts = W.grid(4000, nsteps=12)
-    gs, gd, os_, od, _ = H.run_pair(ts, 12, medlyn=True)
+    gs, gd, os_, od, F = H.run_pair(ts, 12, medlyn=True)
     rep = H.parity_report(gs, gd, os_, od)
-    for k in ("fe_d", "fh_d", "tv_d", "tgg", "wb"):
-        assert rep[k]["frac_within"] > 0.995, (k, rep[k])
+    st32 = oracle.init_state(ts, 1)
+    od32 = oracle.run(ts, st32, 12, forcing=F, precision=1, medlyn=True)
+    os32 = oracle.split_state(st32)
+    ref = H.parity_report({k: os32[k] for k in H.STATE_FIELDS}, {gk: od32[ok] for gk, ok in H.DIAG_MAP.items()},
+                          os_, od)
+    bad = {k: H.noise_criterion(rep[k], ref[k]) for k in ("fe_d", "fh_d", "tv_d", "tgg", "wb", "fgpp_d", "frday_d")}
+    assert not any(bad.values()), {k: (v, rep[k], ref[k]) for k, v in bad.items() if v}
 
 
 def test_autotuned_order_and_block_sizes_leave_results_unchanged(runtime):
@@ -398,9 +404,9 @@ def test_science_switches_match_oracle(oracle, runtime, which):
     os32 = oracle.split_state(st32)
     ref = H.parity_report({k: os32[k] for k in H.STATE_FIELDS}, {gk: od32[ok] for gk, ok in H.DIAG_MAP.items()},
                           os_, od)
-    for k in ("tgg", "tggsn", "wb", "wbice", "ga_d", "fe_d", "fh_d", "tv_d", "fes", "fgpp_d", "frday_d"):
-        assert rep[k]["rms"] <= max(rep[k]["tol"], 3 * ref[k]["rms"]), (k, rep[k], ref[k])
-        assert rep[k]["frac_within"] >= min(0.995, ref[k]["frac_within"] - 0.005), (k, rep[k], ref[k])
+    bad = {k: H.noise_criterion(rep[k], ref[k])
+           for k in ("tgg", "tggsn", "wb", "wbice", "ga_d", "fe_d", "fh_d", "tv_d", "fes", "fgpp_d", "frday_d")}
+    assert not any(bad.values()), {k: (v, rep[k], ref[k]) for k, v in bad.items() if v}
     assert np.abs(gd["ebal"]).max() < 0.05
     # soil respiration (frs) and transpiration (fevc) against the oracle too
     rms = lambda e: float(np.sqrt(np.mean(e ** 2)))
@@ -491,20 +497,15 @@ def test_host_layout_in_device_order_matches_caller_order(oracle, runtime):
 def test_config2_full_size_against_fp64_oracle(runtime):
     """The gridded workload at its full size, 1,000,000 tiles x 48 steps, on
     the benchmarked kernels (diagnostics off), against the FP64 oracle on the
-    GPU's own forcing, every output every step and the soil profiles at the
-    end: each field's RMS error within its tolerance or within the
-    reference's own FP32/FP64 noise on the same inputs, and its fraction of
-    tile-steps within tolerance no lower than that noise's."""
+    GPU's own forcing: every output every step and the soil profiles at the
+    end, each held to harness.noise_criterion against the reference's own
+    REAL = FP32 / r_2 = FP64 build on the same inputs."""
     import parity_full as P
     rep = P.config2_report(mp=1_000_000, nsteps=48)
-    bad = []
+    bad = {}
     for k, r in rep["fields"].items():
         g, m = r["gpu"], r["precision_mix"]
         assert "nonfinite" not in g, (k, g)
-        if r["tol"] is None:
-            continue
-        if not g["rms"] <= max(r["tol"], 1.5 * m["rms"]):
-            bad.append((k, "rms", g, m))
-        if not g["frac_within"] >= m["frac_within"] - 1e-3:
-            bad.append((k, "within", g, m))
-    assert not bad, bad
+        if r["tol"] is not None:
+            bad[k] = H.noise_criterion(g, m)
+    assert not any(bad.values()), {k: (v, rep["fields"][k]) for k, v in bad.items() if v}
