@@ -70,9 +70,12 @@ __global__ void __maxnreg__(kS64 ? CG_MAXNREG_S64 : CG_MAXNREG)
 #endif
 }
 
+// (internal linkage: every phase translation unit has its own copy under
+// this name, launching its own kernel)
+namespace {
 template <bool kS64>
-void CG_PHASE_LAUNCH_S(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
-                       const int* clock, int block) {
+void launch_instance(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
+                     const int* clock, int block) {
   const int grid = (D.mp + block - 1) / block;
 #if CG_PHASE_COUPLED
   if (P.mode != 0) {
@@ -84,16 +87,17 @@ void CG_PHASE_LAUNCH_S(bool diag, cudaStream_t s, const CgDev& D, const CgTables
   if (diag) CG_PHASE_KERNEL<true, false, kS64><<<grid, block, 0, s>>>(D, T, P, clock);
   else CG_PHASE_KERNEL<false, false, kS64><<<grid, block, 0, s>>>(D, T, P, clock);
 }
+}  // namespace
 
 void CG_PHASE_LAUNCH(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
                      const int* clock, int block) {
 #if CG_PHASE_SOLVE
   if (P.solve64) {
-    CG_PHASE_LAUNCH_S<true>(diag, s, D, T, P, clock, block);
+    launch_instance<true>(diag, s, D, T, P, clock, block);
     return;
   }
 #endif
-  CG_PHASE_LAUNCH_S<false>(diag, s, D, T, P, clock, block);
+  launch_instance<false>(diag, s, D, T, P, clock, block);
 }
 #endif
 

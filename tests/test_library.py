@@ -205,3 +205,18 @@ def test_soil_thermal_fix_tables_match_the_oracle(oracle):
     b = (C.c_float * 9)()
     assert L.cablegpu_param_table(1, b"css", b, 9) == 0
     assert np.frombuffer(b, np.float32)[0] == 850.0
+
+
+def test_phase_launchers_are_not_merged_across_translation_units():
+    """Each phase translation unit launches its own kernel: a launch helper
+    with external (weak) linkage and the same name in several units would be
+    merged by the linker into one, so every phase would launch the same
+    kernel.  The helpers must have internal linkage."""
+    import shutil
+    import subprocess
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm not available")
+    out = subprocess.run([nm, "-C", B.build()], capture_output=True, text=True, check=True).stdout
+    weak = [ln for ln in out.splitlines() if re.search(r"\s[WVuw]\s", ln) and "cg::" in ln and "launch" in ln.lower()]
+    assert not weak, weak[:5]
