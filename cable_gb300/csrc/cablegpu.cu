@@ -222,10 +222,12 @@ struct cablegpu_ctx {
   int medlyn = 0, diag = 0, capture_forcing = 0, thermal_fix = 0, litter = 0, rev_corr = 0;
   int switches = 0;                // the CABLEGPU_SW_* mask the fields above come from
   int solve64 = 1;                 // soil Thomas solves: 1 FP64 direct form (default), 0 FP32 on the change
+  int canopy_pool = 1;             // canopy dryLeaf passes: 1 block pool (default), 0 per lane
   int host_layout = 0;             // host buffers of step_host / forcing files: 0 caller order, 1 device order
   cudaGraphExec_t graph = nullptr;
   float graph_dels = -1.f;
   int graph_diag = -1, graph_switches = -1, graph_hostforc = -1, graph_capture = -1, graph_solve64 = -1;
+  int graph_pool = -1;
   unsigned long long graph_seed = 0;
   int graph_doy0 = -1;
   long long launches = 0;
@@ -382,6 +384,7 @@ StepParams make_params(cablegpu_ctx* c, int ktau, float dels) {
   p.final_cycle = 1;
   p.lai_refresh = 0;
   p.solve64 = c->solve64;
+  p.canopy_pool = c->canopy_pool;
   return p;
 }
 
@@ -389,7 +392,7 @@ int ensure_graph(cablegpu_ctx* c, float dels) {
   if (c->graph && c->graph_dels == dels && c->graph_diag == c->diag && c->graph_switches == c->switches &&
       c->graph_hostforc == (int)c->host_forcing && c->graph_capture == c->capture_forcing &&
       c->graph_seed == c->forc.seed && c->graph_doy0 == c->forc.doy0 && c->graph_sur == c->sur_enabled &&
-      c->graph_gate == c->sur_gate && c->graph_solve64 == c->solve64 &&
+      c->graph_gate == c->sur_gate && c->graph_solve64 == c->solve64 && c->graph_pool == c->canopy_pool &&
       std::equal(c->block, c->block + 5, c->graph_block))
     return CABLEGPU_OK;
   if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
@@ -410,6 +413,7 @@ int ensure_graph(cablegpu_ctx* c, float dels) {
   c->graph_hostforc = (int)c->host_forcing; c->graph_capture = c->capture_forcing;
   c->graph_seed = c->forc.seed; c->graph_doy0 = c->forc.doy0;
   c->graph_sur = c->sur_enabled; c->graph_gate = c->sur_gate; c->graph_solve64 = c->solve64;
+  c->graph_pool = c->canopy_pool;
   std::copy(c->block, c->block + 5, c->graph_block);
   return CABLEGPU_OK;
 }
@@ -485,6 +489,7 @@ int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out)
   CG_CUDA(c, cudaMalloc(&c->d_tables, sizeof(CgTables)));
   CG_CUDA(c, cudaMemcpyAsync(c->d_tables, &h, sizeof(CgTables), cudaMemcpyHostToDevice, c->stream));
   upload_canopy_pft_table(h.pft, c->stream);
+  prepare_canopy_kernels();
   CG_CUDA(c, cudaGetLastError());
   // device tile order
   {
@@ -681,6 +686,14 @@ int cablegpu_set_synthetic_forcing(cablegpu_ctx* c, unsigned long long seed, int
   c->host_forcing = false;
   c->forc.seed = seed;
   c->forc.doy0 = doy0;
+  return CABLEGPU_OK;
+}
+
+int cablegpu_set_canopy_schedule(cablegpu_ctx* c, int mode) {
+  if (!c) return CABLEGPU_ERR_ARG;
+  if (mode != CABLEGPU_CANOPY_POOL && mode != CABLEGPU_CANOPY_LANES)
+    return fail(c, CABLEGPU_ERR_ARG, "set_canopy_schedule: unknown mode");
+  c->canopy_pool = mode == CABLEGPU_CANOPY_POOL ? 1 : 0;
   return CABLEGPU_OK;
 }
 

@@ -259,13 +259,15 @@ __device__ __forceinline__ float photosynthesis_leaf(float csx, float cx1, float
   return fminf(fminf(anrubisco, anrubp), ansink);
 }
 
-// cbl_dryLeaf.F90:779-877
+// cbl_dryLeaf.F90:779-877.  alpha * parx is fixed over a dryLeaf call and x
+// changes every pass: the sum is one explicitly rounded multiply-add, so it
+// is computed the same wherever the pass runs.
 __device__ __forceinline__ float ej3x(float parx, float alpha, float convex, float x) {
-  float s = alpha * parx + x;
+  float s = __fmaf_rn(alpha, parx, x);
   return fmaxf(0.0f, 0.25f * ((s - sqrtf(s * s - 4.0f * convex * alpha * parx * x)) / (2.0f * convex)));
 }
 __device__ __forceinline__ float ej4x(float parx, float alpha, float convex, float x) {
-  float s = alpha * parx + x;
+  float s = __fmaf_rn(alpha, parx, x);
   return fmaxf(0.0f, (s - sqrtf(s * s - 4.0f * convex * alpha * parx * x)) / (2.0f * convex));
 }
 __device__ __forceinline__ float xvcmxt4(float x) {
@@ -282,6 +284,19 @@ __device__ __forceinline__ float xejmxt3(float x) {
   return fmaxf(0.0f, num / den);
 }
 
+// 1/x in FP64 by Newton-Raphson iteration on f(r) = 1/r - x, seeded with the
+// FP32 reciprocal of x: each step r <- r + r (1 - x r) squares the relative
+// error (~2^-22 -> ~2^-44 -> below the FP64 rounding), two fused
+// multiply-adds per step.  For 1e-30 < |x| < 1e30 (the FP32 normal range of
+// the seed); the soil systems' pivots and saturation deficits are far inside
+// it.  Tested against CUDA's FP64 division (tests/test_fp64_reciprocal.py).
+__device__ __forceinline__ double rcp64(double x) {
+  double r = (double)__fdividef(1.0f, (float)x);
+  r = fma(r, fma(-x, r, 1.0), r);
+  r = fma(r, fma(-x, r, 1.0), r);
+  return r;
+}
+
 // cbl_trimb.F90:17-53 in FP64, as the reference solves both soil systems,
 // for their diffusion form: the Thomas algorithm on
 //   a(k) u(k-1) + b(k) u(k) + c(k) u(k+1) = rhs(k),  b(k) = 1 - a(k) - c(k)
@@ -293,24 +308,25 @@ __device__ __forceinline__ float xejmxt3(float x) {
 // g(1) = rhs(1)/b(1); temp(k) = 1/(b(k) - a(k) e(k-1)), e(k) = c(k) temp(k),
 // g(k) = (rhs(k) - a(k) g(k-1)) temp(k) for k = 2..N-1; the last row
 // divided by its own pivot; back substitution.  Row 1's two divisions by
-// b(1) are one reciprocal here (the same value to an FP64 ulp), and g(k)
+// b(1) are one reciprocal here, every division a multiplication by an FP64
+// reciprocal (rcp64; the same value to an FP64 ulp or two), and g(k)
 // overwrites rhs(k), so only e and the solution are live in FP64.
 template <int N>
 __device__ __forceinline__ void trimb64(const float* a, const float* c, double db0, double* rhs) {
   double e[N - 1];
-  const double ib = 1.0 / ((1.0 - (double)a[0] - (double)c[0]) + db0);
+  const double ib = rcp64((1.0 - (double)a[0] - (double)c[0]) + db0);
   e[0] = (double)c[0] * ib;
   rhs[0] = rhs[0] * ib;
 #pragma unroll
   for (int k = 1; k < N - 1; ++k) {
     const double ak = a[k], ck = c[k];
-    const double temp = 1.0 / ((1.0 - ak - ck) - ak * e[k - 1]);
+    const double temp = rcp64((1.0 - ak - ck) - ak * e[k - 1]);
     e[k] = ck * temp;
     rhs[k] = (rhs[k] - ak * rhs[k - 1]) * temp;
   }
   {
     const double ak = a[N - 1], ck = c[N - 1];
-    rhs[N - 1] = (rhs[N - 1] - ak * rhs[N - 2]) / ((1.0 - ak - ck) - ak * e[N - 2]);
+    rhs[N - 1] = (rhs[N - 1] - ak * rhs[N - 2]) * rcp64((1.0 - ak - ck) - ak * e[N - 2]);
   }
 #pragma unroll
   for (int k = N - 2; k >= 0; --k) rhs[k] = rhs[k] - e[k] * rhs[k + 1];

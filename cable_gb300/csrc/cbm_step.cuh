@@ -38,6 +38,8 @@ struct StepParams {
   // wetness factor and surface temperature are left as they were), 2 cbm_impl
   int mode;
   int final_cycle;   // cbm_impl: 1 on the last implicit cycle of the step (cycleno == numcycles)
+  int canopy_pool;   // 1: the canopy kernel runs the block's dryLeaf passes as a
+                     // shared-memory pool; 0: each thread its own tile's
   int solve64;       // 1: the soil heat and moisture Thomas solves in FP64 on the
                      // reference's direct form; 0: in FP32 on the step's change
   int lai_refresh;   // cbm_expl: the host model's radiation call ran, so the
@@ -459,8 +461,23 @@ __device__ __forceinline__ float transp_extract(float fe_mm, const float (&froot
   return se;
 }
 
-template <bool kDiag, bool kHarvest = false, bool kSur = false, bool kCoupled = false>
-__device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t) {
+// kPool: the dryLeaf passes of the block's tiles run as a pool in shared
+// memory sm (dryleaf.cuh); every thread of the block must then call this
+// (threads beyond the last tile call dl_pool_idle instead).
+}  // namespace cg
+// the dryLeaf pass and its schedules (uses c_pft, ldk and transp_extract above)
+#include "dryleaf.cuh"
+namespace cg {
+
+template <bool kDiag, bool kHarvest = false, bool kSur = false, bool kCoupled = false, bool kPool = false>
+__device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restrict__ T, const StepParams& P, int t_in,
+                                        float* sm = nullptr) {
+  // A pooling block's threads beyond the last tile ("ghosts") run the last
+  // tile's code path and store nothing, so every thread of the block reaches
+  // the pool's barriers and votes on one path; they leave after the
+  // Monin-Obukhov loop, the last code with barriers.
+  const bool ghost = kPool && t_in >= D.mp;
+  const int t = ghost ? D.mp - 1 : t_in;
   // the coupled-call code exists only in the kCoupled instantiation
   const int mode = kCoupled ? P.mode : 0;
   const int ld = D.ld;
@@ -622,17 +639,15 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
       gbhu[0] = gbvtop * (1.0f - expf(-fminf(vlaiw * (0.5f * coexp + extkb), 20.0f))) / (extkb + 0.5f * coexp);
       gbhu[1] = (2.0f / coexp) * gbvtop * (1.0f - expf(-fminf(0.5f * coexp * vlaiw, 20.0f))) - gbhu[0];
     }
-    rny = sum_rad_rniso; hcy = 0.f; ecy = rny;
-
     // ------------------------------------------------ dryLeaf (cbl_dryLeaf.F90:10-666)
     {
       // surrogate inputs: the state the first iteration starts from
       const float tlf_entry = tlfx;
       bool sampled = false;
-      if (harvesting && iter == 1 && veg_mask) {
-        uint32_t c[4] = {(uint32_t)D.tile_id[t], (uint32_t)P.step_index, 0xD1EAF001u, 0u};
-        cg_philox(c, D.harvest_seed);
-        sampled = cg_u01(c[0]) < D.harvest_prob;
+      if (harvesting && iter == 1 && veg_mask && !ghost) {
+        uint32_t c4[4] = {(uint32_t)D.tile_id[t], (uint32_t)P.step_index, 0xD1EAF001u, 0u};
+        cg_philox(c4, D.harvest_seed);
+        sampled = cg_u01(c4[0]) < D.harvest_prob;
       }
       float feat[12];
       if (sampled) {
@@ -647,19 +662,25 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
         const float dt = D.sur_dt[t];
         if (isfinite(dt)) { sur_try = true; tlf_sur = tlf_entry + dt; }
       }
-      const float gswmin_p = ldk(c_pft.gswmin[v]);
-      float gswmin[2] = {fmaxf(1.e-6f, scalex[0] * gswmin_p), fmaxf(1.e-6f, scalex[1] * gswmin_p)};
-      float gh[2] = {1e-3f, 1e-3f}, ghr[2] = {1e-3f, 1e-3f}, psycst[2] = {psyc, psyc};
-      float rdx[2] = {0.f, 0.f}, anx[2] = {0.f, 0.f};
-      float rdy_sum = 0.f, an_y_sum = 0.f;   // the best iterate's leaf respiration / net assimilation, both leaves
-      float rnx = sum_rad_rniso, ecx = sum_rad_rniso, hcx = 0.f;
-      float abs_deltlf = 999.0f, deltlf = 0.f;
-      float tlfxx = tlfx;
-      fevc = 0.f;
-      float fe_mm_last = 0.f, fe_mm_best = 0.f;   // transpiration (mm) of the latest extracting pass / best iterate
-      hcy = 0.f;
-      if (!veg_mask) { rnx = 0.f; ecx = 0.f; ecy = 0.f; abs_deltlf = 0.f; rny = 0.f; }
-      float deltlfy = abs_deltlf;
+      // the call's inputs and the iteration's start (cbl_dryLeaf.F90:183-237)
+      DlCtx c;
+      c.v = v; c.tk = tk; c.ca = ca; c.cmolar = cmolar; c.psyc = psyc; c.dsatdk = dsatdk; c.fwet = fwet;
+      c.fwsoil = fwsoil;
+#pragma unroll
+      for (int l = 0; l < 2; ++l) {
+        c.scalex[l] = scalex[l]; c.fvlai[l] = fvlai[l]; c.gradis[l] = gradis[l]; c.rniso[l] = rniso[l];
+        c.qcan_par[l] = qcan_par[l]; c.gbhu[l] = gbhu[l];
+      }
+#pragma unroll
+      for (int q = 0; q < CG_MS; ++q) c.dk_avail[q] = dk_avail[q];
+      c.tvair = tvair; c.dva = dva; c.conv = 0.1f;
+      DlState st;
+      st.tlfx = tlfx; st.dsx = dsx;
+#pragma unroll
+      for (int l = 0; l < 2; ++l) { st.csx[l] = csx[l]; st.gswx[l] = gswx[l]; st.gbhf[l] = gbhf[l]; st.psycst[l] = psyc; }
+      st.abs_deltlf = 999.0f; st.deltlfy = 999.0f; st.ecx = sum_rad_rniso;
+      st.rny = sum_rad_rniso; st.hcy = 0.f; st.ecy = sum_rad_rniso; st.tlfy = tlfy;
+      st.rdy_sum = 0.f; st.an_y_sum = 0.f; st.fe_mm_best = 0.f; st.fe_mm_last = 0.f; st.k = 0;
       // With the surrogate the first iteration starts from the network's
       // leaf temperature.  The first pass is the closure test of the
       // prediction: when the leaf energy balance evaluated there moves the
@@ -668,146 +689,72 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
       // its usual start (bitwise the plain result); in warm mode the plain
       // iteration continues from the prediction to the gate as its
       // convergence test (cbl_dryLeaf.F90 uses 0.1 K).
-      float conv = 0.1f;
-      // entry state, for the strict mode's restart of the plain iteration
-      const float dsx_entry = dsx, csx_entry[2] = {csx[0], csx[1]}, gswx_entry[2] = {gswx[0], gswx[1]};
-      const float gbhf_entry[2] = {gbhf[0], gbhf[1]};
+      const DlState entry = st;
       if (sur_try) {
         ++sur_tried;
-        tlfx = tlf_sur;
-        dsx = fmaxf(dva + dsatdk * (tlfx - tvair), 0.0f);
-        conv = D.sur_gate;
+        st.tlfx = tlf_sur;
+        st.dsx = fmaxf(dva + dsatdk * (st.tlfx - tvair), 0.0f);
+        c.conv = D.sur_gate;
       }
-      for (int k = 1; k <= MAXITER; ++k) {
-        const bool active = veg_mask && abs_deltlf > conv;
-        if (active) {
-          ++passes_total;
-          const float dleaf = ldk(c_pft.dleaf[v]);
-          float gras = fmaxf(1.0e-6f, 1.595E8f * fabsf(tlfx - tvair) * (dleaf * dleaf * dleaf));
-          float gr4 = sqrtf(sqrtf(gras));
-#pragma unroll
-          for (int l = 0; l < 2; ++l) {
-            gbhf[l] = fmaxf(1.e-6f, fvlai[l] * cmolar * 0.5f * DHEAT * gr4 / dleaf);
-            gh[l] = 2.0f * (gbhu[l] + gbhf[l]);
-            ghr[l] = gradis[l] + gh[l];
-          }
-          float vcmxt3[2], vcmxt4[2], vx3[2], vx4[2], gs_coeff[2];
-          const float vcmax = ldk(c_pft.vcmax[v]), frac4 = ldk(c_pft.frac4[v]);
-          float temp = xvcmxt3(tlfx) * vcmax * (1.0f - frac4);
-          vcmxt3[0] = scalex[0] * temp; vcmxt3[1] = scalex[1] * temp;
-          temp = xvcmxt4(tlfx - TFRZ) * vcmax * frac4;
-          vcmxt4[0] = scalex[0] * temp; vcmxt4[1] = scalex[1] * temp;
-          temp = xejmxt3(tlfx) * ldk(c_pft.ejmax[v]) * (1.0f - frac4);
-          float ejmxt3[2] = {scalex[0] * temp, scalex[1] * temp};
-          float tdiff = tlfx - TREFK;
-          float arr = (1.0f - TREFK / tlfx) / (RGAS * TREFK);
-          float conkct = ldk(c_pft.conkc0[v]) * expf(ldk(c_pft.ekc[v]) * arr);
-          float conkot = ldk(c_pft.conko0[v]) * expf(ldk(c_pft.eko[v]) * arr);
-          tlfxx = tlfx;
-          float cx1 = conkct * (1.0f + 0.21f / conkot);
-          float cx2 = 2.0f * GAM0 * (1.0f + GAM1 * tdiff + GAM2 * tdiff * tdiff);
-#pragma unroll
-          for (int l = 0; l < 2; ++l) {
-            float par = qcan_par[l] * 4.6e-6f;
-            const float alpha = ldk(c_pft.alpha[v]), convex = ldk(c_pft.convex[v]), cfrd = ldk(c_pft.cfrd[v]);
-            vx3[l] = ej3x(par * (1.0f - frac4), alpha, convex, ejmxt3[l]);
-            vx4[l] = ej4x(par * frac4, alpha, convex, vcmxt4[l]);
-            rdx[l] = cfrd * vcmxt3[l] + cfrd * vcmxt4[l];
-          }
-          if (!P.medlyn) {
-            float f = ldk(c_pft.a1gs[v]) / (1.0f + dsx / ldk(c_pft.d0gs[v]));
-            gs_coeff[0] = (fwsoil / csx[0]) * f;
-            gs_coeff[1] = (fwsoil / csx[1]) * f;
-          } else {
-            gswmin[0] = gswmin[1] = ldk(c_pft.g0[v]);
-            float vpd = (dsx < 50.0f) ? 0.05f : dsx * 1e-3f;
-            float num = (fwsoil <= 0.05f) ? fwsoil / 0.05f : 1.0f;
-            float t2 = (ldk(c_pft.g1[v]) * fwsoil) * rsqrtf(vpd);
-            gs_coeff[0] = (num + t2) / csx[0];
-            gs_coeff[1] = (num + t2) / csx[1];
-          }
-          // photosynthesis: anx is zeroed and recomputed under the masks
-          anx[0] = 0.f; anx[1] = 0.f;
-          if (fvlai[0] + fvlai[1] > LAI_THRESH) {
-#pragma unroll
-            for (int l = 0; l < 2; ++l)
-              if (fvlai[l] > LAI_THRESH)
-                anx[l] = photosynthesis_leaf(csx[l], cx1, cx2, gswmin[l], rdx[l], vcmxt3[l], vcmxt4[l], vx3[l], vx4[l],
-                                             gs_coeff[l], fwsoil);
-          }
-#pragma unroll
-          for (int l = 0; l < 2; ++l) {
-            if (fvlai[l] > LAI_THRESH) {
-              csx[l] = fmaxf(1.0e-4f, ca - RGBWC * anx[l] / (gbhu[l] + gbhf[l]));
-              gswx[l] = fmaxf(1.e-3f, gswmin[l] * fwsoil + fmaxf(0.0f, RGSWC * gs_coeff[l] * anx[l]));
-              float gw = 1.0f / (1.0f / gswx[l] + 1.0f / (1.075f * (gbhu[l] + gbhf[l])));
-              gw = fmaxf(gw, 0.00001f);
-              psycst[l] = psyc * (ghr[l] / gw);
+      bool restarted = false;
+      if constexpr (kPool) {
+        // the block's tiles iterate together (dryleaf.cuh): park this tile's
+        // inputs and state in its slot, run the rounds, take the result back
+        const DlPool<kSur> pool{sm, (int)blockDim.x};
+        const int slot = threadIdx.x;
+        __syncthreads();   // the previous call's slots and round counters are free
+        if (veg_mask) {
+          if (iter == 1) pool.put_step(slot, c);
+          if (kSur && sur_try) pool.put_entry(slot, entry);
+          pool.put_call(slot, c, st, (kSur && sur_try) ? dlp::SUR_TRY : 0);
+        }
+        if (threadIdx.x == 0) { int* cn = pool.cnt(); cn[0] = 0; cn[1] = 0; cn[2] = 0; }
+        __syncthreads();
+        pool.run(veg_mask, P.medlyn, dels, D.sur_strict);
+        if (veg_mask) {
+          pool.get_state(slot, st);
+          const int bits = pool.kv(slot);
+          if (kSur && (bits & dlp::SUR_ACC)) ++sur_accepted;
+          if (kSur && (bits & dlp::SUR_RESTART)) { restarted = true; ++passes_total; }
+        }
+      } else if (veg_mask) {
+        bool more = true, first_sur = sur_try;
+        while (more) {
+          more = dl_pass(c, st, froot, P.medlyn, dels);
+          if (kSur && first_sur) {
+            first_sur = false;
+            if (st.abs_deltlf <= c.conv) {
+              ++sur_accepted;
+            } else if (D.sur_strict) {
+              // strict: the prediction did not close, so the tile runs the
+              // plain iteration from its usual start, exactly as without the
+              // surrogate
+              passes_total += st.k;
+              const float keep_psycst[2] = {st.psycst[0], st.psycst[1]};
+              const float keep_rny = st.rny, keep_ecy = st.ecy, keep_tlfy = st.tlfy;
+              st = entry;
+              st.psycst[0] = keep_psycst[0]; st.psycst[1] = keep_psycst[1];
+              st.rny = keep_rny; st.ecy = keep_ecy; st.tlfy = keep_tlfy;
+              c.conv = 0.1f;
+              restarted = true;
+              more = true;
             }
           }
-          const float cpr = CAPP * RMAIR;
-          ecx = (dsatdk * (rniso[0] - cpr * (tvair - tk) * gradis[0]) + cpr * dva * ghr[0]) / (dsatdk + psycst[0]) +
-                (dsatdk * (rniso[1] - cpr * (tvair - tk) * gradis[1]) + cpr * dva * ghr[1]) / (dsatdk + psycst[1]);
-          float local_fevc = (1.0f - fwet) * ecx;
-          if (local_fevc > 0.0f) {
-            const float fe_mm = local_fevc * dels / HL;
-            float ev[CG_MS];
-            const float se = transp_extract(fe_mm, froot, dk_avail, ev);
-            fevc = se * rlam / dels;
-            ecx = fevc / (1.0f - fwet);
-            fe_mm_last = fe_mm;
-          }
-          float sgh = gh[0] + gh[1];
-          hcx = (sum_rad_rniso - ecx - cpr * (tvair - tk) * sum_rad_gradis) * sgh / (ghr[0] + ghr[1]);
-          tlfx = tvair + hcx / (cpr * sgh);
-          rnx = sum_rad_rniso - cpr * (tlfx - tk) * sum_rad_gradis;
-          dsx = fmaxf(dva + dsatdk * (tlfx - tvair), 0.0f);
-          deltlf = tlfxx - tlfx;
-          abs_deltlf = fabsf(deltlf);
-        } else {
-          anx[0] = 0.f; anx[1] = 0.f;
         }
-        // keep the best iterate (:565-582)
-        if (abs_deltlf < fabsf(deltlfy) || k == 1) {
-          if (abs_deltlf < fabsf(deltlfy)) deltlfy = deltlf;
-          rny = rnx; hcy = hcx; ecy = ecx;
-          rdy_sum = rdx[0] + rdx[1]; an_y_sum = anx[0] + anx[1];
-          fe_mm_best = fe_mm_last;
-          tlfy = tlfx;   // damping below is a no-op for k == 1
-        }
-        // damping once k > 5 (:584-590).  Written with explicitly rounded
-        // operations: a*b + c*d leaves the compiler a choice of which product
-        // to fuse, and that choice may differ between instantiations of the
-        // kernel (diagnostics on or off), which must give identical results.
-        if (abs_deltlf > conv) {
-          float fac = 0.5f * ((float)max(0, k - 5) / ((float)k - 4.9999f));
-          tlfx = __fmaf_rn(fac, tlfxx, __fmul_rn(1.0f - fac, tlfx));
-        }
-        if (kSur && sur_try && k == 1) {
-          if (abs_deltlf <= conv) {
-            ++sur_accepted;
-          } else if (D.sur_strict) {
-            // strict: the prediction did not close, so the tile runs the
-            // plain iteration from its usual start, exactly as without the
-            // surrogate
-            tlfx = tlf_entry; dsx = dsx_entry;
-            csx[0] = csx_entry[0]; csx[1] = csx_entry[1];
-            gswx[0] = gswx_entry[0]; gswx[1] = gswx_entry[1];
-            gbhf[0] = gbhf_entry[0]; gbhf[1] = gbhf_entry[1];
-            rnx = sum_rad_rniso; ecx = sum_rad_rniso; hcx = 0.f;
-            abs_deltlf = 999.0f; deltlf = 0.f; deltlfy = abs_deltlf;
-            fevc = 0.f; hcy = 0.f;
-            fe_mm_last = 0.f; fe_mm_best = 0.f;
-            rdx[0] = rdx[1] = anx[0] = anx[1] = rdy_sum = an_y_sum = 0.f;
-            conv = 0.1f;
-            sur_try = false;
-            k = 0;
-            continue;
-          }
-        }
-        // a tile that has stopped iterating never changes again: leave now
-        if (!(veg_mask && abs_deltlf > conv)) break;
       }
+      if (!veg_mask) {
+        // no pass: the best-iterate store of the first (inactive) pass
+        st.tlfy = st.tlfx; st.rny = 0.f; st.hcy = 0.f; st.ecy = 0.f; st.rdy_sum = 0.f; st.an_y_sum = 0.f;
+        st.fe_mm_best = 0.f; st.fe_mm_last = 0.f; st.ecx = 0.f; st.abs_deltlf = 0.f;
+      }
+      passes_total += st.k;
+      const float conv = restarted ? 0.1f : c.conv;
+      tlfx = st.tlfx; dsx = st.dsx; tlfy = st.tlfy;
+#pragma unroll
+      for (int l = 0; l < 2; ++l) { csx[l] = st.csx[l]; gswx[l] = st.gswx[l]; gbhf[l] = st.gbhf[l]; }
+      rny = st.rny; hcy = st.hcy; ecy = st.ecy;
+      const float ecx = st.ecx, abs_deltlf = st.abs_deltlf;
+      const float rdy_sum = st.rdy_sum, an_y_sum = st.an_y_sum, fe_mm_last = st.fe_mm_last, fe_mm_best = st.fe_mm_best;
       // status bits of this iteration, recorded with diagnostics on (they cost
       // the fast kernel registers in its hottest loop): pass limit reached
       // unconverged; the reference's 'oldevapfbl not right' condition
@@ -832,7 +779,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
           if (kDiag) it_bits |= CG_TS_EVAPFBL;
         }
       }
-      if (kDiag && it_bits) D.tile_status[t] |= it_bits;
+      if (kDiag && it_bits && !ghost) D.tile_status[t] |= it_bits;
       frday = 12.0f * rdy_sum;
       fpn = fminf(-12.0f * an_y_sum, frday);
       // training row: features at entry, converged stomatal conductance,
@@ -955,6 +902,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
     }
   }
 
+  if (ghost) return;
   // ---------------------------------------------------------------- post-loop (:684-1038)
   const float z4 = zeta;   // the last iteration's
   const float cduv = us * us / sqf(fmaxf(ua, UMIN));
@@ -1941,7 +1889,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
         wbid[k] = df_to_double(wbice[k]);
         const double wbd = df_to_double(wb[k]) + (double)dwd[k];
         satd[k] = (double)ssat - wbid[k];
-        rd[k] = (wbd - wbid[k]) / satd[k];
+        rd[k] = (wbd - wbid[k]) * rcp64(satd[k]);
         xf[k] = (float)rd[k];
         dtt[k] = dels / (zse[k] * (ssat - wbicef[k]));
       }

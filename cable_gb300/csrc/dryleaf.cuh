@@ -120,16 +120,22 @@ __device__ __forceinline__ bool dl_pass(const DlCtx& c, DlState& s, const float 
   for (int l = 0; l < 2; ++l) {
     if (c.fvlai[l] > LAI_THRESH) {
       s.csx[l] = fmaxf(1.0e-4f, c.ca - RGBWC * anx[l] / (c.gbhu[l] + s.gbhf[l]));
-      s.gswx[l] = fmaxf(1.e-3f, gswmin[l] * c.fwsoil + fmaxf(0.0f, RGSWC * gs_coeff[l] * anx[l]));
+      s.gswx[l] = fmaxf(1.e-3f, __fmaf_rn(gswmin[l], c.fwsoil, fmaxf(0.0f, RGSWC * gs_coeff[l] * anx[l])));
       float gw = 1.0f / (1.0f / s.gswx[l] + 1.0f / (1.075f * (c.gbhu[l] + s.gbhf[l])));
       gw = fmaxf(gw, 0.00001f);
       s.psycst[l] = c.psyc * (ghr[l] / gw);
     }
   }
+  // Terms that combine a product of the call's fixed inputs with a
+  // per-pass value are written with explicitly rounded operations: where a
+  // pass runs (a per-lane loop, where the compiler hoists the fixed product,
+  // or the pool, where it does not) must not change which products are
+  // fused into multiply-adds, so both schedules compute identical results.
   const float cpr = CAPP * RMAIR;
-  float ecx = (c.dsatdk * (c.rniso[0] - cpr * (c.tvair - c.tk) * c.gradis[0]) + cpr * c.dva * ghr[0]) /
+  const float pc = __fmul_rn(cpr, __fsub_rn(c.tvair, c.tk)), pd = __fmul_rn(cpr, c.dva);
+  float ecx = __fmaf_rn(c.dsatdk, __fmaf_rn(-pc, c.gradis[0], c.rniso[0]), __fmul_rn(pd, ghr[0])) /
                   (c.dsatdk + s.psycst[0]) +
-              (c.dsatdk * (c.rniso[1] - cpr * (c.tvair - c.tk) * c.gradis[1]) + cpr * c.dva * ghr[1]) /
+              __fmaf_rn(c.dsatdk, __fmaf_rn(-pc, c.gradis[1], c.rniso[1]), __fmul_rn(pd, ghr[1])) /
                   (c.dsatdk + s.psycst[1]);
   float local_fevc = (1.0f - c.fwet) * ecx;
   if (local_fevc > 0.0f) {
@@ -143,7 +149,7 @@ __device__ __forceinline__ bool dl_pass(const DlCtx& c, DlState& s, const float 
   const float sum_rad_rniso = c.rniso[0] + c.rniso[1];
   const float sum_rad_gradis = c.gradis[0] + c.gradis[1];
   float sgh = gh[0] + gh[1];
-  const float hcx = (sum_rad_rniso - ecx - cpr * (c.tvair - c.tk) * sum_rad_gradis) * sgh / (ghr[0] + ghr[1]);
+  const float hcx = __fmaf_rn(-pc, sum_rad_gradis, __fsub_rn(sum_rad_rniso, ecx)) * sgh / (ghr[0] + ghr[1]);
   s.tlfx = c.tvair + hcx / (cpr * sgh);
   const float rnx = sum_rad_rniso - cpr * (s.tlfx - c.tk) * sum_rad_gradis;
   s.dsx = fmaxf(c.dva + c.dsatdk * (s.tlfx - c.tvair), 0.0f);
@@ -272,7 +278,7 @@ struct DlPool {
   }
 
   // One pass of the tile in `slot`; returns whether it iterates again.
-  __device__ bool pass(int slot, int medlyn, float dels, int sur_strict, float psyc_unused = 0.f) const {
+  __device__ bool pass(int slot, int medlyn, float dels, int sur_strict) const {
     DlCtx c;
     DlState s;
     get_ctx(slot, c);
@@ -313,8 +319,9 @@ struct DlPool {
 
   // One dryLeaf call of the whole block: every thread of the block calls it
   // (own = whether this thread's tile takes part, its pass inputs and state
-  // already in slot threadIdx.x).  Barrier S1 (before the caller's writes)
-  // is the caller's.
+  // already in slot threadIdx.x).  Before the call the caller has passed a
+  // barrier after the previous call, written its slot, cleared the three
+  // round counters (thread 0) and passed a second barrier.
   __device__ void run(bool own, int medlyn, float dels, int sur_strict) const {
     const int tid = threadIdx.x, lane = tid & 31;
     int* const C = cnt();

@@ -40,6 +40,9 @@ void launch_phase_c3(bool diag, cudaStream_t s, const CgDev& D, const CgTables* 
 
 // the canopy kernel's constant-memory copy of the plant-type table
 void upload_canopy_pft_table(const CgPftTable& pft, cudaStream_t s);
+// sets the canopy kernels' shared-memory limit for the dryLeaf pool (once per
+// device, before the first launch)
+void prepare_canopy_kernels();
 
 #ifdef CG_PHASE
 // CG_PHASE_COUPLED 1: the phase has a second instantiation for the coupled

@@ -42,11 +42,15 @@ EXPORTS = [
     "cablegpu_restart_write", "cablegpu_restart_read", "cablegpu_forcing_file_write", "cablegpu_file_info",
     "cablegpu_run_forcing_file", "cablegpu_set_host_layout", "cablegpu_tile_order",
     "cablegpu_step_explicit", "cablegpu_step_implicit", "cablegpu_coupled_timed", "cablegpu_set_soil_solve",
+    "cablegpu_set_canopy_schedule",
 ]
 NOALLOC_MAX_TILES = 65536
 # soil tridiagonal solve arithmetic (cablegpu_set_soil_solve)
 SOLVE_FP64 = 0
 SOLVE_FP32_CHANGE = 1
+# canopy dryLeaf pass scheduling (cablegpu_set_canopy_schedule)
+CANOPY_POOL = 0
+CANOPY_LANES = 1
 # science switch bits of cablegpu_set_options (include/cablegpu.h)
 SW_MEDLYN = 1
 SW_SOIL_THERMAL_FIX = 2
@@ -169,6 +173,7 @@ def load(build_if_missing: bool = True):
     L.cablegpu_set_synthetic_forcing.argtypes = [vp, C.c_ulonglong, ip]
     L.cablegpu_set_options.argtypes = [vp, ip, ip, ip]
     L.cablegpu_set_soil_solve.argtypes = [vp, ip]
+    L.cablegpu_set_canopy_schedule.argtypes = [vp, ip]
     L.cablegpu_step.argtypes = [vp, ip, C.c_float]
     L.cablegpu_step_explicit.argtypes = [vp, ip, C.c_float, ip]
     L.cablegpu_coupled_timed.argtypes = [vp, ip, ip, C.c_float, ip, C.POINTER(C.c_float)]
@@ -357,6 +362,13 @@ class CableGPU:
         if isinstance(mode, str):
             mode = {"fp64": SOLVE_FP64, "fp32_change": SOLVE_FP32_CHANGE}[mode]
         self._check(self.L.cablegpu_set_soil_solve(self.h, int(mode)))
+
+    def set_canopy_schedule(self, mode):
+        """Canopy dryLeaf passes: CANOPY_POOL (default) or CANOPY_LANES, or
+        "pool" / "lanes"."""
+        if isinstance(mode, str):
+            mode = {"pool": CANOPY_POOL, "lanes": CANOPY_LANES}[mode]
+        self._check(self.L.cablegpu_set_canopy_schedule(self.h, int(mode)))
 
     def set_synthetic_forcing(self, seed: int, doy0: int = 1):
         self._check(self.L.cablegpu_set_synthetic_forcing(self.h, int(seed), int(doy0)))

@@ -201,6 +201,21 @@ int cablegpu_set_options(cablegpu_ctx* ctx, int switches, int diag, int capture_
 #define CABLEGPU_SOLVE_FP32_CHANGE 1
 int cablegpu_set_soil_solve(cablegpu_ctx* ctx, int mode);
 
+/* Scheduling of the canopy kernel's dryLeaf passes (cbl_dryLeaf.F90:10-666,
+ * up to 20 passes per tile and Monin-Obukhov iteration, converging after
+ * different numbers of passes):
+ *   CABLEGPU_CANOPY_POOL  (default) the tiles of a thread block iterate as a
+ *                         pool in shared memory: each round runs one pass of
+ *                         every tile still iterating, one tile per thread,
+ *                         so threads whose tile converged take other tiles'
+ *                         passes
+ *   CABLEGPU_CANOPY_LANES each thread runs its own tile's passes
+ * Results are identical; only the speed differs.  Applies to the steps issued
+ * after the call. */
+#define CABLEGPU_CANOPY_POOL 0
+#define CABLEGPU_CANOPY_LANES 1
+int cablegpu_set_canopy_schedule(cablegpu_ctx* ctx, int mode);
+
 /* One timestep, ktau 1-based (cbm(ktau, dels, ...) followed by the driver's
  * balance checks).  Asynchronous; errors of the step surface at the next
  * synchronising call. */

@@ -100,6 +100,38 @@ def test_plain_kernels_equal_the_diagnostics_kernels(runtime):
         np.testing.assert_array_equal(s0[k], graph[k], err_msg="graph " + k)
 
 
+@pytest.mark.parametrize("blocks", [[128, 128, 128, 128, 128], [256, 64, 64, 64, 64], [64, 32, 32, 32, 32]])
+def test_canopy_pool_equals_per_lane_schedule(runtime, blocks):
+    """The canopy kernel's dryLeaf passes run as a block pool (default) or
+    per lane: outputs every step and state after 24 steps bitwise equal, with
+    diagnostics off and on (20,003 tiles: the last block has threads beyond
+    the last tile, which take part in the pool's barriers as ghosts)."""
+    R = runtime
+    ts = W.snow_grid(20003, nsteps=24)
+    names = [n for n, v in R.fields().items() if v[3] == R.KIND_STATE]
+    for diag in (False, True):
+        runs = []
+        for sched in ("lanes", "pool"):
+            g = R.from_tileset(ts, order=2)
+            g.set_blocks(blocks)
+            g.set_options(diag=diag)
+            g.set_canopy_schedule(sched)
+            outs = []
+            for n in range(24):
+                g.step(1 + n, ts.dels)
+                outs.append(g.get("out"))
+            st = {k: g.get(k) for k in names}
+            if diag:
+                st["dryleaf_passes"] = g.get("dryleaf_passes")
+            runs.append((outs, st))
+            g.close()
+        (o0, s0), (o1, s1) = runs
+        for n in range(24):
+            np.testing.assert_array_equal(o0[n], o1[n], err_msg="diag %d out, step %d" % (diag, n + 1))
+        for k in s0:
+            np.testing.assert_array_equal(s0[k], s1[k], err_msg="diag %d %s" % (diag, k))
+
+
 def test_host_forcing_path_matches_synthetic(runtime):
     """The drop-in path (forcing uploaded from the host every step) gives the
     same state as the in-kernel generator when fed its forcing."""
