@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 #include <condition_variable>
 #include <mutex>
@@ -44,7 +45,7 @@ const char* kDiagNames[CG_NDIAG] = {
   "epot", "fes", "fevc", "dgdtg", "fevw", "fpn", "frday_d", "fgpp_d", "fnpp", "fnee", "fra", "frp", "frs", "trad_d",
   "albedo_vis", "albedo_nir", "transd", "precis", "through", "fwet", "wetfac", "potev", "runoff", "rnof1", "rnof2",
   "smelt", "ghflux", "sghflux", "drybal", "wetbal", "ebal", "wbal", "qssabs", "rniso", "vlaiw_d", "tvair", "qvair",
-  "swnet", "lwnet", "wbtot", "gswx_sun", "gswx_shd", "fwsoil", "dryleaf_passes",
+  "swnet", "lwnet", "wbtot", "gswx_sun", "gswx_shd", "fwsoil", "dryleaf_passes", "delwc", "cls", "frpw", "frpr",
 };
 
 std::vector<FieldDef> make_registry() {
@@ -56,6 +57,9 @@ std::vector<FieldDef> make_registry() {
     {"lonphase", 1, CABLEGPU_F32, CABLEGPU_KIND_PARAM, S_F32},
     {"tbase", 1, CABLEGPU_F32, CABLEGPU_KIND_PARAM, S_F32},
     {"swscale", 1, CABLEGPU_F32, CABLEGPU_KIND_PARAM, S_F32},
+    // soil%albsoil(:,1), the VIS bare-soil albedo (read from the gridded soil
+    // file by the reference); defaults to the soil type's table value
+    {"albsoil", 1, CABLEGPU_F32, CABLEGPU_KIND_PARAM, S_F32},
     {"wb", CG_MS, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_DF},
     {"wbice", CG_MS, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_DF},
     {"gammzz1", 1, CABLEGPU_F64, CABLEGPU_KIND_STATE, S_F64},
@@ -223,6 +227,7 @@ struct cablegpu_ctx {
   int switches = 0;                // the CABLEGPU_SW_* mask the fields above come from
   int solve64 = 1;                 // soil Thomas solves: 1 FP64 direct form (default), 0 FP32 on the change
   int canopy_pool = 1;             // canopy dryLeaf passes: 1 block pool (default), 0 per lane
+  std::vector<int> h_iveg, h_isoilm;   // the tiles' plant and soil types, caller order
   int host_layout = 0;             // host buffers of step_host / forcing files: 0 caller order, 1 device order
   cudaGraphExec_t graph = nullptr;
   float graph_dels = -1.f;
@@ -288,6 +293,7 @@ void bind_device_view(cablegpu_ctx* c) {
   D.iveg = (const uint8_t*)P("iveg"); D.isoilm = (const uint8_t*)P("isoilm");
   D.vlai = (const float*)P("vlai"); D.lat = (const float*)P("lat"); D.lonphase = (const float*)P("lonphase");
   D.tbase = (const float*)P("tbase"); D.swscale = (const float*)P("swscale");
+  D.albsoil = (const float*)P("albsoil");
   D.wb = (float*)P("wb"); D.wbice = (float*)P("wbice"); D.gammzz1 = (double*)P("gammzz1");
   D.tgg = (float*)P("tgg"); D.tggsn = (float*)P("tggsn"); D.ssdn = (float*)P("ssdn"); D.smass = (float*)P("smass");
   D.sdepth = (float*)P("sdepth"); D.flags = (uint8_t*)P("flags"); D.snowd = (float*)P("snowd");
@@ -537,7 +543,10 @@ int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out)
   CG_CUDA(c, cudaMalloc(&c->dev.status, sizeof(unsigned int)));
   CG_CUDA(c, cudaMemsetAsync(c->dev.status, 0, sizeof(unsigned int), c->stream));
   // tile description
-  std::vector<float> lon(c->mp, 0.f), tb(c->mp, 288.f), sw(c->mp, 1.f);
+  std::vector<float> lon(c->mp, 0.f), tb(c->mp, 288.f), sw(c->mp, 1.f), alb(c->mp);
+  for (int i = 0; i < c->mp; ++i) alb[i] = h.soil.albsoil_vis[tiles->isoilm[i] - 1];
+  c->h_iveg.assign(tiles->iveg, tiles->iveg + c->mp);
+  c->h_isoilm.assign(tiles->isoilm, tiles->isoilm + c->mp);
   if (tiles->lonphase) std::memcpy(lon.data(), tiles->lonphase, sizeof(float) * c->mp);
   if (tiles->tbase) std::memcpy(tb.data(), tiles->tbase, sizeof(float) * c->mp);
   if (tiles->swscale) std::memcpy(sw.data(), tiles->swscale, sizeof(float) * c->mp);
@@ -549,6 +558,7 @@ int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out)
   if ((rc = cablegpu_set_field(c, cablegpu_field_id("lonphase"), lon.data()))) return rc;
   if ((rc = cablegpu_set_field(c, cablegpu_field_id("tbase"), tb.data()))) return rc;
   if ((rc = cablegpu_set_field(c, cablegpu_field_id("swscale"), sw.data()))) return rc;
+  if ((rc = cablegpu_set_field(c, cablegpu_field_id("albsoil"), alb.data()))) return rc;
   CG_CUDA(c, cudaStreamSynchronize(c->stream));
   return CABLEGPU_OK;
 }
@@ -1270,6 +1280,15 @@ int cablegpu_restart_read(cablegpu_ctx* c, const char* path, int* ktau) {
       if (rc) return rc;
     }
   }
+  // the per-tile soil albedo, where the file carries it
+  {
+    const int k = cgio::find(f, "albsoil");
+    if (k >= 0 && f.fields[k].dtype == cgio::kF32 && f.fields[k].width == 1) {
+      if (cgio::read_block(f, 0, k, host.data())) return fail(c, CABLEGPU_ERR_IO, "restart_read: read failed");
+      int rc = cablegpu_set_field(c, cablegpu_field_id("albsoil"), host.data());
+      if (rc) return rc;
+    }
+  }
   if (ktau) *ktau = f.h.ktau;
   return CABLEGPU_OK;
 }
@@ -1446,6 +1465,38 @@ int cablegpu_param_table(int table, const char* name, float* out, int n) {
   }
   if (!src || n < len) return CABLEGPU_ERR_ARG;
   std::memcpy(out, src, sizeof(float) * len);
+  return CABLEGPU_OK;
+}
+
+int cablegpu_check_tile_param(cablegpu_ctx* c, const char* name, const float* host) {
+  if (!c || !name || !host) return fail(c, CABLEGPU_ERR_ARG, "check_tile_param: null argument");
+  float tab[CG_MS * CG_NPFT];
+  const int nl = std::strcmp(name, "froot") == 0 ? CG_MS : 1;
+  bool per_pft = true;
+  if (cablegpu_param_table(0, name, tab, CG_MS * CG_NPFT) != CABLEGPU_OK) {
+    per_pft = false;
+    // the soil table in effect: with soil_thermal_fix the parameter set-up
+    // rewrites css, rhosoil and cnsd (cable_parameters.F90:2165-2227)
+    if (cablegpu_param_table(c->thermal_fix ? 2 : 1, name, tab, CG_MS * CG_NPFT) != CABLEGPU_OK)
+      return fail(c, CABLEGPU_ERR_ARG, std::string("check_tile_param: ") + name + " is not a table parameter");
+  }
+  const int ntypes = per_pft ? CG_NPFT : CG_NSOIL;
+  const std::vector<int>& type = per_pft ? c->h_iveg : c->h_isoilm;
+  for (int k = 0; k < nl; ++k) {
+    for (int i = 0; i < c->mp; ++i) {
+      const float want = tab[k * ntypes + type[i] - 1];
+      const float got = host[(size_t)k * c->mp + i];
+      if (!(std::fabs(got - want) <= 1e-6f * std::fabs(want))) {
+        char msg[320];
+        std::snprintf(msg, sizeof msg,
+                      "check_tile_param: %s of tile %d%s is %.9g, the %s type %d table value is %.9g; the kernels "
+                      "take this parameter from per-type tables", name, i + 1,
+                      nl > 1 ? (", layer " + std::to_string(k + 1)).c_str() : "", (double)got,
+                      per_pft ? "plant" : "soil", type[i], (double)want);
+        return fail(c, CABLEGPU_ERR_ARG, msg);
+      }
+    }
+  }
   return CABLEGPU_OK;
 }
 

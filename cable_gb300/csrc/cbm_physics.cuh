@@ -50,7 +50,7 @@ constexpr uint8_t CG_TS_NONFINITE = 1, CG_TS_DRYLEAF_NOCONV = 2, CG_TS_FORCING_R
 __device__ __forceinline__ bool out_of(float x, float lo, float hi) { return !(x >= lo && x <= hi); }
 
 // Number / order of the optional per-tile diagnostics (debug output).
-#define CG_NDIAG 59
+#define CG_NDIAG 63
 // Headline outputs written every step: fe fh fgpp frday tv rnet ga trad
 #define CG_NOUT 8
 
@@ -66,6 +66,7 @@ struct CgDev {
   const float* lonphase;
   const float* tbase;
   const float* swscale;
+  const float* albsoil;    // VIS bare-soil albedo, soil%albsoil(:,1)
   // prognostic state
   float* wb;         // [6] as double-FP32 pairs: hi layers 0..5, lo layers 6..11
   float* wbice;      // [6] likewise

@@ -266,7 +266,7 @@ __device__ __forceinline__ void phase_a(const CgDev& D, const CgTables* __restri
       fbeam[0] = fb; fbeam[1] = fb;
     }
     // surface_albedosn
-    float soilalb = ldf(S.albsoil_vis, so);
+    float soilalb = D.albsoil[t];
     if (iveg == LAKES) soilalb = -0.022f * (fminf(275.0f, fmaxf(260.0f, tgg[0])) - 260.0f) + 0.45f;
     if (snowd > 1.0f && iveg == LAKES) soilalb = 0.85f;
     float sfact = 0.68f;
@@ -1046,13 +1046,13 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
     if (bits) D.tile_status[t] |= bits;
   }
   if (kDiag) {
-    const int idx[37] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 18, 20, 21, 22, 32, 33, 34, 35,
-                         36, 43, 44, 45, 50, 51, 52, 53, 55, 56, 57, 58};
-    const float val[37] = {fe, fh, fev, fhv, fhs, fns, fnv, ga, tv, tscrn, qscrn, rnet, us, cduv, cdtq, epot, fes,
+    const int idx[39] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 18, 20, 21, 22, 32, 33, 34, 35,
+                         36, 43, 44, 45, 50, 51, 52, 53, 55, 56, 57, 58, 59, 60};
+    const float val[39] = {fe, fh, fev, fhv, fhs, fns, fnv, ga, tv, tscrn, qscrn, rnet, us, cduv, cdtq, epot, fes,
                            dgdtg, fpn, frday, fgpp, precis0, through, fwet, owetfac_out, potev, drybal, wetbal, ebal,
-                           tvair, qvair, swnet, lwnet, gswx[0], gswx[1], fwsoil, (float)passes_total};
+                           tvair, qvair, swnet, lwnet, gswx[0], gswx[1], fwsoil, (float)passes_total, delwc, cls};
 #pragma unroll
-    for (int i = 0; i < 37; ++i) D.diag[idx[i] * ld + t] = val[i];
+    for (int i = 0; i < 39; ++i) D.diag[idx[i] * ld + t] = val[i];
   }
 }
 
@@ -2227,11 +2227,11 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     if (bits) D.tile_status[t] |= bits;
   }
   if (kDiag) {
-    const int idx[16] = {17, 19, 23, 24, 25, 26, 27, 28, 37, 38, 39, 40, 41, 42, 46, 54};
-    const float val[16] = {fevc, fevw, -fpn - frp, fpn + frs + frp, frp + frday, frp, frs, trad, runoff_mm,
-                           rnof1 * dels, rnof2 * dels, smelt, ghflux, sghflux, wbal, (float)wbtot};
+    const int idx[18] = {17, 19, 23, 24, 25, 26, 27, 28, 37, 38, 39, 40, 41, 42, 46, 54, 61, 62};
+    const float val[18] = {fevc, fevw, -fpn - frp, fpn + frs + frp, frp + frday, frp, frs, trad, runoff_mm,
+                           rnof1 * dels, rnof2 * dels, smelt, ghflux, sghflux, wbal, (float)wbtot, frpw, frpr};
 #pragma unroll
-    for (int i = 0; i < 16; ++i) D.diag[idx[i] * ld + t] = val[i];
+    for (int i = 0; i < 18; ++i) D.diag[idx[i] * ld + t] = val[i];
   }
 }
 

@@ -11,12 +11,16 @@
 ! same derived types.  On the first call this module creates a device
 ! context for the mp tiles, uploads the tile description (veg%iveg,
 ! soil%isoilm, veg%vlai, rad%latitude) and the prognostic state the driver
-! initialised (defaults or restart file).  Every call then uploads that
-! step's met forcing, advances the device state by one step and copies the
-! per-step fluxes the driver writes every step (canopy%fe, fh, fgpp, frday,
-! tv, rnet, ga, rad%trad) back into the derived types.  The prognostic state
-! stays on the device; call cbm_gpu_state_to_host before writing a restart
-! file and cbm_gpu_finalize at the end of the run.
+! initialised (defaults or restart file), after checking the per-tile veg
+! and soil parameters against the per-type tables the kernels use.  Every
+! call then uploads that step's met forcing, advances the device state by one
+! step and copies back into the derived types everything the driver reads
+! before its next call: the eight output fluxes (canopy%fe, fh, fgpp, frday,
+! tv, rnet, ga, rad%trad), the runoff and melt rates, screen temperature,
+! carbon fluxes, energy and water terms, balances and the soil and snow
+! profiles (driver_fields_to_host).  The rest of the prognostic state stays
+! on the device; call cbm_gpu_state_to_host before writing a restart file
+! and cbm_gpu_finalize at the end of the run.
 !
 ! Build: compile cablegpu_c.F90, cablegpu_shim.F90 and this file in place of
 ! cbl_model_driver_offline.F90 and link cable_gb300/lib/libcablegpu.so.
@@ -89,6 +93,8 @@ CONTAINS
     canopy%rnet(slot_tile) = outb(:, 6)
     canopy%ga(slot_tile) = outb(:, 7)
     rad%trad(slot_tile) = outb(:, 8)
+    ! everything else the driver reads before the next call
+    CALL driver_fields_to_host(dels, bal, canopy, rad, ssnow)
   END SUBROUTINE cbm
 
 END MODULE cable_cbm_module

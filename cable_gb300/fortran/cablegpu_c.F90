@@ -73,6 +73,13 @@ MODULE cablegpu_c
       TYPE(c_ptr), VALUE :: ctx
     END FUNCTION cablegpu_synchronize
 
+    INTEGER(c_int) FUNCTION cablegpu_check_tile_param(ctx, name, host) BIND(C, name="cablegpu_check_tile_param")
+      IMPORT :: c_int, c_ptr, c_char
+      TYPE(c_ptr), VALUE :: ctx
+      CHARACTER(KIND=c_char), DIMENSION(*), INTENT(IN) :: name
+      TYPE(c_ptr), VALUE :: host
+    END FUNCTION cablegpu_check_tile_param
+
     TYPE(c_ptr) FUNCTION cablegpu_last_error(ctx) BIND(C, name="cablegpu_last_error")
       IMPORT :: c_ptr
       TYPE(c_ptr), VALUE :: ctx

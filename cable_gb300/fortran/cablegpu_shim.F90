@@ -100,7 +100,12 @@ CONTAINS
     IF (cable_user%l_new_runoff_speed) switches = switches + 256
     IF (TRIM(cable_user%diag_soil_resp) == 'OFF' .OR. TRIM(cable_user%diag_soil_resp) == 'off') &
       switches = switches + 512
-    CALL check(cablegpu_set_options(ctx, switches, 0_c_int, 0_c_int), 'set_options')
+    ! diagnostics on: the fields the driver reads after cbm() beyond the
+    ! eight output fluxes (driver_fields_to_host) are diagnostics fields
+    CALL check(cablegpu_set_options(ctx, switches, 1_c_int, 0_c_int), 'set_options')
+    ! the kernels take the veg and soil parameters from per-type tables:
+    ! refuse per-tile values that differ from them
+    CALL check_params(soil, veg)
     CALL check(cablegpu_set_host_layout(ctx, 1_c_int), 'set_host_layout')
     ALLOCATE(slot_tile(mp))
     CALL check(cablegpu_tile_order(ctx, C_LOC(slot_tile)), 'tile_order')
@@ -108,6 +113,9 @@ CONTAINS
 
     ! prognostic state (soil_snow_type, canopy, bgc, bal)
     ALLOCATE(r8(mp, ms), r4(mp, ms))
+    ! the per-tile bare-soil albedo (VIS, soil%albsoil(:,1)) of the gridded
+    ! soil file
+    r4(:, 1) = soil%albsoil(:, 1); CALL put('albsoil', C_LOC(r4))
     r8 = ssnow%wb;    CALL put('wb', C_LOC(r8))
     r8 = ssnow%wbice; CALL put('wbice', C_LOC(r8))
     r4 = ssnow%tgg;   CALL put('tgg', C_LOC(r4))
@@ -142,6 +150,123 @@ CONTAINS
     ALLOCATE(forc(mp, CABLEGPU_NFORCING), outb(mp, 8))
     DEALLOCATE(iveg, isoilm, vlai, lat, flags, r8, r4)
   END SUBROUTINE gpu_setup
+
+  ! One per-tile parameter against the library's per-type tables.
+  SUBROUTINE check_one(name, values)
+    CHARACTER(LEN=*), INTENT(IN) :: name
+    REAL, INTENT(IN) :: values(:)
+    REAL(c_float), ALLOCATABLE, TARGET :: v(:)
+    ALLOCATE(v(SIZE(values)))
+    v = values
+    CALL check(cablegpu_check_tile_param(ctx, TRIM(name) // c_null_char, C_LOC(v)), 'check_tile_param ' // name)
+    DEALLOCATE(v)
+  END SUBROUTINE check_one
+
+  ! The veg and soil parameters the kernels take from per-type tables
+  ! (init_veg_from_vegin and derived_parameters fill them per tile,
+  ! cable_parameters.F90:3277-3345, :1759-2343): each must equal its type's
+  ! table value, or the run stops with the tile that differs.
+  SUBROUTINE check_params(soil, veg)
+    USE cable_def_types_mod
+    TYPE(soil_parameter_type), INTENT(IN) :: soil
+    TYPE(veg_parameter_type), INTENT(IN) :: veg
+    INTEGER :: k
+    CALL check_one('canst1', veg%canst1); CALL check_one('dleaf', veg%dleaf); CALL check_one('ejmax', veg%ejmax)
+    CALL check_one('frac4', veg%frac4);   CALL check_one('hc', veg%hc);       CALL check_one('vbeta', veg%vbeta)
+    CALL check_one('rp20', veg%rp20);     CALL check_one('vegcf', veg%vegcf); CALL check_one('extkn', veg%extkn)
+    CALL check_one('a1gs', veg%a1gs);     CALL check_one('d0gs', veg%d0gs);   CALL check_one('alpha', veg%alpha)
+    CALL check_one('convex', veg%convex); CALL check_one('cfrd', veg%cfrd);   CALL check_one('gswmin', veg%gswmin)
+    CALL check_one('conkc0', veg%conkc0); CALL check_one('conko0', veg%conko0); CALL check_one('ekc', veg%ekc)
+    CALL check_one('eko', veg%eko);       CALL check_one('g0', veg%g0);       CALL check_one('g1', veg%g1)
+    CALL check_one('vcmax', veg%vcmax);   CALL check_one('xfang', veg%xfang); CALL check_one('shelrb', veg%shelrb)
+    CALL check_one('refl1', veg%refl(:, 1)); CALL check_one('refl2', veg%refl(:, 2))
+    CALL check_one('taul1', veg%taul(:, 1)); CALL check_one('taul2', veg%taul(:, 2))
+    CALL check_one('froot', [(veg%froot(:, k), k = 1, ms)])
+    CALL check_one('bch', soil%bch);     CALL check_one('css', soil%css);     CALL check_one('hyds', soil%hyds)
+    CALL check_one('rhosoil', soil%rhosoil); CALL check_one('sfc', soil%sfc); CALL check_one('ssat', soil%ssat)
+    CALL check_one('sucs', soil%sucs);   CALL check_one('swilt', soil%swilt); CALL check_one('cnsd', soil%cnsd)
+    CALL check_one('hsbh', soil%hsbh);   CALL check_one('ibp2', soil%ibp2);   CALL check_one('i2bp3', soil%i2bp3)
+    CALL check_one('pwb_min', soil%pwb_min)
+  END SUBROUTINE check_params
+
+  ! After each step: every field the offline driver reads from the derived
+  ! types before its next cbm() call (cable_serial.F90:594-740): the runoff
+  ! and melt rates it rescales by dels (:602-605), the screen temperature
+  ! and humidity (:607-608), the carbon fluxes of sumcflux (:713), the
+  ! energy and water fluxes, stores and balances of mass_balance /
+  ! energy_balance (:725-728; the device runs both checks, so bal%ebal,
+  ! wbal and their totals come back and check%mass_bal / check%energy_bal can
+  ! stay off) and what the output writer accumulates (:734-738): fluxes,
+  ! temperatures, the soil profiles and the snow.  The diagnostics fields hold
+  ! amounts of the step (mm) where the reference holds rates (mm/s).
+  SUBROUTINE driver_fields_to_host(dels, bal, canopy, rad, ssnow)
+    USE cable_def_types_mod
+    REAL, INTENT(IN) :: dels
+    TYPE(balances_type), INTENT(INOUT) :: bal
+    TYPE(canopy_type), INTENT(INOUT) :: canopy
+    TYPE(radiation_type), INTENT(INOUT) :: rad
+    TYPE(soil_snow_type), INTENT(INOUT) :: ssnow
+    REAL(c_float), ALLOCATABLE, TARGET :: r4(:, :)
+    REAL(c_double), ALLOCATABLE, TARGET :: r8(:, :)
+    INTEGER(c_int), ALLOCATABLE, TARGET :: flags(:)
+    ALLOCATE(r8(mp, ms), r4(mp, ms), flags(mp))
+    CALL get('fev', C_LOC(r4));    canopy%fev = r4(:, 1)
+    CALL get('fhv', C_LOC(r4));    canopy%fhv = r4(:, 1)
+    CALL get('fhs', C_LOC(r4));    canopy%fhs = r4(:, 1)
+    CALL get('fns', C_LOC(r4));    canopy%fns = r4(:, 1)
+    CALL get('fnv', C_LOC(r4));    canopy%fnv = r4(:, 1)
+    CALL get('fes', C_LOC(r4));    canopy%fes = r4(:, 1)
+    CALL get('fevc', C_LOC(r4));   canopy%fevc = r4(:, 1)
+    CALL get('fevw', C_LOC(r4));   canopy%fevw = r4(:, 1)
+    CALL get('tscrn', C_LOC(r4));  canopy%tscrn = r4(:, 1)
+    CALL get('qscrn', C_LOC(r4));  canopy%qscrn = r4(:, 1)
+    CALL get('us', C_LOC(r4));     canopy%us = r4(:, 1)
+    CALL get('cduv', C_LOC(r4));   canopy%cduv = r4(:, 1)
+    CALL get('epot', C_LOC(r4));   canopy%epot = r4(:, 1)
+    CALL get('dgdtg', C_LOC(r4));  canopy%dgdtg = r4(:, 1)
+    CALL get('fpn', C_LOC(r4));    canopy%fpn = r4(:, 1)
+    CALL get('fnpp', C_LOC(r4));   canopy%fnpp = r4(:, 1)
+    CALL get('fnee', C_LOC(r4));   canopy%fnee = r4(:, 1)
+    CALL get('fra', C_LOC(r4));    canopy%fra = r4(:, 1)
+    CALL get('frp', C_LOC(r4));    canopy%frp = r4(:, 1)
+    CALL get('frpw', C_LOC(r4));   canopy%frpw = r4(:, 1)
+    CALL get('frpr', C_LOC(r4));   canopy%frpr = r4(:, 1)
+    CALL get('frs', C_LOC(r4));    canopy%frs = r4(:, 1)
+    CALL get('delwc', C_LOC(r4));  canopy%delwc = r4(:, 1)
+    CALL get('through', C_LOC(r4)); canopy%through = r4(:, 1)
+    CALL get('precis', C_LOC(r4)); canopy%precis = r4(:, 1)
+    CALL get('fwet', C_LOC(r4));   canopy%fwet = r4(:, 1)
+    CALL get('ghflux', C_LOC(r4)); canopy%ghflux = r4(:, 1)
+    CALL get('sghflux', C_LOC(r4)); canopy%sghflux = r4(:, 1)
+    CALL get('cansto', C_LOC(r4)); canopy%cansto = r4(:, 1)
+    CALL get('runoff', C_LOC(r4)); ssnow%runoff = r4(:, 1) / dels
+    CALL get('rnof1', C_LOC(r4));  ssnow%rnof1 = r4(:, 1) / dels
+    CALL get('rnof2', C_LOC(r4));  ssnow%rnof2 = r4(:, 1) / dels
+    CALL get('smelt', C_LOC(r4));  ssnow%smelt = r4(:, 1) / dels
+    CALL get('wetfac', C_LOC(r4)); ssnow%wetfac = r4(:, 1)
+    CALL get('potev', C_LOC(r4));  ssnow%potev = r4(:, 1)
+    CALL get('cls', C_LOC(r4));    ssnow%cls = r4(:, 1)
+    CALL get('wbtot', C_LOC(r4));  ssnow%wbtot = r4(:, 1)
+    CALL get('albedo_vis', C_LOC(r4)); rad%albedo(:, 1) = r4(:, 1)
+    CALL get('albedo_nir', C_LOC(r4)); rad%albedo(:, 2) = r4(:, 1)
+    CALL get('transd', C_LOC(r4)); rad%transd = r4(:, 1)
+    CALL get('qssabs', C_LOC(r4)); rad%qssabs = r4(:, 1)
+    CALL get('ebal', C_LOC(r4));   bal%ebal = r4(:, 1)
+    CALL get('wbal', C_LOC(r4));   bal%wbal = r4(:, 1)
+    CALL get('ebal_tot', C_LOC(r8)); bal%ebal_tot = REAL(r8(:, 1))
+    CALL get('wbal_tot', C_LOC(r8)); bal%wbal_tot = REAL(r8(:, 1))
+    ! soil and snow profiles, snow and surface temperature
+    CALL get('wb', C_LOC(r8));     ssnow%wb = r8
+    CALL get('wbice', C_LOC(r8));  ssnow%wbice = r8
+    CALL get('tgg', C_LOC(r4));    ssnow%tgg = r4
+    CALL get('tggsn', C_LOC(r4));  ssnow%tggsn = r4(:, 1:msn)
+    CALL get('sdepth', C_LOC(r4)); ssnow%sdepth = r4(:, 1:msn)
+    CALL get('flags', C_LOC(flags)); ssnow%isflag = IAND(flags, 1)
+    CALL get('snowd', C_LOC(r4));  ssnow%snowd = r4(:, 1)
+    CALL get('ssdnn', C_LOC(r4));  ssnow%ssdnn = r4(:, 1)
+    CALL get('tss', C_LOC(r4));    ssnow%tss = r4(:, 1)
+    DEALLOCATE(r8, r4, flags)
+  END SUBROUTINE driver_fields_to_host
 
   ! Copies the device-resident prognostic state back into the derived types
   ! (before a restart write, cable_output.F90 / create_restart).

@@ -42,7 +42,7 @@ EXPORTS = [
     "cablegpu_restart_write", "cablegpu_restart_read", "cablegpu_forcing_file_write", "cablegpu_file_info",
     "cablegpu_run_forcing_file", "cablegpu_set_host_layout", "cablegpu_tile_order",
     "cablegpu_step_explicit", "cablegpu_step_implicit", "cablegpu_coupled_timed", "cablegpu_set_soil_solve",
-    "cablegpu_set_canopy_schedule",
+    "cablegpu_set_canopy_schedule", "cablegpu_check_tile_param",
 ]
 NOALLOC_MAX_TILES = 65536
 # soil tridiagonal solve arithmetic (cablegpu_set_soil_solve)
@@ -87,6 +87,19 @@ def switch_mask(medlyn=False, soil_thermal_fix=False, litter=False, l_rev_corr=F
             (SW_POTEV_PM if ssnow_potev == "P-M" else 0) | (SW_NEW_REDUCE_SOILEVP if l_new_reduce_soilevp else 0) |
             (SW_NEW_RUNOFF_SPEED if l_new_runoff_speed else 0) |
             (SW_DIAG_SOIL_RESP_OFF if diag_soil_resp.strip().upper() == "OFF" else 0))
+
+
+def param_table(table: int, name: str) -> np.ndarray:
+    """A built-in parameter table (cablegpu_param_table): table 0 per plant
+    type (17 values; "froot" 6 x 17, layer-major), 1 per soil type (9), 2 the
+    per-soil table with the soil_thermal_fix set applied."""
+    L = load()
+    out = np.zeros(6 * 17, np.float32)
+    rc = L.cablegpu_param_table(int(table), name.encode(), _ptr(out, C.c_float), out.size)
+    if rc != 0:
+        raise CableGPUError(rc, "param_table: no entry %r in table %d" % (name, table))
+    n = 6 * 17 if name == "froot" else (17 if table == 0 else 9)
+    return out[:n].copy()
 
 
 def forcing_file_write(path, forcing, doy0: int = 1, dels: float = 1800.0):
@@ -174,6 +187,7 @@ def load(build_if_missing: bool = True):
     L.cablegpu_set_options.argtypes = [vp, ip, ip, ip]
     L.cablegpu_set_soil_solve.argtypes = [vp, ip]
     L.cablegpu_set_canopy_schedule.argtypes = [vp, ip]
+    L.cablegpu_check_tile_param.argtypes = [vp, C.c_char_p, C.POINTER(C.c_float)]
     L.cablegpu_step.argtypes = [vp, ip, C.c_float]
     L.cablegpu_step_explicit.argtypes = [vp, ip, C.c_float, ip]
     L.cablegpu_coupled_timed.argtypes = [vp, ip, ip, C.c_float, ip, C.POINTER(C.c_float)]
@@ -369,6 +383,12 @@ class CableGPU:
         if isinstance(mode, str):
             mode = {"pool": CANOPY_POOL, "lanes": CANOPY_LANES}[mode]
         self._check(self.L.cablegpu_set_canopy_schedule(self.h, int(mode)))
+
+    def check_tile_param(self, name, values):
+        """Raises CableGPUError unless the per-tile parameter equals each
+        tile's built-in per-type table value (cablegpu_check_tile_param)."""
+        v = np.ascontiguousarray(values, np.float32)
+        self._check(self.L.cablegpu_check_tile_param(self.h, name.encode(), _ptr(v, C.c_float)))
 
     def set_synthetic_forcing(self, seed: int, doy0: int = 1):
         self._check(self.L.cablegpu_set_synthetic_forcing(self.h, int(seed), int(doy0)))

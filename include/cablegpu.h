@@ -487,6 +487,20 @@ int cablegpu_mlp_fit(const float* rows, long long ntrain, long long nval, int ep
                      unsigned long long seed, float* params_out, float* norm_out, float* losses);
 const char* cablegpu_mlp_last_error(void);
 
+/* Checks one per-tile veg or soil parameter of the driver (the arrays
+ * init_veg_from_vegin and derived_parameters fill per tile,
+ * cable_parameters.F90:3277-3345, :1759-2343; host array [mp] float in the
+ * caller's order, [6][mp] for "froot") against the value the kernels use for
+ * each tile: the built-in table entry of its plant type (iveg) or soil type
+ * (isoilm), as cablegpu_param_table gives them (the soil_thermal_fix set when
+ * that switch is on).  Returns CABLEGPU_ERR_ARG, naming the first tile that
+ * differs by more than 1e-6 relative in cablegpu_last_error, so a driver
+ * whose per-tile parameters depart from the reference's tables is refused
+ * rather than run with the tables.  name: an entry of cablegpu_param_table
+ * table 0 or 1.  The bare-soil albedo is per tile on the device (field
+ * "albsoil") and needs no check. */
+int cablegpu_check_tile_param(cablegpu_ctx* ctx, const char* name, const float* host_values);
+
 const char* cablegpu_last_error(cablegpu_ctx* ctx);
 
 #ifdef __cplusplus

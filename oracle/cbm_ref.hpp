@@ -100,6 +100,10 @@ struct Diag {
   int dryleaf_passes;            // total dryLeaf passes over the 4 MO iterations
   int dryleaf_noconv;            // MO iterations whose dryLeaf loop ended unconverged at the pass limit
   int evapfbl_err;               // MO iterations with the reference's 'oldevapfbl not right' message
+  // read by the offline driver after cbm(): canopy%delwc (mass_balance,
+  // cable_checks.F90:472-551), ssnow%cls (the balances), canopy%frpw and
+  // frpr (sumcflux)
+  R delwc, cls, frpw, frpr;
 };
 
 // ==========================================================================
@@ -1340,6 +1344,7 @@ struct CbmRef {
     d.fnee = L.fpn + frs + frp;
     d.fra = frp + L.frday;
     d.frp = frp; d.frs = frs; d.trad = trad;
+    d.frpw = frpw; d.frpr = frpr; d.delwc = delwc; d.cls = cls;
     d.albedo[0] = rad.albedo[0]; d.albedo[1] = rad.albedo[1]; d.transd = rad.transd;
     d.precis = precis; d.through = through; d.fwet = fwet; d.wetfac = wetfac; d.potev = potev;
     d.runoff = runoff; d.rnof1 = rnof1; d.rnof2 = rnof2; d.smelt = smelt;

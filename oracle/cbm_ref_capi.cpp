@@ -39,7 +39,7 @@ const char* kDiag[] = {
   "fes", "fevc", "dgdtg", "fevw", "fpn", "frday", "fgpp", "fnpp", "fnee", "fra", "frp", "frs", "trad",
   "albedo_vis", "albedo_nir", "transd", "precis", "through", "fwet", "wetfac", "potev", "runoff", "rnof1", "rnof2",
   "smelt", "ghflux", "sghflux", "drybal", "wetbal", "ebal", "wbal", "qssabs", "rniso", "vlaiw", "tvair", "qvair",
-  "swnet", "lwnet", "wbtot", "gswx_sun", "gswx_shd", "fwsoil", "dryleaf_passes", "dryleaf_noconv", "evapfbl_err",
+  "swnet", "lwnet", "wbtot", "gswx_sun", "gswx_shd", "fwsoil", "dryleaf_passes", "dryleaf_noconv", "evapfbl_err", "delwc", "cls", "frpw", "frpr",
 };
 constexpr int kNDiag = sizeof(kDiag) / sizeof(kDiag[0]);
 
@@ -94,7 +94,7 @@ void pack_diag(const Diag<R, R2>& d, double* dg, int mp, int t) {
     d.albedo[0], d.albedo[1], d.transd, d.precis, d.through, d.fwet, d.wetfac, d.potev, d.runoff, d.rnof1, d.rnof2,
     d.smelt, d.ghflux, d.sghflux, d.drybal, d.wetbal, d.ebal, d.wbal, d.qssabs, d.rniso, d.vlaiw, d.tvair, d.qvair,
     d.swnet, d.lwnet, (double)d.wbtot, d.gswx[0], d.gswx[1], d.fwsoil, (double)d.dryleaf_passes,
-    (double)d.dryleaf_noconv, (double)d.evapfbl_err,
+    (double)d.dryleaf_noconv, (double)d.evapfbl_err, d.delwc, d.cls, d.frpw, d.frpr,
   };
   for (int i = 0; i < kNDiag; ++i) dg[(size_t)i * mp + t] = v[i];
 }

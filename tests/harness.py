@@ -18,6 +18,7 @@ DIAG_MAP = {
     "drybal": "drybal", "wetbal": "wetbal", "ebal": "ebal", "wbal": "wbal", "qssabs": "qssabs", "rniso": "rniso",
     "vlaiw_d": "vlaiw", "tvair": "tvair", "qvair": "qvair", "swnet": "swnet", "lwnet": "lwnet", "wbtot": "wbtot",
     "gswx_sun": "gswx_sun", "gswx_shd": "gswx_shd", "fwsoil": "fwsoil", "dryleaf_passes": "dryleaf_passes",
+    "delwc": "delwc", "cls": "cls", "frpw": "frpw", "frpr": "frpr",
 }
 STATE_FIELDS = ["wb", "wbice", "tgg", "tggsn", "ssdn", "smass", "sdepth", "snowd", "ssdnn", "snage", "pudsto",
                 "owetfac", "rtsoil", "tss", "cansto", "cplant", "csoil", "owb", "ebal_tot", "wbal_tot"]
@@ -30,10 +31,17 @@ STATE_FIELDS = ["wb", "wbice", "tgg", "tggsn", "ssdn", "smass", "sdepth", "snowd
 # (0.008 umol CO2/m2/s, 0.03 % of a midday canopy GPP of 3.7e-4).
 FLUX_FIELDS = {"fe_d", "fh_d", "fev", "fhv", "fhs", "fns", "fnv", "ga_d", "rnet_d", "fes", "fevc", "fevw", "swnet",
                "lwnet", "qssabs", "rniso"}
-CARBON_FLUX_FIELDS = {"fgpp_d", "fpn", "frday_d", "fgpp", "frday"}
+CARBON_FLUX_FIELDS = {"fgpp_d", "fpn", "frday_d", "fgpp", "frday", "frpw", "frpr", "frp", "frs", "fnpp", "fnee"}
 CARBON_FLUX_FLOOR = 1e-7
-TEMP_FIELDS = {"tv_d", "trad_d", "tgg", "tggsn", "tss", "tvair"}
+TEMP_FIELDS = {"tv_d", "trad_d", "tgg", "tggsn", "tss", "tvair", "tscrn"}
 MOIST_FIELDS = {"wb", "wbice"}
+# water amounts of one step (mm = kg/m2): runoff and its surface / drainage
+# parts, snow melt, canopy water change, throughfall and precipitation
+# reaching the soil, the canopy store; 1e-3 relative with a 1e-3 mm floor
+WATER_FIELDS = {"runoff", "rnof1", "rnof2", "smelt", "delwc", "precis", "through", "cansto"}
+WATER_FLOOR = 1e-3
+# screen specific humidity (kg/kg): 1e-3 relative with a 1e-6 floor
+HUMID_FIELDS = {"qscrn", "qvair"}
 
 
 def tolerance(name, ref):
@@ -42,6 +50,10 @@ def tolerance(name, ref):
         return np.maximum(1e-3 * ref, 1.0)
     if name in CARBON_FLUX_FIELDS:
         return np.maximum(1e-3 * ref, CARBON_FLUX_FLOOR)
+    if name in WATER_FIELDS:
+        return np.maximum(1e-3 * ref, WATER_FLOOR)
+    if name in HUMID_FIELDS:
+        return np.maximum(1e-3 * ref, 1e-6)
     if name in TEMP_FIELDS:
         return np.full(ref.shape, 0.01)
     if name in MOIST_FIELDS:
