@@ -16,7 +16,11 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 SOURCES = ["cablegpu.cu", "phase_a.cu", "phase_b.cu", "phase_c1.cu", "phase_c2.cu", "phase_c3.cu", "tables.cpp",
            "surrogate.cu", "cgio.cpp"]
 # Per-file extra flags: the canopy phase is FP32-only and division-heavy, so
-# it uses the approximate division / exp intrinsics; radiation, soil heat and
+# it uses the approximate division / exp intrinsics, without implicit
+# multiply-add contraction (-fmad=false: its instantiations -- diagnostics,
+# surrogate, harvest, coupled -- must compute bit-identical results, and the
+# compiler's contraction choices depend on the surrounding code; its hot
+# arithmetic has explicit multiply-adds instead); radiation, soil heat and
 # soil water use the approximate (2 ulp) FP32 division, keeping IEEE square
 # root and denormals (their state updates are error-free double-FP32 or
 # FP64, and the correction-form solves are insensitive to ulp-level
@@ -30,7 +34,7 @@ SOURCES = ["cablegpu.cu", "phase_a.cu", "phase_b.cu", "phase_c1.cu", "phase_c2.c
 # block size itself is a launch-time choice (autotuned).
 EXTRA_FLAGS = {
     "phase_a.cu": ["-prec-div=false", "-DCG_MAXNREG=80"],
-    "phase_b.cu": ["--use_fast_math", "-DCG_MAXNREG=72"],
+    "phase_b.cu": ["--use_fast_math", "-fmad=false", "-DCG_MAXNREG=72"],
     "phase_c1.cu": ["-DCG_MAXNREG=128"],
     "phase_c2.cu": ["-prec-div=false", "-DCG_MAXNREG=80", "-DCG_MAXNREG_S64=128"],
     "phase_c3.cu": ["-prec-div=false", "-DCG_MAXNREG=112", "-DCG_MAXNREG_S64=128"],

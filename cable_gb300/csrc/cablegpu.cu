@@ -226,7 +226,7 @@ struct cablegpu_ctx {
   int medlyn = 0, diag = 0, capture_forcing = 0, thermal_fix = 0, litter = 0, rev_corr = 0;
   int switches = 0;                // the CABLEGPU_SW_* mask the fields above come from
   int solve64 = 1;                 // soil Thomas solves: 1 FP64 direct form (default), 0 FP32 on the change
-  int canopy_pool = 1;             // canopy dryLeaf passes: 1 block pool (default), 0 per lane
+  int canopy_pool = 0;             // canopy dryLeaf passes: 0 per lane (default), 1 block pool
   std::vector<int> h_iveg, h_isoilm;   // the tiles' plant and soil types, caller order
   int host_layout = 0;             // host buffers of step_host / forcing files: 0 caller order, 1 device order
   cudaGraphExec_t graph = nullptr;

@@ -207,11 +207,18 @@ __device__ __forceinline__ float psis(float zeta) {
   return z * stable + (1.0f - z) * unstable;
 }
 
+// The canopy kernel is built without implicit multiply-add contraction
+// (-fmad=false): the compiler's choice of which products to fuse depends on
+// the code around them, so it differs between the kernel's instantiations
+// (diagnostics on or off, the surrogate's and coupled variants), which must
+// compute identical results.  Its hot arithmetic below is written with
+// explicit fused multiply-adds (__fmaf_rn) instead.
+
 // Positive root of a*x^2 + b*x + c = 0 as the reference writes it,
 // (-b + sqrt(max(0, b^2 - 4ac))) / (2a), evaluated without cancellation:
 // for b > 0 the algebraically identical 2c / (-b - sqrt(...)) is used.
 __device__ __forceinline__ float qroot(float a, float b, float c) {
-  float disc = sqrtf(fmaxf(0.0f, b * b - 4.0f * c * a));
+  float disc = sqrtf(fmaxf(0.0f, __fmaf_rn(b, b, -4.0f * c * a)));
   if (b > 0.0f) {
     float den = -b - disc;
     return (den != 0.0f) ? (2.0f * c) / den : 0.0f;
@@ -219,41 +226,51 @@ __device__ __forceinline__ float qroot(float a, float b, float c) {
   return (-b + disc) / (2.0f * a);
 }
 
-// cbl_photosynthesis.F90:52-213 for one leaf (masks applied by the caller)
+// cbl_photosynthesis.F90:52-213 for one leaf (masks applied by the caller):
+// the Rubisco-, RuBP- and sink-limited net assimilation as roots of the
+// reference's three quadratics, their coefficients grouped into
+// multiply-adds (1 - csx gs, the common term vcmxt3 cx2 / 2 + cx1 (rdx -
+// vcmxt4), and gmf factored out of the sink constant term).
 __device__ __forceinline__ float photosynthesis_leaf(float csx, float cx1, float cx2, float gswmin, float rdx,
                                                      float vcmxt3, float vcmxt4, float vx3, float vx4, float gs_coeff,
                                                      float fwsoil) {
   const float effc4 = 4000.0f;
   const float gmf = gswmin * fwsoil / RGSWC;
+  const float one_m = __fmaf_rn(-csx, gs_coeff, 1.0f);   // 1 - csx gs_coeff
+  const float hc2 = 0.5f * cx2;
   float anrubisco = 0.f, anrubp, ansink = 0.f, ci, coef0, coef1, coef2;
-  coef2 = gmf + gs_coeff * (vcmxt3 - (rdx - vcmxt4));
-  coef1 = (1.0f - csx * gs_coeff) * (vcmxt3 + vcmxt4 - rdx) + gmf * (cx1 - csx) -
-          gs_coeff * (vcmxt3 * cx2 / 2.0f + cx1 * (rdx - vcmxt4));
-  coef0 = -(1.0f - csx * gs_coeff) * (vcmxt3 * cx2 / 2.0f + cx1 * (rdx - vcmxt4)) - gmf * cx1 * csx;
+  float tt = __fmaf_rn(vcmxt3, hc2, cx1 * (rdx - vcmxt4));
+  coef2 = __fmaf_rn(gs_coeff, vcmxt3 - (rdx - vcmxt4), gmf);
+  coef1 = __fmaf_rn(one_m, vcmxt3 + vcmxt4 - rdx, __fmaf_rn(gmf, cx1 - csx, -gs_coeff * tt));
+  coef0 = __fmaf_rn(-one_m, tt, -(gmf * cx1) * csx);
   if (fabsf(coef2) > 1.0e-9f && fabsf(coef1) < 1.0e-9f) anrubisco = 99999.0f;
   if (fabsf(coef2) < 1.e-9f && fabsf(coef1) >= 1e-9f) {
     ci = fmaxf(0.0f, -coef0 / coef1);
-    anrubisco = vcmxt3 * (ci - cx2 / 2.0f) / (ci + cx1) + vcmxt4 - rdx;
+    anrubisco = __fmaf_rn(vcmxt3, (ci - hc2) / (ci + cx1), vcmxt4 - rdx);
   }
   if (fabsf(coef2) >= 1.e-9f) {
     ci = fmaxf(0.0f, qroot(coef2, coef1, coef0));
-    anrubisco = vcmxt3 * (ci - cx2 / 2.0f) / (ci + cx1) + vcmxt4 - rdx;
+    anrubisco = __fmaf_rn(vcmxt3, (ci - hc2) / (ci + cx1), vcmxt4 - rdx);
   }
-  coef2 = gmf + gs_coeff * (vx3 - (rdx - vx4));
-  coef1 = (1.0f - csx * gs_coeff) * (vx3 + vx4 - rdx) + gmf * (cx2 - csx) - gs_coeff * (vx3 * cx2 / 2.0f + cx2 * (rdx - vx4));
-  coef0 = -(1.0f - csx * gs_coeff) * (vx3 * cx2 / 2.0f + cx2 * (rdx - vx4)) - gmf * cx2 * csx;
+  tt = __fmaf_rn(vx3, hc2, cx2 * (rdx - vx4));
+  coef2 = __fmaf_rn(gs_coeff, vx3 - (rdx - vx4), gmf);
+  coef1 = __fmaf_rn(one_m, vx3 + vx4 - rdx, __fmaf_rn(gmf, cx2 - csx, -gs_coeff * tt));
+  coef0 = __fmaf_rn(-one_m, tt, -(gmf * cx2) * csx);
   anrubp = 99999.0f;
   if (fabsf(coef2) < 1.e-9f && fabsf(coef1) >= 1.e-9f) {
     ci = fmaxf(0.0f, -coef0 / coef1);
-    anrubp = vx3 * (ci - cx2 / 2.0f) / (ci + cx2) + vx4 - rdx;
+    anrubp = __fmaf_rn(vx3, (ci - hc2) / (ci + cx2), vx4 - rdx);
   }
   if (fabsf(coef2) >= 1.e-9f) {
     ci = fmaxf(0.0f, qroot(coef2, coef1, coef0));
-    anrubp = vx3 * (ci - cx2 / 2.0f) / (ci + cx2) + vx4 - rdx;
+    anrubp = __fmaf_rn(vx3, (ci - hc2) / (ci + cx2), vx4 - rdx);
   }
+  // sink: coef1 = gmf + gs (rdx - vcmxt3 / 2) + effc4 vcmxt4 (1 - gs csx),
+  // coef0 = gmf (rdx - vcmxt3 / 2 - csx effc4 vcmxt4)
+  const float u = __fmaf_rn(-0.5f, vcmxt3, rdx), e4v = effc4 * vcmxt4;
   coef2 = gs_coeff;
-  coef1 = gmf + gs_coeff * (rdx - 0.5f * vcmxt3) + effc4 * vcmxt4 - gs_coeff * csx * effc4 * vcmxt4;
-  coef0 = -gmf * csx * effc4 * vcmxt4 + (rdx - 0.5f * vcmxt3) * gmf;
+  coef1 = __fmaf_rn(e4v, one_m, __fmaf_rn(gs_coeff, u, gmf));
+  coef0 = gmf * __fmaf_rn(-csx, e4v, u);
   if (fabsf(coef2) < 1.0e-9f && fabsf(coef1) < 1.0e-9f) ansink = 99999.0f;
   if (fabsf(coef2) < 1.e-9f && fabsf(coef1) >= 1.e-9f) ansink = -coef0 / coef1;
   if (fabsf(coef2) >= 1.e-9f) ansink = qroot(coef2, coef1, coef0);
@@ -265,23 +282,23 @@ __device__ __forceinline__ float photosynthesis_leaf(float csx, float cx1, float
 // is computed the same wherever the pass runs.
 __device__ __forceinline__ float ej3x(float parx, float alpha, float convex, float x) {
   float s = __fmaf_rn(alpha, parx, x);
-  return fmaxf(0.0f, 0.25f * ((s - sqrtf(s * s - 4.0f * convex * alpha * parx * x)) / (2.0f * convex)));
+  return fmaxf(0.0f, 0.25f * ((s - sqrtf(__fmaf_rn(s, s, -(4.0f * convex * alpha * parx) * x))) / (2.0f * convex)));
 }
 __device__ __forceinline__ float ej4x(float parx, float alpha, float convex, float x) {
   float s = __fmaf_rn(alpha, parx, x);
-  return fmaxf(0.0f, (s - sqrtf(s * s - 4.0f * convex * alpha * parx * x)) / (2.0f * convex));
+  return fmaxf(0.0f, (s - sqrtf(__fmaf_rn(s, s, -(4.0f * convex * alpha * parx) * x))) / (2.0f * convex));
 }
 __device__ __forceinline__ float xvcmxt4(float x) {
-  return exp2f(0.1f * x - 2.5f) / ((1.0f + expf(0.3f * (13.0f - x))) * (1.0f + expf(0.3f * (x - 36.0f))));
+  return exp2f(__fmaf_rn(0.1f, x, -2.5f)) / ((1.0f + expf(0.3f * (13.0f - x))) * (1.0f + expf(0.3f * (x - 36.0f))));
 }
 __device__ __forceinline__ float xvcmxt3(float x) {
   float num = 1.17461f * expf((73637.0f / (RGAS * TREFK)) * (1.f - TREFK / x));
-  float den = 1.0f + expf((486.0f * x - 149252.0f) / (RGAS * x));
+  float den = 1.0f + expf(__fmaf_rn(486.0f, x, -149252.0f) / (RGAS * x));
   return fmaxf(0.0f, num / den);
 }
 __device__ __forceinline__ float xejmxt3(float x) {
   float num = 1.16715f * expf((50300.0f / (RGAS * TREFK)) * (1.f - TREFK / x));
-  float den = 1.0f + expf((495.0f * x - 152044.0f) / (RGAS * x));
+  float den = 1.0f + expf(__fmaf_rn(495.0f, x, -152044.0f) / (RGAS * x));
   return fmaxf(0.0f, num / den);
 }
 

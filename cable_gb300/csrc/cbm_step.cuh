@@ -654,7 +654,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
         const float sc = scalex[0] + scalex[1];
         feat[0] = qcan_par[0]; feat[1] = qcan_par[1]; feat[2] = tlfx; feat[3] = dsx; feat[4] = ca;
         feat[5] = ldk(c_pft.vcmax[v]) * sc; feat[6] = ldk(c_pft.ejmax[v]) * (1.0f - ldk(c_pft.frac4[v])) * sc; feat[7] = P.medlyn ? ldk(c_pft.g1[v]) : ldk(c_pft.a1gs[v]);
-        feat[8] = fwsoil; feat[9] = vlaiw; feat[10] = us; feat[11] = tvair;
+        feat[8] = fwsoil; feat[9] = vlaiw; feat[10] = ua; feat[11] = tk;
       }
       bool sur_try = false;
       float tlf_sur = tlfx;

@@ -84,14 +84,14 @@ __device__ __forceinline__ bool dl_pass(const DlCtx& c, DlState& s, const float 
   float conkot = ldk(c_pft.conko0[v]) * expf(ldk(c_pft.eko[v]) * arr);
   const float tlfxx = tlfx;
   float cx1 = conkct * (1.0f + 0.21f / conkot);
-  float cx2 = 2.0f * GAM0 * (1.0f + GAM1 * tdiff + GAM2 * tdiff * tdiff);
+  float cx2 = 2.0f * GAM0 * __fmaf_rn(__fmaf_rn(GAM2, tdiff, GAM1), tdiff, 1.0f);
 #pragma unroll
   for (int l = 0; l < 2; ++l) {
     float par = c.qcan_par[l] * 4.6e-6f;
     const float alpha = ldk(c_pft.alpha[v]), convex = ldk(c_pft.convex[v]), cfrd = ldk(c_pft.cfrd[v]);
     vx3[l] = ej3x(par * (1.0f - frac4), alpha, convex, ejmxt3[l]);
     vx4[l] = ej4x(par * frac4, alpha, convex, vcmxt4[l]);
-    rdx[l] = cfrd * vcmxt3[l] + cfrd * vcmxt4[l];
+    rdx[l] = __fmaf_rn(cfrd, vcmxt3[l], cfrd * vcmxt4[l]);
   }
   const float gswmin_p = ldk(c_pft.gswmin[v]);
   float gswmin[2] = {fmaxf(1.e-6f, c.scalex[0] * gswmin_p), fmaxf(1.e-6f, c.scalex[1] * gswmin_p)};
@@ -151,8 +151,8 @@ __device__ __forceinline__ bool dl_pass(const DlCtx& c, DlState& s, const float 
   float sgh = gh[0] + gh[1];
   const float hcx = __fmaf_rn(-pc, sum_rad_gradis, __fsub_rn(sum_rad_rniso, ecx)) * sgh / (ghr[0] + ghr[1]);
   s.tlfx = c.tvair + hcx / (cpr * sgh);
-  const float rnx = sum_rad_rniso - cpr * (s.tlfx - c.tk) * sum_rad_gradis;
-  s.dsx = fmaxf(c.dva + c.dsatdk * (s.tlfx - c.tvair), 0.0f);
+  const float rnx = __fmaf_rn(-(cpr * (s.tlfx - c.tk)), sum_rad_gradis, sum_rad_rniso);
+  s.dsx = fmaxf(__fmaf_rn(c.dsatdk, s.tlfx - c.tvair, c.dva), 0.0f);
   const float deltlf = tlfxx - s.tlfx;
   s.abs_deltlf = fabsf(deltlf);
   s.ecx = ecx;

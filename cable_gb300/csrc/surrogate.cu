@@ -418,9 +418,9 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_kernel(FwdArgs a) {
 // every tile.  The inputs are formed here from the radiation kernel's
 // hand-off record (work_a, one array per word so each load is coalesced) and
 // the plant-type tables, exactly as the canopy kernel sees them when that
-// iteration starts: leaf and canopy air at tk, neutral stability
-// (cbl_friction_vel.F90 with psim(0) = 0), fwsoil_calc_std
-// (cbl_fwsoil.F90:13-38).  Persistent: each CTA walks 128-tile chunks.
+// iteration starts: leaf and canopy air at tk, the wind speed and air
+// temperature of the forcing, fwsoil_calc_std (cbl_fwsoil.F90:13-38).
+// Persistent: each CTA walks 128-tile chunks.
 struct InferArgs {
   const float* work_a;   // [CG_NA][ld]
   const uint8_t* iveg;
@@ -461,8 +461,8 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_soa_kernel(InferArgs a) {
   // the record words the inputs need, loaded one chunk ahead so the loads
   // of chunk c + gridDim.x are in flight while chunk c's tensor-core passes
   // run
-  constexpr int NW = 19;
-  constexpr int words[NW] = {0, 1, 2, 3, 5, 8, 11, 13, 32, 33, 38, 39, 46, 47, 48, 49, 50, 51, 0};
+  constexpr int NW = 17;
+  constexpr int words[NW] = {0, 1, 2, 3, 5, 8, 32, 33, 38, 39, 46, 47, 48, 49, 50, 51, 0};
   auto fetch = [&](int c, float* w, int& iv, int& so) {
     const int t = c * 128 + s;
     if (c < nchunks && t < a.mp) {
@@ -485,21 +485,19 @@ __global__ void __launch_bounds__(128, 1) mlp_infer_soa_kernel(InferArgs a) {
     if (valid) {
       const CgPftTable& V = a.tables->pft;
       const CgSoilTable& S = a.tables->soil;
-      const float tk = w[0], qv = w[1], pmb = w[2], ua = w[3], ca = w[4], vlaiw = w[5], z0m = w[6];
-      const float zref_uv = w[7], sc = w[8] + w[9];
+      const float tk = w[0], qv = w[1], pmb = w[2], ua = w[3], ca = w[4], vlaiw = w[5], sc = w[6] + w[7];
       const float dva = (qsatfjh(tk - TFRZ, pmb) - qv) * RMAIR / RMH2O * pmb * 100.0f;
       // fwsoil from the soil liquid water the radiation kernel recorded
       const float swilt = S.swilt[so], sfc = S.sfc[so];
       float rwater = 0.f;
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k)
-        rwater += V.froot[k][iv] * fmaxf(1.0e-9f, fminf(1.0f, (w[12 + k] - swilt) / (sfc - swilt)));
+        rwater += V.froot[k][iv] * fmaxf(1.0e-9f, fminf(1.0f, (w[10 + k] - swilt) / (sfc - swilt)));
       rwater = fmaxf(1.0e-9f, rwater);
       const float fwsoil = a.medlyn ? fmaxf(1.0e-4f, fminf(1.0f, rwater)) : fmaxf(1.0e-9f, fminf(1.0f, V.vbeta[iv] * rwater));
-      const float us1 = fminf(fmaxf(1.e-6f, VONK * fmaxf(ua, UMIN) / logf(zref_uv / z0m)), 10.0f);
-      const float f[NIN] = {w[10], w[11], tk, fmaxf(dva, 0.0f), ca, V.vcmax[iv] * sc,
+      const float f[NIN] = {w[8], w[9], tk, fmaxf(dva, 0.0f), ca, V.vcmax[iv] * sc,
                             V.ejmax[iv] * (1.0f - V.frac4[iv]) * sc, a.medlyn ? V.g1[iv] : V.a1gs[iv],
-                            fwsoil, vlaiw, us1, tk};
+                            fwsoil, vlaiw, ua, tk};
 #pragma unroll
       for (int q = 0; q < NIN; ++q) xn[q] = (f[q] - nrm[q]) * nrm[12 + q];
     } else {

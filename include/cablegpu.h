@@ -204,12 +204,15 @@ int cablegpu_set_soil_solve(cablegpu_ctx* ctx, int mode);
 /* Scheduling of the canopy kernel's dryLeaf passes (cbl_dryLeaf.F90:10-666,
  * up to 20 passes per tile and Monin-Obukhov iteration, converging after
  * different numbers of passes):
- *   CABLEGPU_CANOPY_POOL  (default) the tiles of a thread block iterate as a
- *                         pool in shared memory: each round runs one pass of
- *                         every tile still iterating, one tile per thread,
- *                         so threads whose tile converged take other tiles'
- *                         passes
- *   CABLEGPU_CANOPY_LANES each thread runs its own tile's passes
+ *   CABLEGPU_CANOPY_LANES (default) each thread runs its own tile's passes
+ *   CABLEGPU_CANOPY_POOL  the tiles of a thread block iterate as a pool in
+ *                         shared memory: each round runs one pass of every
+ *                         tile still iterating, one tile per thread (a warp
+ *                         vote and one atomic per warp build the next
+ *                         round's list), so threads whose tile converged take
+ *                         other tiles' passes; slower on GB300 (the slot
+ *                         traffic and the per-round barrier cost more than
+ *                         the idle lanes it recovers)
  * Results are identical; only the speed differs.  Applies to the steps issued
  * after the call. */
 #define CABLEGPU_CANOPY_POOL 0
@@ -430,8 +433,8 @@ int cablegpu_param_table(int table, const char* name, float* out, int n);
  * leaf temperature at entry (K), leaf-surface vapour pressure deficit (Pa),
  * air CO2 (mol/mol), canopy vcmax and C3 jmax (mol/m2/s, scaled by the
  * sunlit+shaded leaf scaling), stomatal slope (a1gs, or g1 under medlyn),
- * soil-moisture stress factor, LAI, friction velocity (m/s), within-canopy
- * air temperature (K).  Targets (columns 12-14): stomatal conductance to
+ * soil-moisture stress factor, LAI, wind speed at the reference height
+ * (m/s), air temperature (K).  Targets (columns 12-14): stomatal conductance to
  * water (mol/m2/s), net assimilation (mol/m2/s), leaf temperature change
  * over the iteration (K).  Column 15 is unused. */
 
