@@ -2187,11 +2187,14 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   }
 
   // driver rescaling (cable_serial.F90:602-605) and balances (cable_checks.F90)
-  const float runoff_mm = (rnof1 + rnof2) * dels;
+  // rounded operations throughout: the compiler may not fuse a product into
+  // the sums here differently in the kernels with and without diagnostics
+  const float runoff_mm = __fmul_rn(__fadd_rn(rnof1, rnof2), dels);
+  const float evap_mm = __fdiv_rn(__fmul_rn(__fadd_rn(__fadd_rn(fevw, fevc), __fdiv_rn(fes, cls)), dels), rlam);
   double owb = D.owb[t];
   if (P.ktau == 1) owb = wbtot;
   const double delwb = wbtot - owb;
-  const float wbal = (float)((double)(precip - delwc - snowd + osnowd - runoff_mm - (fevw + fevc + fes / cls) * dels / rlam) - delwb);
+  const float wbal = (float)((double)(precip - delwc - snowd + osnowd - runoff_mm - evap_mm) - delwb);
   double wbal_tot = D.wbal_tot[t];
   if (P.ktau == 1) wbal_tot = 0.0;
   if (P.ktau > 10) wbal_tot += (double)wbal;

@@ -18,7 +18,8 @@ DIAG_MAP = {
     "drybal": "drybal", "wetbal": "wetbal", "ebal": "ebal", "wbal": "wbal", "qssabs": "qssabs", "rniso": "rniso",
     "vlaiw_d": "vlaiw", "tvair": "tvair", "qvair": "qvair", "swnet": "swnet", "lwnet": "lwnet", "wbtot": "wbtot",
     "gswx_sun": "gswx_sun", "gswx_shd": "gswx_shd", "fwsoil": "fwsoil", "dryleaf_passes": "dryleaf_passes",
-    "delwc": "delwc", "cls": "cls", "frpw": "frpw", "frpr": "frpr",
+    "delwc": "delwc", "cls": "cls", "frpw": "frpw", "frpr": "frpr", "rnof1": "rnof1", "rnof2": "rnof2",
+    "smelt": "smelt",
 }
 STATE_FIELDS = ["wb", "wbice", "tgg", "tggsn", "ssdn", "smass", "sdepth", "snowd", "ssdnn", "snage", "pudsto",
                 "owetfac", "rtsoil", "tss", "cansto", "cplant", "csoil", "owb", "ebal_tot", "wbal_tot"]

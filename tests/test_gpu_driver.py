@@ -112,5 +112,10 @@ def test_per_tile_soil_albedo():
         g.close()
     for k in runs[0]:
         np.testing.assert_array_equal(runs[0][k], runs[1][k], err_msg=k)
-    bare = ts.iveg >= 14
+    # barren and urban tiles off ice soil: a lake's soil albedo follows its
+    # temperature (surface_albedosn) and an ice soil's is fixed
+    bare = ((ts.iveg == 14) | (ts.iveg == 15)) & (ts.isoilm != 9)
+    assert bare.sum() > 10
     assert np.all(runs[2]["albedo_vis"][0][bare] > runs[0]["albedo_vis"][0][bare])
+    rest = (ts.iveg == 16) | (ts.isoilm == 9)
+    np.testing.assert_array_equal(runs[2]["albedo_vis"][0][rest], runs[0]["albedo_vis"][0][rest])
