@@ -378,8 +378,8 @@ class CableGPU:
         self._check(self.L.cablegpu_set_soil_solve(self.h, int(mode)))
 
     def set_canopy_schedule(self, mode):
-        """Canopy dryLeaf passes: CANOPY_POOL (default) or CANOPY_LANES, or
-        "pool" / "lanes"."""
+        """Canopy dryLeaf passes: CANOPY_LANES (default) or CANOPY_POOL, or
+        "lanes" / "pool"."""
         if isinstance(mode, str):
             mode = {"pool": CANOPY_POOL, "lanes": CANOPY_LANES}[mode]
         self._check(self.L.cablegpu_set_canopy_schedule(self.h, int(mode)))
