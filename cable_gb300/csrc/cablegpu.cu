@@ -495,7 +495,7 @@ int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out)
   CG_CUDA(c, cudaMalloc(&c->d_tables, sizeof(CgTables)));
   CG_CUDA(c, cudaMemcpyAsync(c->d_tables, &h, sizeof(CgTables), cudaMemcpyHostToDevice, c->stream));
   upload_canopy_pft_table(h.pft, c->stream);
-  prepare_canopy_kernels();
+  prepare_phase_kernels();
   CG_CUDA(c, cudaGetLastError());
   // device tile order
   {
@@ -1127,6 +1127,51 @@ int cablegpu_get_config(cablegpu_ctx* c, int* order, int* block5) {
   if (!c) return CABLEGPU_ERR_ARG;
   if (order) *order = c->order;
   if (block5) std::copy(c->block, c->block + 5, block5);
+  return CABLEGPU_OK;
+}
+
+int cablegpu_tune_blocks(cablegpu_ctx* c, int ktau0, int nsteps, float dels, int* block5_out, float* ms_out) {
+  if (!c || nsteps < 1 || nsteps > 64 || !(dels > 0.f)) return fail(c, CABLEGPU_ERR_ARG, "tune_blocks: 1..64 steps, dels > 0");
+  CG_CUDA(c, cudaSetDevice(c->device));
+  // every per-tile field lives in the arena: a copy of it taken before the
+  // candidates' steps and put back after each leaves the context's state as
+  // it was; the status word and the surrogate's counters are read back and
+  // restored the same way
+  char* snap = nullptr;
+  CG_CUDA(c, cudaMalloc(&snap, c->arena_bytes));
+  unsigned int status0 = 0;
+  int rc = CABLEGPU_OK;
+  auto cp = [&](void* dst, const void* src, size_t n, cudaMemcpyKind k) {
+    if (rc) return;
+    cudaError_t e = cudaMemcpyAsync(dst, src, n, k, c->stream);
+    if (e != cudaSuccess) rc = fail(c, CABLEGPU_ERR_CUDA, std::string("tune_blocks: ") + cudaGetErrorString(e));
+  };
+  unsigned long long stats0[2] = {0ull, 0ull};
+  cp(snap, c->arena, c->arena_bytes, cudaMemcpyDeviceToDevice);
+  cp(&status0, c->dev.status, sizeof(unsigned int), cudaMemcpyDeviceToHost);
+  if (c->d_sur_stats) cp(stats0, c->d_sur_stats, sizeof(stats0), cudaMemcpyDeviceToHost);
+  if (!rc && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = fail(c, CABLEGPU_ERR_CUDA, "tune_blocks: sync");
+  const int cand_block[4] = {32, 64, 128, 256};
+  int saved[5], pick[5];
+  std::copy(c->block, c->block + 5, saved);
+  std::copy(c->block, c->block + 5, pick);
+  float per[5] = {1e30f, 1e30f, 1e30f, 1e30f, 1e30f};
+  for (int b = 0; b < 4 && !rc; ++b) {
+    std::fill(c->block, c->block + 5, cand_block[b]);
+    float ms[6];
+    rc = cablegpu_phase_timed(c, ktau0, nsteps, dels, ms);
+    cp(c->arena, snap, c->arena_bytes, cudaMemcpyDeviceToDevice);
+    for (int k = 0; k < 5 && !rc; ++k)
+      if (ms[k] < per[k]) { per[k] = ms[k]; pick[k] = cand_block[b]; }
+  }
+  cp(c->dev.status, &status0, sizeof(unsigned int), cudaMemcpyHostToDevice);
+  if (c->d_sur_stats) cp(c->d_sur_stats, stats0, sizeof(stats0), cudaMemcpyHostToDevice);
+  if (!rc && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = fail(c, CABLEGPU_ERR_CUDA, "tune_blocks: sync");
+  cudaFree(snap);
+  std::copy(rc ? saved : pick, (rc ? saved : pick) + 5, c->block);
+  if (rc) return rc;
+  if (block5_out) std::copy(pick, pick + 5, block5_out);
+  if (ms_out) *ms_out = per[0] + per[1] + per[2] + per[3] + per[4];
   return CABLEGPU_OK;
 }
 

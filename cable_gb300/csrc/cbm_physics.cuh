@@ -308,12 +308,18 @@ __device__ __forceinline__ float xejmxt3(float x) {
 // multiply-adds per step.  For 1e-30 < |x| < 1e30 (the FP32 normal range of
 // the seed); the soil systems' pivots and saturation deficits are far inside
 // it.  Tested against CUDA's FP64 division (tests/test_fp64_reciprocal.py).
-__device__ __forceinline__ double rcp64(double x) {
-  double r = (double)__fdividef(1.0f, (float)x);
+// xf: an FP32 value within ~1e-6 relative of x that seeds the iteration
+// (x rounded to FP32, or an FP32 shadow of the quantity computed beside it);
+// the two steps take a seed error of 2^-20 below the FP64 rounding too.
+// rcp64_from: the same two steps from a given FP32 seed r0 ~ 1/x.
+__device__ __forceinline__ double rcp64_from(double x, float r0) {
+  double r = (double)r0;
   r = fma(r, fma(-x, r, 1.0), r);
   r = fma(r, fma(-x, r, 1.0), r);
   return r;
 }
+__device__ __forceinline__ double rcp64(double x, float xf) { return rcp64_from(x, __fdividef(1.0f, xf)); }
+__device__ __forceinline__ double rcp64(double x) { return rcp64(x, (float)x); }
 
 // cbl_trimb.F90:17-53 in FP64, as the reference solves both soil systems,
 // for their diffusion form: the Thomas algorithm on
@@ -328,23 +334,35 @@ __device__ __forceinline__ double rcp64(double x) {
 // divided by its own pivot; back substitution.  Row 1's two divisions by
 // b(1) are one reciprocal here, every division a multiplication by an FP64
 // reciprocal (rcp64; the same value to an FP64 ulp or two), and g(k)
-// overwrites rhs(k), so only e and the solution are live in FP64.
+// overwrites rhs(k), so only e and the solution are live in FP64.  The
+// reciprocals' seeds come from the pivots' FP32 shadow: the same recursion
+// pf(k) = (1 - a(k) - c(k)) - a(k) ef(k-1), ef(k) = c(k) / pf(k) in FP32
+// beside the FP64 one (within a few FP32 ulps of it: the system is
+// diagonally dominant, |e| < 1), which spares an FP64-to-FP32 conversion
+// per pivot; the FP64 values do not depend on the seed beyond its
+// accuracy.
 template <int N>
 __device__ __forceinline__ void trimb64(const float* a, const float* c, double db0, double* rhs) {
   double e[N - 1];
-  const double ib = rcp64((1.0 - (double)a[0] - (double)c[0]) + db0);
+  const double p0 = (1.0 - (double)a[0] - (double)c[0]) + db0;
+  float rf = __fdividef(1.0f, (float)p0);
+  const double ib = rcp64_from(p0, rf);
+  float ef = c[0] * rf;
   e[0] = (double)c[0] * ib;
   rhs[0] = rhs[0] * ib;
 #pragma unroll
   for (int k = 1; k < N - 1; ++k) {
     const double ak = a[k], ck = c[k];
-    const double temp = rcp64((1.0 - ak - ck) - ak * e[k - 1]);
+    rf = __fdividef(1.0f, (1.0f - a[k] - c[k]) - a[k] * ef);
+    const double temp = rcp64_from((1.0 - ak - ck) - ak * e[k - 1], rf);
+    ef = c[k] * rf;
     e[k] = ck * temp;
     rhs[k] = (rhs[k] - ak * rhs[k - 1]) * temp;
   }
   {
     const double ak = a[N - 1], ck = c[N - 1];
-    rhs[N - 1] = (rhs[N - 1] - ak * rhs[N - 2]) * rcp64((1.0 - ak - ck) - ak * e[N - 2]);
+    rf = __fdividef(1.0f, (1.0f - a[N - 1] - c[N - 1]) - a[N - 1] * ef);
+    rhs[N - 1] = (rhs[N - 1] - ak * rhs[N - 2]) * rcp64_from((1.0 - ak - ck) - ak * e[N - 2], rf);
   }
 #pragma unroll
   for (int k = N - 2; k >= 0; --k) rhs[k] = rhs[k] - e[k] * rhs[k + 1];

@@ -1876,22 +1876,26 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     if constexpr (kS64) {
       // Implicit diffusion of the liquid fraction wblf = (wb - wbice) /
       // (ssat - wbice) on the reference's direct form
-      // (cbl_smoisturev.F90:200-262, :422-427): the state after the explicit
-      // drainage and wblf in FP64, the matrix coefficients
-      // dtt z3 = dels / (zse (ssat - wbice)) z3 in FP32 (bulk arithmetic,
-      // widened exactly), the top layers' infiltration source and the
-      // elimination in FP64 (trimb64), then wb = wblf (ssat - wbice) + wbice
-      // in FP64, stored as double-FP32.
-      double wbid[CG_MS], satd[CG_MS], rd[CG_MS];
+      // (cbl_smoisturev.F90:200-262, :422-427).  The liquid water after the
+      // explicit drainage, wb + dwd - wbice, is formed in double-FP32 from
+      // the state (error-free FP32 operations, 48-bit significand) and
+      // widened; wblf, the top layers' infiltration source and the
+      // elimination (trimb64) are FP64; then wb = wblf (ssat - wbice) +
+      // wbice, the product in FP64, stored as double-FP32.  The pore space
+      // ssat - wbice is the FP32 value (ssat is REAL in the reference) in
+      // wblf, in dtt = dels / (zse (ssat - wbice)) and in the product, so
+      // the scaling in and out of wblf is exactly inverse.  The matrix
+      // coefficients dtt z3 are FP32 (bulk arithmetic, widened exactly).
+      double satd[CG_MS], rd[CG_MS];
       float xf[CG_MS], dtt[CG_MS];
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k) {
-        wbid[k] = df_to_double(wbice[k]);
-        const double wbd = df_to_double(wb[k]) + (double)dwd[k];
-        satd[k] = (double)ssat - wbid[k];
-        rd[k] = (wbd - wbid[k]) * rcp64(satd[k]);
-        xf[k] = (float)rd[k];
-        dtt[k] = dels / (zse[k] * (ssat - wbicef[k]));
+        const float sat = ssat - wbicef[k];
+        const df32 liq = df_add(df_add(wb[k], dwd[k]), df32{-wbice[k].hi, -wbice[k].lo});
+        satd[k] = (double)sat;
+        rd[k] = df_to_double(liq) * rcp64(satd[k], sat);
+        xf[k] = liq.hi / sat;   // the conductivity's weighting, FP32
+        dtt[k] = dels / (zse[k] * sat);
       }
       float a[CG_MS], c[CG_MS];
       a[0] = 0.f; c[CG_MS - 1] = 0.f;
@@ -1910,7 +1914,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
       trimb64<CG_MS>(a, c, 0.0, rd);
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k) {
-        wb[k] = df_from_double(rd[k] * satd[k] + wbid[k]);
+        wb[k] = df_add(df_from_double(rd[k] * satd[k]), wbice[k]);
         wbf[k] = wb[k].hi;
       }
     } else {

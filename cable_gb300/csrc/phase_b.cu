@@ -40,12 +40,14 @@ void launch_variant(cudaStream_t s, const CgDev& D, const CgTables* T, const Ste
 }
 
 template <bool kHarvest, bool kSur, bool kCoupled>
-void set_pool_smem() {
+void prepare_variant() {
   const int bytes = dlp::smem_bytes(kPoolMaxBlock, kSur);
   cudaFuncSetAttribute(cbm_phase_b_kernel<false, kHarvest, kSur, kCoupled, true>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(cbm_phase_b_kernel<true, kHarvest, kSur, kCoupled, true>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  prefer_max_l1(cbm_phase_b_kernel<false, kHarvest, kSur, kCoupled, false>);
+  prefer_max_l1(cbm_phase_b_kernel<true, kHarvest, kSur, kCoupled, false>);
 }
 }  // namespace
 
@@ -76,10 +78,10 @@ void launch_phase_b_sur(bool diag, cudaStream_t s, const CgDev& D, const CgTable
 }
 
 void prepare_canopy_kernels() {
-  set_pool_smem<false, false, false>();
-  set_pool_smem<false, false, true>();
-  set_pool_smem<true, false, false>();
-  set_pool_smem<false, true, false>();
+  prepare_variant<false, false, false>();
+  prepare_variant<false, false, true>();
+  prepare_variant<true, false, false>();
+  prepare_variant<false, true, false>();
 }
 
 void upload_canopy_pft_table(const CgPftTable& pft, cudaStream_t s) {

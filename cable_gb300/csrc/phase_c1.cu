@@ -2,5 +2,6 @@
 #define CG_PHASE phase_c1
 #define CG_PHASE_KERNEL cbm_phase_c1_kernel
 #define CG_PHASE_LAUNCH launch_phase_c1
+#define CG_PHASE_PREPARE prepare_phase_c1
 #define CG_PHASE_COUPLED 1
 #include "phase_kernels.cuh"

@@ -3,6 +3,7 @@
 #define CG_PHASE phase_c3
 #define CG_PHASE_KERNEL cbm_phase_c3_kernel
 #define CG_PHASE_LAUNCH launch_phase_c3
+#define CG_PHASE_PREPARE prepare_phase_c3
 #define CG_PHASE_COUPLED 1
 #define CG_PHASE_SOLVE 1
 #include "phase_kernels.cuh"

@@ -40,9 +40,31 @@ void launch_phase_c3(bool diag, cudaStream_t s, const CgDev& D, const CgTables* 
 
 // the canopy kernel's constant-memory copy of the plant-type table
 void upload_canopy_pft_table(const CgPftTable& pft, cudaStream_t s);
-// sets the canopy kernels' shared-memory limit for the dryLeaf pool (once per
-// device, before the first launch)
+// sets the canopy kernels' shared-memory limit for the dryLeaf pool and the
+// L1 preference of the others (once per device, before the first launch)
 void prepare_canopy_kernels();
+// the L1 preference of the other phases' kernels (prepare_phase_kernels)
+void prepare_phase_a();
+void prepare_phase_c1();
+void prepare_phase_c2();
+void prepare_phase_c3();
+// The step kernels use no shared memory; their register spills and local
+// arrays are served by L1.  Without a preference an SM keeps the
+// L1 / shared-memory split of the kernel it ran before, so after a kernel
+// with a large shared-memory footprint (the surrogate network, the canopy's
+// dryLeaf block pool) the next ones ran with a small L1.  The largest L1
+// split is their stated preference.
+template <class K>
+void prefer_max_l1(K* kernel) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxL1);
+}
+inline void prepare_phase_kernels() {
+  prepare_phase_a();
+  prepare_canopy_kernels();
+  prepare_phase_c1();
+  prepare_phase_c2();
+  prepare_phase_c3();
+}
 
 #ifdef CG_PHASE
 // CG_PHASE_COUPLED 1: the phase has a second instantiation for the coupled
@@ -91,6 +113,23 @@ void launch_instance(bool diag, cudaStream_t s, const CgDev& D, const CgTables* 
   else CG_PHASE_KERNEL<false, false, kS64><<<grid, block, 0, s>>>(D, T, P, clock);
 }
 }  // namespace
+
+void CG_PHASE_PREPARE() {
+  prefer_max_l1(CG_PHASE_KERNEL<false, false, false>);
+  prefer_max_l1(CG_PHASE_KERNEL<true, false, false>);
+#if CG_PHASE_COUPLED
+  prefer_max_l1(CG_PHASE_KERNEL<false, true, false>);
+  prefer_max_l1(CG_PHASE_KERNEL<true, true, false>);
+#endif
+#if CG_PHASE_SOLVE
+  prefer_max_l1(CG_PHASE_KERNEL<false, false, true>);
+  prefer_max_l1(CG_PHASE_KERNEL<true, false, true>);
+#if CG_PHASE_COUPLED
+  prefer_max_l1(CG_PHASE_KERNEL<false, true, true>);
+  prefer_max_l1(CG_PHASE_KERNEL<true, true, true>);
+#endif
+#endif
+}
 
 void CG_PHASE_LAUNCH(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
                      const int* clock, int block) {

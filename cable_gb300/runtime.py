@@ -42,7 +42,7 @@ EXPORTS = [
     "cablegpu_restart_write", "cablegpu_restart_read", "cablegpu_forcing_file_write", "cablegpu_file_info",
     "cablegpu_run_forcing_file", "cablegpu_set_host_layout", "cablegpu_tile_order",
     "cablegpu_step_explicit", "cablegpu_step_implicit", "cablegpu_coupled_timed", "cablegpu_set_soil_solve",
-    "cablegpu_set_canopy_schedule", "cablegpu_check_tile_param",
+    "cablegpu_set_canopy_schedule", "cablegpu_check_tile_param", "cablegpu_tune_blocks",
 ]
 NOALLOC_MAX_TILES = 65536
 # soil tridiagonal solve arithmetic (cablegpu_set_soil_solve)
@@ -200,6 +200,7 @@ def load(build_if_missing: bool = True):
     L.cablegpu_step_host.argtypes = [vp, ip, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.cablegpu_set_blocks.argtypes = [vp, C.POINTER(ip)]
     L.cablegpu_get_config.argtypes = [vp, C.POINTER(ip), C.POINTER(ip)]
+    L.cablegpu_tune_blocks.argtypes = [vp, ip, ip, C.c_float, C.POINTER(ip), C.POINTER(C.c_float)]
     L.cablegpu_autotune.argtypes = [C.POINTER(_Tiles), ip, ip, ip, C.POINTER(ip), C.POINTER(ip), C.POINTER(C.c_float)]
     L.cablegpu_launch_count.argtypes = [vp]
     L.cablegpu_launch_count.restype = C.c_longlong
@@ -541,6 +542,15 @@ class CableGPU:
         tried, acc = C.c_longlong(), C.c_longlong()
         self._check(self.L.cablegpu_surrogate_stats(self.h, C.byref(tried), C.byref(acc), int(reset)))
         return int(tried.value), int(acc.value)
+
+    def tune_blocks(self, ktau0=1, nsteps=4, dels=1800.0):
+        """Times block sizes 32..256 of each step kernel on this context's own
+        tiles and state (restored afterwards), keeps the fastest; returns
+        (blocks, ms per step)."""
+        b = (C.c_int * 5)()
+        ms = C.c_float()
+        self._check(self.L.cablegpu_tune_blocks(self.h, int(ktau0), int(nsteps), float(dels), b, C.byref(ms)))
+        return list(b), ms.value
 
     def set_blocks(self, blocks):
         b = (C.c_int * 5)(*[int(x) for x in blocks])

@@ -344,6 +344,18 @@ long long cablegpu_launch_count(cablegpu_ctx* ctx);
  * the tile order the context was built with and the current block sizes. */
 int cablegpu_set_blocks(cablegpu_ctx* ctx, const int* block5);
 int cablegpu_get_config(cablegpu_ctx* ctx, int* order, int* block5);
+/* Block sizes tuned on the context itself: times block sizes 32, 64, 128
+ * and 256 of each step kernel over `nsteps` steps (1..64) from step ktau0 of
+ * length dels on the context's own tiles, current state and forcing source,
+ * keeps each kernel's fastest (cablegpu_set_blocks) and returns them and the
+ * step time (ms) they give.  The state is copied before the timed steps and
+ * put back after each candidate (one temporary device copy of the context's
+ * fields), so the context's state, outputs and status are as before the
+ * call; results never depend on the block sizes.  Unlike cablegpu_autotune,
+ * which times a cold-started sample without snow, this sees the tiles'
+ * actual snow layers and soil state.  No counterpart in the reference
+ * (scheduling, not physics). */
+int cablegpu_tune_blocks(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, int* block5_out, float* ms_out);
 /* Autotuner: times tile orders 0-3 and block sizes 32, 64, 128, 256 of each
  * step kernel on an evenly strided sample of `sample_tiles` of the tiles
  * (synthetic forcing, nsteps timed steps per candidate) and returns the

@@ -1,7 +1,13 @@
-"""The soil solver's FP64 reciprocal (rcp64 in cbm_physics.cuh: Newton-Raphson
-from the FP32 reciprocal) against CUDA's FP64 division on the GPU: within 2
-units in the last place and a relative error below 4.5e-16 on 2^22 values
-over 1e-20..1e20 and over the soil systems' pivot range."""
+"""The soil solver's FP64 arithmetic on the GPU: its reciprocal (rcp64 in
+cbm_physics.cuh: Newton-Raphson from the FP32 reciprocal) against CUDA's FP64
+division, within 2 units in the last place and a relative error below
+4.5e-16 on 2^22 values over 1e-20..1e20 and over the soil systems' pivot
+range; and its Thomas elimination (trimb64, reciprocals seeded from the
+pivots' FP32 shadow) against the same elimination in long double on the
+host, on 2^18 six-row and 2^18 nine-row systems shaped like the soil heat
+and moisture systems: its largest error (relative to each system's largest
+value) at most twice that of the host's double elimination with IEEE
+division, the reference's arithmetic."""
 import os
 import subprocess
 import tempfile
@@ -20,4 +26,13 @@ def test_rcp64_matches_cuda_fp64_division():
         subprocess.run([B._nvcc(), "-O3", "-std=c++17"] + B.ARCH + ["-I", B.CSRC,
                         os.path.join(HERE, "kernels", "fp64_reciprocal.cu"), "-o", exe], check=True)
         r = subprocess.run([exe, "2", "4.5e-16"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_trimb64_matches_long_double_elimination():
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "fp64_thomas")
+        subprocess.run([B._nvcc(), "-O3", "-std=c++17"] + B.ARCH + ["-I", B.CSRC,
+                        os.path.join(HERE, "kernels", "fp64_thomas.cu"), "-o", exe], check=True)
+        r = subprocess.run([exe, "2.0"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
