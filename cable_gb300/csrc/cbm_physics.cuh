@@ -174,10 +174,12 @@ __device__ __forceinline__ df32 df_mul(df32 a, float c) {
 // a - b rounded to FP32
 __device__ __forceinline__ float df_sub(df32 a, df32 b) { return (a.hi - b.hi) + (a.lo - b.lo); }
 __device__ __forceinline__ bool df_lt(df32 a, df32 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
-__device__ __forceinline__ double df_to_double(df32 a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ double f2d(float x);
+__device__ __forceinline__ float d2f(double x);
+__device__ __forceinline__ double df_to_double(df32 a) { return f2d(a.hi) + f2d(a.lo); }
 __device__ __forceinline__ df32 df_from_double(double d) {
-  const float hi = (float)d;
-  return {hi, (float)(d - (double)hi)};
+  const float hi = d2f(d);
+  return {hi, d2f(d - f2d(hi))};
 }
 __device__ __forceinline__ float pow4(float x) { float y = x * x; return y * y; }
 __device__ __forceinline__ float fsignf(float a, float b) { return signbit(b) ? -fabsf(a) : fabsf(a); }
@@ -302,6 +304,43 @@ __device__ __forceinline__ float xejmxt3(float x) {
   return fmaxf(0.0f, num / den);
 }
 
+// FP32 <-> FP64 conversions on the integer pipe.  GB300 issues the
+// conversion instructions at the FP64 rate (a warp's conversion occupies the
+// FP64 pipe as long as a fused multiply-add), and the soil kernels' FP64
+// solves widen every FP32 coefficient and right-hand side and round every
+// result.  These build the other format's bit pattern from the IEEE-754
+// fields instead: float -> double moves the 8-bit exponent (rebiased by
+// 1023 - 127 = 896) and the 23-bit fraction into place; double -> float
+// rebiases, keeps 23 fraction bits and rounds to nearest, ties to even, on
+// the 29 bits dropped (a carry out of the fraction increments the exponent,
+// as rounding requires).  Zero is handled in place; subnormal, infinite and
+// NaN inputs, and doubles outside the float normal range, take the
+// hardware conversion, so the results are bitwise those of the conversion
+// instructions for every input (tests/test_fp64_reciprocal.py).
+__device__ __forceinline__ double f2d(float x) {
+  const unsigned int b = __float_as_uint(x);
+  const unsigned int mag = b & 0x7fffffffu;
+  if (mag - 1u >= 0x7f7fffffu) {               // mag == 0 or mag >= 0x7f800000: zero, inf, NaN
+    if (mag == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
+    return (double)x;
+  }
+  if (mag < 0x00800000u) return (double)x;    // subnormal
+  const unsigned int hi = ((mag >> 3) + 0x38000000u) | (b & 0x80000000u);
+  return __hiloint2double((int)hi, (int)(b << 29));
+}
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned int hi = (unsigned int)__double2hiint(x), lo = (unsigned int)__double2loint(x);
+  const unsigned int mh = hi & 0x7fffffffu;
+  if (mh - (897u << 20) >= ((1151u - 897u) << 20)) {   // exponent outside [897, 1150]
+    if ((mh | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+    return (float)x;
+  }
+  unsigned int f = ((mh - (896u << 20)) << 3) | (lo >> 29);
+  const unsigned int rem = lo & 0x1fffffffu;
+  f += (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u;
+  return __uint_as_float(f | (hi & 0x80000000u));
+}
+
 // 1/x in FP64 by Newton-Raphson iteration on f(r) = 1/r - x, seeded with the
 // FP32 reciprocal of x: each step r <- r + r (1 - x r) squares the relative
 // error (~2^-22 -> ~2^-44 -> below the FP64 rounding), two fused
@@ -313,13 +352,13 @@ __device__ __forceinline__ float xejmxt3(float x) {
 // the two steps take a seed error of 2^-20 below the FP64 rounding too.
 // rcp64_from: the same two steps from a given FP32 seed r0 ~ 1/x.
 __device__ __forceinline__ double rcp64_from(double x, float r0) {
-  double r = (double)r0;
+  double r = f2d(r0);
   r = fma(r, fma(-x, r, 1.0), r);
   r = fma(r, fma(-x, r, 1.0), r);
   return r;
 }
 __device__ __forceinline__ double rcp64(double x, float xf) { return rcp64_from(x, __fdividef(1.0f, xf)); }
-__device__ __forceinline__ double rcp64(double x) { return rcp64(x, (float)x); }
+__device__ __forceinline__ double rcp64(double x) { return rcp64(x, d2f(x)); }
 
 // cbl_trimb.F90:17-53 in FP64, as the reference solves both soil systems,
 // for their diffusion form: the Thomas algorithm on
@@ -344,15 +383,15 @@ __device__ __forceinline__ double rcp64(double x) { return rcp64(x, (float)x); }
 template <int N>
 __device__ __forceinline__ void trimb64(const float* a, const float* c, double db0, double* rhs) {
   double e[N - 1];
-  const double p0 = (1.0 - (double)a[0] - (double)c[0]) + db0;
-  float rf = __fdividef(1.0f, (float)p0);
+  const double p0 = (1.0 - f2d(a[0]) - f2d(c[0])) + db0;
+  float rf = __fdividef(1.0f, d2f(p0));
   const double ib = rcp64_from(p0, rf);
   float ef = c[0] * rf;
-  e[0] = (double)c[0] * ib;
+  e[0] = f2d(c[0]) * ib;
   rhs[0] = rhs[0] * ib;
 #pragma unroll
   for (int k = 1; k < N - 1; ++k) {
-    const double ak = a[k], ck = c[k];
+    const double ak = f2d(a[k]), ck = f2d(c[k]);
     rf = __fdividef(1.0f, (1.0f - a[k] - c[k]) - a[k] * ef);
     const double temp = rcp64_from((1.0 - ak - ck) - ak * e[k - 1], rf);
     ef = c[k] * rf;
@@ -360,7 +399,7 @@ __device__ __forceinline__ void trimb64(const float* a, const float* c, double d
     rhs[k] = (rhs[k] - ak * rhs[k - 1]) * temp;
   }
   {
-    const double ak = a[N - 1], ck = c[N - 1];
+    const double ak = f2d(a[N - 1]), ck = f2d(c[N - 1]);
     rf = __fdividef(1.0f, (1.0f - a[N - 1] - c[N - 1]) - a[N - 1] * ef);
     rhs[N - 1] = (rhs[N - 1] - ak * rhs[N - 2]) * rcp64_from((1.0 - ak - ck) - ak * e[N - 2], rf);
   }

@@ -1600,11 +1600,11 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
       if constexpr (kS64) {
         double rd[CG_MS];
 #pragma unroll
-        for (int k = 1; k < CG_MS; ++k) rd[k] = tgg[k];
-        rd[0] = (double)(tgg[0] + (ga - tgg[0] * dgdtg) * dtg0);
-        trimb64<CG_MS>(a, c, -(double)dgdtg * (double)dtg0, rd);
+        for (int k = 1; k < CG_MS; ++k) rd[k] = f2d(tgg[k]);
+        rd[0] = f2d(tgg[0] + (ga - tgg[0] * dgdtg) * dtg0);
+        trimb64<CG_MS>(a, c, -f2d(dgdtg) * f2d(dtg0), rd);
 #pragma unroll
-        for (int k = 0; k < CG_MS; ++k) tgg[k] = (float)rd[k];
+        for (int k = 0; k < CG_MS; ++k) tgg[k] = d2f(rd[k]);
       } else {
         float b[CG_MS], r[CG_MS];
 #pragma unroll
@@ -1643,13 +1643,13 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
       if constexpr (kS64) {
         double rd[9];
 #pragma unroll
-        for (int k = 1; k < 9; ++k) rd[k] = x[k];
-        rd[0] = (double)(x[0] + (ga - x[0] * dgdtg) * dtg0);
-        trimb64<9>(a, c, -(double)dgdtg * (double)dtg0, rd);
+        for (int k = 1; k < 9; ++k) rd[k] = f2d(x[k]);
+        rd[0] = f2d(x[0] + (ga - x[0] * dgdtg) * dtg0);
+        trimb64<9>(a, c, -f2d(dgdtg) * f2d(dtg0), rd);
 #pragma unroll
-        for (int k = 0; k < 3; ++k) tggsn[k] = (float)rd[k];
+        for (int k = 0; k < 3; ++k) tggsn[k] = d2f(rd[k]);
 #pragma unroll
-        for (int k = 0; k < CG_MS; ++k) tgg[k] = (float)rd[3 + k];
+        for (int k = 0; k < CG_MS; ++k) tgg[k] = d2f(rd[3 + k]);
       } else {
         float b[9], r[9];
 #pragma unroll
@@ -1892,7 +1892,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
       for (int k = 0; k < CG_MS; ++k) {
         const float sat = ssat - wbicef[k];
         const df32 liq = df_add(df_add(wb[k], dwd[k]), df32{-wbice[k].hi, -wbice[k].lo});
-        satd[k] = (double)sat;
+        satd[k] = f2d(sat);
         rd[k] = df_to_double(liq) * rcp64(satd[k], sat);
         xf[k] = liq.hi / sat;   // the conductivity's weighting, FP32
         dtt[k] = dels / (zse[k] * sat);
@@ -1910,7 +1910,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
         c[k - 2] = -dtt[k - 2] * z3;
       }
 #pragma unroll
-      for (int k = 0; k < 3; ++k) rd[k] = rd[k] + (double)(dtt[k] * fwtop[k] / DLIQ);
+      for (int k = 0; k < 3; ++k) rd[k] = rd[k] + f2d(dtt[k] * fwtop[k] / DLIQ);
       trimb64<CG_MS>(a, c, 0.0, rd);
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k) {

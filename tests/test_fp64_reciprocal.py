@@ -7,7 +7,9 @@ pivots' FP32 shadow) against the same elimination in long double on the
 host, on 2^18 six-row and 2^18 nine-row systems shaped like the soil heat
 and moisture systems: its largest error (relative to each system's largest
 value) at most twice that of the host's double elimination with IEEE
-division, the reference's arithmetic."""
+division, the reference's arithmetic; and its FP32 <-> FP64 conversions on
+the integer pipe (f2d, d2f), bit for bit equal to the hardware conversion
+instructions on 2^23 inputs of every class."""
 import os
 import subprocess
 import tempfile
@@ -35,4 +37,13 @@ def test_trimb64_matches_long_double_elimination():
         subprocess.run([B._nvcc(), "-O3", "-std=c++17"] + B.ARCH + ["-I", B.CSRC,
                         os.path.join(HERE, "kernels", "fp64_thomas.cu"), "-o", exe], check=True)
         r = subprocess.run([exe, "2.0"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_integer_pipe_conversions_equal_the_hardware_conversions():
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "fp64_convert")
+        subprocess.run([B._nvcc(), "-O3", "-std=c++17"] + B.ARCH + ["-I", B.CSRC,
+                        os.path.join(HERE, "kernels", "fp64_convert.cu"), "-o", exe], check=True)
+        r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
