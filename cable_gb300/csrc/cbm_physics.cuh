@@ -309,24 +309,28 @@ __device__ __forceinline__ float xejmxt3(float x) {
 // FP64 pipe as long as a fused multiply-add), and the soil kernels' FP64
 // solves widen every FP32 coefficient and right-hand side and round every
 // result.  These build the other format's bit pattern from the IEEE-754
-// fields instead: float -> double moves the 8-bit exponent (rebiased by
-// 1023 - 127 = 896) and the 23-bit fraction into place; double -> float
+// fields instead.  f2d: float -> double moves the 8-bit exponent (rebiased
+// by 1023 - 127 = 896) and the 23-bit fraction into place, exactly, with no
+// conversion instruction at all (a fallback in a branch was if-converted by
+// the compiler, which then issued the conversion for every value);
+// infinities and NaNs keep their class (the exponent field is rebiased to
+// all ones), zeros their sign, and subnormal floats, which the soil
+// systems' coefficients and states never come near (their magnitudes are
+// above 1e-30), become zero of the same sign.  d2f: double -> float
 // rebiases, keeps 23 fraction bits and rounds to nearest, ties to even, on
 // the 29 bits dropped (a carry out of the fraction increments the exponent,
-// as rounding requires).  Zero is handled in place; subnormal, infinite and
-// NaN inputs, and doubles outside the float normal range, take the
-// hardware conversion, so the results are bitwise those of the conversion
-// instructions for every input (tests/test_fp64_reciprocal.py).
+// as rounding requires); zero is handled in place and doubles outside the
+// float normal range (and infinities, NaNs) take the hardware conversion in
+// a branch that stays a branch.  Both are bitwise the conversion
+// instructions' results for every input but f2d's subnormals
+// (tests/test_fp64_reciprocal.py).
 __device__ __forceinline__ double f2d(float x) {
   const unsigned int b = __float_as_uint(x);
   const unsigned int mag = b & 0x7fffffffu;
-  if (mag - 1u >= 0x7f7fffffu) {               // mag == 0 or mag >= 0x7f800000: zero, inf, NaN
-    if (mag == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
-    return (double)x;
-  }
-  if (mag < 0x00800000u) return (double)x;    // subnormal
-  const unsigned int hi = ((mag >> 3) + 0x38000000u) | (b & 0x80000000u);
-  return __hiloint2double((int)hi, (int)(b << 29));
+  const bool zero = mag < 0x00800000u;                 // zero or subnormal
+  unsigned int hi = (mag >> 3) + (mag >= 0x7f800000u ? 0x70000000u : 0x38000000u);
+  hi = (zero ? 0u : hi) | (b & 0x80000000u);
+  return __hiloint2double((int)hi, zero ? 0 : (int)(b << 29));
 }
 __device__ __forceinline__ float d2f(double x) {
   const unsigned int hi = (unsigned int)__double2hiint(x), lo = (unsigned int)__double2loint(x);

