@@ -301,10 +301,35 @@ def canopy_issue(mp, canopy_ms, sm_mhz):
         return None
     achieved = n * mp / (canopy_ms / 1e3)
     peak = 152 * 4 * sm_mhz * 1e6
+    lanes = profile_figure("canopy_threads_per_warp_instruction")
     return {"kernel": "canopy", "bound": "issue", "achieved": achieved, "peak": peak,
             "unit": "warp instructions/s", "frac": achieved / peak,
+            "lane_weighted_frac": None if lanes is None else achieved / peak * lanes / 32.0,
             "source": "ncu smsp__inst_executed.sum per tile (profiles/cbm_step_snow_grid.md) x tiles / "
                       "CUDA-event kernel time; peak at the sampled median SM clock"}
+
+
+def soil_fp64(mp, kernels_ms, sm_mhz):
+    """The FP64 soil kernels against their bound, the FP64 pipe: FP64-pipe
+    warp instructions per tile-step from the committed ncu summary times the
+    tiles, over each kernel's event-timed duration, against one warp
+    instruction per 64 cycles per SM sub-partition (152 SMs x 4) at the SM
+    clock sampled during the run."""
+    out = {}
+    if not sm_mhz:
+        return None
+    peak = 152 * 4 * sm_mhz * 1e6 / 64
+    for key, fig in (("soil_heat", "soil_heat_fp64_warp_instructions_per_tile_step"),
+                     ("soil_water", "soil_water_fp64_warp_instructions_per_tile_step")):
+        n, ms = profile_figure(fig), kernels_ms.get(key)
+        if n is None or not ms:
+            continue
+        a = n * mp / (ms / 1e3)
+        out[key] = {"achieved": a, "peak": peak, "unit": "FP64 warp instructions/s", "frac": a / peak}
+    if out:
+        out["source"] = ("ncu sass__inst_executed_per_opcode (DFMA, DADD, DMUL, F2F) per tile "
+                         "(profiles/cbm_step_snow_grid.md) x tiles / CUDA-event kernel time")
+    return out or None
 
 
 def surrogate_arm(args, d, ts, plain_value, tuned):
@@ -591,6 +616,7 @@ def run_gb300(args):
                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
                "clocks": clk, "gpu_launches": int(launches),
                "canopy_issue": canopy_issue(args.mp, roof["kernels_ms"].get("canopy"), (clk or {}).get("sm_mhz")),
+               "soil_fp64": soil_fp64(args.mp, roof["kernels_ms"], (clk or {}).get("sm_mhz")),
                "step_kernels_ms": step_ms, "variants": variants, "surrogate": sur, "coupled": coupled}
         print(json.dumps(out))
     d.close()
