@@ -45,7 +45,7 @@ METRIC = "tile-timesteps/sec on 1 GB300: surrogate vs plain GPU cbm() at stated 
 # layers; the scalar state; the FP64 balance accumulators), the static
 # per-tile parameters read (32 B) and the output fluxes written (32 B);
 # forcing is generated in-kernel.  (The state this library actually carries
-# is leaner, 584 B: gammzz for layer 1 only, albedo from the soil table.)
+# is leaner, 588 B: gammzz carried for layer 1 only.)
 ALGO_BYTES_PER_TILE_STEP = 2 * 280 + 32 + 32
 
 

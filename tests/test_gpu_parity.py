@@ -330,16 +330,19 @@ def test_pipelined_host_io_step_equals_set_forcing_step_get(runtime):
     b.close()
 
 
-def test_site5_full_year_against_oracle(oracle, runtime):
+@pytest.mark.parametrize("solve", ["fp64", "fp32_change"])
+def test_site5_full_year_against_oracle(oracle, runtime, solve):
     """The benchmark's site configuration over a full year (5 tiles, PFTs
     1, 2, 5, 6, 9, soil type 2, 17,520 half-hour steps, replayed as CUDA
-    graphs) against the FP64 oracle on the same synthetic forcing: no drift
-    in soil temperature or moisture from the FP32 correction-form solves and
-    the double-FP32 soil water, and the cumulative energy and water balance
+    graphs) against the FP64 oracle on the same synthetic forcing, with the
+    FP64 soil solves (the default) and with the FP32 change-form option: no
+    drift in soil temperature or moisture from either solve or from the
+    double-FP32 soil water, and the cumulative energy and water balance
     residuals stay as closed as the oracle's."""
     R = runtime
     ts = W.site5(nsteps=17520)
     g = R.from_tileset(ts)
+    g.set_soil_solve(solve)
     g.run(1, 17520)
     g.synchronize()
     gs = {k: g.get(k) for k in ("wb", "wbice", "tgg", "snowd", "ebal_tot", "wbal_tot", "cansto", "csoil", "cplant")}
@@ -347,8 +350,13 @@ def test_site5_full_year_against_oracle(oracle, runtime):
     st = oracle.init_state(ts, 0)
     oracle.run(ts, st, 17520, precision=0)
     os_ = oracle.split_state(st)
-    # measured over the year: tgg 0.005 K, wb 8e-7, ebal_tot 1.5, wbal_tot 8e-5,
-    # csoil 0.14 (of 623) -- the same size as the REAL=FP32 oracle's own drift
+    # measured over the year (FP32 change form): tgg 0.005 K, wb 8e-7,
+    # ebal_tot 1.5, wbal_tot 8e-5, csoil 0.14 (of 623) -- the same size as
+    # the REAL=FP32 oracle's own drift
+    print("site5 year, %s solves: tgg %.3g K, wb %.3g, ebal_tot %.3g, wbal_tot %.3g, csoil %.3g" % (
+        solve, np.abs(gs["tgg"] - os_["tgg"]).max(), np.abs(gs["wb"] - os_["wb"]).max(),
+        np.abs(gs["ebal_tot"] - os_["ebal_tot"]).max(), np.abs(gs["wbal_tot"] - os_["wbal_tot"]).max(),
+        np.abs(gs["csoil"] - os_["csoil"]).max()))
     assert np.abs(gs["tgg"] - os_["tgg"]).max() < 0.02                  # K after a year
     assert np.abs(gs["wb"] - os_["wb"]).max() < 1e-5                    # m3/m3 after a year
     assert np.abs(gs["wbice"] - os_["wbice"]).max() < 1e-5
@@ -360,7 +368,8 @@ def test_site5_full_year_against_oracle(oracle, runtime):
     np.testing.assert_allclose(gs["cplant"], os_["cplant"], rtol=1e-3, atol=0.5)
 
 
-def test_snow_grid_full_year_against_oracle(oracle, runtime):
+@pytest.mark.parametrize("solve", ["fp64", "fp32_change"])
+def test_snow_grid_full_year_against_oracle(oracle, runtime, solve):
     """256 snow_grid tiles (40 % snow-covered at the start, air 250-300 K)
     over a year, against the FP64 oracle.  Snow layering and melt are
     threshold events: two FP32 builds of the reference algorithm (the
@@ -368,12 +377,14 @@ def test_snow_grid_full_year_against_oracle(oracle, runtime):
     each flip a different 2-4 tiles by tens of kg/m2 of snow over the
     year, and 0-2 tiles by more than 0.1 K of soil temperature, so snow
     depth is checked as the fraction of tiles within 1 kg/m2 and soil
-    temperature as a count of flipped tiles plus the RMS of the others.  The water balance stays as closed as the FP64 oracle's
-    (flux-form soil water update) and soil moisture and temperature do not
-    drift."""
+    temperature as a count of flipped tiles plus the RMS of the others.  The
+    water balance stays as closed as the FP64 oracle's (with the FP32
+    change-form option, thanks to its flux-form soil water update) and soil
+    moisture and temperature do not drift; both soil solves."""
     R = runtime
     ts = W.snow_grid(mp=256, nsteps=17520)
     g = R.from_tileset(ts)
+    g.set_soil_solve(solve)
     g.run(1, 17520)
     g.synchronize()
     gs = {k: np.asarray(g.get(k), np.float64) for k in ("wb", "tgg", "snowd", "wbal_tot", "csoil", "cplant")}
@@ -386,6 +397,10 @@ def test_snow_grid_full_year_against_oracle(oracle, runtime):
     # 2.2e-4, snow depth within 1 kg/m2 on 252 of 256 tiles; soil
     # temperature: 0-2 tiles flipped beyond 0.1 K (the FP32 oracle builds:
     # 0-2), the rest within 0.01 K RMS
+    dt0 = np.abs(gs["tgg"] - o["tgg"])
+    print("snow_grid year, %s solves: wbal_tot rms %.3g mm, wb rms %.3g, tgg flipped %d, snowd within 1 kg/m2 %.4f" % (
+        solve, rms("wbal_tot"), rms("wb"), int((dt0.max(axis=0) > 0.1).sum()),
+        float(np.mean(np.abs(gs["snowd"] - o["snowd"]) <= 1.0))))
     assert rms("wbal_tot") < 0.05                                       # mm over the year
     assert rms("wb") < 5e-4                                             # m3/m3
     dt = np.abs(gs["tgg"] - o["tgg"])
