@@ -57,7 +57,7 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="snow_grid", choices=["snow_grid", "grid"])
     p.add_argument("--mp", type=int, default=4_000_000)
-    p.add_argument("--e2e-steps", type=int, default=64)
+    p.add_argument("--e2e-steps", type=int, default=256)
     p.add_argument("--cpu-sample-tiles", type=int, default=100_000)
     p.add_argument("--cpu-sample-steps", type=int, default=48)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -484,6 +484,65 @@ def run_gb300(args):
         g.run(ktau, 2, dels)   # graph re-capture with the tuned blocks
         g.synchronize()
         ktau += 2
+    # --- end to end through the C ABI with host buffers: every step uploads
+    # its forcing from pinned host memory and downloads its 8 output fluxes,
+    # the copies overlapping the neighbouring steps (cablegpu_step_host).
+    # Headline: host buffers in the context's device tile order
+    # (cablegpu_set_host_layout(1); a driver fills its arrays through
+    # cablegpu_tile_order once), on the autotuned context.  Beside it: host
+    # buffers in the caller's order, which needs tile order 3 (the
+    # climate-coherent order within 2^18-tile chunks of the caller's order)
+    # to keep the per-step gather and scatter of caller positions L2-local.
+    def host_steps(gc, layout, ktau0):
+        import torch
+        gc.set_options(capture_forcing=True)
+        gc.step(ktau0, dels)
+        f0 = gc.get("forcing")
+        gc.step(ktau0 + 1, dels)
+        f1 = gc.get("forcing")
+        gc.set_options(capture_forcing=False)
+        gc.set_host_layout(layout)
+        if layout == 1:
+            perm = gc.tile_order()
+            f0, f1 = f0[:, perm], f1[:, perm]
+        k = ktau0 + 2
+        pin = torch.cuda.is_available()
+        host_f = [np.ascontiguousarray(torch.from_numpy(np.ascontiguousarray(f)).pin_memory().numpy() if pin else f)
+                  for f in (f0, f1)]
+        outs = [torch.empty((8, args.mp), dtype=torch.float32, pin_memory=pin).numpy() for _ in range(2)]
+        for n in range(2):   # warm the pipelined host path (staging buffers, copy streams)
+            gc.step_host(k, host_f[n], outs[n], dels); k += 1
+        gc.synchronize()
+        d.barrier()
+        ck = ClockSampler(d.local)
+        ck.start()
+        t0 = time.perf_counter()
+        for n in range(args.e2e_steps):
+            gc.step_host(k, host_f[n % 2], outs[n % 2], dels); k += 1
+        gc.synchronize()
+        secs = d.max(time.perf_counter() - t0)
+        ckr = ck.stop()
+        return {"value": d.world * args.mp * args.e2e_steps / secs, "unit": "tile-timesteps/s",
+                "h2d_bytes_per_step": int(f0.nbytes), "d2h_bytes_per_step": int(outs[0].nbytes), "steps": args.e2e_steps,
+                "ms_per_step": secs * 1e3 / args.e2e_steps, "clocks": ckr}
+    # On its own context with the tuned order and blocks, warmed up like the
+    # headline's, so that it times the same early simulated period (the
+    # per-step cost follows the snow and soil state) and leaves the
+    # headline's state untouched.
+    e2e = None
+    try:
+        ge = R.from_tileset(ts, device=d.local, order=order)
+        ge.set_blocks(blocks)
+        ge.run(1, args.warmup, dels)
+        ge.synchronize()
+        e2e = host_steps(ge, 1, 1 + args.warmup)
+        ge.close()
+        e2e.update({"tile_order": order, "host_layout": "device tile order (cablegpu_tile_order)",
+                    "path": "cablegpu_step_host: pinned host buffers, one copy stream per direction",
+                    "when": "steps %d-%d of a fresh context, the headline's period" % (
+                        args.warmup + 3, args.warmup + 2 + args.e2e_steps)})
+    except Exception as exc:  # the line still prints; the failure is stated
+        e2e = {"value": None, "unit": "tile-timesteps/s", "error": str(exc)[:200]}
     # --- device-resident throughput
     clocks = ClockSampler(d.local)
     clocks.start()
@@ -538,55 +597,15 @@ def run_gb300(args):
             "scope": "one timestep (its 5 kernels, CUDA events around each step), %d algorithmic B per tile-step"
                      % ALGO_BYTES_PER_TILE_STEP,
             "kernels_ms": {k: round(v, 4) for k, v in phase_ms.items()}}
-    # --- end to end through the C ABI with host buffers: every step uploads
-    # its forcing from pinned host memory and downloads its 8 output fluxes,
-    # the copies overlapping the neighbouring steps (cablegpu_step_host).
-    # Headline: host buffers in the context's device tile order
-    # (cablegpu_set_host_layout(1); a driver fills its arrays through
-    # cablegpu_tile_order once), on the autotuned context.  Beside it: host
-    # buffers in the caller's order, which needs tile order 3 (the
-    # climate-coherent order within 2^18-tile chunks of the caller's order)
-    # to keep the per-step gather and scatter of caller positions L2-local.
-    def host_steps(gc, layout, ktau0):
-        import torch
-        gc.set_options(capture_forcing=True)
-        gc.step(ktau0, dels)
-        f0 = gc.get("forcing")
-        gc.step(ktau0 + 1, dels)
-        f1 = gc.get("forcing")
-        gc.set_options(capture_forcing=False)
-        gc.set_host_layout(layout)
-        if layout == 1:
-            perm = gc.tile_order()
-            f0, f1 = f0[:, perm], f1[:, perm]
-        k = ktau0 + 2
-        pin = torch.cuda.is_available()
-        host_f = [np.ascontiguousarray(torch.from_numpy(np.ascontiguousarray(f)).pin_memory().numpy() if pin else f)
-                  for f in (f0, f1)]
-        outs = [torch.empty((8, args.mp), dtype=torch.float32, pin_memory=pin).numpy() for _ in range(2)]
-        for n in range(2):   # warm the pipelined host path (staging buffers, copy streams)
-            gc.step_host(k, host_f[n], outs[n], dels); k += 1
-        gc.synchronize()
-        d.barrier()
-        t0 = time.perf_counter()
-        for n in range(args.e2e_steps):
-            gc.step_host(k, host_f[n % 2], outs[n % 2], dels); k += 1
-        gc.synchronize()
-        secs = d.max(time.perf_counter() - t0)
-        return {"value": d.world * args.mp * args.e2e_steps / secs, "unit": "tile-timesteps/s",
-                "h2d_bytes_per_step": int(f0.nbytes), "d2h_bytes_per_step": int(outs[0].nbytes), "steps": args.e2e_steps}
-    e2e = None
-    try:
-        e2e = host_steps(g, 1, ktau + 8)
-        e2e.update({"tile_order": order, "host_layout": "device tile order (cablegpu_tile_order)",
-                    "path": "cablegpu_step_host: pinned host buffers, one copy stream per direction"})
-        g.close()
-        g = R.from_tileset(ts, device=d.local, order=3)
-        g.set_blocks(blocks)
-        cal = host_steps(g, 0, 1)
-        e2e["caller_order"] = {"value": cal["value"], "tile_order": 3, "host_layout": "caller tile order"}
-    except Exception as exc:  # the line still prints; the failure is stated
-        e2e = {"value": None, "unit": "tile-timesteps/s", "error": str(exc)[:200]}
+    if e2e and e2e.get("value"):
+        try:
+            g.close()
+            g = R.from_tileset(ts, device=d.local, order=3)
+            g.set_blocks(blocks)
+            cal = host_steps(g, 0, 1)
+            e2e["caller_order"] = {"value": cal["value"], "tile_order": 3, "host_layout": "caller tile order"}
+        except Exception as exc:  # the line still prints; the failure is stated
+            e2e["caller_order"] = {"value": None, "error": str(exc)[:200]}
     g.close()
     sur = None
     if not args.no_surrogate:
