@@ -206,7 +206,6 @@ __global__ void gather_out_df_kernel(double* stage, const float* src, const int*
 }  // namespace
 
 // ---------------------------------------------------------------- context
-constexpr int kMaxGroups = 4;
 struct cablegpu_ctx {
   int device = 0;
   int mp = 0, ld = 0;
@@ -271,12 +270,6 @@ struct cablegpu_ctx {
   const float* io_forcing = nullptr;          // staging slot the current step_host step reads
   float* io_out = nullptr;                    // staging slot it writes its outputs to (caller order)
   long long io_count = 0;
-  // grouped steps (cablegpu_run_groups): per tile group a stream for the
-  // radiation and canopy kernels, a high-priority one for the soil kernels,
-  // and the events that order them
-  bool groups_ready = false;
-  cudaStream_t gstream[kMaxGroups] = {}, hstream[kMaxGroups] = {};
-  cudaEvent_t ev_b[kMaxGroups] = {}, ev_c[kMaxGroups] = {};
   std::string err;
 };
 
@@ -398,9 +391,6 @@ StepParams make_params(cablegpu_ctx* c, int ktau, float dels) {
   p.lai_refresh = 0;
   p.solve64 = c->solve64;
   p.canopy_pool = c->canopy_pool;
-  p.t0 = 0;
-  p.t1 = c->mp;
-  p.soil_grid = 0;
   return p;
 }
 
@@ -597,16 +587,6 @@ int cablegpu_destroy(cablegpu_ctx* c) {
     }
     cudaStreamDestroy(c->cstream);
     cudaStreamDestroy(c->dstream);
-  }
-  if (c->groups_ready) {
-    for (int g = 0; g < kMaxGroups; ++g) {
-      cudaStreamSynchronize(c->gstream[g]);
-      cudaStreamSynchronize(c->hstream[g]);
-      cudaStreamDestroy(c->gstream[g]);
-      cudaStreamDestroy(c->hstream[g]);
-      cudaEventDestroy(c->ev_b[g]);
-      cudaEventDestroy(c->ev_c[g]);
-    }
   }
   if (c->d_sur_dt) cudaFree(c->d_sur_dt);
   if (c->d_bank) cudaFree(c->d_bank);
@@ -1147,78 +1127,6 @@ int cablegpu_get_config(cablegpu_ctx* c, int* order, int* block5) {
   if (!c) return CABLEGPU_ERR_ARG;
   if (order) *order = c->order;
   if (block5) std::copy(c->block, c->block + 5, block5);
-  return CABLEGPU_OK;
-}
-
-int cablegpu_run_groups(cablegpu_ctx* c, int ktau0, int nsteps, float dels, int ngroups, int soil_blocks_per_sm,
-                        float* ms_total) {
-  if (!c || ktau0 < 1 || nsteps < 1 || !(dels > 0.f) || ngroups < 1 || ngroups > kMaxGroups ||
-      soil_blocks_per_sm < 0 || soil_blocks_per_sm > 64)
-    return fail(c, CABLEGPU_ERR_ARG, "run_groups: bad argument");
-  if (c->sur_enabled || c->harvesting)
-    return fail(c, CABLEGPU_ERR_ARG, "run_groups: the plain kernels only (surrogate and harvest off)");
-  CG_CUDA(c, cudaSetDevice(c->device));
-  if (!c->groups_ready) {
-    int lo = 0, hi = 0;
-    CG_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
-    for (int g = 0; g < kMaxGroups; ++g) {
-      CG_CUDA(c, cudaStreamCreateWithPriority(&c->gstream[g], cudaStreamNonBlocking, lo));
-      CG_CUDA(c, cudaStreamCreateWithPriority(&c->hstream[g], cudaStreamNonBlocking, hi));
-      CG_CUDA(c, cudaEventCreateWithFlags(&c->ev_b[g], cudaEventDisableTiming));
-      CG_CUDA(c, cudaEventCreateWithFlags(&c->ev_c[g], cudaEventDisableTiming));
-    }
-    c->groups_ready = true;
-  }
-  int nsm = 0;
-  CG_CUDA(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
-  bind_device_view(c);
-  const bool diag = c->diag != 0;
-  const int* bk = c->block;
-  // group g: tile slots [g * chunk, (g + 1) * chunk), chunk a multiple of 256
-  const int chunk = (int)((((long long)c->mp + ngroups - 1) / ngroups + 255) / 256 * 256);
-  cudaEvent_t a, b;
-  CG_CUDA(c, cudaEventCreate(&a));
-  CG_CUDA(c, cudaEventCreate(&b));
-  CG_CUDA(c, cudaEventRecord(a, c->stream));
-  for (int g = 0; g < ngroups; ++g) {
-    CG_CUDA(c, cudaStreamWaitEvent(c->gstream[g], a, 0));
-    CG_CUDA(c, cudaStreamWaitEvent(c->hstream[g], a, 0));
-  }
-  // Per step and group: radiation and canopy on the group's stream, then the
-  // snow and soil kernels on its high-priority stream.  A group's radiation
-  // waits for its own soil kernels of the step before (its state) and for the
-  // previous group's canopy (so the groups' canopies run one after another
-  // and each group's FP64 soil solves run beside the next group's canopy).
-  for (int n = 0; n < nsteps; ++n) {
-    for (int g = 0; g < ngroups; ++g) {
-      StepParams p = make_params(c, ktau0 + n, dels);
-      p.t0 = g * chunk;
-      p.t1 = std::min(c->mp, (g + 1) * chunk);
-      if (p.t0 >= p.t1) continue;
-      p.soil_grid = soil_blocks_per_sm * nsm;
-      cudaStream_t sg = c->gstream[g], hg = c->hstream[g];
-      if (n > 0) CG_CUDA(c, cudaStreamWaitEvent(sg, c->ev_c[g], 0));
-      if (g > 0 || n > 0) CG_CUDA(c, cudaStreamWaitEvent(sg, c->ev_b[(g + ngroups - 1) % ngroups], 0));
-      launch_phase_a(diag, sg, c->dev, c->d_tables, p, nullptr, bk[0]);
-      launch_phase_b(diag, sg, c->dev, c->d_tables, p, nullptr, bk[1]);
-      CG_CUDA(c, cudaEventRecord(c->ev_b[g], sg));
-      CG_CUDA(c, cudaStreamWaitEvent(hg, c->ev_b[g], 0));
-      launch_phase_c1(diag, hg, c->dev, c->d_tables, p, nullptr, bk[2]);
-      launch_phase_c2(diag, hg, c->dev, c->d_tables, p, nullptr, bk[3]);
-      launch_phase_c3(diag, hg, c->dev, c->d_tables, p, nullptr, bk[4]);
-      CG_CUDA(c, cudaEventRecord(c->ev_c[g], hg));
-      c->launches += kKernelsPerStep;
-    }
-    CG_CUDA(c, cudaGetLastError());
-  }
-  for (int g = 0; g < ngroups; ++g) CG_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_c[g], 0));
-  CG_CUDA(c, cudaEventRecord(b, c->stream));
-  CG_CUDA(c, cudaEventSynchronize(b));
-  float ms = 0.f;
-  CG_CUDA(c, cudaEventElapsedTime(&ms, a, b));
-  if (ms_total) *ms_total = ms;
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
   return CABLEGPU_OK;
 }
 

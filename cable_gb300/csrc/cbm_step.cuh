@@ -44,11 +44,6 @@ struct StepParams {
                      // reference's direct form; 0: in FP32 on the step's change
   int lai_refresh;   // cbm_expl: the host model's radiation call ran, so the
                      // snow-reduced LAI is recomputed rather than carried
-  int t0, t1;        // the tile slots [t0, t1) a launch covers: the whole
-                     // context, or one tile group of a grouped step
-  int soil_grid;     // > 0: the FP64 soil kernels run this many blocks, each
-                     // looping over the range (they then share the SMs with
-                     // another group's kernels); 0: one thread per tile
 };
 
 __device__ __forceinline__ float ldf(const float* p, int i) { return __ldg(p + i); }
@@ -481,8 +476,8 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
   // tile's code path and store nothing, so every thread of the block reaches
   // the pool's barriers and votes on one path; they leave after the
   // Monin-Obukhov loop, the last code with barriers.
-  const bool ghost = kPool && t_in >= P.t1;
-  const int t = ghost ? P.t1 - 1 : t_in;
+  const bool ghost = kPool && t_in >= D.mp;
+  const int t = ghost ? D.mp - 1 : t_in;
   // the coupled-call code exists only in the kCoupled instantiation
   const int mode = kCoupled ? P.mode : 0;
   const int ld = D.ld;

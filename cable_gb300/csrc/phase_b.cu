@@ -15,9 +15,9 @@ template <bool kDiag, bool kHarvest, bool kSur, bool kCoupled, bool kPool>
 __global__ void __maxnreg__(kPool ? CG_MAXNREG_POOL : CG_MAXNREG)
     cbm_phase_b_kernel(CgDev D, const CgTables* __restrict__ T, StepParams P, const int* __restrict__ clock) {
   extern __shared__ __align__(16) float dl_sm[];
-  const int t = P.t0 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   // a pooling block's threads beyond the last tile run as ghosts (phase_b)
-  if (!kPool && t >= P.t1) return;
+  if (!kPool && t >= D.mp) return;
   StepParams p = P;
   if (clock) { p.ktau = clock[0]; p.step_index = clock[0] - 1; }
   phase_b<kDiag, kHarvest, kSur, kCoupled, kPool>(D, T, p, t, dl_sm);
@@ -31,7 +31,7 @@ constexpr int kPoolMaxBlock = 256;
 template <bool kDiag, bool kHarvest, bool kSur, bool kCoupled>
 void launch_variant(cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P, const int* clock,
                     int block) {
-  const int grid = (P.t1 - P.t0 + block - 1) / block;
+  const int grid = (D.mp + block - 1) / block;
   if (P.canopy_pool)
     cbm_phase_b_kernel<kDiag, kHarvest, kSur, kCoupled, true>
         <<<grid, block, dlp::smem_bytes(block, kSur), s>>>(D, T, P, clock);

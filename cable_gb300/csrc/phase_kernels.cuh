@@ -82,18 +82,10 @@ inline void prepare_phase_kernels() {
 template <bool kDiag, bool kCoupled, bool kS64>
 __global__ void __maxnreg__(kS64 ? CG_MAXNREG_S64 : CG_MAXNREG)
     CG_PHASE_KERNEL(CgDev D, const CgTables* __restrict__ T, StepParams P, const int* __restrict__ clock) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= D.mp) return;
   StepParams p = P;
   if (clock) { p.ktau = clock[0]; p.step_index = clock[0] - 1; }
-#if CG_PHASE_SOLVE
-  if constexpr (kS64) {
-    // FP64 solves: a block may cover several tiles per thread (P.soil_grid)
-    for (int t = P.t0 + blockIdx.x * blockDim.x + threadIdx.x; t < P.t1; t += gridDim.x * blockDim.x)
-      CG_PHASE<kDiag, kCoupled, kS64>(D, T, p, t);
-    return;
-  }
-#endif
-  const int t = P.t0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= P.t1) return;
 #if CG_PHASE_SOLVE
   CG_PHASE<kDiag, kCoupled, kS64>(D, T, p, t);
 #elif CG_PHASE_COUPLED
@@ -109,8 +101,7 @@ namespace {
 template <bool kS64>
 void launch_instance(bool diag, cudaStream_t s, const CgDev& D, const CgTables* T, const StepParams& P,
                      const int* clock, int block) {
-  int grid = (P.t1 - P.t0 + block - 1) / block;
-  if (kS64 && P.soil_grid > 0 && P.soil_grid < grid) grid = P.soil_grid;
+  const int grid = (D.mp + block - 1) / block;
 #if CG_PHASE_COUPLED
   if (P.mode != 0) {
     if (diag) CG_PHASE_KERNEL<true, true, kS64><<<grid, block, 0, s>>>(D, T, P, clock);

@@ -43,7 +43,6 @@ EXPORTS = [
     "cablegpu_run_forcing_file", "cablegpu_set_host_layout", "cablegpu_tile_order",
     "cablegpu_step_explicit", "cablegpu_step_implicit", "cablegpu_coupled_timed", "cablegpu_set_soil_solve",
     "cablegpu_set_canopy_schedule", "cablegpu_check_tile_param", "cablegpu_tune_blocks",
-    "cablegpu_run_groups",
 ]
 NOALLOC_MAX_TILES = 65536
 # soil tridiagonal solve arithmetic (cablegpu_set_soil_solve)
@@ -201,7 +200,6 @@ def load(build_if_missing: bool = True):
     L.cablegpu_step_host.argtypes = [vp, ip, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.cablegpu_set_blocks.argtypes = [vp, C.POINTER(ip)]
     L.cablegpu_get_config.argtypes = [vp, C.POINTER(ip), C.POINTER(ip)]
-    L.cablegpu_run_groups.argtypes = [vp, ip, ip, C.c_float, ip, ip, C.POINTER(C.c_float)]
     L.cablegpu_tune_blocks.argtypes = [vp, ip, ip, C.c_float, C.POINTER(ip), C.POINTER(C.c_float)]
     L.cablegpu_autotune.argtypes = [C.POINTER(_Tiles), ip, ip, ip, C.POINTER(ip), C.POINTER(ip), C.POINTER(C.c_float)]
     L.cablegpu_launch_count.argtypes = [vp]
@@ -544,14 +542,6 @@ class CableGPU:
         tried, acc = C.c_longlong(), C.c_longlong()
         self._check(self.L.cablegpu_surrogate_stats(self.h, C.byref(tried), C.byref(acc), int(reset)))
         return int(tried.value), int(acc.value)
-
-    def run_groups(self, ktau0, nsteps, dels=1800.0, ngroups=2, soil_blocks_per_sm=2):
-        """nsteps steps with the tiles in `ngroups` groups whose FP64 soil
-        kernels run beside another group's canopy; returns the device ms."""
-        ms = C.c_float()
-        self._check(self.L.cablegpu_run_groups(self.h, int(ktau0), int(nsteps), float(dels), int(ngroups),
-                                                int(soil_blocks_per_sm), C.byref(ms)))
-        return ms.value
 
     def tune_blocks(self, ktau0=1, nsteps=4, dels=1800.0):
         """Times block sizes 32..256 of each step kernel on this context's own

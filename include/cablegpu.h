@@ -344,20 +344,6 @@ long long cablegpu_launch_count(cablegpu_ctx* ctx);
  * the tile order the context was built with and the current block sizes. */
 int cablegpu_set_blocks(cablegpu_ctx* ctx, const int* block5);
 int cablegpu_get_config(cablegpu_ctx* ctx, int* order, int* block5);
-/* Grouped steps: runs nsteps steps from ktau0 (synthetic or host-set
- * forcing, plain kernels, diagnostics as set) with the tiles split into
- * `ngroups` (1..4) contiguous groups of device slots, each with its own
- * streams: a group's radiation and canopy kernels on one, its snow and soil
- * kernels on a high-priority one, the groups' canopies one after another
- * and each group's soil kernels beside the next group's canopy.  With
- * soil_blocks_per_sm > 0 the FP64 soil kernels run that many blocks per SM,
- * each looping over its group's tiles, so they leave the rest of every SM
- * to the canopy kernel of another group (FP64 and FP32 pipes busy at once).
- * Results are bitwise those of cablegpu_run (tiles are independent);
- * ms_total receives the device time.  No counterpart in the reference
- * (scheduling). */
-int cablegpu_run_groups(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels, int ngroups, int soil_blocks_per_sm,
-                        float* ms_total);
 /* Block sizes tuned on the context itself: times block sizes 32, 64, 128
  * and 256 of each step kernel over `nsteps` steps (1..64) from step ktau0 of
  * length dels on the context's own tiles, current state and forcing source,
