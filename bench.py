@@ -58,7 +58,7 @@ def parse():
     p.add_argument("--workload", default="snow_grid", choices=["snow_grid", "grid"])
     p.add_argument("--mp", type=int, default=4_000_000)
     p.add_argument("--e2e-steps", type=int, default=240)
-    p.add_argument("--e2e-records", type=int, default=48, help="forcing records the end-to-end steps cycle through")
+    p.add_argument("--e2e-records", type=int, default=8, help="forcing records the end-to-end steps cycle through")
     p.add_argument("--cpu-sample-tiles", type=int, default=100_000)
     p.add_argument("--cpu-sample-steps", type=int, default=48)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -496,10 +496,14 @@ def run_gb300(args):
     # to keep the per-step gather and scatter of caller positions L2-local.
     def host_steps(gc, layout, ktau0):
         """End-to-end steps through cablegpu_step_host: the forcing of
-        args.e2e_records consecutive steps (one day of half-hours by
-        default) is captured from the generator into pinned host buffers,
-        then args.e2e_steps steps cycle through them, so the timed steps
-        follow the diurnal cycle as the device-resident steps do."""
+        args.e2e_records consecutive steps (four hours by default) is
+        captured from the generator into pinned host buffers, then
+        args.e2e_steps steps cycle through them.  A few records keep the
+        timed steps' physics close to the device-resident steps' (two
+        records repeated make an unnatural state); many (48: 10 GB of pinned
+        buffers) make the copies themselves slow on this host (address
+        translation of the host pages), which a driver refilling one forcing
+        array per step does not see."""
         import torch
         pin = torch.cuda.is_available()
         gc.set_host_layout(layout)

@@ -869,6 +869,16 @@ int cablegpu_step_host(cablegpu_ctx* c, int ktau, float dels, const float* host_
   return CABLEGPU_OK;
 }
 
+int cablegpu_host_register(void* ptr, size_t bytes) {
+  if (!ptr || bytes == 0) return CABLEGPU_ERR_ARG;
+  return cudaHostRegister(ptr, bytes, cudaHostRegisterDefault) == cudaSuccess ? CABLEGPU_OK : CABLEGPU_ERR_CUDA;
+}
+
+int cablegpu_host_unregister(void* ptr) {
+  if (!ptr) return CABLEGPU_ERR_ARG;
+  return cudaHostUnregister(ptr) == cudaSuccess ? CABLEGPU_OK : CABLEGPU_ERR_CUDA;
+}
+
 int cablegpu_set_host_layout(cablegpu_ctx* c, int layout) {
   if (!c || (layout != 0 && layout != 1)) return fail(c, CABLEGPU_ERR_ARG, "set_host_layout: layout must be 0 or 1");
   if (c->io_ready) CG_CUDA(c, cudaStreamSynchronize(c->stream));   // no step in flight changes layout

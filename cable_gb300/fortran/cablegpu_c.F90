@@ -119,6 +119,16 @@ MODULE cablegpu_c
       INTEGER(c_int), VALUE :: ktau, cycleno, numcycles
       REAL(c_float), VALUE :: dels
     END FUNCTION cablegpu_step_implicit
+    INTEGER(c_int) FUNCTION cablegpu_host_register(ptr, bytes) BIND(C, name="cablegpu_host_register")
+      IMPORT :: c_int, c_ptr, c_size_t
+      TYPE(c_ptr), VALUE :: ptr
+      INTEGER(c_size_t), VALUE :: bytes
+    END FUNCTION cablegpu_host_register
+
+    INTEGER(c_int) FUNCTION cablegpu_host_unregister(ptr) BIND(C, name="cablegpu_host_unregister")
+      IMPORT :: c_int, c_ptr
+      TYPE(c_ptr), VALUE :: ptr
+    END FUNCTION cablegpu_host_unregister
   END INTERFACE
 
 CONTAINS

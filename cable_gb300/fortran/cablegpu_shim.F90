@@ -148,6 +148,10 @@ CONTAINS
     r8(:, 1) = 0.0_c_double;  CALL put('owb', C_LOC(r8))
 
     ALLOCATE(forc(mp, CABLEGPU_NFORCING), outb(mp, 8))
+    ! page-locked, so that each step's forcing upload and flux download are
+    ! asynchronous copies at full speed
+    CALL check(cablegpu_host_register(C_LOC(forc), INT(4, c_size_t) * mp * CABLEGPU_NFORCING), 'host_register forc')
+    CALL check(cablegpu_host_register(C_LOC(outb), INT(4, c_size_t) * mp * 8), 'host_register outb')
     DEALLOCATE(iveg, isoilm, vlai, lat, flags, r8, r4)
   END SUBROUTINE gpu_setup
 
@@ -311,8 +315,14 @@ CONTAINS
   SUBROUTINE cbm_gpu_finalize()
     IF (C_ASSOCIATED(ctx)) CALL check(cablegpu_destroy(ctx), 'destroy')
     ctx = c_null_ptr
-    IF (ALLOCATED(forc)) DEALLOCATE(forc)
-    IF (ALLOCATED(outb)) DEALLOCATE(outb)
+    IF (ALLOCATED(forc)) THEN
+      CALL check(cablegpu_host_unregister(C_LOC(forc)), 'host_unregister forc')
+      DEALLOCATE(forc)
+    END IF
+    IF (ALLOCATED(outb)) THEN
+      CALL check(cablegpu_host_unregister(C_LOC(outb)), 'host_unregister outb')
+      DEALLOCATE(outb)
+    END IF
     IF (ALLOCATED(slot_tile)) DEALLOCATE(slot_tile)
   END SUBROUTINE cbm_gpu_finalize
 

@@ -43,6 +43,7 @@ EXPORTS = [
     "cablegpu_run_forcing_file", "cablegpu_set_host_layout", "cablegpu_tile_order",
     "cablegpu_step_explicit", "cablegpu_step_implicit", "cablegpu_coupled_timed", "cablegpu_set_soil_solve",
     "cablegpu_set_canopy_schedule", "cablegpu_check_tile_param", "cablegpu_tune_blocks",
+    "cablegpu_host_register", "cablegpu_host_unregister",
 ]
 NOALLOC_MAX_TILES = 65536
 # soil tridiagonal solve arithmetic (cablegpu_set_soil_solve)
@@ -200,6 +201,8 @@ def load(build_if_missing: bool = True):
     L.cablegpu_step_host.argtypes = [vp, ip, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.cablegpu_set_blocks.argtypes = [vp, C.POINTER(ip)]
     L.cablegpu_get_config.argtypes = [vp, C.POINTER(ip), C.POINTER(ip)]
+    L.cablegpu_host_register.argtypes = [vp, C.c_size_t]
+    L.cablegpu_host_unregister.argtypes = [vp]
     L.cablegpu_tune_blocks.argtypes = [vp, ip, ip, C.c_float, C.POINTER(ip), C.POINTER(C.c_float)]
     L.cablegpu_autotune.argtypes = [C.POINTER(_Tiles), ip, ip, ip, C.POINTER(ip), C.POINTER(ip), C.POINTER(C.c_float)]
     L.cablegpu_launch_count.argtypes = [vp]
@@ -445,6 +448,14 @@ class CableGPU:
         assert out.dtype == np.float32 and out.flags["C_CONTIGUOUS"] and out.shape == (8, self.mp)
         self._check(self.L.cablegpu_step_host(self.h, int(ktau), float(dels), _ptr(forcing, C.c_float),
                                               _ptr(out, C.c_float)))
+
+    def host_register(self, a: np.ndarray):
+        """Page-locks the memory of a C-contiguous array (cablegpu_host_register)."""
+        assert a.flags["C_CONTIGUOUS"]
+        self._check(self.L.cablegpu_host_register(a.ctypes.data, a.nbytes))
+
+    def host_unregister(self, a: np.ndarray):
+        self._check(self.L.cablegpu_host_unregister(a.ctypes.data))
 
     def synchronize(self):
         self._check(self.L.cablegpu_synchronize(self.h))

@@ -279,6 +279,12 @@ int cablegpu_run(cablegpu_ctx* ctx, int ktau0, int nsteps, float dels);
  * only.  Replaces the per-step get_met_data -> cbm -> write_output sequence
  * of the offline driver (cable_serial.F90:594-640). */
 int cablegpu_step_host(cablegpu_ctx* ctx, int ktau, float dels, const float* host_forcing, float* host_out);
+/* Page-locks (and releases) an existing host buffer, such as the Fortran
+ * shim's forcing and output arrays, so that the copies of
+ * cablegpu_step_host run asynchronously at full speed (cudaHostRegister /
+ * cudaHostUnregister).  No counterpart in the reference (host I/O). */
+int cablegpu_host_register(void* ptr, size_t bytes);
+int cablegpu_host_unregister(void* ptr);
 /* Layout of the host buffers of cablegpu_step_host and of the records of
  * cablegpu_run_forcing_file: 0 (default) the caller's tile order, 1 the
  * context's device tile order (cablegpu_tile_order), which spares the kernels

@@ -119,3 +119,39 @@ def test_per_tile_soil_albedo():
     assert np.all(runs[2]["albedo_vis"][0][bare] > runs[0]["albedo_vis"][0][bare])
     rest = (ts.iveg == 16) | (ts.isoilm == 9)
     np.testing.assert_array_equal(runs[2]["albedo_vis"][0][rest], runs[0]["albedo_vis"][0][rest])
+
+
+def test_host_registered_buffers_step_like_any_host_buffers():
+    """cablegpu_host_register page-locks the driver's own forcing and output
+    arrays (the Fortran shim registers its forc and outb): the pipelined host
+    steps then give bitwise the outputs of unregistered buffers."""
+    from cable_gb300 import runtime as R
+    ts = W.grid(20000, seed=5, nsteps=4)
+    cap = R.from_tileset(ts)
+    cap.set_options(capture_forcing=True)
+    forc = []
+    for k in range(1, 4):
+        cap.step(k)
+        forc.append(np.ascontiguousarray(cap.get("forcing")))
+    cap.close()
+    outs = []
+    for register in (False, True):
+        g = R.from_tileset(ts)
+        f = np.zeros_like(forc[0])
+        o = np.zeros((8, ts.mp), np.float32)
+        if register:
+            g.host_register(f)
+            g.host_register(o)
+        got = []
+        for k in range(3):
+            f[...] = forc[k]
+            g.step_host(k + 1, f, o)
+            g.synchronize()
+            got.append(o.copy())
+        if register:
+            g.host_unregister(f)
+            g.host_unregister(o)
+        outs.append(got)
+        g.close()
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a, b)
