@@ -345,24 +345,32 @@ __device__ __forceinline__ float d2f(double x) {
   return __uint_as_float(f | (hi & 0x80000000u));
 }
 
-// 1/x in FP64 by Newton-Raphson iteration on f(r) = 1/r - x, seeded with the
-// FP32 reciprocal of x: each step r <- r + r (1 - x r) squares the relative
-// error (~2^-22 -> ~2^-44 -> below the FP64 rounding), two fused
-// multiply-adds per step.  For 1e-30 < |x| < 1e30 (the FP32 normal range of
-// the seed); the soil systems' pivots and saturation deficits are far inside
-// it.  Tested against CUDA's FP64 division (tests/test_fp64_reciprocal.py).
-// xf: an FP32 value within ~1e-6 relative of x that seeds the iteration
-// (x rounded to FP32, or an FP32 shadow of the quantity computed beside it);
-// the two steps take a seed error of 2^-20 below the FP64 rounding too.
-// rcp64_from: the same two steps from a given FP32 seed r0 ~ 1/x.
-__device__ __forceinline__ double rcp64_from(double x, float r0) {
-  double r = f2d(r0);
-  r = fma(r, fma(-x, r, 1.0), r);
-  r = fma(r, fma(-x, r, 1.0), r);
-  return r;
+// 1/x in FP64: one Newton-Raphson step r <- r + r (1 - x r) (two fused
+// multiply-adds; it squares the seed's relative error) from a double-float
+// seed accurate to ~2^-46, which leaves the result within an ulp of the
+// correctly rounded reciprocal.  The seed is formed on the FP32 and integer
+// pipes: x is split, with integer operations on its IEEE-754 fields, into
+// hi (x truncated to 24 significant bits, an FP32 value) and lo (the next
+// 23 bits of x, as an FP32 value); r = the FP32 reciprocal of hi, and the
+// FP32 correction c = r (1 - (hi + lo) r), the residual formed with fused
+// multiply-adds, makes r + c the reciprocal of x to about 2^-46.  One FP64
+// addition joins r and c.  Three FP64-pipe instructions in all, against
+// four for two Newton steps from an FP32 seed.  For 2^-74 <= |x| < 2^127
+// (the soil systems' pivots are >= 1, their pore spaces 0.01-0.6).  Tested
+// against CUDA's FP64 division (tests/test_fp64_reciprocal.py).
+__device__ __forceinline__ double rcp64(double x) {
+  const unsigned int h = (unsigned int)__double2hiint(x), l = (unsigned int)__double2loint(x);
+  const unsigned int mh = h & 0x7fffffffu, sign = h & 0x80000000u;
+  const float hi = __uint_as_float(sign | ((mh - (896u << 20)) << 3) | (l >> 29));
+  // the low 29 fraction bits, top 23 of them, as the integer they spell
+  // (2^23 + m - 2^23, exact), scaled by 2^(e - 1069)
+  const float m = __fsub_rn(__uint_as_float(0x4B000000u | ((l & 0x1fffffffu) >> 6)), 8388608.0f);
+  const float lo = __fmul_rn(m, __uint_as_float(((mh >> 20) - 1069u + 127u) << 23));
+  const float r = __fdividef(1.0f, hi);
+  const float e = __fmaf_rn(sign ? lo : -lo, r, __fmaf_rn(-hi, r, 1.0f));
+  const double r0 = f2d(r) + f2d(__fmul_rn(r, e));
+  return fma(r0, fma(-x, r0, 1.0), r0);
 }
-__device__ __forceinline__ double rcp64(double x, float xf) { return rcp64_from(x, __fdividef(1.0f, xf)); }
-__device__ __forceinline__ double rcp64(double x) { return rcp64(x, d2f(x)); }
 
 // cbl_trimb.F90:17-53 in FP64, as the reference solves both soil systems,
 // for their diffusion form: the Thomas algorithm on
@@ -376,36 +384,24 @@ __device__ __forceinline__ double rcp64(double x) { return rcp64(x, d2f(x)); }
 // g(k) = (rhs(k) - a(k) g(k-1)) temp(k) for k = 2..N-1; the last row
 // divided by its own pivot; back substitution.  Row 1's two divisions by
 // b(1) are one reciprocal here, every division a multiplication by an FP64
-// reciprocal (rcp64; the same value to an FP64 ulp or two), and g(k)
-// overwrites rhs(k), so only e and the solution are live in FP64.  The
-// reciprocals' seeds come from the pivots' FP32 shadow: the same recursion
-// pf(k) = (1 - a(k) - c(k)) - a(k) ef(k-1), ef(k) = c(k) / pf(k) in FP32
-// beside the FP64 one (within a few FP32 ulps of it: the system is
-// diagonally dominant, |e| < 1), which spares an FP64-to-FP32 conversion
-// per pivot; the FP64 values do not depend on the seed beyond its
-// accuracy.
+// reciprocal (rcp64, within an ulp of the division), and g(k) overwrites
+// rhs(k), so only e and the solution are live in FP64.
 template <int N>
 __device__ __forceinline__ void trimb64(const float* a, const float* c, double db0, double* rhs) {
   double e[N - 1];
-  const double p0 = (1.0 - f2d(a[0]) - f2d(c[0])) + db0;
-  float rf = __fdividef(1.0f, d2f(p0));
-  const double ib = rcp64_from(p0, rf);
-  float ef = c[0] * rf;
+  const double ib = rcp64((1.0 - f2d(a[0]) - f2d(c[0])) + db0);
   e[0] = f2d(c[0]) * ib;
   rhs[0] = rhs[0] * ib;
 #pragma unroll
   for (int k = 1; k < N - 1; ++k) {
     const double ak = f2d(a[k]), ck = f2d(c[k]);
-    rf = __fdividef(1.0f, (1.0f - a[k] - c[k]) - a[k] * ef);
-    const double temp = rcp64_from((1.0 - ak - ck) - ak * e[k - 1], rf);
-    ef = c[k] * rf;
+    const double temp = rcp64((1.0 - ak - ck) - ak * e[k - 1]);
     e[k] = ck * temp;
     rhs[k] = (rhs[k] - ak * rhs[k - 1]) * temp;
   }
   {
     const double ak = f2d(a[N - 1]), ck = f2d(c[N - 1]);
-    rf = __fdividef(1.0f, (1.0f - a[N - 1] - c[N - 1]) - a[N - 1] * ef);
-    rhs[N - 1] = (rhs[N - 1] - ak * rhs[N - 2]) * rcp64_from((1.0 - ak - ck) - ak * e[N - 2], rf);
+    rhs[N - 1] = (rhs[N - 1] - ak * rhs[N - 2]) * rcp64((1.0 - ak - ck) - ak * e[N - 2]);
   }
 #pragma unroll
   for (int k = N - 2; k >= 0; --k) rhs[k] = rhs[k] - e[k] * rhs[k + 1];

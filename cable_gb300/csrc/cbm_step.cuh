@@ -1893,7 +1893,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
         const float sat = ssat - wbicef[k];
         const df32 liq = df_add(df_add(wb[k], dwd[k]), df32{-wbice[k].hi, -wbice[k].lo});
         satd[k] = f2d(sat);
-        rd[k] = df_to_double(liq) * rcp64(satd[k], sat);
+        rd[k] = df_to_double(liq) * rcp64(satd[k]);
         xf[k] = liq.hi / sat;   // the conductivity's weighting, FP32
         dtt[k] = dels / (zse[k] * sat);
       }
