@@ -181,6 +181,31 @@ __device__ __forceinline__ df32 df_from_double(double d) {
   const float hi = d2f(d);
   return {hi, d2f(d - f2d(hi))};
 }
+// A double as double-FP32 without FP64 instructions: hi = x truncated to 24
+// significant bits, lo = its next 23 bits (the rest, below 2^-47 of x, is
+// dropped), both built with integer operations on the IEEE-754 fields.  For
+// |x| < 2^127; below 2^-80 (and zero) the result is a zero of x's sign.
+__device__ __forceinline__ df32 df_split(double x) {
+  const unsigned int h = (unsigned int)__double2hiint(x), l = (unsigned int)__double2loint(x);
+  const unsigned int mh = h & 0x7fffffffu, sign = h & 0x80000000u;
+  const bool tiny = mh < (943u << 20);
+  const float hi = __uint_as_float(sign | (tiny ? 0u : ((mh - (896u << 20)) << 3) | (l >> 29)));
+  // the low 29 fraction bits, top 23 of them, as the integer they spell
+  // (2^23 + m - 2^23, exact), scaled by 2^(e - 1069)
+  const float m = __fsub_rn(__uint_as_float(0x4B000000u | ((l & 0x1fffffffu) >> 6)), 8388608.0f);
+  const float lo = tiny ? 0.f : __fmul_rn(m, __uint_as_float(((mh >> 20) - 1069u + 127u) << 23));
+  return {hi, sign ? -lo : lo};
+}
+// x / s for a double-FP32 x and an FP32 s != 0, as double-FP32 to about
+// 2^-46: q1 = x.hi / s approximately, then the remainder x - q1 s with the
+// product's exact error (Sterbenz: x.hi - q1 s is exact) divided by s.
+__device__ __forceinline__ df32 df_div(df32 x, float s) {
+  const float r = __fdividef(1.0f, s);
+  const float q1 = __fmul_rn(x.hi, r);
+  const float p = __fmul_rn(q1, s);
+  const float rem = __fadd_rn(__fsub_rn(__fsub_rn(x.hi, p), __fmaf_rn(q1, s, -p)), x.lo);
+  return df_norm(q1, __fmul_rn(rem, r));
+}
 __device__ __forceinline__ float pow4(float x) { float y = x * x; return y * y; }
 __device__ __forceinline__ float fsignf(float a, float b) { return signbit(b) ? -fabsf(a) : fabsf(a); }
 
@@ -349,9 +374,8 @@ __device__ __forceinline__ float d2f(double x) {
 // multiply-adds; it squares the seed's relative error) from a double-float
 // seed accurate to ~2^-46, which leaves the result within an ulp of the
 // correctly rounded reciprocal.  The seed is formed on the FP32 and integer
-// pipes: x is split, with integer operations on its IEEE-754 fields, into
-// hi (x truncated to 24 significant bits, an FP32 value) and lo (the next
-// 23 bits of x, as an FP32 value); r = the FP32 reciprocal of hi, and the
+// pipes: x is split (df_split) into hi (x truncated to 24 significant bits)
+// and lo (its next 23 bits); r = the FP32 reciprocal of hi, and the
 // FP32 correction c = r (1 - (hi + lo) r), the residual formed with fused
 // multiply-adds, makes r + c the reciprocal of x to about 2^-46.  One FP64
 // addition joins r and c.  Three FP64-pipe instructions in all, against
@@ -359,15 +383,9 @@ __device__ __forceinline__ float d2f(double x) {
 // (the soil systems' pivots are >= 1, their pore spaces 0.01-0.6).  Tested
 // against CUDA's FP64 division (tests/test_fp64_reciprocal.py).
 __device__ __forceinline__ double rcp64(double x) {
-  const unsigned int h = (unsigned int)__double2hiint(x), l = (unsigned int)__double2loint(x);
-  const unsigned int mh = h & 0x7fffffffu, sign = h & 0x80000000u;
-  const float hi = __uint_as_float(sign | ((mh - (896u << 20)) << 3) | (l >> 29));
-  // the low 29 fraction bits, top 23 of them, as the integer they spell
-  // (2^23 + m - 2^23, exact), scaled by 2^(e - 1069)
-  const float m = __fsub_rn(__uint_as_float(0x4B000000u | ((l & 0x1fffffffu) >> 6)), 8388608.0f);
-  const float lo = __fmul_rn(m, __uint_as_float(((mh >> 20) - 1069u + 127u) << 23));
-  const float r = __fdividef(1.0f, hi);
-  const float e = __fmaf_rn(sign ? lo : -lo, r, __fmaf_rn(-hi, r, 1.0f));
+  const df32 xs = df_split(x);
+  const float r = __fdividef(1.0f, xs.hi);
+  const float e = __fmaf_rn(-xs.lo, r, __fmaf_rn(-xs.hi, r, 1.0f));
   const double r0 = f2d(r) + f2d(__fmul_rn(r, e));
   return fma(r0, fma(-x, r0, 1.0), r0);
 }

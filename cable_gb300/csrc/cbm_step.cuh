@@ -1012,7 +1012,7 @@ __device__ __forceinline__ void phase_b(const CgDev& D, const CgTables* __restri
   // the coupled calls run no balance checks; cbm_expl restores the canopy
   // water and wetness factor (cbl_cbm_mod.F90:150-152), so the step's
   // state is what the implicit call leaves
-  if (mode == 0) D.ebal_tot[t] = D.ebal_tot[t] + (double)ebal;
+  if (mode == 0) D.ebal_tot[t] = D.ebal_tot[t] + f2d(ebal);
   if (mode != 1) {
     D.cansto[t] = cansto;
     D.owetfac[t] = owetfac_out;
@@ -1136,7 +1136,7 @@ __device__ __forceinline__ void phase_c1(const CgDev& D, const CgTables* __restr
               (double)((float)(1 - isflag) * CGSNOW * snowd);
     first_call = false;
   }
-  float g1f = (float)gammzz1;   // layer-1 heat capacity, FP32 working copy
+  float g1f = d2f(gammzz1);   // layer-1 heat capacity, FP32 working copy
   float wblf[CG_MS], wbfice[CG_MS];
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) {
@@ -1362,7 +1362,7 @@ __device__ __forceinline__ void phase_c1(const CgDev& D, const CgTables* __restr
   }
   D.tgg[t] = tgg[0];
   D.flags[t] = (uint8_t)(isflag | (first_call ? 2 : 0));
-  D.gammzz1[t] = (double)g1f;
+  D.gammzz1[t] = f2d(g1f);
   D.snowd[t] = snowd; D.ssdnn[t] = ssdnn;
   D.work_c[0 * ld + t] = osnowd;
   D.work_c[1 * ld + t] = precis;
@@ -1481,7 +1481,7 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
   // dtmlt(:,1) so far this step (the snow-pack kernel's part); only the
   // implicit coupled call uses it
   float dtmlt0 = mode == 2 ? D.work_c[CG_NC * ld + t] : 0.f;
-  float g1f = (float)gammzz1;
+  float g1f = d2f(gammzz1);
   float smelt = D.work_c[3 * ld + t];
   float wblf[CG_MS], wbfice[CG_MS];
 #pragma unroll
@@ -1725,7 +1725,7 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
     D.tggsn[k * ld + t] = tggsn[k]; D.ssdn[k * ld + t] = ssdn[k]; D.smass[k * ld + t] = smass[k];
     D.sdepth[k * ld + t] = sdepth[k];
   }
-  D.gammzz1[t] = (double)g1f;
+  D.gammzz1[t] = f2d(g1f);
   D.snowd[t] = snowd;
   D.work_c[3 * ld + t] = smelt;
   D.work_c[4 * ld + t] = ghflux;
@@ -1803,7 +1803,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   float gf[CG_MS];
 #pragma unroll
   for (int k = 0; k < CG_MS; ++k) gf[k] = D.work_c[(6 + k) * ld + t];
-  float g1f = (float)gammzz1;
+  float g1f = d2f(gammzz1);
   // remove_trans moved negative transpiration into wet-canopy evaporation
   if (fevc < 0.0f) { fevw = fevw + fevc; fevc = 0.0f; }
   // infiltration (cbl_soilsnow_main.F90:139-159)
@@ -1876,26 +1876,30 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
     if constexpr (kS64) {
       // Implicit diffusion of the liquid fraction wblf = (wb - wbice) /
       // (ssat - wbice) on the reference's direct form
-      // (cbl_smoisturev.F90:200-262, :422-427).  The liquid water after the
-      // explicit drainage, wb + dwd - wbice, is formed in double-FP32 from
-      // the state (error-free FP32 operations, 48-bit significand) and
-      // widened; wblf, the top layers' infiltration source and the
-      // elimination (trimb64) are FP64; then wb = wblf (ssat - wbice) +
-      // wbice, the product in FP64, stored as double-FP32.  The pore space
-      // ssat - wbice is the FP32 value (ssat is REAL in the reference) in
-      // wblf, in dtt = dels / (zse (ssat - wbice)) and in the product, so
-      // the scaling in and out of wblf is exactly inverse.  The matrix
+      // (cbl_smoisturev.F90:200-262, :422-427), the elimination (trimb64) in
+      // FP64.  Its right-hand side is formed at the soil water state's own
+      // precision, double-FP32 (48-bit significand), on the FP32 pipe: the
+      // liquid water after the explicit drainage, wb + dwd - wbice, with
+      // error-free FP32 operations, divided by the pore space (df_div,
+      // ~2^-46), plus the top layers' infiltration source, then widened to
+      // FP64 once.  The solution goes back the same way: wb = wblf
+      // (ssat - wbice) + wbice as a double-FP32 product and sum (df_split,
+      // df_mul), the state's storage format.  The pore space ssat - wbice
+      // is the FP32 value (ssat is REAL in the reference) in wblf, in
+      // dtt = dels / (zse (ssat - wbice)) and in the product, so the scaling
+      // in and out of wblf is inverse to the state's precision.  The matrix
       // coefficients dtt z3 are FP32 (bulk arithmetic, widened exactly).
-      double satd[CG_MS], rd[CG_MS];
-      float xf[CG_MS], dtt[CG_MS];
+      double rd[CG_MS];
+      float sat[CG_MS], xf[CG_MS], dtt[CG_MS];
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k) {
-        const float sat = ssat - wbicef[k];
+        sat[k] = ssat - wbicef[k];
         const df32 liq = df_add(df_add(wb[k], dwd[k]), df32{-wbice[k].hi, -wbice[k].lo});
-        satd[k] = f2d(sat);
-        rd[k] = df_to_double(liq) * rcp64(satd[k]);
-        xf[k] = liq.hi / sat;   // the conductivity's weighting, FP32
-        dtt[k] = dels / (zse[k] * sat);
+        df32 q = df_div(liq, sat[k]);
+        xf[k] = q.hi;   // the conductivity's weighting, FP32
+        dtt[k] = dels / (zse[k] * sat[k]);
+        if (k < 3) q = df_add(q, dtt[k] * fwtop[k] / DLIQ);
+        rd[k] = df_to_double(q);
       }
       float a[CG_MS], c[CG_MS];
       a[0] = 0.f; c[CG_MS - 1] = 0.f;
@@ -1909,12 +1913,10 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
         a[k - 1] = -dtt[k - 1] * z3;
         c[k - 2] = -dtt[k - 2] * z3;
       }
-#pragma unroll
-      for (int k = 0; k < 3; ++k) rd[k] = rd[k] + f2d(dtt[k] * fwtop[k] / DLIQ);
       trimb64<CG_MS>(a, c, 0.0, rd);
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k) {
-        wb[k] = df_add(df_from_double(rd[k] * satd[k]), wbice[k]);
+        wb[k] = df_add(df_mul(df_split(rd[k]), sat[k]), wbice[k]);
         wbf[k] = wb[k].hi;
       }
     } else {
@@ -2198,10 +2200,10 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
   double owb = D.owb[t];
   if (P.ktau == 1) owb = wbtot;
   const double delwb = wbtot - owb;
-  const float wbal = (float)((double)(precip - delwc - snowd + osnowd - runoff_mm - evap_mm) - delwb);
+  const float wbal = d2f(f2d(precip - delwc - snowd + osnowd - runoff_mm - evap_mm) - delwb);
   double wbal_tot = D.wbal_tot[t];
   if (P.ktau == 1) wbal_tot = 0.0;
-  if (P.ktau > 10) wbal_tot += (double)wbal;
+  if (P.ktau > 10) wbal_tot += f2d(wbal);
 
   // store
 #pragma unroll
