@@ -29,15 +29,16 @@ SOURCES = ["cablegpu.cu", "phase_a.cu", "phase_b.cu", "phase_c1.cu", "phase_c2.c
 # reference's own FP32 build does.  CG_MAXNREG caps registers per thread
 # (CG_MAXNREG_S64: of the soil kernels' FP64-solve instantiations),
 # chosen per kernel from measured step times at 4M tiles (radiation 80, soil
-# heat 80, canopy 72, soil water 112, snow pack 128), trading a few hundred
-# bytes of spills for occupancy; the
+# heat 80, canopy 72, soil water 112, snow pack 128; FP64 solves: soil heat
+# 80, soil water 96, where the FP64 recursion's latency wants the warps),
+# trading a few hundred bytes of spills for occupancy; the
 # block size itself is a launch-time choice (autotuned).
 EXTRA_FLAGS = {
     "phase_a.cu": ["-prec-div=false", "-DCG_MAXNREG=80"],
     "phase_b.cu": ["--use_fast_math", "-fmad=false", "-DCG_MAXNREG=72"],
     "phase_c1.cu": ["-DCG_MAXNREG=128"],
-    "phase_c2.cu": ["-prec-div=false", "-DCG_MAXNREG=80", "-DCG_MAXNREG_S64=128"],
-    "phase_c3.cu": ["-prec-div=false", "-DCG_MAXNREG=112", "-DCG_MAXNREG_S64=128"],
+    "phase_c2.cu": ["-prec-div=false", "-DCG_MAXNREG=80", "-DCG_MAXNREG_S64=80"],
+    "phase_c3.cu": ["-prec-div=false", "-DCG_MAXNREG=112", "-DCG_MAXNREG_S64=96"],
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
