@@ -144,3 +144,38 @@ def test_tensor_core_give_up_falls_back_and_is_reported(trained, monkeypatch):
     y = R.mlp_forward(params, norm, rows[:4096])
     assert np.all(np.isfinite(y))
     g.close()
+
+
+def test_surrogate_error_against_fp64_every_step(oracle, trained):
+    """The benchmark's error statement over a run rather than at its end:
+    latent heat and canopy temperature of every tile-step of 96 half-hour
+    steps on 8,000 snow tiles, strict surrogate against the FP64 oracle on
+    the same forcing (RMSE at most 2 W/m2 and 0.05 K), beside the
+    reference's own FP32 build against the same oracle."""
+    from cable_gb300 import runtime as R
+    _, _, params, norm = trained
+    ts = W.snow_grid(8000, seed=79, nsteps=96)
+    g = R.from_tileset(ts)
+    g.set_options(diag=True, capture_forcing=True)
+    g.surrogate_weights(params, norm)
+    g.set_surrogate(1, 0.1)
+    st64, st32 = oracle.init_state(ts, 0), oracle.init_state(ts, 1)
+    se = {"sur_fe": 0.0, "sur_tv": 0.0, "mix_fe": 0.0, "mix_tv": 0.0}
+    n = 0
+    for k in range(96):
+        g.step(1 + k)
+        F = g.get("forcing")[None]
+        fe, tv = g.get("fe_d")[0], g.get("tv_d")[0]
+        d64 = oracle.run(ts, st64, 1, ktau0=1 + k, forcing=F, precision=0)
+        d32 = oracle.run(ts, st32, 1, ktau0=1 + k, forcing=F, precision=1)
+        se["sur_fe"] += float(np.sum((fe - d64["fe"]) ** 2))
+        se["sur_tv"] += float(np.sum((tv - d64["tv"]) ** 2))
+        se["mix_fe"] += float(np.sum((d32["fe"] - d64["fe"]) ** 2))
+        se["mix_tv"] += float(np.sum((d32["tv"] - d64["tv"]) ** 2))
+        n += fe.size
+    g.synchronize()
+    g.close()
+    rmse = {k: np.sqrt(v / n) for k, v in se.items()}
+    print("surrogate over 96 steps x 8000 tiles:", {k: round(v, 4) for k, v in rmse.items()})
+    assert rmse["sur_fe"] <= 2.0, rmse
+    assert rmse["sur_tv"] <= 0.05, rmse
