@@ -44,20 +44,6 @@ __device__ __forceinline__ float sigmoid_fast(float z) {
   return fmaf(0.5f, t, 0.5f);
 }
 __device__ __forceinline__ float silu(float z) { return z * sigmoid_fast(z); }
-// SiLU of two pre-activations, computed and returned as a BF16 pair (the
-// next layer's operand format): with h = z / 2, z sigmoid(z) = h (1 +
-// tanh(h)) = h tanh(h) + h, one hardware tanh for the pair.  The in-step
-// forward pass uses it: half the transcendental work of the FP32 form, with
-// the activations' error (a few BF16 roundings) of the order of the BF16
-// storage the FP32 form rounds to anyway.
-__device__ __forceinline__ uint32_t silu_bf16x2(float z0, float z1) {
-  const uint32_t z = tc::pack_bf16x2(z0, z1);
-  uint32_t h, t, r;
-  asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(h) : "r"(z), "r"(0x3F003F00u));   // z / 2 (0.5 = 0x3F00)
-  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(h));
-  asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(r) : "r"(h), "r"(t), "r"(h));
-  return r;
-}
 __device__ __forceinline__ float dsilu(float z) {
   const float s = sigmoid_fast(z);
   return s * fmaf(z, 1.0f - s, 1.0f);
@@ -124,7 +110,7 @@ __device__ __forceinline__ bool forward128(uint8_t* smem, uint32_t taddr, uint32
     uint32_t w[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j)
-      w[j] = silu_bf16x2(v[2 * j] + b1[c * 16 + 2 * j], v[2 * j + 1] + b1[c * 16 + 2 * j + 1]);
+      w[j] = pack_bf16x2(silu(v[2 * j] + b1[c * 16 + 2 * j]), silu(v[2 * j + 1] + b1[c * 16 + 2 * j + 1]));
     *reinterpret_cast<uint4*>(smem + FW_A1 + kmajor_offset(s, c * 16, NH)) = make_uint4(w[0], w[1], w[2], w[3]);
     *reinterpret_cast<uint4*>(smem + FW_A1 + kmajor_offset(s, c * 16 + 8, NH)) = make_uint4(w[4], w[5], w[6], w[7]);
   }
@@ -151,7 +137,7 @@ __device__ __forceinline__ bool forward128(uint8_t* smem, uint32_t taddr, uint32
     uint32_t w[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j)
-      w[j] = silu_bf16x2(v[2 * j] + b2[c * 16 + 2 * j], v[2 * j + 1] + b2[c * 16 + 2 * j + 1]);
+      w[j] = pack_bf16x2(silu(v[2 * j] + b2[c * 16 + 2 * j]), silu(v[2 * j + 1] + b2[c * 16 + 2 * j + 1]));
     *reinterpret_cast<uint4*>(smem + FW_A2 + kmajor_offset(s, c * 16, NH)) = make_uint4(w[0], w[1], w[2], w[3]);
     *reinterpret_cast<uint4*>(smem + FW_A2 + kmajor_offset(s, c * 16 + 8, NH)) = make_uint4(w[4], w[5], w[6], w[7]);
   }

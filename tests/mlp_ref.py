@@ -26,14 +26,6 @@ def silu(z):
     return z / (1.0 + np.exp(-z))
 
 
-def silu_bf16(z):
-    """The in-step forward pass's SiLU in BF16 arithmetic: the
-    pre-activation rounded to BF16, h = z / 2, t = tanh(h) rounded to BF16,
-    then h t + h rounded once (a fused multiply-add)."""
-    h = bf16(z) / 2.0
-    return bf16(h * bf16(np.tanh(h)) + h)
-
-
 def dsilu(z):
     s = 1.0 / (1.0 + np.exp(-z))
     return s * (1.0 + z * (1.0 - s))
@@ -50,17 +42,14 @@ def init(seed=0):
     }
 
 
-def forward(p, x, quantise=False, bf16_silu=False):
-    """bf16_silu: the activations as the in-step forward pass computes them
-    (silu_bf16); otherwise SiLU in FP64, rounded to BF16 if quantise."""
+def forward(p, x, quantise=False):
     q = bf16 if quantise else (lambda a: np.asarray(a, np.float64))
-    act = silu_bf16 if bf16_silu else (lambda z: q(silu(z)))
     W1, W2, W3 = q(p["W1"]), q(p["W2"]), q(p["W3"])
     a0 = q(x)
     z1 = a0 @ W1.T + p["b1"]
-    a1 = act(z1)
+    a1 = q(silu(z1))
     z2 = a1 @ W2.T + p["b2"]
-    a2 = act(z2)
+    a2 = q(silu(z2))
     y = a2 @ W3.T + p["b3"]
     return y, {"a0": a0, "z1": z1, "a1": a1, "z2": z2, "a2": a2, "W1": W1, "W2": W2, "W3": W3}
 

@@ -72,7 +72,7 @@ def test_forward_matches_reference():
         p[k] = 0.1 * np.random.default_rng(2).standard_normal(p[k].shape)
     y = R.mlp_forward(R.mlp_pack(p), nrm, _rows(x, t))
     xn, _ = _normalised(nrm, x, t)
-    yn_ref, _ = M.forward(p, xn, quantise=True, bf16_silu=True)
+    yn_ref, _ = M.forward(p, xn, quantise=True)
     yn = (y - nrm[24:27]) / nrm[27:30]
     err = np.abs(yn - yn_ref)
     assert err.max() < 0.02 * max(1.0, np.abs(yn_ref).max()), err.max()
