@@ -526,6 +526,26 @@ def run_gb300(args):
         ktau0 = ktau0 + args.e2e_records * every
         k = ktau0
         outs = [torch.empty((8, args.mp), dtype=torch.float32, pin_memory=pin) for _ in range(2)]
+        # this host's pinned copy bandwidth for the step's two transfers
+        # (end to end is at best max(device step, upload, download))
+        copy_gbs = None
+        if pin:
+            dev_in = torch.empty(host_f[0].shape, dtype=torch.float32, device="cuda:%d" % d.local)
+            dev_out = torch.empty(outs[0].shape, dtype=torch.float32, device="cuda:%d" % d.local)
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            dev_in.copy_(host_f[0], non_blocking=True)
+            torch.cuda.synchronize()
+            ev[0].record()
+            for i in range(len(host_f)):
+                dev_in.copy_(host_f[i], non_blocking=True)
+            ev[1].record()
+            for i in range(4):
+                outs[i % 2].copy_(dev_out, non_blocking=True)
+            ev[2].record()
+            torch.cuda.synchronize()
+            copy_gbs = {"h2d": len(host_f) * host_f[0].numel() * 4 / (ev[0].elapsed_time(ev[1]) * 1e6),
+                        "d2h": 4 * outs[0].numel() * 4 / (ev[1].elapsed_time(ev[2]) * 1e6)}
+            del dev_in, dev_out
         for n in range(2):   # warm the pipelined host path (staging buffers, copy streams)
             gc.step_host(k, host_f[(k - ktau0) % args.e2e_records].numpy(), outs[n].numpy(), dels); k += 1
         gc.synchronize()
@@ -542,7 +562,8 @@ def run_gb300(args):
         del host_f, outs
         return {"value": d.world * args.mp * args.e2e_steps / secs, "unit": "tile-timesteps/s",
                 "h2d_bytes_per_step": nb_in, "d2h_bytes_per_step": nb_out, "steps": args.e2e_steps,
-                "forcing_records": args.e2e_records, "ms_per_step": secs * 1e3 / args.e2e_steps, "clocks": ckr}
+                "forcing_records": args.e2e_records, "ms_per_step": secs * 1e3 / args.e2e_steps, "clocks": ckr,
+                "copy_gbs": copy_gbs}
     # On its own context with the tuned order and blocks, warmed up like the
     # headline's, so that it times the same early simulated period (the
     # per-step cost follows the snow and soil state) and leaves the
