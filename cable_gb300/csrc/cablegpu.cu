@@ -626,7 +626,10 @@ int cablegpu_set_field(cablegpu_ctx* c, int id, const void* host) {
   return CABLEGPU_OK;
 }
 
-int cablegpu_get_field(cablegpu_ctx* c, int id, void* host) {
+namespace {
+// Gathers one field into caller order in the staging buffer and queues its
+// copy to host on the context's stream (no synchronisation).
+int issue_get_field(cablegpu_ctx* c, int id, void* host) {
   if (!c || !host || id < 0 || id >= cablegpu_num_fields()) return fail(c, CABLEGPU_ERR_ARG, "get_field: bad argument");
   const FieldDef& f = registry()[id];
   if (f.kind == CABLEGPU_KIND_DIAG && !c->diag) return fail(c, CABLEGPU_ERR_STATE, "get_field: diagnostics are disabled");
@@ -646,6 +649,29 @@ int cablegpu_get_field(cablegpu_ctx* c, int id, void* host) {
     gather_out_kernel<double, double><<<grid, 256, 0, c->stream>>>((double*)c->d_stage, (const double*)d, c->d_order, c->mp, c->ld, f.nlayer);
   CG_CUDA(c, cudaGetLastError());
   CG_CUDA(c, cudaMemcpyAsync(host, c->d_stage, bytes, cudaMemcpyDeviceToHost, c->stream));
+  return CABLEGPU_OK;
+}
+}  // namespace
+
+int cablegpu_get_field(cablegpu_ctx* c, int id, void* host) {
+  const int rc = issue_get_field(c, id, host);
+  if (rc) return rc;
+  CG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CABLEGPU_OK;
+}
+
+int cablegpu_get_fields(cablegpu_ctx* c, int n, const int* ids, void* const* host) {
+  if (!c || n < 0 || (n > 0 && (!ids || !host))) return fail(c, CABLEGPU_ERR_ARG, "get_fields: bad argument");
+  // the gathers reuse one staging buffer: each waits on the stream for the
+  // copy before it, so the copies of all n fields go out back to back and
+  // the caller waits once
+  for (int i = 0; i < n; ++i) {
+    const int rc = issue_get_field(c, ids[i], host[i]);
+    if (rc) {
+      cudaStreamSynchronize(c->stream);
+      return rc;
+    }
+  }
   CG_CUDA(c, cudaStreamSynchronize(c->stream));
   return CABLEGPU_OK;
 }

@@ -119,6 +119,14 @@ MODULE cablegpu_c
       INTEGER(c_int), VALUE :: ktau, cycleno, numcycles
       REAL(c_float), VALUE :: dels
     END FUNCTION cablegpu_step_implicit
+    INTEGER(c_int) FUNCTION cablegpu_get_fields(ctx, n, ids, host) BIND(C, name="cablegpu_get_fields")
+      IMPORT :: c_int, c_ptr
+      TYPE(c_ptr), VALUE :: ctx
+      INTEGER(c_int), VALUE :: n
+      INTEGER(c_int), INTENT(IN) :: ids(*)
+      TYPE(c_ptr), INTENT(IN) :: host(*)
+    END FUNCTION cablegpu_get_fields
+
     INTEGER(c_int) FUNCTION cablegpu_host_register(ptr, bytes) BIND(C, name="cablegpu_host_register")
       IMPORT :: c_int, c_ptr, c_size_t
       TYPE(c_ptr), VALUE :: ptr

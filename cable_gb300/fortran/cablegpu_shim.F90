@@ -13,6 +13,12 @@ MODULE cablegpu_shim
   PUBLIC
 
   TYPE(c_ptr), SAVE :: ctx = c_null_ptr
+  ! Copy-back after each step: .TRUE. (default) copies every field the
+  ! offline driver reads; a driver may set it to .FALSE. on steps where it
+  ! neither writes output nor runs its own mass / energy balance checks,
+  ! and then only the fields it uses every step come back (runoff and melt,
+  ! screen temperature and humidity, the carbon fluxes, the balances).
+  LOGICAL, SAVE :: cbm_gpu_copy_all = .TRUE.
   INTEGER, SAVE :: mp_gpu = 0
   REAL(c_float), ALLOCATABLE, TARGET, SAVE :: forc(:, :)   ! (mp, 13)
   REAL(c_float), ALLOCATABLE, TARGET, SAVE :: outb(:, :)   ! (mp, 8)
@@ -214,20 +220,14 @@ CONTAINS
     REAL(c_double), ALLOCATABLE, TARGET :: r8(:, :)
     INTEGER(c_int), ALLOCATABLE, TARGET :: flags(:)
     ALLOCATE(r8(mp, ms), r4(mp, ms), flags(mp))
-    CALL get('fev', C_LOC(r4));    canopy%fev = r4(:, 1)
-    CALL get('fhv', C_LOC(r4));    canopy%fhv = r4(:, 1)
-    CALL get('fhs', C_LOC(r4));    canopy%fhs = r4(:, 1)
-    CALL get('fns', C_LOC(r4));    canopy%fns = r4(:, 1)
-    CALL get('fnv', C_LOC(r4));    canopy%fnv = r4(:, 1)
-    CALL get('fes', C_LOC(r4));    canopy%fes = r4(:, 1)
-    CALL get('fevc', C_LOC(r4));   canopy%fevc = r4(:, 1)
-    CALL get('fevw', C_LOC(r4));   canopy%fevw = r4(:, 1)
+    ! every step: the rates the driver rescales, the screen temperature of
+    ! its daily extremes, sumcflux's carbon fluxes and the balances
+    CALL get('runoff', C_LOC(r4)); ssnow%runoff = r4(:, 1) / dels
+    CALL get('rnof1', C_LOC(r4));  ssnow%rnof1 = r4(:, 1) / dels
+    CALL get('rnof2', C_LOC(r4));  ssnow%rnof2 = r4(:, 1) / dels
+    CALL get('smelt', C_LOC(r4));  ssnow%smelt = r4(:, 1) / dels
     CALL get('tscrn', C_LOC(r4));  canopy%tscrn = r4(:, 1)
     CALL get('qscrn', C_LOC(r4));  canopy%qscrn = r4(:, 1)
-    CALL get('us', C_LOC(r4));     canopy%us = r4(:, 1)
-    CALL get('cduv', C_LOC(r4));   canopy%cduv = r4(:, 1)
-    CALL get('epot', C_LOC(r4));   canopy%epot = r4(:, 1)
-    CALL get('dgdtg', C_LOC(r4));  canopy%dgdtg = r4(:, 1)
     CALL get('fpn', C_LOC(r4));    canopy%fpn = r4(:, 1)
     CALL get('fnpp', C_LOC(r4));   canopy%fnpp = r4(:, 1)
     CALL get('fnee', C_LOC(r4));   canopy%fnee = r4(:, 1)
@@ -236,6 +236,28 @@ CONTAINS
     CALL get('frpw', C_LOC(r4));   canopy%frpw = r4(:, 1)
     CALL get('frpr', C_LOC(r4));   canopy%frpr = r4(:, 1)
     CALL get('frs', C_LOC(r4));    canopy%frs = r4(:, 1)
+    CALL get('ebal', C_LOC(r4));   bal%ebal = r4(:, 1)
+    CALL get('wbal', C_LOC(r4));   bal%wbal = r4(:, 1)
+    CALL get('ebal_tot', C_LOC(r8)); bal%ebal_tot = REAL(r8(:, 1))
+    CALL get('wbal_tot', C_LOC(r8)); bal%wbal_tot = REAL(r8(:, 1))
+    IF (.NOT. cbm_gpu_copy_all) THEN
+      DEALLOCATE(r8, r4, flags)
+      RETURN
+    END IF
+    ! output steps and the driver's own balance checks: their inputs and
+    ! what the output writer accumulates
+    CALL get('fev', C_LOC(r4));    canopy%fev = r4(:, 1)
+    CALL get('fhv', C_LOC(r4));    canopy%fhv = r4(:, 1)
+    CALL get('fhs', C_LOC(r4));    canopy%fhs = r4(:, 1)
+    CALL get('fns', C_LOC(r4));    canopy%fns = r4(:, 1)
+    CALL get('fnv', C_LOC(r4));    canopy%fnv = r4(:, 1)
+    CALL get('fes', C_LOC(r4));    canopy%fes = r4(:, 1)
+    CALL get('fevc', C_LOC(r4));   canopy%fevc = r4(:, 1)
+    CALL get('fevw', C_LOC(r4));   canopy%fevw = r4(:, 1)
+    CALL get('us', C_LOC(r4));     canopy%us = r4(:, 1)
+    CALL get('cduv', C_LOC(r4));   canopy%cduv = r4(:, 1)
+    CALL get('epot', C_LOC(r4));   canopy%epot = r4(:, 1)
+    CALL get('dgdtg', C_LOC(r4));  canopy%dgdtg = r4(:, 1)
     CALL get('delwc', C_LOC(r4));  canopy%delwc = r4(:, 1)
     CALL get('through', C_LOC(r4)); canopy%through = r4(:, 1)
     CALL get('precis', C_LOC(r4)); canopy%precis = r4(:, 1)
@@ -243,10 +265,6 @@ CONTAINS
     CALL get('ghflux', C_LOC(r4)); canopy%ghflux = r4(:, 1)
     CALL get('sghflux', C_LOC(r4)); canopy%sghflux = r4(:, 1)
     CALL get('cansto', C_LOC(r4)); canopy%cansto = r4(:, 1)
-    CALL get('runoff', C_LOC(r4)); ssnow%runoff = r4(:, 1) / dels
-    CALL get('rnof1', C_LOC(r4));  ssnow%rnof1 = r4(:, 1) / dels
-    CALL get('rnof2', C_LOC(r4));  ssnow%rnof2 = r4(:, 1) / dels
-    CALL get('smelt', C_LOC(r4));  ssnow%smelt = r4(:, 1) / dels
     CALL get('wetfac', C_LOC(r4)); ssnow%wetfac = r4(:, 1)
     CALL get('potev', C_LOC(r4));  ssnow%potev = r4(:, 1)
     CALL get('cls', C_LOC(r4));    ssnow%cls = r4(:, 1)
@@ -255,10 +273,6 @@ CONTAINS
     CALL get('albedo_nir', C_LOC(r4)); rad%albedo(:, 2) = r4(:, 1)
     CALL get('transd', C_LOC(r4)); rad%transd = r4(:, 1)
     CALL get('qssabs', C_LOC(r4)); rad%qssabs = r4(:, 1)
-    CALL get('ebal', C_LOC(r4));   bal%ebal = r4(:, 1)
-    CALL get('wbal', C_LOC(r4));   bal%wbal = r4(:, 1)
-    CALL get('ebal_tot', C_LOC(r8)); bal%ebal_tot = REAL(r8(:, 1))
-    CALL get('wbal_tot', C_LOC(r8)); bal%wbal_tot = REAL(r8(:, 1))
     ! soil and snow profiles, snow and surface temperature
     CALL get('wb', C_LOC(r8));     ssnow%wb = r8
     CALL get('wbice', C_LOC(r8));  ssnow%wbice = r8

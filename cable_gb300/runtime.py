@@ -43,7 +43,7 @@ EXPORTS = [
     "cablegpu_run_forcing_file", "cablegpu_set_host_layout", "cablegpu_tile_order",
     "cablegpu_step_explicit", "cablegpu_step_implicit", "cablegpu_coupled_timed", "cablegpu_set_soil_solve",
     "cablegpu_set_canopy_schedule", "cablegpu_check_tile_param", "cablegpu_tune_blocks",
-    "cablegpu_host_register", "cablegpu_host_unregister",
+    "cablegpu_host_register", "cablegpu_host_unregister", "cablegpu_get_fields",
 ]
 NOALLOC_MAX_TILES = 65536
 # soil tridiagonal solve arithmetic (cablegpu_set_soil_solve)
@@ -201,6 +201,7 @@ def load(build_if_missing: bool = True):
     L.cablegpu_step_host.argtypes = [vp, ip, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.cablegpu_set_blocks.argtypes = [vp, C.POINTER(ip)]
     L.cablegpu_get_config.argtypes = [vp, C.POINTER(ip), C.POINTER(ip)]
+    L.cablegpu_get_fields.argtypes = [vp, ip, C.POINTER(ip), C.POINTER(vp)]
     L.cablegpu_host_register.argtypes = [vp, C.c_size_t]
     L.cablegpu_host_unregister.argtypes = [vp]
     L.cablegpu_tune_blocks.argtypes = [vp, ip, ip, C.c_float, C.POINTER(ip), C.POINTER(C.c_float)]
@@ -408,6 +409,14 @@ class CableGPU:
         out = np.empty((nl, self.mp), _NP[dt])
         self._check(self.L.cablegpu_get_field(self.h, fid, out.ctypes.data_as(C.c_void_p)))
         return out
+
+    def get_many(self, names):
+        """Several fields in one call (cablegpu_get_fields): {name: array}."""
+        outs = {n: np.empty((self.fields[n][1], self.mp), _NP[self.fields[n][2]]) for n in names}
+        ids = (C.c_int * len(names))(*[self.fields[n][0] for n in names])
+        ptrs = (C.c_void_p * len(names))(*[outs[n].ctypes.data for n in names])
+        self._check(self.L.cablegpu_get_fields(self.h, len(names), ids, ptrs))
+        return outs
 
     def set(self, name, value):
         fid, nl, dt, _ = self.fields[name]

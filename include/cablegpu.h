@@ -124,6 +124,15 @@ int cablegpu_field_id(const char* name);
  * get: the caller reads them back (output / restart write). */
 int cablegpu_set_field(cablegpu_ctx* ctx, int id, const void* host);
 int cablegpu_get_field(cablegpu_ctx* ctx, int id, void* host);
+/* Copies n fields to host buffers in one call (host[i] as for
+ * cablegpu_get_field of field ids[i]): the gathers and device-to-host copies
+ * go out back to back on the context's stream and the call waits once,
+ * where n calls of cablegpu_get_field wait n times.  The per-step copy-back
+ * of a driver (the Fortran shim's groups of driver-read fields; the
+ * reference's types are filled in place between cbm() calls, which needs no
+ * copy).  Stops at the first bad id with CABLEGPU_ERR_ARG; fields before it
+ * have been copied. */
+int cablegpu_get_fields(cablegpu_ctx* ctx, int n, const int* ids, void* const* host);
 /* Device pointer and leading dimension (elements between layers) of a field,
  * for callers that keep their own device-side pipelines. */
 int cablegpu_field_device_ptr(cablegpu_ctx* ctx, int id, void** dptr, int* ld);

@@ -155,3 +155,24 @@ def test_host_registered_buffers_step_like_any_host_buffers():
         g.close()
     for a, b in zip(*outs):
         np.testing.assert_array_equal(a, b)
+
+
+def test_batched_copy_back_equals_single_copies():
+    """cablegpu_get_fields (one wait for many fields) gives the same arrays
+    as cablegpu_get_field per field, for state of every storage type
+    (double-FP32, FP64, FP32, bytes) and diagnostics."""
+    from cable_gb300 import runtime as R
+    ts = W.snow_grid(6000, seed=9, nsteps=3)
+    g = R.from_tileset(ts)
+    g.set_options(diag=True)
+    for k in (1, 2, 3):
+        g.step(k)
+    names = ["wb", "wbice", "gammzz1", "tgg", "tggsn", "flags", "snowd", "cansto", "out", "fev", "runoff", "tscrn",
+             "ebal_tot", "wbal_tot"]
+    many = g.get_many(names)
+    for n in names:
+        np.testing.assert_array_equal(many[n], g.get(n), err_msg=n)
+    # an unknown field id is refused
+    rc = g.L.cablegpu_get_fields(g.h, 1, (R.C.c_int * 1)(-1), (R.C.c_void_p * 1)(None))
+    assert rc == -1, rc
+    g.close()
