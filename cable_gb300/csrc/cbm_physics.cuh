@@ -404,6 +404,34 @@ __device__ __forceinline__ double rcp64(double x) {
 // b(1) are one reciprocal here, every division a multiplication by an FP64
 // reciprocal (rcp64, within an ulp of the division), and g(k) overwrites
 // rhs(k), so only e and the solution are live in FP64.
+// Both are written with explicit fused multiply-adds, so their rounding does
+// not depend on where the compiler inlines them: a soil column solves to the
+// same bits in either (the heat kernel's warps choose between them).
+// trimb64_s: the same with db added to the diagonal of row srow, 0 or S
+// (the surface row of a system whose first S rows may be identity rows):
+// adding 0.0 to the other candidate row changes nothing.
+template <int N, int S>
+__device__ __forceinline__ void trimb64_s(const float* a, const float* c, double db, bool s_first, double* rhs) {
+  double e[N - 1];
+  const double ib = rcp64((1.0 - f2d(a[0]) - f2d(c[0])) + (s_first ? db : 0.0));
+  e[0] = f2d(c[0]) * ib;
+  rhs[0] = rhs[0] * ib;
+#pragma unroll
+  for (int k = 1; k < N - 1; ++k) {
+    const double ak = f2d(a[k]), ck = f2d(c[k]);
+    const double bk = (k == S) ? (1.0 - ak - ck) + (s_first ? 0.0 : db) : (1.0 - ak - ck);
+    const double temp = rcp64(fma(-ak, e[k - 1], bk));
+    e[k] = ck * temp;
+    rhs[k] = fma(-ak, rhs[k - 1], rhs[k]) * temp;
+  }
+  {
+    const double ak = f2d(a[N - 1]), ck = f2d(c[N - 1]);
+    rhs[N - 1] = fma(-ak, rhs[N - 2], rhs[N - 1]) * rcp64(fma(-ak, e[N - 2], 1.0 - ak - ck));
+  }
+#pragma unroll
+  for (int k = N - 2; k >= 0; --k) rhs[k] = fma(-e[k], rhs[k + 1], rhs[k]);
+}
+
 template <int N>
 __device__ __forceinline__ void trimb64(const float* a, const float* c, double db0, double* rhs) {
   double e[N - 1];
@@ -413,16 +441,16 @@ __device__ __forceinline__ void trimb64(const float* a, const float* c, double d
 #pragma unroll
   for (int k = 1; k < N - 1; ++k) {
     const double ak = f2d(a[k]), ck = f2d(c[k]);
-    const double temp = rcp64((1.0 - ak - ck) - ak * e[k - 1]);
+    const double temp = rcp64(fma(-ak, e[k - 1], 1.0 - ak - ck));
     e[k] = ck * temp;
-    rhs[k] = (rhs[k] - ak * rhs[k - 1]) * temp;
+    rhs[k] = fma(-ak, rhs[k - 1], rhs[k]) * temp;
   }
   {
     const double ak = f2d(a[N - 1]), ck = f2d(c[N - 1]);
-    rhs[N - 1] = (rhs[N - 1] - ak * rhs[N - 2]) * rcp64((1.0 - ak - ck) - ak * e[N - 2]);
+    rhs[N - 1] = fma(-ak, rhs[N - 2], rhs[N - 1]) * rcp64(fma(-ak, e[N - 2], 1.0 - ak - ck));
   }
 #pragma unroll
-  for (int k = N - 2; k >= 0; --k) rhs[k] = rhs[k] - e[k] * rhs[k + 1];
+  for (int k = N - 2; k >= 0; --k) rhs[k] = fma(-e[k], rhs[k + 1], rhs[k]);
 }
 
 // Tridiagonal solve in correction form (the elimination of cbl_trimb.F90:17-53

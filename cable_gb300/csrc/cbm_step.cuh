@@ -1585,7 +1585,15 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
     //   (trid_correction).  Subtracting A T_old leaves ga * dtg on the
     //   surface row and -a_k (T_{k-1} - T_k) - c_k (T_{k+1} - T_k)
     //   everywhere: the surface-coupling terms in dgdtg cancel exactly.
-    if (isflag == 0) {
+    // kS64: a warp whose tiles all lack snow layers solves the 6 soil rows;
+    // a warp with a snow-layered tile solves the 9-row system for each of
+    // its tiles, the others with identity snow rows (zero coefficients and
+    // right-hand side) and the surface coupling on soil row 1, which gives
+    // them the soil temperatures of their 6-row solve to the bit (the
+    // identity rows add exact zeros) instead of running both solves one
+    // after the other in the warp.
+    const bool rows9 = kS64 ? __any_sync(__activemask(), isflag != 0) : (isflag != 0);
+    if (!rows9) {
       // soil-only system: the snow rows of the reference's 9-row system are
       // identity rows decoupled from the soil (coeff(1) = 0), so the 6-row
       // solve gives the same soil temperatures
@@ -1601,7 +1609,9 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
         double rd[CG_MS];
 #pragma unroll
         for (int k = 1; k < CG_MS; ++k) rd[k] = f2d(tgg[k]);
-        rd[0] = f2d(tgg[0] + (ga - tgg[0] * dgdtg) * dtg0);
+        // the explicit surface update T_1 + (ga - T_1 dgdtg) dtg, rounded
+        // the same in both solves
+        rd[0] = f2d(__fmaf_rn(__fmaf_rn(-tgg[0], dgdtg, ga), dtg0, tgg[0]));
         trimb64<CG_MS>(a, c, -f2d(dgdtg) * f2d(dtg0), rd);
 #pragma unroll
         for (int k = 0; k < CG_MS; ++k) tgg[k] = d2f(rd[k]);
@@ -1622,15 +1632,17 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
       }
       ghflux = coefb * (tgg[0] - tgg[1]);
     } else {
-      // rows 0-2 snow layers, 3-8 soil layers
+      // rows 0-2 snow layers (identity rows for a tile without them), 3-8
+      // soil layers
+      const bool snow = isflag != 0;
       const float csnow[4] = {0.f, csn[0], csn[1], coeff[0]};   // coeff(-2..1)
       float x[9], a[9], c[9];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        x[k] = tggsn[k];
-        const float dtg = dels / (ssdn[k] * CGSNOW * sdepth[k]);
-        a[k] = -dtg * csnow[k];
-        c[k] = -dtg * csnow[k + 1];
+        x[k] = snow ? tggsn[k] : 0.f;
+        const float dtg = snow ? dels / (ssdn[k] * CGSNOW * sdepth[k]) : 0.f;
+        a[k] = snow ? -dtg * csnow[k] : 0.f;
+        c[k] = snow ? -dtg * csnow[k + 1] : 0.f;
       }
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k) {
@@ -1639,18 +1651,23 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
         a[3 + k] = -dtg * coeff[k];
         c[3 + k] = -dtg * coeff[k + 1];
       }
-      const float dtg0 = dels / (ssdn[0] * CGSNOW * sdepth[0]);
       if constexpr (kS64) {
+        // the surface row: the top snow layer, or soil layer 1
+        const float dtg0 = snow ? dels / (ssdn[0] * CGSNOW * sdepth[0]) : dels / gf[0];
+        const int s0 = snow ? 0 : 3;
         double rd[9];
 #pragma unroll
-        for (int k = 1; k < 9; ++k) rd[k] = f2d(x[k]);
-        rd[0] = f2d(x[0] + (ga - x[0] * dgdtg) * dtg0);
-        trimb64<9>(a, c, -f2d(dgdtg) * f2d(dtg0), rd);
+        for (int k = 0; k < 9; ++k) rd[k] = f2d(x[k]);
+        rd[s0] = f2d(__fmaf_rn(__fmaf_rn(-x[s0], dgdtg, ga), dtg0, x[s0]));
+        trimb64_s<9, 3>(a, c, -f2d(dgdtg) * f2d(dtg0), snow, rd);
+        if (snow) {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) tggsn[k] = d2f(rd[k]);
+          for (int k = 0; k < 3; ++k) tggsn[k] = d2f(rd[k]);
+        }
 #pragma unroll
         for (int k = 0; k < CG_MS; ++k) tgg[k] = d2f(rd[3 + k]);
       } else {
+        const float dtg0 = dels / (ssdn[0] * CGSNOW * sdepth[0]);
         float b[9], r[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
@@ -1667,7 +1684,7 @@ __device__ __forceinline__ void phase_c2(const CgDev& D, const CgTables* __restr
 #pragma unroll
         for (int k = 0; k < CG_MS; ++k) tgg[k] = x[3 + k] + r[3 + k];
       }
-      sghflux = csn[0] * (tggsn[0] - tggsn[1]);
+      if (snow) sghflux = csn[0] * (tggsn[0] - tggsn[1]);
       ghflux = coefb * (tgg[0] - tgg[1]);
     }
   }
