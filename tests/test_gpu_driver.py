@@ -176,3 +176,25 @@ def test_batched_copy_back_equals_single_copies():
     rc = g.L.cablegpu_get_fields(g.h, 1, (R.C.c_int * 1)(-1), (R.C.c_void_p * 1)(None))
     assert rc == -1, rc
     g.close()
+
+
+def test_tune_blocks_leaves_the_run_unchanged():
+    """cablegpu_tune_blocks times block sizes on the context's own state and
+    puts the state back: the steps after it are bitwise those of a context
+    that was not tuned (results do not depend on block sizes either)."""
+    from cable_gb300 import runtime as R
+    ts = W.snow_grid(20000, seed=13, nsteps=12)
+    runs = []
+    for tune in (False, True):
+        g = R.from_tileset(ts)
+        g.run(1, 4)
+        g.synchronize()
+        if tune:
+            blocks, ms = g.tune_blocks(5, 2)
+            assert len(blocks) == 5 and all(b in (32, 64, 128, 256) for b in blocks) and ms > 0
+        g.run(5, 8)
+        g.synchronize()
+        runs.append({k: g.get(k) for k in ("out", "wb", "tgg", "snowd", "cansto", "wbal_tot", "tile_status")})
+        g.close()
+    for k in runs[0]:
+        np.testing.assert_array_equal(runs[0][k], runs[1][k], err_msg=k)
