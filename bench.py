@@ -533,7 +533,13 @@ def run_gb300(args):
             dev_in = torch.empty(host_f[0].shape, dtype=torch.float32, device="cuda:%d" % d.local)
             dev_out = torch.empty(outs[0].shape, dtype=torch.float32, device="cuda:%d" % d.local)
             ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-            dev_in.copy_(host_f[0], non_blocking=True)
+            # one untimed pass first: the first transfer from a freshly
+            # pinned buffer is several times slower than the later ones,
+            # and the timed steps below each reuse buffers already copied
+            for i in range(len(host_f)):
+                dev_in.copy_(host_f[i], non_blocking=True)
+            for i in range(2):
+                outs[i].copy_(dev_out, non_blocking=True)
             torch.cuda.synchronize()
             ev[0].record()
             for i in range(len(host_f)):
