@@ -370,24 +370,30 @@ __device__ __forceinline__ float d2f(double x) {
   return __uint_as_float(f | (hi & 0x80000000u));
 }
 
-// 1/x in FP64: one Newton-Raphson step r <- r + r (1 - x r) (two fused
-// multiply-adds; it squares the seed's relative error) from a double-float
-// seed accurate to ~2^-46, which leaves the result within an ulp of the
-// correctly rounded reciprocal.  The seed is formed on the FP32 and integer
-// pipes: x is split (df_split) into hi (x truncated to 24 significant bits)
-// and lo (its next 23 bits); r = the FP32 reciprocal of hi, and the
-// FP32 correction c = r (1 - (hi + lo) r), the residual formed with fused
-// multiply-adds, makes r + c the reciprocal of x to about 2^-46.  One FP64
-// addition joins r and c.  Three FP64-pipe instructions in all, against
-// four for two Newton steps from an FP32 seed.  For 2^-74 <= |x| < 2^127
-// (the soil systems' pivots are >= 1, their pore spaces 0.01-0.6).  Tested
-// against CUDA's FP64 division (tests/test_fp64_reciprocal.py).
+// 1/x in FP64 from two fused multiply-adds.  R, the FP32 reciprocal of x's
+// leading 24 bits (df_split: integer operations), is within about 2^-22 of
+// 1/x; widened exactly (f2d) it has 29 zero fraction bits at the bottom.
+// With t = 1 - x R (the first FMA; exact before its one rounding),
+// 1/x = R (1 + t + t^2 + ...).  c = R (1 + t^2) is R's bit pattern plus the
+// integer k = R t^2 / ulp(R), rounded, formed on the FP32 pipe from t
+// truncated to FP32 (k < 2^10, so it lands in R's zero bits: no carry, no
+// normalisation); r = R t + c is the second FMA.  The error is below one
+// ulp (the roundings of k and of the second FMA; t^3 is below 2^-64):
+// faithfully rounded.  Two FP64-pipe instructions, against three for a
+// Newton step from a double-float seed (1/(1 - t) is the geometric series;
+// the t^2 term rides in the addend's spare bits).  For 2^-80 <= |x| < 2^126 (the soil systems' pivots are >= 1).  Tested against
+// CUDA's FP64 division (tests/test_fp64_reciprocal.py).
 __device__ __forceinline__ double rcp64(double x) {
-  const df32 xs = df_split(x);
-  const float r = __fdividef(1.0f, xs.hi);
-  const float e = __fmaf_rn(-xs.lo, r, __fmaf_rn(-xs.hi, r, 1.0f));
-  const double r0 = f2d(r) + f2d(__fmul_rn(r, e));
-  return fma(r0, fma(-x, r0, 1.0), r0);
+  const float r = __fdividef(1.0f, df_split(x).hi);
+  const double rd = f2d(r);
+  const double t = fma(-x, rd, 1.0);
+  const float tf = df_split(t).hi;
+  const float mf = __uint_as_float((__float_as_uint(r) & 0x007fffffu) | 0x3f800000u);   // R's significand
+  // k + 2^23 in the float whose ulp is 1: k = round(t^2 mf 2^52)
+  const float kf = __fmaf_rn(__fmul_rn(__fmul_rn(tf, tf), mf), 4503599627370496.0f, 8388608.0f);
+  const unsigned int k = __float_as_uint(kf) - 0x4B000000u;
+  const double c = __hiloint2double(__double2hiint(rd), (int)((unsigned int)__double2loint(rd) + k));
+  return fma(rd, t, c);
 }
 
 // cbl_trimb.F90:17-53 in FP64, as the reference solves both soil systems,
@@ -432,10 +438,12 @@ __device__ __forceinline__ void trimb64_s(const float* a, const float* c, double
   for (int k = N - 2; k >= 0; --k) rhs[k] = fma(-e[k], rhs[k + 1], rhs[k]);
 }
 
-template <int N>
+// kDb0 false: no surface term (db0 is ignored), one FP64 addition fewer.
+template <int N, bool kDb0 = true>
 __device__ __forceinline__ void trimb64(const float* a, const float* c, double db0, double* rhs) {
   double e[N - 1];
-  const double ib = rcp64((1.0 - f2d(a[0]) - f2d(c[0])) + db0);
+  const double b0 = 1.0 - f2d(a[0]) - f2d(c[0]);
+  const double ib = rcp64(kDb0 ? b0 + db0 : b0);
   e[0] = f2d(c[0]) * ib;
   rhs[0] = rhs[0] * ib;
 #pragma unroll

@@ -1930,7 +1930,7 @@ __device__ __forceinline__ void phase_c3(const CgDev& D, const CgTables* __restr
         a[k - 1] = -dtt[k - 1] * z3;
         c[k - 2] = -dtt[k - 2] * z3;
       }
-      trimb64<CG_MS>(a, c, 0.0, rd);
+      trimb64<CG_MS, false>(a, c, 0.0, rd);
 #pragma unroll
       for (int k = 0; k < CG_MS; ++k) {
         wb[k] = df_add(df_mul(df_split(rd[k]), sat[k]), wbice[k]);
