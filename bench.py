@@ -551,6 +551,26 @@ def run_gb300(args):
             torch.cuda.synchronize()
             copy_gbs = {"h2d": len(host_f) * host_f[0].numel() * 4 / (ev[0].elapsed_time(ev[1]) * 1e6),
                         "d2h": 4 * outs[0].numel() * 4 / (ev[1].elapsed_time(ev[2]) * 1e6)}
+            # both directions at once, as the pipelined steps run them: a
+            # step's upload and download on two streams, repeated
+            sa, sb = torch.cuda.Stream(), torch.cuda.Stream()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            sa.wait_event(e0)
+            sb.wait_event(e0)
+            for i in range(len(host_f)):
+                with torch.cuda.stream(sa):
+                    dev_in.copy_(host_f[i], non_blocking=True)
+                with torch.cuda.stream(sb):
+                    outs[i % 2].copy_(dev_out, non_blocking=True)
+            torch.cuda.current_stream().wait_stream(sa)
+            torch.cuda.current_stream().wait_stream(sb)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            copy_gbs["both_ms_per_step"] = ms / len(host_f)
+            copy_gbs["both_gbs"] = len(host_f) * (host_f[0].numel() + outs[0].numel()) * 4 / (ms * 1e6)
             del dev_in, dev_out
         for n in range(2):   # warm the pipelined host path (staging buffers, copy streams)
             gc.step_host(k, host_f[(k - ktau0) % args.e2e_records].numpy(), outs[n].numpy(), dels); k += 1
