@@ -29,6 +29,13 @@ namespace {
 
 constexpr int kGraphSteps = 8;      // steps per captured CUDA graph
 constexpr int kKernelsPerStep = 5;  // radiation, canopy, snow pack, soil heat, soil water
+// The kernels index row r of a field as r * ld + t in 32-bit int: every
+// multi-row block (the diagnostics, the hand-off records, the forcing) has
+// at most 64 rows, and ld (mp rounded up to 256) stays at most
+// CABLEGPU_MAX_TILES, so no offset reaches 2^31.
+static_assert(CG_NDIAG <= 64 && CG_NA <= 64 && CG_NFORC <= 64 && CG_NOUT <= 64, "row blocks of at most 64 rows");
+static_assert(CABLEGPU_MAX_TILES % 256 == 0 && 64LL * CABLEGPU_MAX_TILES <= 2147483647LL,
+              "the largest context's row offsets fit 32 bits");
 
 // ---------------------------------------------------------------- field registry
 enum Storage { S_U8, S_F32, S_F64, S_DF };   // S_DF: double-FP32 pairs (hi rows, then lo rows)
@@ -449,8 +456,8 @@ int cablegpu_field_id(const char* name) {
 }
 
 int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out) {
-  if (!tiles || !out || tiles->mp <= 0 || !tiles->iveg || !tiles->isoilm || !tiles->vlai || !tiles->lat ||
-      tiles->order < -1 || tiles->order > 3)
+  if (!tiles || !out || tiles->mp <= 0 || tiles->mp > CABLEGPU_MAX_TILES || !tiles->iveg || !tiles->isoilm ||
+      !tiles->vlai || !tiles->lat || tiles->order < -1 || tiles->order > 3)
     return CABLEGPU_ERR_ARG;
   for (int i = 0; i < tiles->mp; ++i)
     if (tiles->iveg[i] < 1 || tiles->iveg[i] > CG_NPFT || tiles->isoilm[i] < 1 || tiles->isoilm[i] > CG_NSOIL)

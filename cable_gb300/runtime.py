@@ -46,6 +46,7 @@ EXPORTS = [
     "cablegpu_host_register", "cablegpu_host_unregister", "cablegpu_get_fields",
 ]
 NOALLOC_MAX_TILES = 65536
+MAX_TILES = 33554176      # CABLEGPU_MAX_TILES: the most tiles one context takes
 # soil tridiagonal solve arithmetic (cablegpu_set_soil_solve)
 SOLVE_FP64 = 0
 SOLVE_FP32_CHANGE = 1

@@ -84,7 +84,13 @@ typedef struct {
 
 /* Creates a context on CUDA device `device` for tiles->mp tiles and uploads
  * the tile description.  Replaces the per-run set-up the reference driver
- * does before its time loop (load_parameters, cable_serial.F90:399).  */
+ * does before its time loop (load_parameters, cable_serial.F90:399).
+ * 1 <= tiles->mp <= CABLEGPU_MAX_TILES, else CABLEGPU_ERR_ARG: the kernels
+ * address a tile's row of a multi-row field (up to 64 rows: the
+ * diagnostics block, the hand-off records) with 32-bit offsets, and a
+ * context of that many tiles takes ~34 GB of device memory; a larger grid
+ * is split over several contexts. */
+#define CABLEGPU_MAX_TILES 33554176
 int cablegpu_create(const cablegpu_tiles* tiles, int device, cablegpu_ctx** out);
 int cablegpu_destroy(cablegpu_ctx* ctx);
 

@@ -35,6 +35,7 @@ def test_binding_constants_match_the_header():
     txt = open(HEADER).read()
     defs = dict(re.findall(r"#define\s+(CABLEGPU_\w+)\s+\(?(-?\d+)\)?", txt))
     assert int(defs["CABLEGPU_NOALLOC_MAX_TILES"]) == R.NOALLOC_MAX_TILES
+    assert int(defs["CABLEGPU_MAX_TILES"]) == R.MAX_TILES
     assert int(defs["CABLEGPU_NFORCING"]) == R.NFORCING
     for name in ("MEDLYN", "SOIL_THERMAL_FIX", "LITTER", "L_REV_CORR", "FWSOIL_NONLINEAR", "FWSOIL_LAI_KTAUL",
                  "POTEV_PM", "NEW_REDUCE_SOILEVP", "NEW_RUNOFF_SPEED", "DIAG_SOIL_RESP_OFF"):
@@ -71,6 +72,15 @@ def test_create_rejects_bad_tiles_without_a_gpu():
     ts.isoilm[0] = 0
     with pytest.raises(R.CableGPUError):
         R.CableGPU(ts)
+    # more tiles than 32-bit row offsets address: refused before the arrays
+    # are read (these hold 16 tiles) and before any CUDA call
+    ts.isoilm[0] = 1
+    L = R.load()
+    t = R._Tiles(R.MAX_TILES + 1, ts.iveg.ctypes.data_as(C.POINTER(C.c_int)),
+                 ts.isoilm.ctypes.data_as(C.POINTER(C.c_int)), ts.vlai.ctypes.data_as(C.POINTER(C.c_float)),
+                 ts.lat.ctypes.data_as(C.POINTER(C.c_float)), None, None, None, 0)
+    h = C.c_void_p()
+    assert L.cablegpu_create(C.byref(t), 0, C.byref(h)) == -1 and not h.value
 
 
 def test_null_arguments_are_errors():
