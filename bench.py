@@ -27,9 +27,7 @@ Multi-GPU: one process per GPU (torchrun); every rank advances its own
 from __future__ import annotations
 
 import argparse
-import ctypes
 import json
-import mmap
 import os
 import statistics
 import subprocess
@@ -168,47 +166,28 @@ class ClockSampler:
 
 # ---------------------------------------------------------------- host buffers
 class PinnedHost:
-    """Host arrays of the end-to-end steps: one anonymous mapping for all of
-    them, aligned to and sized in the kernel's transparent huge pages and
-    advised MADV_HUGEPAGE before it is first touched, then page-locked once
-    through the library's own cablegpu_host_register.  The copy engines
-    translate every page they move while the step's kernels run; the same
-    forcing records on small pages, one allocation each, ran the end-to-end
-    steps at 3.0 to 7.1 ms from one process to the next on one machine, and
-    at 3.0 ms from huge pages."""
-
-    ALIGN = 1 << 16
+    """Host arrays of the end-to-end steps, all in one block of page-locked
+    memory from the library's cablegpu_host_alloc (runtime.HostBlock): one
+    mapping aligned to the kernel's transparent huge page size, advised
+    MADV_HUGEPAGE before its first touch and registered once.  The copy
+    engines translate every page they move while the step's kernels run; the
+    same forcing records on small pages, one pinned allocation each, ran the
+    end-to-end steps at 3.0 to 7.1 ms from one process to the next on one
+    machine, and at 3.0 ms from huge pages."""
 
     def __init__(self, g, shapes):
-        import numpy as np
-        self.g = g
-        try:
-            self.hp = int(open("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size").read())
-        except (OSError, ValueError):
-            self.hp = 2 << 20
-        counts = [int(np.prod(sh)) for sh in shapes]
-        offs, tot = [], 0
-        for n in counts:
-            offs.append(tot)
-            tot += -(-4 * n // self.ALIGN) * self.ALIGN
-        size = -(-tot // self.hp) * self.hp
+        from cable_gb300 import runtime as R
         thp0 = self.anon_huge_kb()
-        self.map = mmap.mmap(-1, size + self.hp, flags=mmap.MAP_PRIVATE | mmap.MAP_ANONYMOUS)
-        base = ctypes.addressof(ctypes.c_char.from_buffer(self.map))
-        off = (-base) % self.hp
-        if hasattr(mmap, "MADV_HUGEPAGE"):
-            try:
-                self.map.madvise(mmap.MADV_HUGEPAGE, off, size)
-            except OSError:
-                pass
-        self.whole = np.frombuffer(self.map, dtype=np.float32, count=size // 4, offset=off)
-        self.whole.fill(0)
-        g.host_register(self.whole)
+        self.block = R.HostBlock(shapes)
         thp1 = self.anon_huge_kb()
-        self.arrays = [self.whole[o // 4:o // 4 + n].reshape(sh) for o, n, sh in zip(offs, counts, shapes)]
-        self.info = {"huge_page_bytes": self.hp, "bytes": int(size), "arrays": len(shapes),
+        self.arrays = self.block.arrays
+        try:
+            hp = int(open("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size").read())
+        except (OSError, ValueError):
+            hp = None
+        self.info = {"huge_page_bytes": hp, "bytes": int(self.block.nbytes), "arrays": len(shapes),
                      "anon_huge_pages_gained_bytes": None if thp0 is None or thp1 is None else 1024 * (thp1 - thp0),
-                     "locked_by": "cablegpu_host_register, one region"}
+                     "allocated_by": "cablegpu_host_alloc, one block"}
 
     @staticmethod
     def anon_huge_kb():
@@ -221,10 +200,8 @@ class PinnedHost:
         return None
 
     def close(self):
-        if self.whole is not None:
-            self.g.host_unregister(self.whole)
         self.arrays = []
-        self.whole = None
+        self.block.free()
 
 
 # ---------------------------------------------------------------- CPU (oracle)

@@ -137,6 +137,18 @@ MODULE cablegpu_c
       IMPORT :: c_int, c_ptr
       TYPE(c_ptr), VALUE :: ptr
     END FUNCTION cablegpu_host_unregister
+
+    ! page-locked host memory on huge pages, for the per-step buffers
+    INTEGER(c_int) FUNCTION cablegpu_host_alloc(bytes, out) BIND(C, name="cablegpu_host_alloc")
+      IMPORT :: c_int, c_ptr, c_size_t
+      INTEGER(c_size_t), VALUE :: bytes
+      TYPE(c_ptr) :: out
+    END FUNCTION cablegpu_host_alloc
+
+    INTEGER(c_int) FUNCTION cablegpu_host_free(ptr) BIND(C, name="cablegpu_host_free")
+      IMPORT :: c_int, c_ptr
+      TYPE(c_ptr), VALUE :: ptr
+    END FUNCTION cablegpu_host_free
   END INTERFACE
 
 CONTAINS

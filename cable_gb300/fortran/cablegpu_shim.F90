@@ -20,8 +20,11 @@ MODULE cablegpu_shim
   ! screen temperature and humidity, the carbon fluxes, the balances).
   LOGICAL, SAVE :: cbm_gpu_copy_all = .TRUE.
   INTEGER, SAVE :: mp_gpu = 0
-  REAL(c_float), ALLOCATABLE, TARGET, SAVE :: forc(:, :)   ! (mp, 13)
-  REAL(c_float), ALLOCATABLE, TARGET, SAVE :: outb(:, :)   ! (mp, 8)
+  ! the per-step forcing and output buffers, in page-locked host memory
+  ! from cablegpu_host_alloc (huge pages, so that the copies that overlap
+  ! the kernels are not slowed by page translation)
+  REAL(c_float), POINTER, SAVE :: forc(:, :) => NULL()   ! (mp, 13)
+  REAL(c_float), POINTER, SAVE :: outb(:, :) => NULL()   ! (mp, 8)
   ! caller tile (1-based) of each device slot: the per-step forcing and
   ! outputs move in device order (cablegpu_set_host_layout), gathered and
   ! scattered through this index on the host
@@ -72,6 +75,7 @@ CONTAINS
     TYPE(soil_snow_type), INTENT(IN) :: ssnow
     TYPE(veg_parameter_type), INTENT(IN) :: veg
     TYPE(cablegpu_tiles) :: tiles
+    TYPE(c_ptr) :: pbuf
     INTEGER(c_int), ALLOCATABLE, TARGET :: iveg(:), isoilm(:), flags(:)
     REAL(c_float), ALLOCATABLE, TARGET :: vlai(:), lat(:), r4(:, :)
     REAL(c_double), ALLOCATABLE, TARGET :: r8(:, :)
@@ -153,11 +157,12 @@ CONTAINS
     ! re-initialised by the step at ktau = 1; zero otherwise
     r8(:, 1) = 0.0_c_double;  CALL put('owb', C_LOC(r8))
 
-    ALLOCATE(forc(mp, CABLEGPU_NFORCING), outb(mp, 8))
     ! page-locked, so that each step's forcing upload and flux download are
     ! asynchronous copies at full speed
-    CALL check(cablegpu_host_register(C_LOC(forc), INT(4, c_size_t) * mp * CABLEGPU_NFORCING), 'host_register forc')
-    CALL check(cablegpu_host_register(C_LOC(outb), INT(4, c_size_t) * mp * 8), 'host_register outb')
+    CALL check(cablegpu_host_alloc(INT(4, c_size_t) * mp * CABLEGPU_NFORCING, pbuf), 'host_alloc forc')
+    CALL C_F_POINTER(pbuf, forc, [mp, CABLEGPU_NFORCING])
+    CALL check(cablegpu_host_alloc(INT(4, c_size_t) * mp * 8, pbuf), 'host_alloc outb')
+    CALL C_F_POINTER(pbuf, outb, [mp, 8])
     DEALLOCATE(iveg, isoilm, vlai, lat, flags, r8, r4)
   END SUBROUTINE gpu_setup
 
@@ -329,13 +334,13 @@ CONTAINS
   SUBROUTINE cbm_gpu_finalize()
     IF (C_ASSOCIATED(ctx)) CALL check(cablegpu_destroy(ctx), 'destroy')
     ctx = c_null_ptr
-    IF (ALLOCATED(forc)) THEN
-      CALL check(cablegpu_host_unregister(C_LOC(forc)), 'host_unregister forc')
-      DEALLOCATE(forc)
+    IF (ASSOCIATED(forc)) THEN
+      CALL check(cablegpu_host_free(C_LOC(forc)), 'host_free forc')
+      NULLIFY(forc)
     END IF
-    IF (ALLOCATED(outb)) THEN
-      CALL check(cablegpu_host_unregister(C_LOC(outb)), 'host_unregister outb')
-      DEALLOCATE(outb)
+    IF (ASSOCIATED(outb)) THEN
+      CALL check(cablegpu_host_free(C_LOC(outb)), 'host_free outb')
+      NULLIFY(outb)
     END IF
     IF (ALLOCATED(slot_tile)) DEALLOCATE(slot_tile)
   END SUBROUTINE cbm_gpu_finalize

@@ -44,6 +44,7 @@ EXPORTS = [
     "cablegpu_step_explicit", "cablegpu_step_implicit", "cablegpu_coupled_timed", "cablegpu_set_soil_solve",
     "cablegpu_set_canopy_schedule", "cablegpu_check_tile_param", "cablegpu_tune_blocks",
     "cablegpu_host_register", "cablegpu_host_unregister", "cablegpu_get_fields",
+    "cablegpu_host_alloc", "cablegpu_host_free",
 ]
 NOALLOC_MAX_TILES = 65536
 MAX_TILES = 33554176      # CABLEGPU_MAX_TILES: the most tiles one context takes
@@ -205,6 +206,8 @@ def load(build_if_missing: bool = True):
     L.cablegpu_get_fields.argtypes = [vp, ip, C.POINTER(ip), C.POINTER(vp)]
     L.cablegpu_host_register.argtypes = [vp, C.c_size_t]
     L.cablegpu_host_unregister.argtypes = [vp]
+    L.cablegpu_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
+    L.cablegpu_host_free.argtypes = [vp]
     L.cablegpu_tune_blocks.argtypes = [vp, ip, ip, C.c_float, C.POINTER(ip), C.POINTER(C.c_float)]
     L.cablegpu_autotune.argtypes = [C.POINTER(_Tiles), ip, ip, ip, C.POINTER(ip), C.POINTER(ip), C.POINTER(C.c_float)]
     L.cablegpu_launch_count.argtypes = [vp]
@@ -605,6 +608,40 @@ def autotune(ts, device: int = 0, sample_tiles: int = 262144, nsteps: int = 8):
     if rc != 0:
         raise CableGPUError(rc, "autotune failed")
     return int(o.value), list(b), float(ms.value)
+
+
+class HostBlock:
+    """Page-locked host memory from cablegpu_host_alloc (one mapping on
+    transparent huge pages where the kernel grants them, registered once),
+    carved into arrays for cablegpu_step_host's forcing and output buffers.
+    ``HostBlock([(13, mp), (8, mp)])`` -> ``.arrays``; ``free()`` releases it
+    (the arrays must not be used after)."""
+
+    ALIGN = 1 << 16
+
+    def __init__(self, shapes, dtype=np.float32):
+        L = load()
+        dt = np.dtype(dtype)
+        counts = [int(np.prod(sh)) for sh in shapes]
+        offs, tot = [], 0
+        for n in counts:
+            offs.append(tot)
+            tot += -(-n * dt.itemsize // self.ALIGN) * self.ALIGN
+        p = C.c_void_p()
+        rc = L.cablegpu_host_alloc(C.c_size_t(max(tot, 1)), C.byref(p))
+        if rc != 0:
+            raise CableGPUError(rc, "host_alloc of %d bytes failed" % tot)
+        self.L, self.ptr, self.nbytes = L, p.value, tot
+        self.arrays = [np.ctypeslib.as_array((C.c_byte * (n * dt.itemsize)).from_address(self.ptr + o))
+                       .view(dt).reshape(sh) for o, n, sh in zip(offs, counts, shapes)]
+
+    def free(self):
+        if self.ptr:
+            self.arrays = []
+            rc = self.L.cablegpu_host_free(C.c_void_p(self.ptr))
+            self.ptr = None
+            if rc != 0:
+                raise CableGPUError(rc, "host_free failed")
 
 
 def from_tileset(ts, device: int = 0, seed=None, order: int = 0) -> CableGPU:

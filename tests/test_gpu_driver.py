@@ -11,6 +11,8 @@ its daily extremes (canopy%tscrn :607-608), the carbon fluxes of sumcflux
 of mass_balance / energy_balance (:725-728; cable_checks.F90:472-618; the
 library runs both on the device: bal%ebal, wbal and their totals) and the
 output writer's fluxes, temperatures, soil profiles and snow (:734-738)."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -123,8 +125,9 @@ def test_per_tile_soil_albedo():
 
 def test_host_registered_buffers_step_like_any_host_buffers():
     """cablegpu_host_register page-locks the driver's own forcing and output
-    arrays (the Fortran shim registers its forc and outb): the pipelined host
-    steps then give bitwise the outputs of unregistered buffers."""
+    arrays, and cablegpu_host_alloc provides page-locked huge-page memory for
+    them (the Fortran shim's forc and outb): the pipelined host steps then
+    give bitwise the outputs of ordinary buffers."""
     from cable_gb300 import runtime as R
     ts = W.grid(20000, seed=5, nsteps=4)
     cap = R.from_tileset(ts)
@@ -135,11 +138,18 @@ def test_host_registered_buffers_step_like_any_host_buffers():
         forc.append(np.ascontiguousarray(cap.get("forcing")))
     cap.close()
     outs = []
-    for register in (False, True):
+    for mode in ("plain", "register", "alloc"):
         g = R.from_tileset(ts)
-        f = np.zeros_like(forc[0])
-        o = np.zeros((8, ts.mp), np.float32)
-        if register:
+        blk = None
+        if mode == "alloc":
+            blk = R.HostBlock([forc[0].shape, (8, ts.mp)])
+            f, o = blk.arrays
+            assert not f.any() and not o.any()   # zeroed
+            assert f.ctypes.data % R.HostBlock.ALIGN == 0 and o.ctypes.data % R.HostBlock.ALIGN == 0
+        else:
+            f = np.zeros_like(forc[0])
+            o = np.zeros((8, ts.mp), np.float32)
+        if mode == "register":
             g.host_register(f)
             g.host_register(o)
         got = []
@@ -148,13 +158,18 @@ def test_host_registered_buffers_step_like_any_host_buffers():
             g.step_host(k + 1, f, o)
             g.synchronize()
             got.append(o.copy())
-        if register:
+        if mode == "register":
             g.host_unregister(f)
             g.host_unregister(o)
+        if blk is not None:
+            ptr = blk.ptr
+            blk.free()
+            assert blk.L.cablegpu_host_free(C.c_void_p(ptr)) == -1   # released once only
         outs.append(got)
         g.close()
-    for a, b in zip(*outs):
-        np.testing.assert_array_equal(a, b)
+    for other in outs[1:]:
+        for a, b in zip(outs[0], other):
+            np.testing.assert_array_equal(a, b)
 
 
 def test_batched_copy_back_equals_single_copies():

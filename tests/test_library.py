@@ -83,6 +83,22 @@ def test_create_rejects_bad_tiles_without_a_gpu():
     assert L.cablegpu_create(C.byref(t), 0, C.byref(h)) == -1 and not h.value
 
 
+def test_host_alloc_arguments_and_failure_leave_nothing_behind():
+    """cablegpu_host_alloc refuses zero bytes and a null out; without a GPU
+    its registration fails and it returns CABLEGPU_ERR_CUDA with the mapping
+    undone and *out null; cablegpu_host_free refuses unknown addresses."""
+    L = R.load()
+    p = C.c_void_p()
+    assert L.cablegpu_host_alloc(C.c_size_t(0), C.byref(p)) == -1 and not p.value
+    assert L.cablegpu_host_alloc(C.c_size_t(4096), None) == -1
+    buf = np.zeros(16, np.float32)
+    assert L.cablegpu_host_free(C.c_void_p(buf.ctypes.data)) == -1
+    assert L.cablegpu_host_free(None) == -1
+    import torch
+    if not torch.cuda.is_available():
+        assert L.cablegpu_host_alloc(C.c_size_t(1 << 20), C.byref(p)) == -2 and not p.value
+
+
 def test_null_arguments_are_errors():
     L = R.load()
     assert L.cablegpu_create(None, 0, None) == -1
