@@ -167,37 +167,17 @@ class ClockSampler:
 # ---------------------------------------------------------------- host buffers
 class PinnedHost:
     """Host arrays of the end-to-end steps, all in one block of page-locked
-    memory from the library's cablegpu_host_alloc (runtime.HostBlock): one
-    mapping aligned to the kernel's transparent huge page size, advised
-    MADV_HUGEPAGE before its first touch and registered once.  The copy
-    engines translate every page they move while the step's kernels run; the
-    same forcing records on small pages, one pinned allocation each, ran the
-    end-to-end steps at 3.0 to 7.1 ms from one process to the next on one
-    machine, and at 3.0 ms from huge pages."""
+    memory from the library's cablegpu_host_alloc (runtime.HostBlock, the
+    CUDA driver's pinned allocator).  Arrays on 64 KB pages page-locked with
+    cablegpu_host_register ran the end-to-end steps at 3.7 to 7.1 ms on one
+    machine, pinned allocations at 3.0 to 3.7 ms."""
 
     def __init__(self, g, shapes):
         from cable_gb300 import runtime as R
-        thp0 = self.anon_huge_kb()
         self.block = R.HostBlock(shapes)
-        thp1 = self.anon_huge_kb()
         self.arrays = self.block.arrays
-        try:
-            hp = int(open("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size").read())
-        except (OSError, ValueError):
-            hp = None
-        self.info = {"huge_page_bytes": hp, "bytes": int(self.block.nbytes), "arrays": len(shapes),
-                     "anon_huge_pages_gained_bytes": None if thp0 is None or thp1 is None else 1024 * (thp1 - thp0),
-                     "allocated_by": "cablegpu_host_alloc, one block"}
-
-    @staticmethod
-    def anon_huge_kb():
-        try:
-            for line in open("/proc/meminfo"):
-                if line.startswith("AnonHugePages:"):
-                    return int(line.split()[1])
-        except OSError:
-            pass
-        return None
+        self.info = {"bytes": int(self.block.nbytes), "arrays": len(shapes),
+                     "allocated_by": "cablegpu_host_alloc (the CUDA driver's pinned allocator), one block"}
 
     def close(self):
         self.arrays = []
@@ -498,6 +478,115 @@ def coupled_arm(args, d, ts, plain_value, tuned, steps=32, numcycles=2):
             "gpu_launches": int(launches)}
 
 
+# ---------------------------------------------------------------- end to end
+def host_steps(args, d, gc, layout, ktau0, dels):
+    """End-to-end steps through cablegpu_step_host: the forcing of
+    args.e2e_records steps spread over one day is captured from the
+    generator into pinned host buffers, then args.e2e_steps steps cycle
+    through them.  A few records spread over the day keep the timed
+    steps' cost close to the device-resident steps' (consecutive
+    daytime records make every step a daytime step); many (48: 10 GB of
+    pinned buffers) make the copies themselves slow on this host
+    (address translation of the host pages), which a driver refilling
+    one forcing array per step does not see."""
+    import numpy as np
+    import torch
+    from cable_gb300 import runtime as R
+    pin = torch.cuda.is_available()
+    gc.set_host_layout(layout)
+    perm = gc.tile_order() if layout == 1 else None
+    # records spread over one day (every 48 / e2e_records steps), so the
+    # timed steps sample the diurnal cycle: the step's cost follows the
+    # sun (the dryLeaf iteration runs by day)
+    every = max(1, 48 // args.e2e_records)
+    recs = []
+    for i in range(args.e2e_records * every):
+        gc.set_options(capture_forcing=(i % every == 0))
+        gc.step(ktau0 + i, dels)
+        if i % every == 0:
+            f = gc.get("forcing")
+            recs.append(f[:, perm] if perm is not None else f)
+    gc.set_options(capture_forcing=False)
+    # the page-locked block, taken once the records exist and filled in one pass
+    ph = PinnedHost(gc, [r.shape for r in recs] + [(8, args.mp)] * 2)
+    host_f, outs = ph.arrays[:args.e2e_records], ph.arrays[args.e2e_records:]
+    for a, r in zip(host_f, recs):
+        a[...] = r
+    del recs
+    ktau0 = ktau0 + args.e2e_records * every
+    k = ktau0
+    tf = [torch.from_numpy(a) for a in host_f]
+    to = [torch.from_numpy(a) for a in outs]
+    for n in range(2):   # warm the pipelined host path (staging buffers, copy streams)
+        gc.step_host(k, host_f[(k - ktau0) % args.e2e_records], outs[n], dels); k += 1
+    gc.synchronize()
+    d.barrier()
+    ck = ClockSampler(d.local)
+    ck.start()
+    t0 = time.perf_counter()
+    for n in range(args.e2e_steps):
+        gc.step_host(k, host_f[(k - ktau0) % args.e2e_records], outs[n % 2], dels); k += 1
+    gc.synchronize()
+    secs = d.max(time.perf_counter() - t0)
+    ckr = ck.stop()
+    # this host's copy bandwidth for the step's two transfers from the same
+    # buffers (end to end is at best max(device step, upload, download)),
+    # measured after the timed steps so that they see the buffers as a
+    # driver's steps would
+    copy_gbs = None
+    if pin:
+        dev_in = torch.empty(tf[0].shape, dtype=torch.float32, device="cuda:%d" % d.local)
+        dev_out = torch.empty(to[0].shape, dtype=torch.float32, device="cuda:%d" % d.local)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        # one untimed pass first: the first transfer from a freshly
+        # pinned buffer is several times slower than the later ones,
+        # and the timed steps below each reuse buffers already copied
+        for i in range(len(tf)):
+            dev_in.copy_(tf[i], non_blocking=True)
+        for i in range(2):
+            to[i].copy_(dev_out, non_blocking=True)
+        torch.cuda.synchronize()
+        ev[0].record()
+        for i in range(len(tf)):
+            dev_in.copy_(tf[i], non_blocking=True)
+        ev[1].record()
+        for i in range(4):
+            to[i % 2].copy_(dev_out, non_blocking=True)
+        ev[2].record()
+        torch.cuda.synchronize()
+        copy_gbs = {"h2d": len(tf) * tf[0].numel() * 4 / (ev[0].elapsed_time(ev[1]) * 1e6),
+                    "d2h": 4 * to[0].numel() * 4 / (ev[1].elapsed_time(ev[2]) * 1e6)}
+        # both directions at once, as the pipelined steps run them: a
+        # step's upload and download on two streams, repeated
+        sa, sb = torch.cuda.Stream(), torch.cuda.Stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        sa.wait_event(e0)
+        sb.wait_event(e0)
+        for i in range(len(tf)):
+            with torch.cuda.stream(sa):
+                dev_in.copy_(tf[i], non_blocking=True)
+            with torch.cuda.stream(sb):
+                to[i % 2].copy_(dev_out, non_blocking=True)
+        torch.cuda.current_stream().wait_stream(sa)
+        torch.cuda.current_stream().wait_stream(sb)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        copy_gbs["both_ms_per_step"] = ms / len(host_f)
+        copy_gbs["both_gbs"] = len(tf) * (tf[0].numel() + to[0].numel()) * 4 / (ms * 1e6)
+        del dev_in, dev_out
+    nb_in, nb_out = int(host_f[0].nbytes), int(outs[0].nbytes)
+    buffers = ph.info
+    del tf, to, host_f, outs
+    ph.close()
+    return {"value": d.world * args.mp * args.e2e_steps / secs, "unit": "tile-timesteps/s",
+            "h2d_bytes_per_step": nb_in, "d2h_bytes_per_step": nb_out, "steps": args.e2e_steps,
+            "forcing_records": args.e2e_records, "ms_per_step": secs * 1e3 / args.e2e_steps, "clocks": ckr,
+            "copy_gbs": copy_gbs, "host_buffers": buffers}
+
+
 def run_gb300(args):
     import numpy as np
     from cable_gb300 import runtime as R
@@ -534,104 +623,6 @@ def run_gb300(args):
     # buffers in the caller's order, which needs tile order 3 (the
     # climate-coherent order within 2^18-tile chunks of the caller's order)
     # to keep the per-step gather and scatter of caller positions L2-local.
-    def host_steps(gc, layout, ktau0):
-        """End-to-end steps through cablegpu_step_host: the forcing of
-        args.e2e_records steps spread over one day is captured from the
-        generator into pinned host buffers, then args.e2e_steps steps cycle
-        through them.  A few records spread over the day keep the timed
-        steps' cost close to the device-resident steps' (consecutive
-        daytime records make every step a daytime step); many (48: 10 GB of
-        pinned buffers) make the copies themselves slow on this host
-        (address translation of the host pages), which a driver refilling
-        one forcing array per step does not see."""
-        import torch
-        pin = torch.cuda.is_available()
-        gc.set_host_layout(layout)
-        perm = gc.tile_order() if layout == 1 else None
-        # records spread over one day (every 48 / e2e_records steps), so the
-        # timed steps sample the diurnal cycle: the step's cost follows the
-        # sun (the dryLeaf iteration runs by day)
-        every = max(1, 48 // args.e2e_records)
-        nf = R.NFORCING
-        ph = PinnedHost(gc, [(nf, args.mp)] * args.e2e_records + [(8, args.mp)] * 2)
-        host_f, outs = ph.arrays[:args.e2e_records], ph.arrays[args.e2e_records:]
-        for i in range(args.e2e_records * every):
-            gc.set_options(capture_forcing=(i % every == 0))
-            gc.step(ktau0 + i, dels)
-            if i % every == 0:
-                f = gc.get("forcing")
-                host_f[i // every][...] = f[:, perm] if perm is not None else f
-        gc.set_options(capture_forcing=False)
-        ktau0 = ktau0 + args.e2e_records * every
-        k = ktau0
-        tf = [torch.from_numpy(a) for a in host_f]
-        to = [torch.from_numpy(a) for a in outs]
-        # this host's pinned copy bandwidth for the step's two transfers
-        # (end to end is at best max(device step, upload, download))
-        copy_gbs = None
-        if pin:
-            dev_in = torch.empty(tf[0].shape, dtype=torch.float32, device="cuda:%d" % d.local)
-            dev_out = torch.empty(to[0].shape, dtype=torch.float32, device="cuda:%d" % d.local)
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-            # one untimed pass first: the first transfer from a freshly
-            # pinned buffer is several times slower than the later ones,
-            # and the timed steps below each reuse buffers already copied
-            for i in range(len(tf)):
-                dev_in.copy_(tf[i], non_blocking=True)
-            for i in range(2):
-                to[i].copy_(dev_out, non_blocking=True)
-            torch.cuda.synchronize()
-            ev[0].record()
-            for i in range(len(tf)):
-                dev_in.copy_(tf[i], non_blocking=True)
-            ev[1].record()
-            for i in range(4):
-                to[i % 2].copy_(dev_out, non_blocking=True)
-            ev[2].record()
-            torch.cuda.synchronize()
-            copy_gbs = {"h2d": len(tf) * tf[0].numel() * 4 / (ev[0].elapsed_time(ev[1]) * 1e6),
-                        "d2h": 4 * to[0].numel() * 4 / (ev[1].elapsed_time(ev[2]) * 1e6)}
-            # both directions at once, as the pipelined steps run them: a
-            # step's upload and download on two streams, repeated
-            sa, sb = torch.cuda.Stream(), torch.cuda.Stream()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            e0.record()
-            sa.wait_event(e0)
-            sb.wait_event(e0)
-            for i in range(len(tf)):
-                with torch.cuda.stream(sa):
-                    dev_in.copy_(tf[i], non_blocking=True)
-                with torch.cuda.stream(sb):
-                    to[i % 2].copy_(dev_out, non_blocking=True)
-            torch.cuda.current_stream().wait_stream(sa)
-            torch.cuda.current_stream().wait_stream(sb)
-            e1.record()
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1)
-            copy_gbs["both_ms_per_step"] = ms / len(host_f)
-            copy_gbs["both_gbs"] = len(tf) * (tf[0].numel() + to[0].numel()) * 4 / (ms * 1e6)
-            del dev_in, dev_out
-        for n in range(2):   # warm the pipelined host path (staging buffers, copy streams)
-            gc.step_host(k, host_f[(k - ktau0) % args.e2e_records], outs[n], dels); k += 1
-        gc.synchronize()
-        d.barrier()
-        ck = ClockSampler(d.local)
-        ck.start()
-        t0 = time.perf_counter()
-        for n in range(args.e2e_steps):
-            gc.step_host(k, host_f[(k - ktau0) % args.e2e_records], outs[n % 2], dels); k += 1
-        gc.synchronize()
-        secs = d.max(time.perf_counter() - t0)
-        ckr = ck.stop()
-        nb_in, nb_out = int(host_f[0].nbytes), int(outs[0].nbytes)
-        buffers = ph.info
-        del tf, to, host_f, outs
-        ph.close()
-        return {"value": d.world * args.mp * args.e2e_steps / secs, "unit": "tile-timesteps/s",
-                "h2d_bytes_per_step": nb_in, "d2h_bytes_per_step": nb_out, "steps": args.e2e_steps,
-                "forcing_records": args.e2e_records, "ms_per_step": secs * 1e3 / args.e2e_steps, "clocks": ckr,
-                "copy_gbs": copy_gbs, "host_buffers": buffers}
     # On its own context with the tuned order and blocks, warmed up like the
     # headline's, so that it times the same early simulated period (the
     # per-step cost follows the snow and soil state) and leaves the
@@ -642,10 +633,11 @@ def run_gb300(args):
         ge.set_blocks(blocks)
         ge.run(1, args.warmup, dels)
         ge.synchronize()
-        e2e = host_steps(ge, 1, 1 + args.warmup)
+        e2e = host_steps(args, d, ge, 1, 1 + args.warmup, dels)
         ge.close()
         e2e.update({"tile_order": order, "host_layout": "device tile order (cablegpu_tile_order)",
-                    "path": "cablegpu_step_host: pinned host buffers, one copy stream per direction",
+                    "path": "cablegpu_step_host: page-locked host buffers (cablegpu_host_alloc), one copy stream "
+                            "per direction",
                     "when": "a fresh context after %d warm-up steps and one day of forcing capture: the "
                             "headline's period" % args.warmup})
     except Exception as exc:  # the line still prints; the failure is stated
@@ -715,7 +707,7 @@ def run_gb300(args):
             g.close()
             g = R.from_tileset(ts, device=d.local, order=3)
             g.set_blocks(blocks)
-            cal = host_steps(g, 0, 1)
+            cal = host_steps(args, d, g, 0, 1, dels)
             e2e["caller_order"] = {"value": cal["value"], "tile_order": 3, "host_layout": "caller tile order"}
         except Exception as exc:  # the line still prints; the failure is stated
             e2e["caller_order"] = {"value": None, "error": str(exc)[:200]}

@@ -6,8 +6,6 @@
 #include <cmath>
 #include <cstring>
 #include <condition_variable>
-#include <cstdint>
-#include <sys/mman.h>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -907,20 +905,9 @@ int cablegpu_step_host(cablegpu_ctx* c, int ktau, float dels, const float* host_
 }  // extern "C"
 
 namespace {
-// regions of cablegpu_host_alloc: the registered address -> its mapping
+// blocks handed out by cablegpu_host_alloc (cablegpu_host_free takes only these)
 std::mutex g_host_mu;
-std::vector<std::pair<void*, std::pair<void*, size_t>>> g_host_maps;
-
-// the transparent huge page size (PMD), 2 MB where the kernel does not say
-size_t huge_page_bytes() {
-  size_t hp = (size_t)2 << 20;
-  if (FILE* f = std::fopen("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size", "r")) {
-    unsigned long long v = 0;
-    if (std::fscanf(f, "%llu", &v) == 1 && v >= 4096 && (v & (v - 1)) == 0 && v <= (1ull << 32)) hp = (size_t)v;
-    std::fclose(f);
-  }
-  return hp;
-}
+std::vector<void*> g_host_blocks;
 }  // namespace
 
 extern "C" {
@@ -928,23 +915,12 @@ extern "C" {
 int cablegpu_host_alloc(size_t bytes, void** out) {
   if (!out || bytes == 0) return CABLEGPU_ERR_ARG;
   *out = nullptr;
-  const size_t hp = huge_page_bytes();
-  if (bytes > ((size_t)1 << 48)) return CABLEGPU_ERR_ARG;
-  const size_t span = (bytes + hp - 1) / hp * hp + hp;   // room to align to hp
-  void* base = mmap(nullptr, span, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
-  if (base == MAP_FAILED) return CABLEGPU_ERR_CUDA;
-  char* p = (char*)(((uintptr_t)base + hp - 1) / hp * hp);
-#ifdef MADV_HUGEPAGE
-  madvise(p, span - (size_t)(p - (char*)base), MADV_HUGEPAGE);   // a hint: small pages if refused
-#endif
-  std::memset(p, 0, bytes);   // first touch, after the advice
-  if (cudaHostRegister(p, bytes, cudaHostRegisterDefault) != cudaSuccess) {
-    munmap(base, span);
-    return CABLEGPU_ERR_CUDA;
-  }
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess || !p) return CABLEGPU_ERR_CUDA;
+  std::memset(p, 0, bytes);
   {
     std::lock_guard<std::mutex> lk(g_host_mu);
-    g_host_maps.push_back({p, {base, span}});
+    g_host_blocks.push_back(p);
   }
   *out = p;
   return CABLEGPU_OK;
@@ -952,17 +928,13 @@ int cablegpu_host_alloc(size_t bytes, void** out) {
 
 int cablegpu_host_free(void* ptr) {
   if (!ptr) return CABLEGPU_ERR_ARG;
-  std::pair<void*, size_t> m{nullptr, 0};
   {
     std::lock_guard<std::mutex> lk(g_host_mu);
-    auto it = std::find_if(g_host_maps.begin(), g_host_maps.end(), [&](const auto& e) { return e.first == ptr; });
-    if (it == g_host_maps.end()) return CABLEGPU_ERR_ARG;
-    m = it->second;
-    g_host_maps.erase(it);
+    auto it = std::find(g_host_blocks.begin(), g_host_blocks.end(), ptr);
+    if (it == g_host_blocks.end()) return CABLEGPU_ERR_ARG;
+    g_host_blocks.erase(it);
   }
-  const cudaError_t e = cudaHostUnregister(ptr);
-  munmap(m.first, m.second);
-  return e == cudaSuccess ? CABLEGPU_OK : CABLEGPU_ERR_CUDA;
+  return cudaFreeHost(ptr) == cudaSuccess ? CABLEGPU_OK : CABLEGPU_ERR_CUDA;
 }
 
 int cablegpu_host_register(void* ptr, size_t bytes) {

@@ -138,7 +138,7 @@ MODULE cablegpu_c
       TYPE(c_ptr), VALUE :: ptr
     END FUNCTION cablegpu_host_unregister
 
-    ! page-locked host memory on huge pages, for the per-step buffers
+    ! page-locked host memory (cudaHostAlloc), for the per-step buffers
     INTEGER(c_int) FUNCTION cablegpu_host_alloc(bytes, out) BIND(C, name="cablegpu_host_alloc")
       IMPORT :: c_int, c_ptr, c_size_t
       INTEGER(c_size_t), VALUE :: bytes

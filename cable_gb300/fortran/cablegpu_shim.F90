@@ -21,8 +21,8 @@ MODULE cablegpu_shim
   LOGICAL, SAVE :: cbm_gpu_copy_all = .TRUE.
   INTEGER, SAVE :: mp_gpu = 0
   ! the per-step forcing and output buffers, in page-locked host memory
-  ! from cablegpu_host_alloc (huge pages, so that the copies that overlap
-  ! the kernels are not slowed by page translation)
+  ! from cablegpu_host_alloc (the CUDA driver's pinned allocator: steadier
+  ! end-to-end steps than registering ALLOCATE-d arrays)
   REAL(c_float), POINTER, SAVE :: forc(:, :) => NULL()   ! (mp, 13)
   REAL(c_float), POINTER, SAVE :: outb(:, :) => NULL()   ! (mp, 8)
   ! caller tile (1-based) of each device slot: the per-step forcing and

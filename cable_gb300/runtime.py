@@ -611,9 +611,9 @@ def autotune(ts, device: int = 0, sample_tiles: int = 262144, nsteps: int = 8):
 
 
 class HostBlock:
-    """Page-locked host memory from cablegpu_host_alloc (one mapping on
-    transparent huge pages where the kernel grants them, registered once),
-    carved into arrays for cablegpu_step_host's forcing and output buffers.
+    """Page-locked host memory from cablegpu_host_alloc (the CUDA driver's
+    pinned allocator), carved into arrays for cablegpu_step_host's forcing
+    and output buffers.
     ``HostBlock([(13, mp), (8, mp)])`` -> ``.arrays``; ``free()`` releases it
     (the arrays must not be used after)."""
 

@@ -300,17 +300,15 @@ int cablegpu_step_host(cablegpu_ctx* ctx, int ktau, float dels, const float* hos
  * cudaHostUnregister).  No counterpart in the reference (host I/O). */
 int cablegpu_host_register(void* ptr, size_t bytes);
 int cablegpu_host_unregister(void* ptr);
-/* Allocates bytes of page-locked host memory for such buffers: one
- * anonymous mapping aligned to the kernel's transparent huge page size,
- * advised MADV_HUGEPAGE before it is first touched, zeroed and registered
- * (cudaHostRegister).  The copy engines translate every page they move
- * while the step's kernels run; on Grace-hosted GB300s (64 KB base pages)
- * the end-to-end step ran at 103 % of the device step from such memory and
- * up to 2.4x slower from small-page pinned buffers.  *out receives the
- * address; cablegpu_host_free(ptr) unregisters and unmaps it.
- * CABLEGPU_ERR_ARG for bytes == 0 or a null out, CABLEGPU_ERR_CUDA when the
- * mapping or the registration fails (nothing is left allocated).  No
- * counterpart in the reference (host I/O). */
+/* Allocates bytes of zeroed page-locked host memory for such buffers from
+ * the CUDA driver's own pinned allocator (cudaHostAlloc).  On Grace-hosted
+ * GB300s the end-to-end step from such buffers ran at 3.0-3.7 ms (against
+ * 2.95-3.1 ms device-resident), and from arrays on 64 KB pages page-locked
+ * with cablegpu_host_register at 3.7-7.1 ms.  *out receives the address;
+ * cablegpu_host_free(ptr) releases it (CABLEGPU_ERR_ARG for an address not
+ * from cablegpu_host_alloc).  CABLEGPU_ERR_ARG for bytes == 0 or a null
+ * out, CABLEGPU_ERR_CUDA when the allocation fails.  No counterpart in the
+ * reference (host I/O). */
 int cablegpu_host_alloc(size_t bytes, void** out);
 int cablegpu_host_free(void* ptr);
 /* Layout of the host buffers of cablegpu_step_host and of the records of

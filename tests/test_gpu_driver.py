@@ -125,8 +125,8 @@ def test_per_tile_soil_albedo():
 
 def test_host_registered_buffers_step_like_any_host_buffers():
     """cablegpu_host_register page-locks the driver's own forcing and output
-    arrays, and cablegpu_host_alloc provides page-locked huge-page memory for
-    them (the Fortran shim's forc and outb): the pipelined host steps then
+    arrays, and cablegpu_host_alloc provides page-locked memory for them
+    (the Fortran shim's forc and outb): the pipelined host steps then
     give bitwise the outputs of ordinary buffers."""
     from cable_gb300 import runtime as R
     ts = W.grid(20000, seed=5, nsteps=4)
@@ -145,7 +145,7 @@ def test_host_registered_buffers_step_like_any_host_buffers():
             blk = R.HostBlock([forc[0].shape, (8, ts.mp)])
             f, o = blk.arrays
             assert not f.any() and not o.any()   # zeroed
-            assert f.ctypes.data % R.HostBlock.ALIGN == 0 and o.ctypes.data % R.HostBlock.ALIGN == 0
+            assert f.ctypes.data % 256 == 0 and o.ctypes.data % 256 == 0
         else:
             f = np.zeros_like(forc[0])
             o = np.zeros((8, ts.mp), np.float32)
