@@ -172,7 +172,7 @@ class PinnedHost:
     cablegpu_host_register ran the end-to-end steps at 3.7 to 7.1 ms on one
     machine, pinned allocations at 3.0 to 3.7 ms."""
 
-    def __init__(self, g, shapes):
+    def __init__(self, shapes):
         from cable_gb300 import runtime as R
         self.block = R.HostBlock(shapes)
         self.arrays = self.block.arrays
@@ -508,7 +508,7 @@ def host_steps(args, d, gc, layout, ktau0, dels):
             recs.append(f[:, perm] if perm is not None else f)
     gc.set_options(capture_forcing=False)
     # the page-locked block, taken once the records exist and filled in one pass
-    ph = PinnedHost(gc, [r.shape for r in recs] + [(8, args.mp)] * 2)
+    ph = PinnedHost([r.shape for r in recs] + [(8, args.mp)] * 2)
     host_f, outs = ph.arrays[:args.e2e_records], ph.arrays[args.e2e_records:]
     for a, r in zip(host_f, recs):
         a[...] = r
