@@ -392,7 +392,7 @@ def surrogate_arm(args, d, ts, plain_value, tuned):
         g.set_canopy_schedule(sched)
         g.run(ktau, 8, dels); ktau += 8
         plain_canopy[sched] = g.phase_timed(ktau, 8, dels)["canopy"]; ktau += 8
-    configs = {}
+    arms = {}
     launches = 0
     for name, mode, sched in (("strict_lanes", 1, "lanes"), ("strict_pool", 1, "pool"), ("warm_pool", 2, "pool")):
         g.set_canopy_schedule(sched)
@@ -412,7 +412,7 @@ def surrogate_arm(args, d, ts, plain_value, tuned):
         ph = g.phase_timed(ktau, 8, dels)
         ktau += 8
         value = d.world * args.mp * steps / (d.max(ms) / 1e3)
-        configs[name] = {"value": value, "unit": "tile-timesteps/s", "vs_plain": value / plain_value,
+        arms[name] = {"value": value, "unit": "tile-timesteps/s", "vs_plain": value / plain_value,
                          "ms_per_step": d.max(ms) / steps, "canopy_schedule": sched,
                          "mode": "strict" if mode == 1 else "warm", "gate_k": 0.1,
                          "network_ms": round(ph["surrogate_net"], 4), "canopy_ms": round(ph["canopy"], 4),
@@ -421,7 +421,7 @@ def surrogate_arm(args, d, ts, plain_value, tuned):
                          "fallback_frac": (1.0 - acc / tried) if tried else None}
     g.set_surrogate(0, 0.1)
     g.close()
-    best = max(configs, key=lambda k: configs[k]["value"])
+    best = max(arms, key=lambda k: arms[k]["value"])
     # error against the plain kernel from the same state, same forcing
     nerr = 24
     pl = R.from_tileset(ts, device=d.local, order=tuned[0])
@@ -429,8 +429,8 @@ def surrogate_arm(args, d, ts, plain_value, tuned):
     pl.set_blocks(tuned[1])
     sg.set_blocks(tuned[1])
     sg.surrogate_weights(params, norm)
-    sg.set_canopy_schedule(configs[best]["canopy_schedule"])
-    sg.set_surrogate(1 if configs[best]["mode"] == "strict" else 2, 0.1)
+    sg.set_canopy_schedule(arms[best]["canopy_schedule"])
+    sg.set_surrogate(1 if arms[best]["mode"] == "strict" else 2, 0.1)
     se = {"fe": 0.0, "fh": 0.0, "tv": 0.0}
     mx = {"fe": 0.0, "fh": 0.0, "tv": 0.0}
     for k in range(nerr):
@@ -443,8 +443,8 @@ def surrogate_arm(args, d, ts, plain_value, tuned):
             mx[f] = max(mx[f], float(np.abs(e).max()))
     pl.close()
     sg.close()
-    out = dict(configs[best])
-    out.update({"best_of": configs, "gpu_launches": int(launches), "timed_steps": steps,
+    out = dict(arms[best])
+    out.update({"best_of": arms, "gpu_launches": int(launches), "timed_steps": steps,
                 "vs_plain_kernel_%d_steps" % nerr: {
                     "config": best,
                     "le_rmse_wm2": float(np.sqrt(se["fe"] / nerr)), "h_rmse_wm2": float(np.sqrt(se["fh"] / nerr)),

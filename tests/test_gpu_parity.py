@@ -16,8 +16,8 @@ from cable_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
 
-# the benchmark spec's outputs (latent and sensible heat, GPP, canopy and soil
-# temperature, soil moisture) and the fluxes that make them up
+# the outputs the accuracy targets name (latent and sensible heat, GPP,
+# canopy and soil temperature, soil moisture) and the fluxes that make them up
 FIELDS = ["fe_d", "fh_d", "ga_d", "rnet_d", "fes", "fevc", "tv_d", "trad_d", "tgg", "tggsn", "wb", "wbice",
           "fgpp_d", "fpn", "frday_d"]
 
