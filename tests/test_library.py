@@ -81,6 +81,10 @@ def test_create_rejects_bad_tiles_without_a_gpu():
                  ts.lat.ctypes.data_as(C.POINTER(C.c_float)), None, None, None, 0)
     h = C.c_void_p()
     assert L.cablegpu_create(C.byref(t), 0, C.byref(h)) == -1 and not h.value
+    # and an empty or negative tile count
+    for mp in (0, -5):
+        t.mp = mp
+        assert L.cablegpu_create(C.byref(t), 0, C.byref(h)) == -1 and not h.value
 
 
 def test_host_alloc_arguments_and_failure_leave_nothing_behind():
